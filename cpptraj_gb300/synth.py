@@ -1,0 +1,119 @@
+"""Seeded synthetic trajectories with the shapes of the all-pairs RMSD workloads.
+
+No public dataset is named for this path, so these generators stand in for
+real trajectories.  A reference chain is a 3-D random walk with 3.8 Angstrom
+steps (Gaussian direction, normalised).  Each frame is the chain plus i.i.d.
+Gaussian displacement, then a uniformly random rotation (normalised Gaussian
+quaternion) and a translation drawn from U[-20, 20]^3.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+#: Element masses and their probabilities used for mass-weighted workloads
+#: (H, C, N, O, S).
+MASS_VALUES = np.array([1.008, 12.011, 14.007, 15.999, 32.06])
+MASS_PROBS = np.array([0.50, 0.32, 0.09, 0.08, 0.01])
+
+
+def random_walk(rng: np.random.Generator, n_atom: int, step: float = 3.8) -> np.ndarray:
+    """Return an (n_atom, 3) random-walk chain with fixed step length."""
+    d = rng.standard_normal((n_atom, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d[0] = 0.0
+    return np.cumsum(d * step, axis=0)
+
+
+def random_rotations(rng: np.random.Generator, n: int) -> np.ndarray:
+    """Uniform random rotation matrices from normalised Gaussian quaternions."""
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    a, b, c, d = q.T
+    R = np.empty((n, 3, 3))
+    R[:, 0, 0] = a * a + b * b - c * c - d * d
+    R[:, 0, 1] = 2 * (b * c - a * d)
+    R[:, 0, 2] = 2 * (b * d + a * c)
+    R[:, 1, 0] = 2 * (b * c + a * d)
+    R[:, 1, 1] = a * a - b * b + c * c - d * d
+    R[:, 1, 2] = 2 * (c * d - a * b)
+    R[:, 2, 0] = 2 * (b * d - a * c)
+    R[:, 2, 1] = 2 * (c * d + a * b)
+    R[:, 2, 2] = a * a - b * b - c * c + d * d
+    return R
+
+
+def perturb_frames(rng, chains, labels, sigma):
+    """chains[labels[f]] + N(0, sigma[f]^2), rotated and translated."""
+    n_frame = len(labels)
+    n_atom = chains.shape[1]
+    X = chains[labels] + rng.standard_normal((n_frame, n_atom, 3)) * sigma[:, None, None]
+    R = random_rotations(rng, n_frame)
+    X = np.einsum("fij,faj->fai", R, X)
+    X += rng.uniform(-20.0, 20.0, (n_frame, 1, 3))
+    return X
+
+
+def masses(rng: np.random.Generator, n_atom: int) -> np.ndarray:
+    return rng.choice(MASS_VALUES, size=n_atom, p=MASS_PROBS)
+
+
+def trajectory(seed: int, n_frame: int, n_atom: int, sigma_lo: float, sigma_hi: float,
+               dtype=np.float32, weighted: bool = False):
+    """One chain, per-frame sigma ~ U(sigma_lo, sigma_hi).
+
+    Returns (coords[n_frame, n_atom, 3] of ``dtype``, masses[n_atom] float64 or None).
+    """
+    rng = np.random.default_rng(seed)
+    chain = random_walk(rng, n_atom)[None]
+    sigma = rng.uniform(sigma_lo, sigma_hi, n_frame)
+    X = perturb_frames(rng, chain, np.zeros(n_frame, dtype=np.int64), sigma)
+    m = masses(rng, n_atom) if weighted else None
+    return np.ascontiguousarray(X.astype(dtype)), m
+
+
+def clustered(seed: int, n_frame: int, n_atom: int, n_centroid: int = 20, sigma: float = 0.8,
+              dtype=np.float32):
+    """Frames drawn around ``n_centroid`` random-walk centroids.
+
+    Returns (coords, labels) where labels[f] is the centroid index of frame f.
+    """
+    rng = np.random.default_rng(seed)
+    chains = np.stack([random_walk(rng, n_atom) for _ in range(n_centroid)])
+    labels = rng.integers(0, n_centroid, n_frame)
+    X = perturb_frames(rng, chains, labels, np.full(n_frame, sigma))
+    return np.ascontiguousarray(X.astype(dtype)), labels
+
+
+# Named workloads ---------------------------------------------------------------------------
+
+def workload_c0(seed: int = 0, n_frame: int = 500, n_atom: int = 304):
+    """rms2d fit, 500 frames x 304 atoms, FP64, unweighted, sigma ~ U(0.5, 2.0)."""
+    X, _ = trajectory(seed, n_frame, n_atom, 0.5, 2.0, dtype=np.float64, weighted=False)
+    return X, None
+
+
+def workload_c1(seed: int = 1, n_frame: int = 10000, n_atom: int = 2000):
+    """10,000 frames x 2,000 atoms, FP32, mass-weighted, sigma ~ U(0.1, 3.0)."""
+    return trajectory(seed, n_frame, n_atom, 0.1, 3.0, dtype=np.float32, weighted=True)
+
+
+def workload_c2(seed: int = 2, n_frame: int = 50000, n_atom: int = 500):
+    """Clustering cache: 50,000 frames x 500 atoms around 20 centroids, sigma 0.8."""
+    return clustered(seed, n_frame, n_atom, 20, 0.8, dtype=np.float32)
+
+
+def workload_c3(seed: int = 3, n_traj: int = 256, f_range=(100, 4000), n_range=(50, 3000)):
+    """Batch of independent trajectories with random frame/atom counts, mass-weighted."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for t in range(n_traj):
+        nf = int(rng.integers(f_range[0], f_range[1] + 1))
+        na = int(rng.integers(n_range[0], n_range[1] + 1))
+        out.append(trajectory(seed * 100003 + t, nf, na, 0.1, 3.0, np.float32, True))
+    return out
+
+
+def workload_c4(seed: int = 4, n_frame: int = 4096, n_atom: int = 1000):
+    """Differentiation workload: 4,096 frames x 1,000 atoms, sigma 1.0, unweighted."""
+    X, _ = trajectory(seed, n_frame, n_atom, 1.0, 1.0, dtype=np.float32, weighted=False)
+    return X, None

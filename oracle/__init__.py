@@ -1,0 +1,171 @@
+"""ctypes access to the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+``librmsd_oracle.so`` is the FP64 restatement in ``rmsd_oracle.c``;
+``_ref/libcpptraj_rmsd_ref.so`` is cpptraj's own Frame RMSD code compiled from
+its sources (present only where those sources were available at build time).
+Only tests, ``__graft_entry__.smoke`` and bench.py's CPU-baseline leg use this.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "librmsd_oracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libcpptraj_rmsd_ref.so")
+REF_SRC = "/root/reference/src"
+
+FIT, NOFIT, QCP = 0, 1, 2
+TRI, FULL = 0, 1
+
+_lib = None
+_ref = None
+
+
+def build(with_ref: bool = True) -> None:
+    """Compile the oracle (and, when the reference sources exist, oracle/_ref)."""
+    subprocess.run(["make", "-s", "-C", HERE, "-j8"], check=True)
+    if with_ref and os.path.isdir(REF_SRC):
+        subprocess.run(["make", "-s", "-C", HERE, "-j8", "ref"], check=True)
+
+
+def _p(a):
+    return ctypes.c_void_p(0) if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build(with_ref=False)
+        L = ctypes.CDLL(LIB)
+        L.orc_allpairs.restype = ctypes.c_int
+        L.orc_allpairs.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int64,
+                                   ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64,
+                                   ctypes.c_int64, ctypes.c_int]
+        L.orc_allpairs_f64.restype = ctypes.c_int
+        L.orc_allpairs_f64.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int64,
+                                       ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+        L.orc_pairs_f64.restype = ctypes.c_int
+        L.orc_pairs_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                    ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                    ctypes.c_void_p, ctypes.c_int]
+        L.orc_max_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        L = ctypes.CDLL(REF_LIB)
+        L.ref_allpairs.restype = ctypes.c_int
+        L.ref_allpairs.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int64,
+                                   ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+        L.ref_pairs_f64.restype = ctypes.c_int
+        L.ref_pairs_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                    ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                    ctypes.c_void_p]
+        _ref = L
+    return _ref
+
+
+def _dtype_code(x):
+    if x.dtype == np.float64:
+        return 1
+    if x.dtype == np.float32:
+        return 0
+    raise TypeError("coordinates must be float32 or float64")
+
+
+def n_out(n_ref, n_tgt, out_kind, row_begin=0, row_end=None):
+    if row_end is None:
+        row_end = n_ref
+    if out_kind == TRI:
+        def cnt(i):
+            return i * n_ref - (i * (i + 1)) // 2
+        return cnt(row_end) - cnt(row_begin)
+    return (row_end - row_begin) * n_tgt
+
+
+def allpairs(ref, tgt=None, ref_mass=None, tgt_mass=None, mode=FIT, out_kind=None,
+             row_begin=0, row_end=None, nthreads=0, use_reference_code=False):
+    """All-pairs RMSD with rms2d semantics; returns the float32 output array."""
+    ref = np.ascontiguousarray(ref)
+    n_ref, n_atom = ref.shape[0], ref.shape[1]
+    if tgt is not None:
+        tgt = np.ascontiguousarray(tgt, dtype=ref.dtype)
+    n_tgt = n_ref if tgt is None else tgt.shape[0]
+    if out_kind is None:
+        out_kind = TRI if tgt is None else FULL
+    if tgt_mass is not None:
+        tgt_mass = np.ascontiguousarray(tgt_mass, dtype=np.float64)
+    if ref_mass is not None:
+        ref_mass = np.ascontiguousarray(ref_mass, dtype=np.float64)
+    elif tgt_mass is not None:
+        ref_mass = tgt_mass
+    if row_end is None:
+        row_end = n_ref
+    if use_reference_code:
+        out = np.zeros(n_out(n_ref, n_tgt, out_kind), np.float32)
+        rc = ref_lib().ref_allpairs(_p(ref), _p(tgt), _dtype_code(ref), n_ref, n_tgt, n_atom,
+                                    _p(ref_mass), _p(tgt_mass), mode, out_kind, _p(out), nthreads)
+    else:
+        out = np.zeros(n_out(n_ref, n_tgt, out_kind, row_begin, row_end), np.float32)
+        rc = lib().orc_allpairs(_p(ref), _p(tgt), _dtype_code(ref), n_ref, n_tgt, n_atom,
+                                _p(ref_mass), _p(tgt_mass), mode, out_kind, _p(out),
+                                row_begin, row_end, nthreads)
+    if rc & 1:
+        raise ValueError("oracle rejected arguments")
+    return out
+
+
+def allpairs_f64(ref, tgt=None, ref_mass=None, tgt_mass=None, mode=FIT, out_kind=None, nthreads=0):
+    ref = np.ascontiguousarray(ref)
+    n_ref, n_atom = ref.shape[0], ref.shape[1]
+    if tgt is not None:
+        tgt = np.ascontiguousarray(tgt, dtype=ref.dtype)
+    n_tgt = n_ref if tgt is None else tgt.shape[0]
+    if out_kind is None:
+        out_kind = TRI if tgt is None else FULL
+    if tgt_mass is not None:
+        tgt_mass = np.ascontiguousarray(tgt_mass, dtype=np.float64)
+    if ref_mass is None:
+        ref_mass = tgt_mass
+    else:
+        ref_mass = np.ascontiguousarray(ref_mass, dtype=np.float64)
+    out = np.zeros(n_out(n_ref, n_tgt, out_kind), np.float64)
+    lib().orc_allpairs_f64(_p(ref), _p(tgt), _dtype_code(ref), n_ref, n_tgt, n_atom,
+                           _p(ref_mass), _p(tgt_mass), mode, out_kind, _p(out), nthreads)
+    return out
+
+
+def pairs_f64(xyz, pi, pj, mass=None, mode=FIT, nthreads=0, use_reference_code=False):
+    """RMSD for an explicit list of (ref=pi, tgt=pj) pairs, FP64."""
+    xyz = np.ascontiguousarray(xyz)
+    pi = np.ascontiguousarray(pi, dtype=np.int64)
+    pj = np.ascontiguousarray(pj, dtype=np.int64)
+    if mass is not None:
+        mass = np.ascontiguousarray(mass, dtype=np.float64)
+    out = np.zeros(len(pi), np.float64)
+    if use_reference_code:
+        ref_lib().ref_pairs_f64(_p(xyz), _dtype_code(xyz), xyz.shape[1], _p(mass), mode,
+                                _p(pj), _p(pi), len(pi), _p(out))
+    else:
+        lib().orc_pairs_f64(_p(xyz), _dtype_code(xyz), xyz.shape[1], _p(mass), mode, _p(pi), _p(pj),
+                            len(pi), _p(out), nthreads)
+    return out
+
+
+def tri_index(n, i, j):
+    return n * i - ((i + 1) * i) // 2 + j - i - 1

@@ -1,0 +1,87 @@
+// ref_shim.cpp -- TEST INFRASTRUCTURE ONLY.
+//
+// Thin C entry points over cpptraj's own Frame RMSD code, compiled from the
+// reference sources by `make -C oracle ref` into oracle/_ref/.  Used to pin
+// the FP64 restatement in rmsd_oracle.c and, in this container, as the
+// "reference" CPU baseline.  The loops mirror
+//   Analysis_Rms2d::Calculate_2D      (src/Analysis_Rms2d.cpp:247-290)  and
+//   Metric_RMS::FrameDist             (src/Cluster/Metric_RMS.cpp:44-63)
+// with the work itself done by Frame::RMSD_CenteredRef / RMSD_NoFit /
+// QuaternionRMSD_CenteredRef.
+#include <cstdint>
+#include <vector>
+#include "Frame.h"
+#include "QuaternionRMSD.h"
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+void fill(Frame& fr, const void* base, int dtype, int64_t f, int n) {
+  double* x = fr.xAddress();
+  if (dtype == 1) {
+    const double* s = (const double*)base + (size_t)f * 3 * n;
+    for (int k = 0; k < 3 * n; ++k) x[k] = s[k];
+  } else {
+    const float* s = (const float*)base + (size_t)f * 3 * n;
+    for (int k = 0; k < 3 * n; ++k) x[k] = (double)s[k];
+  }
+}
+int64_t tri(int64_t n, int64_t i, int64_t j) { return n * i - ((i + 1) * i) / 2 + j - i - 1; }
+Frame make(int n, const double* mass) {
+  std::vector<double> X(3 * (size_t)n, 0.0), M(n, 1.0);
+  if (mass) M.assign(mass, mass + n);
+  Frame f;
+  f.SetupFrameXM(X, M);
+  return f;
+}
+}  // namespace
+
+// mode: 0 = fit (RMSD_CenteredRef), 1 = nofit, 2 = qrmsd.  Same argument meaning
+// as orc_allpairs in rmsd_oracle.c.
+extern "C" int ref_allpairs(const void* ref_xyz, const void* tgt_xyz, int dtype, int64_t n_ref,
+                            int64_t n_tgt, int n_atom, const double* ref_mass, const double* tgt_mass,
+                            int mode, int out_kind, float* out, int nthreads) {
+  if (tgt_xyz == nullptr) { tgt_xyz = ref_xyz; n_tgt = n_ref; }
+  bool use_mass = (tgt_mass != nullptr);
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel
+#endif
+  {
+    Frame R = make(n_atom, ref_mass ? ref_mass : tgt_mass);
+    Frame T = make(n_atom, tgt_mass);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic)
+#endif
+    for (int64_t i = 0; i < n_ref; ++i) {
+      fill(R, ref_xyz, dtype, i, n_atom);
+      if (mode != 1) R.CenterOnOrigin(use_mass);
+      int64_t j0 = (out_kind == 0) ? i + 1 : 0;
+      for (int64_t j = j0; j < n_tgt; ++j) {
+        fill(T, tgt_xyz, dtype, j, n_atom);
+        double r;
+        if (mode == 0) r = T.RMSD_CenteredRef(R, use_mass);
+        else if (mode == 1) r = T.RMSD_NoFit(R, use_mass);
+        else r = QuaternionRMSD_CenteredRef(R, T, use_mass);
+        int64_t idx = (out_kind == 0) ? tri(n_ref, i, j) : j * n_ref + i;
+        out[idx] = (float)r;
+      }
+    }
+  }
+  return 0;
+}
+
+// Pair list in FP64, cluster-metric convention: frame pi[k] is the target
+// ("this"), frame pj[k] is centred as the reference (Frame::RMSD).
+extern "C" int ref_pairs_f64(const void* xyz, int dtype, int n_atom, const double* mass, int mode,
+                             const int64_t* pi, const int64_t* pj, int64_t npairs, double* out) {
+  bool use_mass = (mass != nullptr);
+  Frame A = make(n_atom, mass), B = make(n_atom, mass);
+  for (int64_t k = 0; k < npairs; ++k) {
+    fill(A, xyz, dtype, pi[k], n_atom);
+    fill(B, xyz, dtype, pj[k], n_atom);
+    out[k] = (mode == 1) ? A.RMSD_NoFit(B, use_mass) : A.RMSD(B, use_mass);
+  }
+  return 0;
+}

@@ -1,0 +1,94 @@
+"""The CPU oracle against the reference's own golden vectors (no GPU).
+
+tz2 fixtures come from test/Test_2DRMS (printed at %8.3f); ref_pairs come from
+cpptraj's Frame code compiled from its sources (tests/golden/make_golden.py).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def square(tri, n):
+    M = np.zeros((n, n))
+    k = 0
+    for i in range(n):
+        for j in range(i + 1, n):
+            M[i, j] = M[j, i] = tri[k]
+            k += 1
+    return M
+
+
+def fmt3(M):
+    return np.array([[float("%8.3f" % v) for v in row] for row in M])
+
+
+@pytest.fixture(scope="module")
+def tz2():
+    return np.load(os.path.join(GOLD, "tz2_rms2d.npz"))
+
+
+@pytest.mark.parametrize("save,xyz,mass,mode", [
+    ("rmsd_save", "fit_xyz", None, oracle.FIT),           # unit 1
+    ("rmsd_mass_save", "fit_xyz", "fit_mass", oracle.FIT),  # unit 2
+    ("nofit_save", "nofit_xyz", None, oracle.NOFIT),      # unit 6
+    ("rmsd_save", "fit_xyz", None, oracle.QCP),           # unit 8 (qrmsd)
+])
+def test_tz2_triangle(tz2, save, xyz, mass, mode):
+    out = oracle.allpairs(tz2[xyz], tgt_mass=tz2[mass] if mass else None, mode=mode)
+    assert np.array_equal(fmt3(square(out, 10)), tz2[save])
+
+
+def test_tz2_full_ref_mask(tz2):
+    # unit 5: `2drms :2 :11` -> target mask :2, reference mask :11, FULL matrix
+    out = oracle.allpairs(tz2["trp_ref_xyz"], tz2["trp_tgt_xyz"])
+    M = out.reshape(10, 10)  # printed row = target frame, column = reference frame
+    assert np.array_equal(fmt3(M), tz2["trp_save"])
+
+
+@pytest.fixture(scope="module")
+def refp():
+    return np.load(os.path.join(GOLD, "ref_pairs.npz"))
+
+
+@pytest.mark.parametrize("mode,tag", [(oracle.FIT, "fit"), (oracle.NOFIT, "nofit")])
+@pytest.mark.parametrize("wt", ["w", "u"])
+def test_pairs_match_reference_code(refp, mode, tag, wt):
+    m = refp["mass"] if wt == "w" else None
+    got = oracle.pairs_f64(refp["xyz"], refp["pi"], refp["pj"], mass=m, mode=mode)
+    # rms2d centres the row frame, the cluster metric the second frame: the same
+    # math, so agreement is at FP64 rounding level.
+    np.testing.assert_allclose(got, refp[f"{tag}_{wt}"], rtol=0, atol=1e-9)
+
+
+@pytest.mark.parametrize("mode,tag", [(oracle.FIT, "fit"), (oracle.QCP, "qcp"), (oracle.NOFIT, "nofit")])
+def test_tri_bitwise_vs_reference_code(refp, mode, tag):
+    got = oracle.allpairs(refp["xyz"], tgt_mass=refp["mass"], mode=mode)
+    assert np.array_equal(got, refp[f"tri_{tag}"])
+
+
+def test_row_ranges_concatenate(refp):
+    X, m = refp["xyz"], refp["mass"]
+    full = oracle.allpairs(X, tgt_mass=m)
+    parts = [oracle.allpairs(X, tgt_mass=m, row_begin=a, row_end=b) for a, b in ((0, 5), (5, 17), (17, 24))]
+    assert np.array_equal(np.concatenate(parts), full)
+
+
+def test_zero_mass_reports_error():
+    X = np.random.default_rng(0).standard_normal((3, 4, 3))
+    out = oracle.allpairs_f64(X, tgt_mass=np.zeros(4))
+    assert np.all(out == -1.0)
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference sources not built here")
+def test_live_reference_random():
+    from cpptraj_gb300 import synth
+    X, m = synth.trajectory(21, 40, 211, 0.1, 2.0, np.float64, True)
+    for mode in (oracle.FIT, oracle.NOFIT, oracle.QCP):
+        a = oracle.allpairs(X, tgt_mass=m, mode=mode)
+        b = oracle.allpairs(X, tgt_mass=m, mode=mode, use_reference_code=True)
+        assert np.array_equal(a, b)

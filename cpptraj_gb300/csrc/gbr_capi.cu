@@ -1,0 +1,515 @@
+// gbr_capi.cu -- the extern "C" boundary (include/gbrmsd.h) and the host-side
+// orchestration of one all-pairs call:
+//   stage inputs -> centre + pick references + superpose (gbr_prep.cu)
+//   -> per-frame terms -> pair contraction (FP32 CUDA cores or tcgen05)
+//   -> FP64 re-check of flagged pairs (gbr_exact.cu) -> results to the caller.
+// It replaces the OpenMP pair loops of Analysis_Rms2d::Calculate_2D
+// (src/Analysis_Rms2d.cpp:247-290) and MetricArray::calcFrameDistances
+// (src/Cluster/MetricArray.cpp:777-800) as one call from the master thread.
+#include <cuda_fp16.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gbrmsd.h"
+#include "gbr_internal.h"
+
+using namespace gbr;
+
+namespace {
+
+struct Arena {
+  char* base = nullptr;
+  size_t off = 0;
+  template <class T>
+  T* take(size_t n) {
+    off = (off + 255) & ~size_t(255);
+    T* p = reinterpret_cast<T*>(base ? base + off : nullptr);
+    off += n * sizeof(T);
+    return p;
+  }
+};
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+struct gbr_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;      // stream in use
+  cudaStream_t own_stream = nullptr;  // created with the handle
+  std::string err;
+  gbr_stats stats{};
+  double tau = 4.0;
+  int max_refs = 32;
+  double tol = 5e-5;
+  bool timing = false;
+  char* ws = nullptr;
+  size_t ws_cap = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  int num_sms = 0;
+  int tc_ok = 0;
+
+  int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    err = buf;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* where) {
+    return fail(GBR_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+  }
+  bool reserve(size_t bytes) {
+    if (bytes <= ws_cap) return true;
+    if (ws) cudaFree(ws);
+    ws = nullptr;
+    ws_cap = 0;
+    if (cudaMalloc(&ws, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    ws_cap = bytes;
+    return true;
+  }
+};
+
+extern "C" {
+
+gbr_handle* gbr_create(int device) {
+  if (cudaSetDevice(device) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  gbr_handle* h = new gbr_handle();
+  h->device = device;
+  if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return nullptr;
+  }
+  h->stream = h->own_stream;
+  for (auto& e : h->ev) cudaEventCreate(&e);
+  cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device);
+  h->tc_ok = tc_supported(device);
+  return h;
+}
+
+void gbr_destroy(gbr_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (auto& e : h->ev)
+    if (e) cudaEventDestroy(e);
+  if (h->ws) cudaFree(h->ws);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  delete h;
+}
+
+int gbr_set_stream(gbr_handle* h, void* stream) {
+  if (!h) return GBR_ERR_ARG;
+  h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+  return GBR_OK;
+}
+
+const char* gbr_last_error(const gbr_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int gbr_get_stats(const gbr_handle* h, gbr_stats* out) {
+  if (!h || !out) return GBR_ERR_ARG;
+  *out = h->stats;
+  return GBR_OK;
+}
+
+int gbr_set_option(gbr_handle* h, int key, double value) {
+  if (!h) return GBR_ERR_ARG;
+  switch (key) {
+    case GBR_OPT_TAU:
+      if (!(value >= 0.0)) return h->fail(GBR_ERR_ARG, "tau must be >= 0");
+      h->tau = value;
+      return GBR_OK;
+    case GBR_OPT_MAX_REFS:
+      if (value < 1 || value > kMaxRefs) return h->fail(GBR_ERR_ARG, "max_refs must be in [1, %d]", kMaxRefs);
+      h->max_refs = (int)value;
+      return GBR_OK;
+    case GBR_OPT_TOL:
+      if (!(value > 0.0)) return h->fail(GBR_ERR_ARG, "tol must be > 0");
+      h->tol = value;
+      return GBR_OK;
+    case GBR_OPT_TIMING:
+      h->timing = value != 0.0;
+      return GBR_OK;
+  }
+  return h->fail(GBR_ERR_ARG, "unknown option %d", key);
+}
+
+int64_t gbr_output_count(int64_t n_ref, int64_t n_tgt, int out_kind, int64_t row_begin, int64_t row_end) {
+  if (out_kind == GBR_TRI) {
+    if (row_end < 0 || row_end > n_ref) row_end = n_ref;
+    if (row_begin < 0) row_begin = 0;
+    if (row_end <= row_begin) return 0;
+    auto cnt = [&](int64_t i) { return i * n_ref - (i * (i + 1)) / 2; };
+    return cnt(row_end) - cnt(row_begin);
+  }
+  if (row_end < 0 || row_end > n_tgt) row_end = n_tgt;
+  if (row_begin < 0) row_begin = 0;
+  if (row_end <= row_begin) return 0;
+  return (row_end - row_begin) * n_ref;
+}
+
+int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dtype, int64_t n_ref,
+                 int64_t n_tgt, int32_t n_atom, const double* ref_mass, const double* tgt_mass, int mode,
+                 int out_kind, int precision, float* out, int64_t row_begin, int64_t row_end) {
+  if (!h) return GBR_ERR_ARG;
+  h->err.clear();
+  h->stats = gbr_stats{};
+  const auto t_start = std::chrono::steady_clock::now();
+  if (!ref_xyz) return h->fail(GBR_ERR_ARG, "ref_xyz is NULL");
+  if (!out) return h->fail(GBR_ERR_ARG, "out is NULL");
+  if (dtype != GBR_F32 && dtype != GBR_F64) return h->fail(GBR_ERR_ARG, "dtype must be GBR_F32 or GBR_F64");
+  if (mode != GBR_FIT && mode != GBR_NOFIT) return h->fail(GBR_ERR_ARG, "mode must be GBR_FIT or GBR_NOFIT");
+  if (out_kind != GBR_TRI && out_kind != GBR_FULL) return h->fail(GBR_ERR_ARG, "out_kind must be TRI or FULL");
+  if (precision < GBR_PREC_FP32 || precision > GBR_PREC_FP64) return h->fail(GBR_ERR_ARG, "bad precision");
+  if (n_atom < 1) return h->fail(GBR_ERR_ARG, "n_atom must be >= 1 (no atoms selected)");
+  if (n_ref < 0 || n_tgt < 0) return h->fail(GBR_ERR_ARG, "negative frame count");
+  if (tgt_xyz == nullptr || tgt_xyz == ref_xyz) {
+    tgt_xyz = nullptr;
+    n_tgt = n_ref;
+  }
+  if (out_kind == GBR_TRI && tgt_xyz != nullptr)
+    return h->fail(GBR_ERR_ARG, "GBR_TRI needs one frame set (tgt_xyz NULL)");
+  if (n_ref > INT32_MAX || n_tgt > INT32_MAX) return h->fail(GBR_ERR_ARG, "frame count exceeds 2^31-1");
+  const int64_t n_rows = (out_kind == GBR_TRI) ? n_ref : n_tgt;
+  if (row_end < 0 || row_end > n_rows) row_end = n_rows;
+  if (row_begin < 0 || row_begin > row_end) return h->fail(GBR_ERR_ARG, "bad row range [%lld, %lld)",
+                                                         (long long)row_begin, (long long)row_end);
+  if (precision == GBR_PREC_TC && !h->tc_ok)
+    return h->fail(GBR_ERR_UNSUPPORTED, "tensor-core precision needs an sm_103 (GB300) device");
+  const int64_t n_out = gbr_output_count(n_ref, n_tgt, out_kind, row_begin, row_end);
+  if (cudaSetDevice(h->device) != cudaSuccess) return h->cuda_fail(cudaGetLastError(), "cudaSetDevice");
+  cudaStream_t st = h->stream;
+
+  // Masses: small, read them on the host whatever their memory kind.
+  const int N = n_atom;
+  const bool nofit = (mode == GBR_NOFIT);
+  std::vector<double> w_h, wref_h;
+  if (tgt_mass) {
+    w_h.resize(N);
+    if (cudaMemcpy(w_h.data(), tgt_mass, sizeof(double) * N, cudaMemcpyDefault) != cudaSuccess)
+      return h->cuda_fail(cudaGetLastError(), "reading tgt_mass");
+    if (ref_mass && tgt_xyz != nullptr) {
+      wref_h.resize(N);
+      if (cudaMemcpy(wref_h.data(), ref_mass, sizeof(double) * N, cudaMemcpyDefault) != cudaSuccess)
+        return h->cuda_fail(cudaGetLastError(), "reading ref_mass");
+    }
+  }
+  double Wsum = 0.0;
+  if (tgt_mass) {
+    for (double v : w_h) Wsum += v;
+  } else {
+    Wsum = (double)N;
+  }
+  if (Wsum < 1e-14) return h->fail(GBR_ERR_ZERO_MASS, "total mass %g is below 1e-14 (divide by zero)", Wsum);
+  if (n_out == 0) {
+    h->stats.precision = precision;
+    return GBR_OK;
+  }
+
+  const bool ref_dev = is_device_ptr(ref_xyz);
+  const bool tgt_dev = tgt_xyz ? is_device_ptr(tgt_xyz) : ref_dev;
+  const bool out_dev = is_device_ptr(out);
+  const size_t esz = (dtype == GBR_F64) ? 8 : 4;
+  const int64_t F = (tgt_xyz ? n_ref + n_tgt : n_ref);
+  const int64_t tgt0 = tgt_xyz ? n_ref : 0;
+  const int Np = (N + 63) / 64 * 64;
+  const int Kmax = std::min<int>(h->max_refs, (int)std::max<int64_t>(F, 1));
+  const bool need_planes = (precision != GBR_PREC_FP64);
+  const bool tc = (precision == GBR_PREC_TC);
+  const int64_t total_pairs = n_out;
+  const unsigned long long flag_cap = (unsigned long long)std::min<int64_t>(total_pairs, 1 << 22);
+
+  // ---- workspace layout (sizing pass, then carve) ----
+  auto layout = [&](Arena& A, void** p) {
+    p[0] = ref_dev ? nullptr : A.take<char>(esz * 3 * (size_t)N * n_ref);
+    p[1] = (tgt_xyz && !tgt_dev) ? A.take<char>(esz * 3 * (size_t)N * n_tgt) : nullptr;
+    p[2] = A.take<double>(N);        // w
+    p[3] = A.take<double>(N);        // wref
+    p[4] = A.take<double>(3 * F);    // cen
+    p[5] = A.take<int64_t>(1);       // fsel
+    p[6] = A.take<float>(1);         // dmax
+    p[7] = A.take<float>(F);         // dist
+    p[8] = A.take<int>(F);           // assign
+    p[9] = A.take<double>((size_t)Kmax * 3 * N);  // refs
+    p[10] = A.take<float>((size_t)Kmax * 3 * N);  // swr
+    p[11] = A.take<double>(Kmax);                 // Eref
+    p[12] = need_planes ? A.take<float>((size_t)F * 3 * Np) : nullptr;  // plane
+    p[13] = A.take<unsigned>(1);                                        // pmax
+    p[14] = A.take<float>(F);                                           // nrm
+    p[15] = A.take<float>((size_t)F * Kmax * 9);                        // P
+    p[16] = A.take<float>((size_t)F * Kmax);                            // trP
+    p[17] = A.take<float>((size_t)Kmax * Kmax * 9);                     // S
+    p[18] = A.take<float>((size_t)Kmax * Kmax * 3);                     // SA
+    p[19] = A.take<float>((size_t)Kmax * Kmax);                         // SSd
+    p[20] = A.take<int2>(flag_cap);                                     // flagged
+    p[21] = A.take<unsigned long long>(1);                              // count
+    p[22] = out_dev ? nullptr : A.take<float>(n_out);                   // out staging
+    p[23] = tc ? A.take<__half_raw>((size_t)F * 4 * Np) : nullptr;      // hi
+    p[24] = tc ? A.take<__half_raw>((size_t)F * 4 * Np) : nullptr;      // lo
+    p[25] = A.take<int>(1);                                             // device error flag
+  };
+  void* P[26];
+  Arena sizing;
+  layout(sizing, P);
+  if (!h->reserve(sizing.off + 256))
+    return h->fail(GBR_ERR_NOMEM, "cannot allocate %.2f GB of device workspace", (sizing.off + 256) / 1e9);
+  Arena A{h->ws, 0};
+  layout(A, P);
+
+  int launches = 0;
+  cudaError_t e;
+  if (h->timing) cudaEventRecord(h->ev[0], st);
+  // ---- stage inputs ----
+  const void* d_ref = ref_dev ? ref_xyz : P[0];
+  const void* d_tgt = tgt_xyz ? (tgt_dev ? tgt_xyz : P[1]) : nullptr;
+  if (!ref_dev) cudaMemcpyAsync(P[0], ref_xyz, esz * 3 * (size_t)N * n_ref, cudaMemcpyDefault, st);
+  if (tgt_xyz && !tgt_dev) cudaMemcpyAsync(P[1], tgt_xyz, esz * 3 * (size_t)N * n_tgt, cudaMemcpyDefault, st);
+  double* d_w = tgt_mass ? (double*)P[2] : nullptr;
+  double* d_wref = nullptr;
+  if (tgt_mass) {
+    cudaMemcpyAsync(d_w, w_h.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st);
+    if (!wref_h.empty()) {
+      d_wref = (double*)P[3];
+      cudaMemcpyAsync(d_wref, wref_h.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st);
+    }
+  }
+  cudaMemsetAsync(P[21], 0, sizeof(unsigned long long), st);
+  cudaMemsetAsync(P[25], 0, sizeof(int), st);
+
+  OutMap map{};
+  map.out = out_dev ? out : (float*)P[22];
+  map.n_ref = n_ref;
+  map.tgt0 = tgt0;
+  map.n_tgt = n_tgt;
+  map.tri = (out_kind == GBR_TRI);
+  map.row_begin = row_begin;
+  map.row_end = row_end;
+  map.base = (map.tri && row_begin < n_ref - 1) ? tri_index(n_ref, row_begin, row_begin + 1) : 0;
+
+  PrepArgs pa{};
+  pa.dtype_f64 = (dtype == GBR_F64);
+  pa.ref = d_ref;
+  pa.tgt = d_tgt;
+  pa.n_ref = n_ref;
+  pa.F = F;
+  pa.N = N;
+  pa.Np = Np;
+  pa.nofit = nofit;
+  pa.cmass_tgt = d_w;
+  pa.cmass_ref = d_wref ? d_wref : d_w;
+  pa.w = d_w;
+  pa.Wsum = Wsum;
+  pa.tau = h->tau;
+  pa.max_refs = Kmax;
+  pa.cen = (double*)P[4];
+  pa.fsel = (int64_t*)P[5];
+  pa.dmax = (float*)P[6];
+  pa.dist = (float*)P[7];
+  pa.assign = (int*)P[8];
+  pa.refs = (double*)P[9];
+  pa.swr = (float*)P[10];
+  pa.Eref = (double*)P[11];
+  pa.rot = nullptr;
+  pa.plane = (float*)P[12];
+  pa.pmax_bits = (unsigned*)P[13];
+
+  ExactLaunch ex{};
+  ex.dtype_f64 = pa.dtype_f64;
+  ex.ref = d_ref;
+  ex.tgt = d_tgt;
+  ex.n_ref = n_ref;
+  ex.N = N;
+  ex.cen = pa.cen;
+  ex.w = d_w;
+  ex.Wsum = Wsum;
+  ex.nofit = nofit;
+  ex.tgt0 = tgt0;
+  ex.map = map;
+
+  int K = 1;
+  unsigned long long nflag = 0;
+  if (!need_planes) {
+    // FP64 checking mode: centres only, then every pair directly.
+    PrepArgs c = pa;
+    c.centroid_only = 1;
+    PrepOut po;
+    if ((e = run_prep(c, po, st)) != cudaSuccess) return h->cuda_fail(e, "prep");
+    launches += po.launches;
+    if (h->timing) cudaEventRecord(h->ev[1], st);
+    if (h->timing) cudaEventRecord(h->ev[2], st);
+    ex.list = nullptr;
+    ex.count = n_out;
+    if ((e = run_exact(ex, st)) != cudaSuccess) return h->cuda_fail(e, "exact kernel");
+    ++launches;
+  } else {
+    PrepOut po;
+    if ((e = run_prep(pa, po, st)) != cudaSuccess) return h->cuda_fail(e, "prep");
+    launches += po.launches;
+    K = po.K;
+    float scale = 1.0f;
+    if (tc) {
+      unsigned bits = 0;
+      cudaMemcpyAsync(&bits, pa.pmax_bits, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return h->cuda_fail(e, "prep sync");
+      float pmax;
+      std::memcpy(&pmax, &bits, sizeof pmax);
+      // Largest power of two keeping max |p| * scale <= 2^14 (FP16 max 65504).
+      int ex2 = 0;
+      if (pmax > 0.0f && std::isfinite(pmax)) std::frexp(pmax, &ex2);
+      scale = std::ldexp(1.0f, 14 - ex2);
+      if ((e = run_split_f16(pa.plane, F, Np, scale, P[23], P[24], st)) != cudaSuccess)
+        return h->cuda_fail(e, "split");
+      ++launches;
+    }
+    FrameTerms terms{};
+    terms.assign = pa.assign;
+    terms.nrm = (float*)P[14];
+    terms.P = (float*)P[15];
+    terms.trP = (float*)P[16];
+    terms.S = (float*)P[17];
+    terms.SA = (float*)P[18];
+    terms.SSd = (float*)P[19];
+    terms.K = K;
+    terms.W = (float)Wsum;
+    terms.tol = (float)h->tol;
+    terms.gemm_coef = tc ? 2.4e-7f : 1.2e-7f;
+    terms.epi_coef = 8e-7f;
+    terms.sqrtN = std::sqrt((float)N);
+    terms.nofit = nofit;
+    if ((e = run_terms(pa.plane, F, Np, N, pa.swr, K, (float*)terms.nrm, (float*)terms.P, (float*)terms.trP,
+                       pa.refs, d_w, (float*)terms.S, (float*)terms.SA, (float*)terms.SSd, st)) != cudaSuccess)
+      return h->cuda_fail(e, "frame terms");
+    launches += 2;
+    FlagList fl{(int2*)P[20], (unsigned long long*)P[21], flag_cap};
+    if (h->timing) cudaEventRecord(h->ev[1], st);
+    if (tc) {
+      TcLaunch L{};
+      L.hi = P[23];
+      L.lo = P[24];
+      L.F = F;
+      L.Np = Np;
+      L.N = N;
+      L.tgt0 = tgt0;
+      L.inv_scale2 = 1.0f / (scale * scale);
+      L.terms = terms;
+      L.map = map;
+      L.flags = fl;
+      L.tiles = make_tiles(map, 32, 32);
+      L.dev_error = (int*)P[25];
+      L.num_sms = h->num_sms;
+      if ((e = run_pairs_tc(L, st)) != cudaSuccess) return h->cuda_fail(e, "tensor-core pair kernel");
+    } else {
+      PairLaunch L{};
+      L.plane = pa.plane;
+      L.Np = Np;
+      L.N = N;
+      L.tgt0 = tgt0;
+      L.terms = terms;
+      L.map = map;
+      L.flags = fl;
+      L.tiles = make_tiles(map, 64, 64);
+      if ((e = run_pairs_fp32(L, st)) != cudaSuccess) return h->cuda_fail(e, "fp32 pair kernel");
+    }
+    ++launches;
+    if (h->timing) cudaEventRecord(h->ev[2], st);
+    cudaMemcpyAsync(&nflag, P[21], sizeof nflag, cudaMemcpyDeviceToHost, st);
+    int derr = 0;
+    cudaMemcpyAsync(&derr, P[25], sizeof derr, cudaMemcpyDeviceToHost, st);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return h->cuda_fail(e, "pair kernel");
+    if (derr != 0)
+      return h->fail(GBR_ERR_DEVICE, "pair kernel reported device error %d (bounded wait expired)", derr);
+    if (nflag > 0) {
+      if (nflag <= flag_cap) {
+        ex.list = (const int2*)P[20];
+        ex.count = (int64_t)nflag;
+      } else {
+        ex.list = nullptr;  // too many: recompute everything exactly
+        ex.count = n_out;
+      }
+      if ((e = run_exact(ex, st)) != cudaSuccess) return h->cuda_fail(e, "fix-up kernel");
+      ++launches;
+    }
+  }
+  if (h->timing) cudaEventRecord(h->ev[3], st);
+  if (!out_dev) cudaMemcpyAsync(out, map.out, sizeof(float) * n_out, cudaMemcpyDefault, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return h->cuda_fail(e, "call");
+  h->stats.pairs = n_out;
+  h->stats.pairs_fixed = (int64_t)std::min<unsigned long long>(nflag, (unsigned long long)n_out);
+  h->stats.n_refs = K;
+  h->stats.precision = precision;
+  h->stats.kernel_launches = launches;
+  if (h->timing) {
+    float a = 0, b = 0, c = 0;
+    cudaEventElapsedTime(&a, h->ev[0], h->ev[1]);
+    cudaEventElapsedTime(&b, h->ev[1], h->ev[2]);
+    cudaEventElapsedTime(&c, h->ev[2], h->ev[3]);
+    h->stats.ms_prep = a;
+    h->stats.ms_pairs = b;
+    h->stats.ms_fixup = c;
+  }
+  h->stats.ms_total =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+  return GBR_OK;
+}
+
+int gbr_allpairs_batched(gbr_handle* h, int32_t n_traj, const float* const* xyz, const int64_t* n_frames,
+                         const int32_t* n_atoms, const double* const* mass, int mode, int precision,
+                         float* const* out) {
+  if (!h) return GBR_ERR_ARG;
+  if (n_traj < 0 || (n_traj > 0 && (!xyz || !n_frames || !n_atoms || !out)))
+    return h->fail(GBR_ERR_ARG, "batched: null array argument");
+  gbr_stats total{};
+  total.precision = precision;
+  const auto t0 = std::chrono::steady_clock::now();
+  for (int32_t t = 0; t < n_traj; ++t) {
+    const double* m = mass ? mass[t] : nullptr;
+    const int rc = gbr_allpairs(h, xyz[t], nullptr, GBR_F32, n_frames[t], n_frames[t], n_atoms[t], m, m, mode,
+                                GBR_TRI, precision, out[t], 0, -1);
+    if (rc != GBR_OK) {
+      std::string msg = "trajectory " + std::to_string(t) + ": " + h->err;
+      h->err = msg;
+      return rc;
+    }
+    total.pairs += h->stats.pairs;
+    total.pairs_fixed += h->stats.pairs_fixed;
+    total.n_refs = std::max(total.n_refs, h->stats.n_refs);
+    total.kernel_launches += h->stats.kernel_launches;
+    total.ms_prep += h->stats.ms_prep;
+    total.ms_pairs += h->stats.ms_pairs;
+    total.ms_fixup += h->stats.ms_fixup;
+  }
+  total.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  h->stats = total;
+  return GBR_OK;
+}
+
+int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t n_atom, const double* mass,
+                      const float* g, float* grad_xyz, float* rmsd_out) {
+  if (!h) return GBR_ERR_ARG;
+  (void)xyz; (void)n_frame; (void)n_atom; (void)mass; (void)g; (void)grad_xyz; (void)rmsd_out;
+  return h->fail(GBR_ERR_UNSUPPORTED, "backward not built yet");
+}
+
+}  // extern "C"

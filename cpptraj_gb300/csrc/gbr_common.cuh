@@ -1,0 +1,379 @@
+// gbr_common.cuh -- shared device code of libgbrmsd: reductions, the FP64
+// per-frame superposition used for pre-alignment, and the FP32 pair epilogue.
+//
+// Numerical scheme (why the pair kernels can run in FP32 / split FP16).
+// cpptraj computes, per pair, RMSD^2 = 2*(E0 - lambda_max)/W with E0 and the
+// 3x3 covariance accumulated in FP64 (src/Frame.cpp:1184-1268).  For similar
+// frames E0 and lambda_max are ~W*Rg^2 while E0-lambda is ~W*RMSD^2, so the
+// subtraction cancels 4-6 digits and FP32 accumulation of the raw covariance
+// cannot reach 1e-4 Angstrom.  Instead every frame is first superposed (in
+// FP64, exact rotation) onto its nearest of K reference structures r_k, which
+// leaves RMSD unchanged, and split as x'_f = r_{a(f)} + d_f with d_f small.
+// For a pair (ref i, target j), a = a(i), b = a(j):
+//     M = sum w x'_j x'_i^T = S_ba + P_ja + P_ib^T + D_ji
+// with S_ba = sum w r_b r_a^T, P_fc = sum w d_f r_c^T (per frame and
+// reference) and D_ji = sum w d_j d_i^T (the only per-pair contraction, on
+// small numbers).  The quaternion key matrix enters through
+// G = E0*I - K(M), whose smallest eigenvalue is W*RMSD^2/2.  Its (0,0) entry
+//     G00 = 1/2 sum w |x'_i - x'_j|^2
+//         = 1/2 (SSd_ab + n_i + n_j) + (trP_ia - trP_ib) - (trP_ja - trP_jb) - tr D_ji
+// is assembled from small terms, so the smallest eigenvalue can be found in
+// FP32 without cancellation: a Schur-complement (secular equation) iteration
+// on G around q = (1, v), or, when the pair's relative rotation is large,
+// QCP (Theobald 2005; Liu, Agrafiotis & Theobald 2010) on K(M) for the
+// eigenvector followed by the Rayleigh quotient of G.  Each pair carries an
+// a-priori error bound; pairs whose bound exceeds the tolerance are listed
+// and recomputed directly in FP64 by gbr_exact.cu.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gbr {
+
+constexpr int kMaxRefs = 64;
+
+// --------------------------------------------------------------------------
+// Block reductions (blockDim.x a multiple of 32, <= 1024).
+// --------------------------------------------------------------------------
+template <int NV>
+__device__ __forceinline__ void block_sum_f64(double (&v)[NV], double* scratch /* >= 32*NV */) {
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) scratch[k * 32 + warp] = v[k];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double s = (lane < nw) ? scratch[k * 32 + lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    v[k] = s;
+  }
+  __syncthreads();
+}
+
+// --------------------------------------------------------------------------
+// FP64 QCP on a 3x3 cross-covariance A[p][q] = sum w t_p r_q (target first):
+// the largest eigenvalue lambda of the key matrix by Newton from E0, and the
+// proper rotation R (row-major) minimising sum w |R t - r|^2.  R is the
+// identity when no adjugate column of (K - lambda I) is usable.
+// --------------------------------------------------------------------------
+__device__ inline double qcp_lambda_rot(const double A[9], double E0, double R[9]) {
+  const double xx = A[0], xy = A[1], xz = A[2], yx = A[3], yy = A[4], yz = A[5], zx = A[6],
+               zy = A[7], zz = A[8];
+  const double xx2 = xx * xx, yy2 = yy * yy, zz2 = zz * zz, xy2 = xy * xy, yz2 = yz * yz,
+               xz2 = xz * xz, yx2 = yx * yx, zy2 = zy * zy, zx2 = zx * zx;
+  const double c2 = -2.0 * (xx2 + yy2 + zz2 + xy2 + yx2 + xz2 + zx2 + yz2 + zy2);
+  const double c1 = 8.0 * (xx * yz * zy + yy * zx * xz + zz * xy * yx - xx * yy * zz - yz * zx * xy -
+                           zy * yx * xz);
+  const double t1 = 2.0 * (yz * zy - yy * zz);
+  const double t2 = yy2 + zz2 - xx2 + yz2 + zy2;
+  const double t3 = xy2 + xz2 - yx2 - zx2;
+  const double pxz = xz + zx, pyz = yz + zy, pxy = xy + yx, myz = yz - zy, mxz = xz - zx,
+               mxy = xy - yx, pxx = xx + yy, mxx = xx - yy;
+  const double c0 = t3 * t3 + (t2 + t1) * (t2 - t1) +
+                    (-pxz * myz + mxy * (mxx - zz)) * (-mxz * pyz + mxy * (mxx + zz)) +
+                    (-pxz * pyz - pxy * (pxx - zz)) * (-mxz * myz - pxy * (pxx + zz)) +
+                    (pxy * pyz + pxz * (mxx + zz)) * (-mxy * myz + pxz * (pxx + zz)) +
+                    (pxy * myz + mxz * (mxx - zz)) * (-mxy * pyz + mxz * (pxx - zz));
+  double lam = E0;
+  for (int it = 0; it < 50; ++it) {
+    const double prev = lam, l2 = lam * lam, b = (l2 + c2) * lam, a = b + c1;
+    const double den = 2.0 * l2 * lam + b + a;
+    if (den == 0.0) break;
+    lam -= (a * lam + c0) / den;
+    if (fabs(lam - prev) < fabs(1e-11 * lam)) break;
+  }
+  // Eigenvector of the key matrix by the adjugate of (K - lam I): try each
+  // column until one has a usable norm.
+  const double k11 = pxx + zz - lam, k12 = myz, k13 = -mxz, k14 = mxy;
+  const double k22 = mxx - zz - lam, k23 = pxy, k24 = pxz;
+  const double k33 = yy - xx - zz - lam, k34 = pyz;
+  const double k44 = zz - pxx - lam;
+  const double K[16] = {k11, k12, k13, k14, k12, k22, k23, k24, k13, k23, k33, k34, k14, k24, k34, k44};
+  double q[4] = {1.0, 0.0, 0.0, 0.0};
+  double best = 0.0;
+  const double scale = fabs(E0) > 0.0 ? fabs(E0) : 1.0;
+  for (int col = 0; col < 4; ++col) {
+    // cofactors C[r][col] for r = 0..3 of the 4x4 matrix K
+    double c[4];
+    for (int r = 0; r < 4; ++r) {
+      int rr[3], cc[3], nr = 0, nc = 0;
+      for (int k = 0; k < 4; ++k) {
+        if (k != r) rr[nr++] = k;
+        if (k != col) cc[nc++] = k;
+      }
+      const double m00 = K[rr[0] * 4 + cc[0]], m01 = K[rr[0] * 4 + cc[1]], m02 = K[rr[0] * 4 + cc[2]];
+      const double m10 = K[rr[1] * 4 + cc[0]], m11 = K[rr[1] * 4 + cc[1]], m12 = K[rr[1] * 4 + cc[2]];
+      const double m20 = K[rr[2] * 4 + cc[0]], m21 = K[rr[2] * 4 + cc[1]], m22 = K[rr[2] * 4 + cc[2]];
+      const double det = m00 * (m11 * m22 - m12 * m21) - m01 * (m10 * m22 - m12 * m20) +
+                         m02 * (m10 * m21 - m11 * m20);
+      c[r] = ((r + col) & 1) ? -det : det;
+    }
+    const double n2 = c[0] * c[0] + c[1] * c[1] + c[2] * c[2] + c[3] * c[3];
+    if (n2 > best) {
+      best = n2;
+      q[0] = c[0]; q[1] = c[1]; q[2] = c[2]; q[3] = c[3];
+    }
+    if (n2 > 1e-12 * scale * scale * scale * scale * scale * scale) break;
+  }
+  if (!(best > 0.0)) { q[0] = 1.0; q[1] = q[2] = q[3] = 0.0; }
+  const double inv = 1.0 / sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  const double a0 = q[0] * inv, a1 = q[1] * inv, a2 = q[2] * inv, a3 = q[3] * inv;
+  // Rotation of the unit quaternion, row-major, oriented so that R * t best
+  // matches r (the transpose of the matrix QCP reports for this covariance).
+  const double aa = a0 * a0, bb = a1 * a1, cc2 = a2 * a2, dd = a3 * a3;
+  R[0] = aa + bb - cc2 - dd;
+  R[3] = 2.0 * (a1 * a2 + a0 * a3);
+  R[6] = 2.0 * (a3 * a1 - a0 * a2);
+  R[1] = 2.0 * (a1 * a2 - a0 * a3);
+  R[4] = aa - bb + cc2 - dd;
+  R[7] = 2.0 * (a2 * a3 + a0 * a1);
+  R[2] = 2.0 * (a3 * a1 + a0 * a2);
+  R[5] = 2.0 * (a2 * a3 - a0 * a1);
+  R[8] = aa - bb - cc2 + dd;
+  return lam;
+}
+
+// --------------------------------------------------------------------------
+// Per-pair data and the FP32 epilogue.
+// --------------------------------------------------------------------------
+struct FrameTerms {
+  const int* assign;  // [F] reference index of each set frame
+  const float* nrm;   // [F] n_f = sum |p_f|^2  (p = sqrt(w) d)
+  const float* P;     // [F][K][9] P_fc[p][q] = sum p_f[p] * (sqrt(w) r_c)[q]
+  const float* trP;   // [F][K]
+  const float* S;     // [K][K][9] S_ba[p][q] = sum w r_b[p] r_a[q], index (b*K + a)
+  const float* SA;    // [K][K][3] antisymmetric combos of S_ba (yz-zy, zx-xz, xy-yx)
+  const float* SSd;   // [K][K] sum w |r_a - r_b|^2
+  int K;
+  float W;            // total weight
+  float tol;          // per-pair tolerance (Angstrom)
+  float gemm_coef;    // contraction error coefficient (times sqrt(N)*sqrt(n_i n_j))
+  float epi_coef;     // epilogue rounding coefficient
+  float sqrtN;
+  int nofit;
+};
+
+// 3x3 symmetric solve by cofactors; returns det.
+__device__ __forceinline__ float solve_sym3(float a00, float a01, float a02, float a11, float a12,
+                                            float a22, float b0, float b1, float b2, float& x0,
+                                            float& x1, float& x2, float& m2) {
+  const float c00 = a11 * a22 - a12 * a12;
+  const float c01 = a02 * a12 - a01 * a22;
+  const float c02 = a01 * a12 - a02 * a11;
+  const float c11 = a00 * a22 - a02 * a02;
+  const float c12 = a01 * a02 - a00 * a12;
+  const float c22 = a00 * a11 - a01 * a01;
+  const float det = a00 * c00 + a01 * c01 + a02 * c02;
+  const float id = 1.0f / det;
+  x0 = (c00 * b0 + c01 * b1 + c02 * b2) * id;
+  x1 = (c01 * b0 + c11 * b1 + c12 * b2) * id;
+  x2 = (c02 * b0 + c12 * b1 + c22 * b2) * id;
+  m2 = c22;
+  return det;
+}
+
+// FP32 QCP eigenvector of the key matrix of M (scaled by 1/E0).
+__device__ inline void qcp_vec_f32(const float M[9], float E0, float q[4]) {
+  const float s = 1.0f / E0;
+  const float xx = M[0] * s, xy = M[1] * s, xz = M[2] * s, yx = M[3] * s, yy = M[4] * s,
+              yz = M[5] * s, zx = M[6] * s, zy = M[7] * s, zz = M[8] * s;
+  const float xx2 = xx * xx, yy2 = yy * yy, zz2 = zz * zz, xy2 = xy * xy, yz2 = yz * yz,
+              xz2 = xz * xz, yx2 = yx * yx, zy2 = zy * zy, zx2 = zx * zx;
+  const float c2 = -2.0f * (xx2 + yy2 + zz2 + xy2 + yx2 + xz2 + zx2 + yz2 + zy2);
+  const float c1 = 8.0f * (xx * yz * zy + yy * zx * xz + zz * xy * yx - xx * yy * zz -
+                           yz * zx * xy - zy * yx * xz);
+  const float t1 = 2.0f * (yz * zy - yy * zz);
+  const float t2 = yy2 + zz2 - xx2 + yz2 + zy2;
+  const float t3 = xy2 + xz2 - yx2 - zx2;
+  const float pxz = xz + zx, pyz = yz + zy, pxy = xy + yx, myz = yz - zy, mxz = xz - zx,
+              mxy = xy - yx, pxx = xx + yy, mxx = xx - yy;
+  const float c0 = t3 * t3 + (t2 + t1) * (t2 - t1) +
+                   (-pxz * myz + mxy * (mxx - zz)) * (-mxz * pyz + mxy * (mxx + zz)) +
+                   (-pxz * pyz - pxy * (pxx - zz)) * (-mxz * myz - pxy * (pxx + zz)) +
+                   (pxy * pyz + pxz * (mxx + zz)) * (-mxy * myz + pxz * (pxx + zz)) +
+                   (pxy * myz + mxz * (mxx - zz)) * (-mxy * pyz + mxz * (pxx - zz));
+  float lam = 1.0f;
+  for (int it = 0; it < 40; ++it) {
+    const float l2 = lam * lam, b = (l2 + c2) * lam, a = b + c1;
+    const float den = 2.0f * l2 * lam + b + a;
+    if (den == 0.0f) break;
+    const float dl = (a * lam + c0) / den;
+    lam -= dl;
+    if (fabsf(dl) <= 1e-7f * fabsf(lam)) break;
+  }
+  const float k11 = pxx + zz - lam, k12 = myz, k13 = -mxz, k14 = mxy;
+  const float k22 = mxx - zz - lam, k23 = pxy, k24 = pxz;
+  const float k33 = yy - xx - zz - lam, k34 = pyz;
+  const float k44 = zz - pxx - lam;
+  // Adjugate columns, largest norm wins (QCP's fallback order, all four tried).
+  const float a3344 = k33 * k44 - k34 * k34, a3244 = k23 * k44 - k24 * k34,
+              a3243 = k23 * k34 - k24 * k33, a3143 = k13 * k34 - k14 * k33,
+              a3144 = k13 * k44 - k14 * k34, a3142 = k13 * k24 - k14 * k23;
+  float best[4], bn;
+  best[0] = k22 * a3344 - k23 * a3244 + k24 * a3243;
+  best[1] = -k12 * a3344 + k23 * a3144 - k24 * a3143;
+  best[2] = k12 * a3244 - k22 * a3144 + k24 * a3142;
+  best[3] = -k12 * a3243 + k22 * a3143 - k23 * a3142;
+  bn = best[0] * best[0] + best[1] * best[1] + best[2] * best[2] + best[3] * best[3];
+  {
+    float c[4];
+    c[0] = k12 * a3344 - k13 * a3244 + k14 * a3243;
+    c[1] = -k11 * a3344 + k13 * a3144 - k14 * a3143;
+    c[2] = k11 * a3244 - k12 * a3144 + k14 * a3142;
+    c[3] = -k11 * a3243 + k12 * a3143 - k13 * a3142;
+    const float n = c[0] * c[0] + c[1] * c[1] + c[2] * c[2] + c[3] * c[3];
+    if (n > bn) { bn = n; best[0] = c[0]; best[1] = c[1]; best[2] = c[2]; best[3] = c[3]; }
+  }
+  {
+    const float a1324 = k13 * k24 - k14 * k23, a1224 = k12 * k24 - k14 * k22,
+                a1223 = k12 * k23 - k13 * k22, a1124 = k11 * k24 - k14 * k12,
+                a1123 = k11 * k23 - k13 * k12, a1122 = k11 * k22 - k12 * k12;
+    float c[4];
+    c[0] = k24 * a1324 - k34 * a1224 + k44 * a1223;
+    c[1] = -k14 * a1324 + k34 * a1124 - k44 * a1123;
+    c[2] = k14 * a1224 - k24 * a1124 + k44 * a1122;
+    c[3] = -k14 * a1223 + k24 * a1123 - k34 * a1122;
+    float n = c[0] * c[0] + c[1] * c[1] + c[2] * c[2] + c[3] * c[3];
+    if (n > bn) { bn = n; best[0] = c[0]; best[1] = c[1]; best[2] = c[2]; best[3] = c[3]; }
+    c[0] = k23 * a1324 - k33 * a1224 + k34 * a1223;
+    c[1] = -k13 * a1324 + k33 * a1124 - k34 * a1123;
+    c[2] = k13 * a1224 - k23 * a1124 + k34 * a1122;
+    c[3] = -k13 * a1223 + k23 * a1123 - k33 * a1122;
+    n = c[0] * c[0] + c[1] * c[1] + c[2] * c[2] + c[3] * c[3];
+    if (n > bn) { bn = n; best[0] = c[0]; best[1] = c[1]; best[2] = c[2]; best[3] = c[3]; }
+  }
+  if (!(bn > 0.0f)) { best[0] = 1.0f; best[1] = best[2] = best[3] = 0.0f; }
+  q[0] = best[0]; q[1] = best[1]; q[2] = best[2]; q[3] = best[3];
+}
+
+// The pair epilogue.  D[pj*3+pi] = sum p_j[pj] p_i[pi] (target j first).
+// Returns the RMSD (Angstrom, >= 0); sets *flag when the error bound exceeds
+// the tolerance and the pair must be recomputed in FP64.
+static __device__ __noinline__ float pair_epilogue(const float D[9], int64_t i, int64_t j, const FrameTerms& t,
+                                      bool* flag) {
+  const int K = t.K;
+  const int a = (K > 1) ? __ldg(t.assign + i) : 0;
+  const int b = (K > 1) ? __ldg(t.assign + j) : 0;
+  const float ni = __ldg(t.nrm + i), nj = __ldg(t.nrm + j);
+  const float* Pja = t.P + ((size_t)j * K + a) * 9;
+  const float* Pib = t.P + ((size_t)i * K + b) * 9;
+  const int ab = b * K + a;
+  const float trD = D[0] + D[4] + D[8];
+  float G00 = 0.5f * (ni + nj) - trD;
+  if (a != b) {
+    G00 += 0.5f * __ldg(t.SSd + a * K + b) + (__ldg(t.trP + i * K + a) - __ldg(t.trP + i * K + b)) -
+           (__ldg(t.trP + j * K + a) - __ldg(t.trP + j * K + b));
+  }
+  const float W = t.W;
+  const float gem = t.gemm_coef * t.sqrtN * sqrtf(fmaxf(ni, 0.0f) * fmaxf(nj, 0.0f));
+  if (t.nofit) {
+    // RMSD_NoFit: sum w |x_i - x_j|^2 / W = 2*G00/W (no rotation, no centring).
+    const float msd = fmaxf(2.0f * G00 / W, 0.0f);
+    const float r = sqrtf(msd);
+    float err = 2.0f * gem + t.epi_coef * (fabsf(G00) + ni + nj);
+    *flag = err > t.tol * W * fmaxf(r, 1e-3f);
+    return r;
+  }
+  float X[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) X[k] = __ldg(Pja + k) + D[k];
+  X[0] += __ldg(Pib + 0); X[1] += __ldg(Pib + 3); X[2] += __ldg(Pib + 6);
+  X[3] += __ldg(Pib + 1); X[4] += __ldg(Pib + 4); X[5] += __ldg(Pib + 7);
+  X[6] += __ldg(Pib + 2); X[7] += __ldg(Pib + 5); X[8] += __ldg(Pib + 8);
+  const float* S = t.S + (size_t)ab * 9;
+  float M[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) M[k] = __ldg(S + k) + X[k];
+  // g = G[0][1..3] = -(antisymmetric combos of M), from the small parts.
+  const float g1 = -(X[5] - X[7] + __ldg(t.SA + ab * 3 + 0));
+  const float g2 = -(X[6] - X[2] + __ldg(t.SA + ab * 3 + 1));
+  const float g3 = -(X[1] - X[3] + __ldg(t.SA + ab * 3 + 2));
+  const float G11 = G00 + 2.0f * (M[4] + M[8]);
+  const float G22 = G00 + 2.0f * (M[0] + M[8]);
+  const float G33 = G00 + 2.0f * (M[0] + M[4]);
+  const float G12 = -(M[1] + M[3]);
+  const float G13 = -(M[6] + M[2]);
+  const float G23 = -(M[5] + M[7]);
+  // Fast path: secular iteration mu = G00 + g.v, v = -(Gs - mu I)^-1 g.
+  float mu = G00, v1 = 0.f, v2 = 0.f, v3 = 0.f, det = 0.f, m2 = 0.f;
+  bool conv = false;
+#pragma unroll 1
+  for (int it = 0; it < 5; ++it) {
+    det = solve_sym3(G11 - mu, G12, G13, G22 - mu, G23, G33 - mu, -g1, -g2, -g3, v1, v2, v3, m2);
+    const float mn = G00 + g1 * v1 + g2 * v2 + g3 * v3;
+    conv = fabsf(mn - mu) <= 1e-5f * fabsf(mn) + 1e-30f;
+    mu = mn;
+    if (conv) break;
+  }
+  const float a00 = G11 - mu;
+  const bool pd = (a00 > 0.0f) && ((G11 - mu) * (G22 - mu) - G12 * G12 > 0.0f) && (det > 0.0f);
+  float q0, q1, q2, q3;
+  if (conv && pd && (v1 * v1 + v2 * v2 + v3 * v3) < 0.25f) {
+    q0 = 1.0f; q1 = v1; q2 = v2; q3 = v3;
+  } else {
+    float q[4];
+    qcp_vec_f32(M, G00 + M[0] + M[4] + M[8], q);
+    q0 = q[0]; q1 = q[1]; q2 = q[2]; q3 = q[3];
+  }
+  const float qq = q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3;
+  const float t00 = q0 * q0 * G00, t01 = 2.f * q0 * (q1 * g1 + q2 * g2 + q3 * g3);
+  const float t11 = q1 * q1 * G11 + q2 * q2 * G22 + q3 * q3 * G33;
+  const float t12 = 2.f * (q1 * q2 * G12 + q1 * q3 * G13 + q2 * q3 * G23);
+  const float rq = (t00 + t01 + t11 + t12) / qq;
+  const float mag = (fabsf(t00) + 2.f * fabsf(q0) * (fabsf(q1 * g1) + fabsf(q2 * g2) + fabsf(q3 * g3)) +
+                     fabsf(t11) + 2.f * (fabsf(q1 * q2 * G12) + fabsf(q1 * q3 * G13) + fabsf(q2 * q3 * G23))) /
+                    qq;
+  const float r = sqrtf(fmaxf(2.0f * rq / W, 0.0f));
+  const float err = t.epi_coef * mag + 3.0f * gem;
+  *flag = !(err <= t.tol * W * fmaxf(r, 1e-3f));
+  return r;
+}
+
+__host__ __device__ inline int64_t tri_index(int64_t n, int64_t i, int64_t j) {
+  return n * i - ((i + 1) * i) / 2 + j - i - 1;
+}
+
+// Where each pair's value goes, and which pairs exist.
+struct OutMap {
+  float* out;
+  int64_t n_ref;      // reference frames (set frames [0, n_ref))
+  int64_t tgt0;       // set index of target frame 0 (0 for TRI, n_ref for FULL)
+  int64_t n_tgt;
+  int tri;            // 1 = triangle
+  int64_t row_begin;  // TRI: ref rows; FULL: target rows
+  int64_t row_end;
+  int64_t base;       // TRI: tri_index of the first element of row_begin
+};
+
+// i: reference frame (0..n_ref), jt: target frame (0..n_tgt).  Returns -1 if
+// the pair is not part of this call's output.
+__device__ __forceinline__ int64_t out_index(const OutMap& m, int64_t i, int64_t jt) {
+  if (m.tri) {
+    if (!(jt > i) || i < m.row_begin || i >= m.row_end || jt >= m.n_tgt) return -1;
+    return tri_index(m.n_ref, i, jt) - m.base;
+  }
+  if (i >= m.n_ref || jt < m.row_begin || jt >= m.row_end) return -1;
+  return (jt - m.row_begin) * m.n_ref + i;
+}
+
+struct FlagList {
+  int2* pairs;               // (ref frame, target frame) of flagged pairs
+  unsigned long long* count; // atomically incremented
+  unsigned long long cap;
+};
+
+__device__ __forceinline__ void flag_pair(const FlagList& fl, int64_t i, int64_t jt) {
+  const unsigned long long k = atomicAdd(fl.count, 1ull);
+  if (k < fl.cap) fl.pairs[k] = make_int2((int)i, (int)jt);
+}
+
+}  // namespace gbr

@@ -1,0 +1,112 @@
+// gbr_internal.h -- host-side interfaces between the C-ABI layer (gbr_capi.cu)
+// and the kernel files.  Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "gbr_common.cuh"
+
+namespace gbr {
+
+struct PrepArgs {
+  int dtype_f64;
+  const void* ref;  // device, [n_ref][N][3]
+  const void* tgt;  // device or nullptr (TRI)
+  int64_t n_ref;
+  int64_t F;        // set frames (n_ref, or n_ref + n_tgt)
+  int N, Np;
+  int nofit;
+  int centroid_only;        // only compute centres (FP64 checking mode)
+  const double* cmass_ref;  // centring masses of reference frames (nullptr = geometric)
+  const double* cmass_tgt;  // centring masses of target frames
+  const double* w;          // weights (target masses) or nullptr
+  double Wsum;
+  double tau;
+  int max_refs;
+  // workspace
+  double* cen;     // [F][3]
+  int64_t* fsel;   // [1]
+  float* dmax;     // [1]
+  float* dist;     // [F]
+  int* assign;     // [F]
+  double* refs;    // [max_refs][N][3]
+  float* swr;      // [max_refs][N][3]
+  double* Eref;    // [max_refs]
+  double* rot;     // [F][9] or nullptr
+  float* plane;    // [F][3][Np]
+  unsigned* pmax_bits;
+};
+
+struct PrepOut {
+  int K = 1;
+  int launches = 0;
+};
+
+cudaError_t run_prep(const PrepArgs& A, PrepOut& o, cudaStream_t st);
+cudaError_t run_split_f16(float* plane, int64_t F, int Np, float scale, void* hi, void* lo, cudaStream_t st);
+cudaError_t run_terms(const float* plane, int64_t F, int Np, int N, const float* swr, int K, float* nrm,
+                      float* P, float* trP, const double* refs, const double* w, float* S, float* SA,
+                      float* SSd, cudaStream_t st);
+
+// Tiles of the pair space: rows = reference frames, cols = target frames.
+struct TileSpace {
+  int tri;          // upper-triangle tiles only
+  int64_t i0, j0;   // first reference / target frame covered
+  int64_t ni, nj;   // frames covered
+  int64_t ti, tj;   // tiles along i / j
+  int64_t count;    // tiles launched
+};
+
+TileSpace make_tiles(const OutMap& m, int bm, int bn);
+
+struct PairLaunch {
+  const float* plane;  // FP32 plane [F][3][Np]
+  int Np, N;
+  int64_t tgt0;        // set index of target frame 0
+  FrameTerms terms;
+  OutMap map;
+  FlagList flags;
+  TileSpace tiles;
+};
+
+cudaError_t run_pairs_fp32(const PairLaunch& L, cudaStream_t st);
+
+// Tensor-core contraction (tcgen05).  hi/lo: FP16 planes [F][4][Np].
+struct TcLaunch {
+  const void* hi;
+  const void* lo;
+  int64_t F;
+  int Np, N;
+  int64_t tgt0;
+  float inv_scale2;  // 1 / scale^2
+  FrameTerms terms;
+  OutMap map;
+  FlagList flags;
+  TileSpace tiles;
+  int* dev_error;    // set non-zero when a bounded wait gives up
+  int num_sms;
+};
+cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st);
+int tc_supported(int device);
+
+// Direct FP64 recomputation (flagged pairs or every pair).
+struct ExactLaunch {
+  int dtype_f64;
+  const void* ref;
+  const void* tgt;
+  int64_t n_ref;
+  int N;
+  const double* cen;  // [F][3] set-frame centres (zeros for no-fit)
+  const double* w;    // target masses or nullptr
+  double Wsum;
+  int nofit;
+  int64_t tgt0;
+  OutMap map;
+  const int2* list;   // pairs (i, jt) or nullptr => every pair of the map
+  int64_t count;      // pairs in list (or total pairs when list == nullptr)
+};
+cudaError_t run_exact(const ExactLaunch& L, cudaStream_t st);
+
+}  // namespace gbr

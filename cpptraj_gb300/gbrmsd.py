@@ -1,0 +1,239 @@
+"""ctypes binding of libgbrmsd.so (the C ABI declared in include/gbrmsd.h).
+
+The functions here take numpy arrays or torch tensors (host or CUDA) and call
+the library directly; no computation happens in Python.  If the shared
+library is missing the import of a function raises -- there is no CPU
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgbrmsd.so")
+
+GBR_OK = 0
+GBR_F32, GBR_F64 = 0, 1
+FIT, NOFIT = 0, 1
+TRI, FULL = 0, 1
+PREC_FP32, PREC_TC, PREC_FP64 = 0, 1, 2
+OPT_TAU, OPT_MAX_REFS, OPT_TOL, OPT_TIMING = 0, 1, 2, 3
+
+PRECISIONS = {"fp32": PREC_FP32, "tc": PREC_TC, "fp64": PREC_FP64}
+MODES = {"fit": FIT, "nofit": NOFIT}
+
+#: Every symbol include/gbrmsd.h declares.
+EXPORTED = ("gbr_create", "gbr_destroy", "gbr_last_error", "gbr_allpairs", "gbr_output_count",
+            "gbr_allpairs_batched", "gbr_rmsd_backward", "gbr_get_stats", "gbr_set_option", "gbr_set_stream")
+
+
+class GbrError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"gbrmsd error {code}: {msg}")
+        self.code = code
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("pairs", ctypes.c_int64), ("pairs_fixed", ctypes.c_int64), ("n_refs", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("kernel_launches", ctypes.c_int32),
+                ("ms_prep", ctypes.c_double), ("ms_pairs", ctypes.c_double), ("ms_fixup", ctypes.c_double),
+                ("ms_total", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load():
+    """Load libgbrmsd.so (raises if it has not been built)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} not built; run `python -m cpptraj_gb300.build`")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i64, i32, ci, cd = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int, ctypes.c_double
+        L.gbr_create.restype = vp
+        L.gbr_create.argtypes = [ci]
+        L.gbr_destroy.restype = None
+        L.gbr_destroy.argtypes = [vp]
+        L.gbr_last_error.restype = ctypes.c_char_p
+        L.gbr_last_error.argtypes = [vp]
+        L.gbr_allpairs.restype = ci
+        L.gbr_allpairs.argtypes = [vp, vp, vp, ci, i64, i64, i32, vp, vp, ci, ci, ci, vp, i64, i64]
+        L.gbr_output_count.restype = i64
+        L.gbr_output_count.argtypes = [i64, i64, ci, i64, i64]
+        L.gbr_allpairs_batched.restype = ci
+        L.gbr_allpairs_batched.argtypes = [vp, i32, vp, vp, vp, vp, ci, ci, vp]
+        L.gbr_rmsd_backward.restype = ci
+        L.gbr_rmsd_backward.argtypes = [vp, vp, i64, i32, vp, vp, vp, vp]
+        L.gbr_get_stats.restype = ci
+        L.gbr_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+        L.gbr_set_option.restype = ci
+        L.gbr_set_option.argtypes = [vp, ci, cd]
+        L.gbr_set_stream.restype = ci
+        L.gbr_set_stream.argtypes = [vp, vp]
+        _lib = L
+        return L
+
+
+def _ptr(x):
+    """Raw pointer of a numpy array / torch tensor (or None)."""
+    if x is None:
+        return None
+    if isinstance(x, np.ndarray):
+        if not x.flags.c_contiguous:
+            raise ValueError("arrays must be C-contiguous")
+        return x.ctypes.data
+    # torch tensor
+    if not x.is_contiguous():
+        raise ValueError("tensors must be contiguous")
+    return x.data_ptr()
+
+
+def _dtype_code(x):
+    dt = str(x.dtype)
+    if dt.endswith("float32"):
+        return GBR_F32
+    if dt.endswith("float64"):
+        return GBR_F64
+    raise TypeError(f"coordinates must be float32 or float64, got {dt}")
+
+
+def output_count(n_ref, n_tgt, out_kind, row_begin=0, row_end=-1):
+    return load().gbr_output_count(n_ref, n_tgt, out_kind, row_begin, row_end)
+
+
+class Handle:
+    """One gbr_handle (device memory, stream).  Not thread-safe."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        self.h = self.lib.gbr_create(device)
+        if not self.h:
+            raise GbrError(2, f"gbr_create({device}) failed (no usable CUDA device?)")
+        self.device = device
+
+    def close(self):
+        if self.h:
+            self.lib.gbr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != GBR_OK:
+            raise GbrError(rc, self.lib.gbr_last_error(self.h).decode())
+
+    def set_option(self, key, value):
+        self._check(self.lib.gbr_set_option(self.h, key, float(value)))
+
+    def set_stream(self, stream_ptr):
+        """Use a caller's cudaStream_t (an int pointer value, e.g.
+        torch.cuda.current_stream().cuda_stream); None restores the handle's own."""
+        self._check(self.lib.gbr_set_stream(self.h, stream_ptr))
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._check(self.lib.gbr_get_stats(self.h, ctypes.byref(s)))
+        return s.as_dict()
+
+    def allpairs_raw(self, ref, tgt, n_ref, n_tgt, n_atom, dtype, ref_mass, tgt_mass, mode, out_kind,
+                     precision, out, row_begin=0, row_end=-1):
+        """Direct call with raw pointers / arrays (the C ABI, unchanged)."""
+        rc = self.lib.gbr_allpairs(self.h, _ptr(ref), _ptr(tgt), dtype, n_ref, n_tgt, n_atom, _ptr(ref_mass),
+                                   _ptr(tgt_mass), mode, out_kind, precision, _ptr(out), row_begin, row_end)
+        self._check(rc)
+
+    def allpairs(self, ref, tgt=None, ref_mass=None, tgt_mass=None, mode="fit", out_kind=None,
+                 precision="fp32", out=None, row_begin=0, row_end=-1):
+        """All-pairs RMSD (rms2d semantics).  ref/tgt: [frames, atoms, 3].
+
+        Returns ``out`` (allocated like ``ref`` -- numpy or torch, same
+        device -- when not given).  TRI for one set, FULL when ``tgt`` is given.
+        """
+        n_ref, n_atom = int(ref.shape[0]), int(ref.shape[1])
+        n_tgt = int(tgt.shape[0]) if tgt is not None else n_ref
+        if out_kind is None:
+            out_kind = TRI if tgt is None else FULL
+        m = MODES[mode] if isinstance(mode, str) else mode
+        p = PRECISIONS[precision] if isinstance(precision, str) else precision
+        count = output_count(n_ref, n_tgt, out_kind, row_begin, row_end)
+        if out is None:
+            if isinstance(ref, np.ndarray):
+                out = np.zeros(count, np.float32)
+            else:
+                import torch
+                out = torch.zeros(count, dtype=torch.float32, device=ref.device)
+        if tgt_mass is not None and isinstance(tgt_mass, np.ndarray):
+            tgt_mass = np.ascontiguousarray(tgt_mass, dtype=np.float64)
+        if ref_mass is not None and isinstance(ref_mass, np.ndarray):
+            ref_mass = np.ascontiguousarray(ref_mass, dtype=np.float64)
+        self.allpairs_raw(ref, tgt, n_ref, n_tgt, n_atom, _dtype_code(ref), ref_mass, tgt_mass, m, out_kind, p,
+                          out, row_begin, row_end)
+        return out
+
+    def allpairs_batched(self, trajs, masses=None, mode="fit", precision="fp32"):
+        """trajs: list of float32 [F_t, N_t, 3] arrays; returns list of TRI outputs."""
+        n = len(trajs)
+        outs = [np.zeros(max(int(t.shape[0]) * (int(t.shape[0]) - 1) // 2, 1), np.float32) for t in trajs]
+        xyz = (ctypes.c_void_p * n)(*[_ptr(t) for t in trajs])
+        nf = (ctypes.c_int64 * n)(*[int(t.shape[0]) for t in trajs])
+        na = (ctypes.c_int32 * n)(*[int(t.shape[1]) for t in trajs])
+        ms = None
+        if masses is not None:
+            masses = [None if m is None else np.ascontiguousarray(m, np.float64) for m in masses]
+            ms = (ctypes.c_void_p * n)(*[_ptr(m) for m in masses])
+        op = (ctypes.c_void_p * n)(*[_ptr(o) for o in outs])
+        m = MODES[mode] if isinstance(mode, str) else mode
+        p = PRECISIONS[precision] if isinstance(precision, str) else precision
+        rc = self.lib.gbr_allpairs_batched(self.h, n, ctypes.cast(xyz, ctypes.c_void_p),
+                                           ctypes.cast(nf, ctypes.c_void_p), ctypes.cast(na, ctypes.c_void_p),
+                                           None if ms is None else ctypes.cast(ms, ctypes.c_void_p), m, p,
+                                           ctypes.cast(op, ctypes.c_void_p))
+        self._check(rc)
+        return [o[: int(t.shape[0]) * (int(t.shape[0]) - 1) // 2] for o, t in zip(outs, trajs)]
+
+    def backward(self, xyz, mass=None, g=None, grad=None, rmsd_out=None):
+        """dL/dxyz for L = sum_{i<j} g_ij RMSD_ij (float32 frames)."""
+        n_frame, n_atom = int(xyz.shape[0]), int(xyz.shape[1])
+        if grad is None:
+            if isinstance(xyz, np.ndarray):
+                grad = np.zeros_like(xyz)
+            else:
+                import torch
+                grad = torch.zeros_like(xyz)
+        if mass is not None and isinstance(mass, np.ndarray):
+            mass = np.ascontiguousarray(mass, dtype=np.float64)
+        rc = self.lib.gbr_rmsd_backward(self.h, _ptr(xyz), n_frame, n_atom, _ptr(mass), _ptr(g), _ptr(grad),
+                                        _ptr(rmsd_out))
+        self._check(rc)
+        return grad
+
+
+_default = {}
+
+
+def default_handle(device: int = 0) -> Handle:
+    h = _default.get(device)
+    if h is None:
+        h = _default[device] = Handle(device)
+    return h

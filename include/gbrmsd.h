@@ -1,0 +1,150 @@
+/*
+ * gbrmsd.h -- C ABI of the GB300 all-pairs best-fit RMSD library (libgbrmsd.so).
+ *
+ * This is the drop-in boundary for cpptraj's all-pairs RMSD path.  Each entry
+ * point replaces one loop of the reference:
+ *
+ *   gbr_allpairs      <- Analysis_Rms2d::Calculate_2D pair loop for RMS_FIT and
+ *                        RMS_NOFIT (src/Analysis_Rms2d.cpp:247-290), and the
+ *                        Metric_RMS branch of MetricArray::calcFrameDistances
+ *                        (src/Cluster/MetricArray.cpp:770-800).  The per-pair
+ *                        arithmetic it reproduces is Frame::RMSD_CenteredRef
+ *                        (src/Frame.cpp:1137-1273), Frame::RMSD
+ *                        (src/Frame.cpp:1102-1109) and Frame::RMSD_NoFit
+ *                        (src/Frame.cpp:1279-1307).
+ *   gbr_allpairs_batched <- the same loop run over many independent COORDS
+ *                        sets, one rms2d per set.
+ *   gbr_rmsd_backward <- no reference counterpart (cpptraj has no gradient of
+ *                        RMSD); dL/dx for L = sum_{i<j} g_ij RMSD_ij.
+ *
+ * Conventions (all from the reference):
+ *   - Coordinates are frame-major, atom-major xyz: frame f, atom a, component
+ *     p at xyz[(f*n_atom + a)*3 + p], i.e. what DataSet_Coords::GetFrame with
+ *     the analysis mask (src/DataSet_Coords_CRD.cpp:142-147) gathers, stored
+ *     contiguously.  dtype GBR_F32 matches COORDS sets (CompactFrameArray is
+ *     float, src/CompactFrameArray.h:75-76); GBR_F64 matches `loadcrd ... prec
+ *     double` FRAMES sets (src/Exec_LoadCrd.cpp:20-25).
+ *   - Masses: when tgt_mass is NULL every atom weighs 1 (no `mass` keyword).
+ *     Otherwise reference frames are centred with ref_mass (NULL => tgt_mass)
+ *     and every sum is weighted by tgt_mass, as in Frame::CenterOnOrigin on the
+ *     reference followed by RMSD_CenteredRef on the target.
+ *   - Rows are reference frames (nref), columns target frames (ntgt).
+ *     GBR_TRI: one set (tgt_xyz == NULL), pairs nref < ntgt, element index
+ *       n*i - (i+1)*i/2 + j - i - 1 (Matrix<T>::calcTriIndex, src/Matrix.h:110-122);
+ *       the layout of DataSet_MatrixFlt::AllocateTriangle and of
+ *       DataSet_PairwiseCache_MEM (src/DataSet_PairwiseCache_MEM.cpp:20-41).
+ *     GBR_FULL: every (nref, ntgt), index ntgt*n_ref + nref
+ *       (Matrix<T>::calcFullIndex, src/Matrix.h:94-96; DataSet_MatrixFlt::Allocate2D).
+ *   - Row ranges: TRI rows are reference frames; FULL rows are target frames
+ *     (the slow index of calcFullIndex).  `out` receives exactly the elements
+ *     of rows [row_begin, row_end) in index order, starting at out[0].  Pass
+ *     row_begin = 0, row_end = -1 for the whole matrix.
+ *   - Results are cast to float as SetElement does (src/Analysis_Rms2d.cpp:276).
+ *     A negative E0 - lambda is clamped to 0 (src/Frame.cpp:1264-1266).
+ *     Zero total mass (< 1e-14, src/Constants.h:35) is an error for the call
+ *     (the reference returns -1 for the pair and prints an error).
+ *   - Pointers may be host or device memory (detected per call).  Host
+ *     buffers are staged through the handle's device memory.
+ *   - Return value: GBR_OK (0) or an error code; gbr_last_error gives text.
+ *     No exception crosses the ABI.  One handle must not be used from two
+ *     threads at once; separate handles are independent.
+ */
+#ifndef GBRMSD_H
+#define GBRMSD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum gbr_status {
+  GBR_OK = 0,
+  GBR_ERR_ARG = 1,        /* invalid argument (sizes, null pointers, modes)   */
+  GBR_ERR_CUDA = 2,       /* CUDA runtime or launch error                     */
+  GBR_ERR_NOMEM = 3,      /* device workspace could not be allocated          */
+  GBR_ERR_ZERO_MASS = 4,  /* total mass below 1e-14                           */
+  GBR_ERR_DEVICE = 5,     /* a kernel reported a device-side error (timeout)  */
+  GBR_ERR_UNSUPPORTED = 6 /* precision/mode not available on this device      */
+};
+
+enum gbr_dtype { GBR_F32 = 0, GBR_F64 = 1 };
+enum gbr_mode { GBR_FIT = 0, GBR_NOFIT = 1 };
+enum gbr_out_kind { GBR_TRI = 0, GBR_FULL = 1 };
+enum gbr_precision {
+  GBR_PREC_FP32 = 0, /* CUDA-core FP32 contraction of pre-aligned residuals    */
+  GBR_PREC_TC = 1,   /* tcgen05 tensor cores, FP16 hi+lo split of residuals     */
+  GBR_PREC_FP64 = 2  /* every pair recomputed directly in FP64 (slow; checking) */
+};
+
+typedef struct gbr_handle gbr_handle;
+
+/* Create a handle bound to CUDA device `device`; NULL on failure. */
+gbr_handle *gbr_create(int device);
+
+/* Destroy a handle and free its device memory and streams. */
+void gbr_destroy(gbr_handle *h);
+
+/* Run this handle's work on `stream` (a cudaStream_t of the handle's device,
+ * or NULL to go back to the handle's own stream).  Calls still return only
+ * when their results are in `out`. */
+int gbr_set_stream(gbr_handle *h, void *stream);
+
+/* Last error message of this handle ("" if none).  Valid until the next call. */
+const char *gbr_last_error(const gbr_handle *h);
+
+/* All-pairs RMSD; see the conventions above. */
+int gbr_allpairs(gbr_handle *h, const void *ref_xyz, const void *tgt_xyz, int dtype,
+                 int64_t n_ref, int64_t n_tgt, int32_t n_atom,
+                 const double *ref_mass, const double *tgt_mass,
+                 int mode, int out_kind, int precision,
+                 float *out, int64_t row_begin, int64_t row_end);
+
+/* Number of output elements gbr_allpairs writes for these arguments. */
+int64_t gbr_output_count(int64_t n_ref, int64_t n_tgt, int out_kind,
+                         int64_t row_begin, int64_t row_end);
+
+/* Many independent rms2d runs (GBR_TRI, one set each) in one call.  Trajectory
+ * t has n_frames[t] frames of n_atoms[t] atoms at xyz[t] (GBR_F32), masses
+ * mass[t] (NULL, or mass == NULL, for unweighted) and writes its triangle to
+ * out[t].  All pointers of one call must be of the same kind (host or device). */
+int gbr_allpairs_batched(gbr_handle *h, int32_t n_traj, const float *const *xyz,
+                         const int64_t *n_frames, const int32_t *n_atoms,
+                         const double *const *mass, int mode, int precision,
+                         float *const *out);
+
+/* Gradient of L = sum_{i<j} g[tri(i,j)] * RMSD_ij (best fit, one set, GBR_F32)
+ * with respect to every coordinate.  g NULL means g = 1.  grad_xyz has the
+ * shape of xyz.  rmsd_out (optional, may be NULL) receives the forward TRI.
+ * Pairs with RMSD == 0 contribute no gradient. */
+int gbr_rmsd_backward(gbr_handle *h, const float *xyz, int64_t n_frame, int32_t n_atom,
+                      const double *mass, const float *g, float *grad_xyz, float *rmsd_out);
+
+/* Per-call statistics of the last gbr_allpairs / batched / backward call. */
+typedef struct gbr_stats {
+  int64_t pairs;          /* pairs computed                                      */
+  int64_t pairs_fixed;    /* pairs whose error bound sent them to the FP64 kernel */
+  int32_t n_refs;         /* pre-alignment reference structures used             */
+  int32_t precision;      /* precision actually run                              */
+  int32_t kernel_launches;/* kernels launched by the call                        */
+  double ms_prep;         /* device time of centring/alignment kernels (ms)      */
+  double ms_pairs;        /* device time of the pair contraction kernel(s) (ms)  */
+  double ms_fixup;        /* device time of the FP64 re-check kernel (ms)        */
+  double ms_total;        /* wall time of the call (ms)                          */
+} gbr_stats;
+
+int gbr_get_stats(const gbr_handle *h, gbr_stats *out);
+
+/* Tuning knobs (mostly for tests and benchmarks).  Keys:
+ *   GBR_OPT_TAU          reference-selection radius in Angstrom (default 4.0)
+ *   GBR_OPT_MAX_REFS     maximum pre-alignment references (1..64, default 32)
+ *   GBR_OPT_TOL          per-pair error target in Angstrom (default 5e-5)
+ *   GBR_OPT_TIMING       1 = record per-kernel device times in gbr_stats
+ */
+enum gbr_option { GBR_OPT_TAU = 0, GBR_OPT_MAX_REFS = 1, GBR_OPT_TOL = 2, GBR_OPT_TIMING = 3 };
+int gbr_set_option(gbr_handle *h, int key, double value);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBRMSD_H */

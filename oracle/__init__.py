@@ -89,13 +89,18 @@ def _dtype_code(x):
 
 
 def n_out(n_ref, n_tgt, out_kind, row_begin=0, row_end=None):
-    if row_end is None:
-        row_end = n_ref
+    """Elements in rows [row_begin, row_end): TRI rows are reference frames,
+    FULL rows are target frames (the slow index of the FULL layout)."""
     if out_kind == TRI:
+        if row_end is None or row_end < 0:
+            row_end = n_ref
+
         def cnt(i):
             return i * n_ref - (i * (i + 1)) // 2
         return cnt(row_end) - cnt(row_begin)
-    return (row_end - row_begin) * n_tgt
+    if row_end is None or row_end < 0:
+        row_end = n_tgt
+    return (row_end - row_begin) * n_ref
 
 
 def allpairs(ref, tgt=None, ref_mass=None, tgt_mass=None, mode=FIT, out_kind=None,
@@ -115,7 +120,7 @@ def allpairs(ref, tgt=None, ref_mass=None, tgt_mass=None, mode=FIT, out_kind=Non
     elif tgt_mass is not None:
         ref_mass = tgt_mass
     if row_end is None:
-        row_end = n_ref
+        row_end = -1
     if use_reference_code:
         out = np.zeros(n_out(n_ref, n_tgt, out_kind), np.float32)
         rc = ref_lib().ref_allpairs(_p(ref), _p(tgt), _dtype_code(ref), n_ref, n_tgt, n_atom,

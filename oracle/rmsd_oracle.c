@@ -257,7 +257,8 @@ double orc_rmsd_nofit(const double *ref, const double *tgt, int n, const double 
 /*   rows = reference frames (nref), columns = target frames (ntgt).         */
 /*   TRI  : ref set == tgt set, pairs nref < ntgt, index calcTriIndex.       */
 /*   FULL : every (nref, ntgt), index ntgt*n_ref + nref (calcFullIndex).     */
-/*   Rows [row_begin, row_end) only; out holds exactly those rows' elements. */
+/*   Row ranges: TRI rows are reference frames, FULL rows are target frames */
+/*   (the slow index); out holds exactly rows [row_begin, row_end).          */
 /* ------------------------------------------------------------------------ */
 int64_t orc_tri_index(int64_t n, int64_t i, int64_t j) {
   return n * i - ((i + 1) * i) / 2 + j - i - 1;
@@ -278,10 +279,16 @@ int orc_allpairs(const void *ref_xyz, const void *tgt_xyz, int dtype, int64_t n_
   if (n_atom < 1 || n_ref < 0 || n_tgt < 0) return 1;
   if (tgt_xyz == NULL) { tgt_xyz = ref_xyz; n_tgt = n_ref; }
   if (out_kind == ORC_TRI && n_tgt != n_ref) return 1;
-  if (row_end < 0 || row_end > n_ref) row_end = n_ref;
+  int64_t n_rows = (out_kind == ORC_TRI) ? n_ref : n_tgt;
+  if (row_end < 0 || row_end > n_rows) row_end = n_rows;
   if (row_begin < 0) row_begin = 0;
   int64_t base = 0;
   if (out_kind == ORC_TRI) base = (row_begin < n_ref - 1) ? orc_tri_index(n_ref, row_begin, row_begin + 1) : 0;
+  /* reference frames to visit: TRI restricts them, FULL restricts targets */
+  int64_t i_begin = (out_kind == ORC_TRI) ? row_begin : 0;
+  int64_t i_end = (out_kind == ORC_TRI) ? row_end : n_ref;
+  int64_t j_lo = (out_kind == ORC_TRI) ? 0 : row_begin;
+  int64_t j_hi = (out_kind == ORC_TRI) ? n_tgt : row_end;
   int err = 0;
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -293,7 +300,7 @@ int orc_allpairs(const void *ref_xyz, const void *tgt_xyz, int dtype, int64_t n_
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic)
 #endif
-    for (int64_t i = row_begin; i < row_end; ++i) {
+    for (int64_t i = i_begin; i < i_end; ++i) {
       load_frame(ref_xyz, dtype, i, n_atom, R);
       if (mode != ORC_NOFIT) {
         double c[3];
@@ -302,15 +309,15 @@ int orc_allpairs(const void *ref_xyz, const void *tgt_xyz, int dtype, int64_t n_
           R[3 * a] -= c[0]; R[3 * a + 1] -= c[1]; R[3 * a + 2] -= c[2];
         }
       }
-      int64_t j0 = (out_kind == ORC_TRI) ? i + 1 : 0;
-      for (int64_t j = j0; j < n_tgt; ++j) {
+      int64_t j0 = (out_kind == ORC_TRI) ? i + 1 : j_lo;
+      for (int64_t j = j0; j < j_hi; ++j) {
         load_frame(tgt_xyz, dtype, j, n_atom, T);
         double r;
         if (mode == ORC_FIT) r = orc_rmsd_centered_ref(R, T, n_atom, tgt_mass);
         else if (mode == ORC_QCP) r = orc_rmsd_qcp(R, T, n_atom, tgt_mass);
         else r = orc_rmsd_nofit(R, T, n_atom, tgt_mass);
         if (r < 0.0) err |= 2;
-        int64_t idx = (out_kind == ORC_TRI) ? orc_tri_index(n_ref, i, j) - base : j * n_ref + i - row_begin;
+        int64_t idx = (out_kind == ORC_TRI) ? orc_tri_index(n_ref, i, j) - base : (j - row_begin) * n_ref + i;
         out[idx] = (float)r;
       }
     }

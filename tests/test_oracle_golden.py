@@ -92,3 +92,12 @@ def test_live_reference_random():
         a = oracle.allpairs(X, tgt_mass=m, mode=mode)
         b = oracle.allpairs(X, tgt_mass=m, mode=mode, use_reference_code=True)
         assert np.array_equal(a, b)
+
+
+def test_full_row_ranges_are_target_rows(refp):
+    X, m = refp["xyz"], refp["mass"]
+    A, B = X[:10], X[10:]
+    full = oracle.allpairs(A, B, tgt_mass=m)
+    assert full.size == 10 * 14
+    parts = [oracle.allpairs(A, B, tgt_mass=m, row_begin=a, row_end=b) for a, b in ((0, 3), (3, 14))]
+    assert np.array_equal(np.concatenate(parts), full)

@@ -53,7 +53,7 @@ struct gbr_handle {
   cudaStream_t own_stream = nullptr;  // created with the handle
   std::string err;
   gbr_stats stats{};
-  double tau = 4.0;
+  double tau = 6.0;
   int max_refs = 32;
   double tol = 5e-5;
   bool timing = false;
@@ -241,6 +241,16 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
   const int64_t total_pairs = n_out;
   const unsigned long long flag_cap = (unsigned long long)std::min<int64_t>(total_pairs, 1 << 22);
 
+  OutMap map{};
+  map.n_ref = n_ref;
+  map.tgt0 = tgt0;
+  map.n_tgt = n_tgt;
+  map.tri = (out_kind == GBR_TRI);
+  map.row_begin = row_begin;
+  map.row_end = row_end;
+  map.base = (map.tri && row_begin < n_ref - 1) ? tri_index(n_ref, row_begin, row_begin + 1) : 0;
+  const int64_t tc_tiles = tc ? tc_max_tiles(map) : 0;
+
   // ---- workspace layout (sizing pass, then carve) ----
   auto layout = [&](Arena& A, void** p) {
     p[0] = ref_dev ? nullptr : A.take<char>(esz * 3 * (size_t)N * n_ref);
@@ -260,17 +270,19 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     p[14] = A.take<float>(F);                                           // nrm
     p[15] = A.take<float>((size_t)F * Kmax * 9);                        // P
     p[16] = A.take<float>((size_t)F * Kmax);                            // trP
-    p[17] = A.take<float>((size_t)Kmax * Kmax * 9);                     // S
-    p[18] = A.take<float>((size_t)Kmax * Kmax * 3);                     // SA
-    p[19] = A.take<float>((size_t)Kmax * Kmax);                         // SSd
+    p[17] = A.take<float>((size_t)Kmax * Kmax * kRefPairStride);        // reference-pair table
+    p[18] = A.take<int>(F);                                             // frames by reference
+    p[19] = A.take<int>(Kmax + 1);                                      // offsets
     p[20] = A.take<int2>(flag_cap);                                     // flagged
     p[21] = A.take<unsigned long long>(1);                              // count
     p[22] = out_dev ? nullptr : A.take<float>(n_out);                   // out staging
-    p[23] = tc ? A.take<__half_raw>((size_t)F * 4 * Np) : nullptr;      // hi
-    p[24] = tc ? A.take<__half_raw>((size_t)F * 4 * Np) : nullptr;      // lo
+    p[23] = tc ? A.take<__half_raw>((size_t)F * 3 * Np) : nullptr;      // hi
+    p[24] = tc ? A.take<__half_raw>((size_t)F * 3 * Np) : nullptr;      // lo
     p[25] = A.take<int>(1);                                             // device error flag
+    p[26] = tc ? A.take<int2>(tc_tiles) : nullptr;                      // tile list
+    p[27] = need_planes ? A.take<float>((size_t)Kmax * 3 * Np) : nullptr;  // reference means
   };
-  void* P[26];
+  void* P[28];
   Arena sizing;
   layout(sizing, P);
   if (!h->reserve(sizing.off + 256))
@@ -298,15 +310,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
   cudaMemsetAsync(P[21], 0, sizeof(unsigned long long), st);
   cudaMemsetAsync(P[25], 0, sizeof(int), st);
 
-  OutMap map{};
   map.out = out_dev ? out : (float*)P[22];
-  map.n_ref = n_ref;
-  map.tgt0 = tgt0;
-  map.n_tgt = n_tgt;
-  map.tri = (out_kind == GBR_TRI);
-  map.row_begin = row_begin;
-  map.row_end = row_end;
-  map.base = (map.tri && row_begin < n_ref - 1) ? tri_index(n_ref, row_begin, row_begin + 1) : 0;
 
   PrepArgs pa{};
   pa.dtype_f64 = (dtype == GBR_F64);
@@ -334,6 +338,9 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
   pa.rot = nullptr;
   pa.plane = (float*)P[12];
   pa.pmax_bits = (unsigned*)P[13];
+  pa.order = (int*)P[18];
+  pa.offsets = (int*)P[19];
+  pa.mean = (float*)P[27];
 
   ExactLaunch ex{};
   ex.dtype_f64 = pa.dtype_f64;
@@ -388,9 +395,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     terms.nrm = (float*)P[14];
     terms.P = (float*)P[15];
     terms.trP = (float*)P[16];
-    terms.S = (float*)P[17];
-    terms.SA = (float*)P[18];
-    terms.SSd = (float*)P[19];
+    terms.RP = (float*)P[17];
     terms.K = K;
     terms.W = (float)Wsum;
     terms.tol = (float)h->tol;
@@ -399,7 +404,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     terms.sqrtN = std::sqrt((float)N);
     terms.nofit = nofit;
     if ((e = run_terms(pa.plane, F, Np, N, pa.swr, K, (float*)terms.nrm, (float*)terms.P, (float*)terms.trP,
-                       pa.refs, d_w, (float*)terms.S, (float*)terms.SA, (float*)terms.SSd, st)) != cudaSuccess)
+                       pa.refs, d_w, nofit, (float*)terms.RP, st)) != cudaSuccess)
       return h->cuda_fail(e, "frame terms");
     launches += 2;
     FlagList fl{(int2*)P[20], (unsigned long long*)P[21], flag_cap};
@@ -408,6 +413,8 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
       TcLaunch L{};
       L.hi = P[23];
       L.lo = P[24];
+      L.tile_buf = P[26];
+      L.tile_cap = tc_tiles;
       L.F = F;
       L.Np = Np;
       L.N = N;
@@ -416,7 +423,6 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
       L.terms = terms;
       L.map = map;
       L.flags = fl;
-      L.tiles = make_tiles(map, 32, 32);
       L.dev_error = (int*)P[25];
       L.num_sms = h->num_sms;
       if ((e = run_pairs_tc(L, st)) != cudaSuccess) return h->cuda_fail(e, "tensor-core pair kernel");

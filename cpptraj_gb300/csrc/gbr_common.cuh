@@ -9,19 +9,21 @@
 // cannot reach 1e-4 Angstrom.  Instead every frame is first superposed (in
 // FP64, exact rotation) onto its nearest of K reference structures r_k, which
 // leaves RMSD unchanged, and split as x'_f = r_{a(f)} + d_f with d_f small.
-// For a pair (ref i, target j), a = a(i), b = a(j):
+// Each reference is then refined to the mean of its superposed frames, so d_f
+// is of the size of the frame's own fluctuation.  For a pair (ref i, target
+// j), a = a(i), b = a(j):
 //     M = sum w x'_j x'_i^T = S_ba + P_ja + P_ib^T + D_ji
 // with S_ba = sum w r_b r_a^T, P_fc = sum w d_f r_c^T (per frame and
 // reference) and D_ji = sum w d_j d_i^T (the only per-pair contraction, on
 // small numbers).  The quaternion key matrix enters through
-// G = E0*I - K(M), whose smallest eigenvalue is W*RMSD^2/2.  Its (0,0) entry
-//     G00 = 1/2 sum w |x'_i - x'_j|^2
-//         = 1/2 (SSd_ab + n_i + n_j) + (trP_ia - trP_ib) - (trP_ja - trP_jb) - tr D_ji
-// is assembled from small terms, so the smallest eigenvalue can be found in
-// FP32 without cancellation: a Schur-complement (secular equation) iteration
-// on G around q = (1, v), or, when the pair's relative rotation is large,
-// QCP (Theobald 2005; Liu, Agrafiotis & Theobald 2010) on K(M) for the
-// eigenvector followed by the Rayleigh quotient of G.  Each pair carries an
+// G = E0*I - K(M), whose smallest eigenvalue is W*RMSD^2/2.  After rotating
+// the target by the exact inter-reference rotation U_ab (pair_epilogue), its
+// (0,0) entry G00 = 1/2 sum w |x'_i - U_ab x'_j|^2 is assembled from small
+// terms, so the smallest eigenvalue can be found in FP32 without
+// cancellation: a Schur-complement (secular equation) iteration on G around
+// q = (1, v), or, when the pair's relative rotation is large, QCP (Theobald
+// 2005; Liu, Agrafiotis & Theobald 2010) on K(M) for the eigenvector followed
+// by the Rayleigh quotient of G.  Each pair carries an
 // a-priori error bound; pairs whose bound exceeds the tolerance are listed
 // and recomputed directly in FP64 by gbr_exact.cu.
 #pragma once
@@ -145,19 +147,26 @@ __device__ inline double qcp_lambda_rot(const double A[9], double E0, double R[9
 // --------------------------------------------------------------------------
 // Per-pair data and the FP32 epilogue.
 // --------------------------------------------------------------------------
+// Per reference pair (index b*K + a; a = reference of the reference frame,
+// b = reference of the target frame), 24 floats:
+//   [0..8]   U_ab   proper rotation minimising sum w |r_a - U r_b|^2 (identity
+//                   when a == b or in no-fit mode), row-major, from FP64
+//   [9..17]  SU_ab  U_ab * S_ba with S_ba = sum w r_b r_a^T
+//   [18..20] antisymmetric combos (yz-zy, zx-xz, xy-yx) of SU_ab, from FP64
+//   [21]     SS_ab  sum w |r_a - U_ab r_b|^2
+constexpr int kRefPairStride = 24;
+
 struct FrameTerms {
   const int* assign;  // [F] reference index of each set frame
   const float* nrm;   // [F] n_f = sum |p_f|^2  (p = sqrt(w) d)
   const float* P;     // [F][K][9] P_fc[p][q] = sum p_f[p] * (sqrt(w) r_c)[q]
   const float* trP;   // [F][K]
-  const float* S;     // [K][K][9] S_ba[p][q] = sum w r_b[p] r_a[q], index (b*K + a)
-  const float* SA;    // [K][K][3] antisymmetric combos of S_ba (yz-zy, zx-xz, xy-yx)
-  const float* SSd;   // [K][K] sum w |r_a - r_b|^2
+  const float* RP;    // [K][K][kRefPairStride]
   int K;
   float W;            // total weight
   float tol;          // per-pair tolerance (Angstrom)
   float gemm_coef;    // contraction error coefficient (times sqrt(N)*sqrt(n_i n_j))
-  float epi_coef;     // epilogue rounding coefficient
+  float epi_coef;     // epilogue rounding coefficient (times the Rayleigh-quotient terms)
   float sqrtN;
   int nofit;
 };
@@ -258,45 +267,82 @@ __device__ inline void qcp_vec_f32(const float M[9], float E0, float q[4]) {
 // The pair epilogue.  D[pj*3+pi] = sum p_j[pj] p_i[pi] (target j first).
 // Returns the RMSD (Angstrom, >= 0); sets *flag when the error bound exceeds
 // the tolerance and the pair must be recomputed in FP64.
+//
+// With x'_i = r_a + d_i and x'_j = r_b + d_j, the pair is solved in the frame
+// where target j is additionally rotated by U_ab (exact, per reference pair),
+// so the remaining optimal rotation is close to the identity for every pair:
+//   M'' = U_ab M = SU_ab + U_ab (P_ja + P_ib^T + D_ji)
+//   G00 = 1/2 sum w |x'_i - U_ab x'_j|^2
+//       = 1/2 (SS_ab + n_i + n_j) + trP_ia - <U,P_ib> - <U,P_ja^T> + trP_jb - tr(U D_ji)
+// (for a == b: U = I and G00 = 1/2 (n_i + n_j) - tr D_ji).
 static __device__ __noinline__ float pair_epilogue(const float D[9], int64_t i, int64_t j, const FrameTerms& t,
-                                      bool* flag) {
+                                                   bool* flag) {
   const int K = t.K;
   const int a = (K > 1) ? __ldg(t.assign + i) : 0;
   const int b = (K > 1) ? __ldg(t.assign + j) : 0;
   const float ni = __ldg(t.nrm + i), nj = __ldg(t.nrm + j);
   const float* Pja = t.P + ((size_t)j * K + a) * 9;
   const float* Pib = t.P + ((size_t)i * K + b) * 9;
-  const int ab = b * K + a;
-  const float trD = D[0] + D[4] + D[8];
-  float G00 = 0.5f * (ni + nj) - trD;
-  if (a != b) {
-    G00 += 0.5f * __ldg(t.SSd + a * K + b) + (__ldg(t.trP + i * K + a) - __ldg(t.trP + i * K + b)) -
-           (__ldg(t.trP + j * K + a) - __ldg(t.trP + j * K + b));
-  }
+  const float* rp = t.RP + (size_t)(b * K + a) * kRefPairStride;
   const float W = t.W;
+  // X = P_ja + P_ib^T + D_ji
+  float X[9];
+  X[0] = __ldg(Pja + 0) + __ldg(Pib + 0) + D[0];
+  X[1] = __ldg(Pja + 1) + __ldg(Pib + 3) + D[1];
+  X[2] = __ldg(Pja + 2) + __ldg(Pib + 6) + D[2];
+  X[3] = __ldg(Pja + 3) + __ldg(Pib + 1) + D[3];
+  X[4] = __ldg(Pja + 4) + __ldg(Pib + 4) + D[4];
+  X[5] = __ldg(Pja + 5) + __ldg(Pib + 7) + D[5];
+  X[6] = __ldg(Pja + 6) + __ldg(Pib + 2) + D[6];
+  X[7] = __ldg(Pja + 7) + __ldg(Pib + 5) + D[7];
+  X[8] = __ldg(Pja + 8) + __ldg(Pib + 8) + D[8];
+  float G00, g00mag;
+  float Y[9];
+  if (a == b) {
+    const float trD = D[0] + D[4] + D[8];
+    const float h = 0.5f * (ni + nj);
+    G00 = h - trD;
+    g00mag = h + fabsf(trD);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Y[k] = X[k];
+  } else {
+    float U[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) U[k] = __ldg(rp + k);
+    float uPib = 0.f, uPjaT = 0.f, trUD = 0.f;
+#pragma unroll
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        uPib += U[p * 3 + q] * __ldg(Pib + p * 3 + q);
+        uPjaT += U[p * 3 + q] * __ldg(Pja + q * 3 + p);
+        trUD += U[p * 3 + q] * D[q * 3 + p];
+      }
+    const float trPia = __ldg(t.trP + i * K + a), trPjb = __ldg(t.trP + j * K + b);
+    const float h = 0.5f * (__ldg(rp + 21) + ni + nj);
+    G00 = h + trPia - uPib - uPjaT + trPjb - trUD;
+    g00mag = h + fabsf(trPia) + fabsf(uPib) + fabsf(uPjaT) + fabsf(trPjb) + fabsf(trUD);
+#pragma unroll
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+      for (int q = 0; q < 3; ++q)
+        Y[p * 3 + q] = U[p * 3] * X[q] + U[p * 3 + 1] * X[3 + q] + U[p * 3 + 2] * X[6 + q];
+  }
   const float gem = t.gemm_coef * t.sqrtN * sqrtf(fmaxf(ni, 0.0f) * fmaxf(nj, 0.0f));
   if (t.nofit) {
-    // RMSD_NoFit: sum w |x_i - x_j|^2 / W = 2*G00/W (no rotation, no centring).
-    const float msd = fmaxf(2.0f * G00 / W, 0.0f);
-    const float r = sqrtf(msd);
-    float err = 2.0f * gem + t.epi_coef * (fabsf(G00) + ni + nj);
-    *flag = err > t.tol * W * fmaxf(r, 1e-3f);
+    // RMSD_NoFit: sum w |x_i - x_j|^2 / W = 2*G00/W (references are not rotated).
+    const float r = sqrtf(fmaxf(2.0f * G00 / W, 0.0f));
+    const float err = 2.0f * gem + t.epi_coef * g00mag;
+    *flag = !(err <= t.tol * W * fmaxf(r, 1e-3f));
     return r;
   }
-  float X[9];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) X[k] = __ldg(Pja + k) + D[k];
-  X[0] += __ldg(Pib + 0); X[1] += __ldg(Pib + 3); X[2] += __ldg(Pib + 6);
-  X[3] += __ldg(Pib + 1); X[4] += __ldg(Pib + 4); X[5] += __ldg(Pib + 7);
-  X[6] += __ldg(Pib + 2); X[7] += __ldg(Pib + 5); X[8] += __ldg(Pib + 8);
-  const float* S = t.S + (size_t)ab * 9;
   float M[9];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) M[k] = __ldg(S + k) + X[k];
-  // g = G[0][1..3] = -(antisymmetric combos of M), from the small parts.
-  const float g1 = -(X[5] - X[7] + __ldg(t.SA + ab * 3 + 0));
-  const float g2 = -(X[6] - X[2] + __ldg(t.SA + ab * 3 + 1));
-  const float g3 = -(X[1] - X[3] + __ldg(t.SA + ab * 3 + 2));
+  for (int k = 0; k < 9; ++k) M[k] = __ldg(rp + 9 + k) + Y[k];
+  // g = G[0][1..3] = -(antisymmetric combos of M''), from the small parts.
+  const float g1 = -(Y[5] - Y[7] + __ldg(rp + 18));
+  const float g2 = -(Y[6] - Y[2] + __ldg(rp + 19));
+  const float g3 = -(Y[1] - Y[3] + __ldg(rp + 20));
   const float G11 = G00 + 2.0f * (M[4] + M[8]);
   const float G22 = G00 + 2.0f * (M[0] + M[8]);
   const float G33 = G00 + 2.0f * (M[0] + M[4]);
@@ -329,7 +375,7 @@ static __device__ __noinline__ float pair_epilogue(const float D[9], int64_t i, 
   const float t11 = q1 * q1 * G11 + q2 * q2 * G22 + q3 * q3 * G33;
   const float t12 = 2.f * (q1 * q2 * G12 + q1 * q3 * G13 + q2 * q3 * G23);
   const float rq = (t00 + t01 + t11 + t12) / qq;
-  const float mag = (fabsf(t00) + 2.f * fabsf(q0) * (fabsf(q1 * g1) + fabsf(q2 * g2) + fabsf(q3 * g3)) +
+  const float mag = (q0 * q0 * g00mag + 2.f * fabsf(q0) * (fabsf(q1 * g1) + fabsf(q2 * g2) + fabsf(q3 * g3)) +
                      fabsf(t11) + 2.f * (fabsf(q1 * q2 * G12) + fabsf(q1 * q3 * G13) + fabsf(q2 * q3 * G23))) /
                     qq;
   const float r = sqrtf(fmaxf(2.0f * rq / W, 0.0f));

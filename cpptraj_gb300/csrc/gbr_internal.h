@@ -37,6 +37,9 @@ struct PrepArgs {
   double* rot;     // [F][9] or nullptr
   float* plane;    // [F][3][Np]
   unsigned* pmax_bits;
+  int* order;      // [F] frames grouped by reference
+  int* offsets;    // [max_refs + 1]
+  float* mean;     // [max_refs][3][Np]
 };
 
 struct PrepOut {
@@ -47,8 +50,8 @@ struct PrepOut {
 cudaError_t run_prep(const PrepArgs& A, PrepOut& o, cudaStream_t st);
 cudaError_t run_split_f16(float* plane, int64_t F, int Np, float scale, void* hi, void* lo, cudaStream_t st);
 cudaError_t run_terms(const float* plane, int64_t F, int Np, int N, const float* swr, int K, float* nrm,
-                      float* P, float* trP, const double* refs, const double* w, float* S, float* SA,
-                      float* SSd, cudaStream_t st);
+                      float* P, float* trP, const double* refs, const double* w, int nofit, float* RP,
+                      cudaStream_t st);
 
 // Tiles of the pair space: rows = reference frames, cols = target frames.
 struct TileSpace {
@@ -73,10 +76,12 @@ struct PairLaunch {
 
 cudaError_t run_pairs_fp32(const PairLaunch& L, cudaStream_t st);
 
-// Tensor-core contraction (tcgen05).  hi/lo: FP16 planes [F][4][Np].
+// Tensor-core contraction (tcgen05).  hi/lo: FP16 planes [F][3][Np].
 struct TcLaunch {
   const void* hi;
   const void* lo;
+  void* tile_buf;     // device scratch for the tile list (int2)
+  int64_t tile_cap;
   int64_t F;
   int Np, N;
   int64_t tgt0;
@@ -90,6 +95,7 @@ struct TcLaunch {
 };
 cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st);
 int tc_supported(int device);
+int64_t tc_max_tiles(const OutMap& m);
 
 // Direct FP64 recomputation (flagged pairs or every pair).
 struct ExactLaunch {

@@ -1,8 +1,481 @@
-// gbr_pair_tc.cu -- tensor-core (tcgen05) pair contraction.  Placeholder until
-// the sm_103a kernel lands: reports the precision as unsupported.
+// gbr_pair_tc.cu -- tensor-core (tcgen05, sm_103a) all-pairs contraction (K2).
+//
+// Same job as gbr_pair_fp32.cu -- the pair loop of
+// Analysis_Rms2d::Calculate_2D (src/Analysis_Rms2d.cpp:252-286) and
+// MetricArray::calcFrameDistances (src/Cluster/MetricArray.cpp:786-793) --
+// with the residual contraction D_ji = sum_a p_j[a] p_i[a]^T run on the
+// 5th-generation tensor cores.
+//
+// Operands.  p = sqrt(w)*d is split into FP16 hi + lo (scaled by a power of
+// two); hi*hi + lo*hi + hi*lo is accumulated in FP32 in tensor memory, which
+// reproduces the products to ~2^-22 relative.  The planes are [F][3][Np]
+// FP16 (atoms contiguous), so one 3-D TMA box (64 atoms, 3 components, n
+// frames) lands in shared memory as (frame, component) rows of 128 bytes with
+// the 128-byte swizzle the UMMA K-major descriptor expects.
+//
+// Tile.  A (M = 128 rows) holds 42 reference frames x 3 components (rows
+// 126-127 unused); B (N = 192) holds 64 target frames x 3 components.  The
+// 128 x 192 FP32 accumulator therefore contains the 3x3 block of all 42 x 64
+// pairs; two accumulators (columns 0 and 256 of a 512-column TMEM allocation)
+// let the epilogue of one tile overlap the MMAs of the next.
+//
+// Warp roles (320 threads, one persistent CTA per SM):
+//   warp 0      TMA producer: 4 boxes (A hi/lo, B hi/lo) per 64-atom stage,
+//               two stages in shared memory.
+//   warp 1      TMEM allocation and the single MMA-issuing thread.
+//   warps 2-9   epilogue: tcgen05.ld 48-column chunks, stage them through
+//               shared memory, then the per-pair FP32 eigen epilogue
+//               (gbr_common.cuh) and coalesced stores into TRI/FULL output.
+// Every mbarrier wait is bounded (about 2 s); on expiry the kernel records
+// an error code, drains its own MMAs, frees tensor memory and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_fp16.h>
+
+#include <vector>
+
+#include "gbr_common.cuh"
 #include "gbr_internal.h"
 
 namespace gbr {
-int tc_supported(int) { return 0; }
-cudaError_t run_pairs_tc(const TcLaunch&, cudaStream_t) { return cudaErrorNotSupported; }
+
+namespace {
+constexpr int TI = 42;                 // reference frames per tile
+constexpr int TJ = 64;                 // target frames per tile
+constexpr int UM = 128;                // MMA M
+constexpr int UN = 3 * TJ;             // MMA N = 192
+constexpr int KA = 64;                 // atoms per stage (128-byte FP16 rows)
+constexpr int STAGES = 2;
+constexpr int A_BYTES = UM * 128;      // 16384 (TMA writes 126 rows)
+constexpr int B_BYTES = UN * 128;      // 24576
+constexpr int A_TX = 3 * TI * 128;     // bytes one A box delivers
+constexpr int B_TX = UN * 128;
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+constexpr int EPI_WARPS = 8;
+constexpr int THREADS = 64 + 32 * EPI_WARPS;
+constexpr int CH_TGT = 16;             // target frames per epilogue chunk
+constexpr int CH_COLS = 3 * CH_TGT;    // 48 accumulator columns
+constexpr int ST_STRIDE = CH_COLS + 1;
+constexpr int STAGING_BYTES = 128 * ST_STRIDE * 4;
+constexpr int BAR_BYTES = 128;
+constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + 2 * STAGING_BYTES + BAR_BYTES;
+constexpr uint32_t TMEM_COLS = 512;
+constexpr uint32_t ACC_STRIDE = 256;
+constexpr long long TIMEOUT_CYCLES = 4000000000LL;
+
+// Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = F16
+// (bits 7-12 = 0), both K-major (bits 15-16 = 0), N >> 3 at bits 17-22,
+// M >> 4 at bits 24-28.
+constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(UN >> 3) << 17) | ((uint32_t)(UM >> 4) << 24);
+
+struct TcParams {
+  const int2* tiles;  // (ti, tj) per tile
+  int64_t n_tiles;
+  int64_t i_base;     // first reference frame of tile row 0
+  int64_t jt_base;    // first target frame of tile column 0
+  int64_t i_end, jt_end;
+  int64_t tgt0;
+  int nk;             // 64-atom stages per tile
+  float inv_scale2;
+  FrameTerms terms;
+  OutMap map;
+  FlagList flags;
+  int* err;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: false (and *err set) when the phase does not complete in
+// time or another thread already reported an error.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+  if (mbar_try(bar, parity)) return true;
+  const long long t0 = clock64();
+  for (uint32_t it = 1;; ++it) {
+    if (mbar_try(bar, parity)) return true;
+    if ((it & 255u) == 0) {
+      if (*(volatile int*)err != 0) return false;
+      if (clock64() - t0 > TIMEOUT_CYCLES) {
+        atomicCAS(err, 0, code);
+        return false;
+      }
+    }
+  }
+}
+
+// Bounded wait that ignores the error flag (used to drain our own TMA copies).
+__device__ __forceinline__ void mbar_wait_quiet(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try(bar, parity)) {
+    if (clock64() - t0 > TIMEOUT_CYCLES) return;
+  }
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+          dst),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
+// UMMA shared-memory descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (SBO), version bits 46-48 = 0b001.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)(1024u >> 4) << 32;
+  d |= 1ull << 46;
+  d |= 2ull << 61;
+  return d;
+}
+
+__device__ __forceinline__ void umma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(IDESC), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ void named_sync(int id, int n) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_pairs_tc(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
+               const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
+               const TcParams P) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* stage_base = smem;
+  float* staging = (float*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES + 2 * STAGING_BYTES);
+  // bars: full[2] empty[2] accfull[2] accempty[2] done[1]; then the TMEM address.
+  uint32_t* tmem_slot = (uint32_t*)(bars + 12);
+  volatile int* grp_ok = (volatile int*)(bars + 13);  // two ints, one per epilogue warpgroup
+  const uint32_t full0 = smem_u32(bars + 0), empty0 = smem_u32(bars + 2), accf0 = smem_u32(bars + 4),
+                 acce0 = smem_u32(bars + 6), done = smem_u32(bars + 8);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(accf0 + 8 * b, 1);
+      mbar_init(acce0 + 8 * b, EPI_WARPS);
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&tmAh) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&tmAl) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&tmBh) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&tmBl) : "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int s = 0;
+      uint32_t ph = 0;
+      bool ok = true;
+      int last_par[STAGES];
+      for (int k = 0; k < STAGES; ++k) last_par[k] = -1;
+      for (int64_t t = blockIdx.x; t < P.n_tiles && ok; t += gridDim.x) {
+        const int2 tl = P.tiles[t];
+        const int iz = (int)(P.i_base + (int64_t)tl.x * TI);
+        const int jz = (int)(P.tgt0 + P.jt_base + (int64_t)tl.y * TJ);
+        for (int kc = 0; kc < P.nk; ++kc) {
+          if (!mbar_wait(empty0 + 8 * s, ph ^ 1u, P.err, 1)) { ok = false; break; }
+          const uint32_t fb = full0 + 8 * s;
+          mbar_expect_tx(fb, 2 * A_TX + 2 * B_TX);
+          const uint32_t sb = smem_u32(stage_base + s * STAGE_BYTES);
+          tma_load_3d(sb, &tmAh, kc * KA, 0, iz, fb);
+          tma_load_3d(sb + A_BYTES, &tmAl, kc * KA, 0, iz, fb);
+          tma_load_3d(sb + 2 * A_BYTES, &tmBh, kc * KA, 0, jz, fb);
+          tma_load_3d(sb + 2 * A_BYTES + B_BYTES, &tmBl, kc * KA, 0, jz, fb);
+          last_par[s] = (int)ph;
+          if (++s == STAGES) { s = 0; ph ^= 1u; }
+        }
+      }
+      // Our copies land before the CTA may exit (immediate on the normal path).
+      for (int k = 0; k < STAGES; ++k)
+        if (last_par[k] >= 0) mbar_wait_quiet(full0 + 8 * k, (uint32_t)last_par[k]);
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      int s = 0;
+      uint32_t ph = 0;
+      uint32_t it = 0;
+      bool ok = true;
+      for (int64_t t = blockIdx.x; t < P.n_tiles && ok; t += gridDim.x, ++it) {
+        const uint32_t b = it & 1u, aph = (it >> 1) & 1u;
+        if (!mbar_wait(acce0 + 8 * b, aph ^ 1u, P.err, 2)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t d = tmem_base + b * ACC_STRIDE;
+        for (int kc = 0; kc < P.nk; ++kc) {
+          if (!mbar_wait(full0 + 8 * s, ph, P.err, 3)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t sb = smem_u32(stage_base + s * STAGE_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < KA / 16; ++kk) {
+            const uint64_t ah = smem_desc(sb + kk * 32), al = smem_desc(sb + A_BYTES + kk * 32);
+            const uint64_t bh = smem_desc(sb + 2 * A_BYTES + kk * 32);
+            const uint64_t bl = smem_desc(sb + 2 * A_BYTES + B_BYTES + kk * 32);
+            umma_f16(d, ah, bh, (kc | kk) != 0);
+            umma_f16(d, al, bh, 1u);
+            umma_f16(d, ah, bl, 1u);
+          }
+          umma_commit(empty0 + 8 * s);  // frees the stage once these MMAs retire
+          if (++s == STAGES) { s = 0; ph ^= 1u; }
+        }
+        if (!ok) break;
+        umma_commit(accf0 + 8 * b);
+      }
+      // Drain: every MMA issued above has retired once `done` completes.
+      umma_commit(done);
+      mbar_wait_quiet(done, 0);
+    }
+  } else {
+    // ---------------- epilogue ----------------
+    const int e = warp - 2;
+    const int g = e >> 2;                 // warpgroup 0/1
+    const int q = warp & 3;               // TMEM lane quadrant this warp may access
+    const int row = 32 * q + lane;        // accumulator row = (ref frame, component)
+    const int tid = (e & 3) * 32 + lane;  // 0..127 within the warpgroup
+    float* st = staging + g * (128 * ST_STRIDE);
+    const bool tri = P.map.tri;
+    uint32_t it = 0;
+    bool ok = true;
+    for (int64_t t = blockIdx.x; t < P.n_tiles; t += gridDim.x, ++it) {
+      const uint32_t b = it & 1u, aph = (it >> 1) & 1u;
+      // One thread per warpgroup waits; the verdict is shared so that every
+      // thread of the group takes the same path through the named barriers.
+      if (tid == 0) grp_ok[g] = mbar_wait(accf0 + 8 * b, aph, P.err, 5) ? 1 : 0;
+      named_sync(1 + g, 128);
+      ok = grp_ok[g] != 0;
+      const int2 tl = P.tiles[t];
+      const int64_t i0 = P.i_base + (int64_t)tl.x * TI;
+      const int64_t jt0 = P.jt_base + (int64_t)tl.y * TJ;
+      if (ok) {
+        tc_fence_after();
+        for (int c = g; c < TJ / CH_TGT; c += 2) {
+          float v[CH_COLS];
+          const uint32_t taddr = tmem_base + ((uint32_t)(32 * q) << 16) + b * ACC_STRIDE + c * CH_COLS;
+          tmem_ld16(taddr, v);
+          tmem_ld16(taddr + 16, v + 16);
+          tmem_ld16(taddr + 32, v + 32);
+          tmem_wait_ld();
+#pragma unroll
+          for (int k = 0; k < CH_COLS; ++k) st[row * ST_STRIDE + k] = v[k];
+          named_sync(1 + g, 128);
+          const int64_t jc0 = jt0 + (int64_t)c * CH_TGT;
+#pragma unroll 1
+          for (int p = tid; p < TI * CH_TGT; p += 128) {
+            const int il = tri ? p / CH_TGT : p % TI;
+            const int jl = tri ? p % CH_TGT : p / TI;
+            const int64_t i = i0 + il, jt = jc0 + jl;
+            if (i >= P.i_end || jt >= P.jt_end) continue;
+            const int64_t idx = out_index(P.map, i, jt);
+            if (idx < 0) continue;
+            float D[9];
+#pragma unroll
+            for (int pj = 0; pj < 3; ++pj)
+#pragma unroll
+              for (int pi = 0; pi < 3; ++pi) D[pj * 3 + pi] = st[(3 * il + pi) * ST_STRIDE + 3 * jl + pj] * P.inv_scale2;
+            bool flag = false;
+            const float r = pair_epilogue(D, i, P.tgt0 + jt, P.terms, &flag);
+            if (flag) flag_pair(P.flags, i, jt);
+            P.map.out[idx] = r;
+          }
+          named_sync(1 + g, 128);
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acce0 + 8 * b);
+      if (!ok) break;
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) {
+    __syncwarp();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS)
+                 : "memory");
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+bool make_map(CUtensorMap* m, const void* base, int64_t F, int Np, int box_frames) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)Np, 3, (cuuint64_t)F};
+  cuuint64_t strides[2] = {(cuuint64_t)Np * 2, (cuuint64_t)Np * 2 * 3};
+  cuuint32_t box[3] = {(cuuint32_t)KA, 3, (cuuint32_t)box_frames};
+  cuuint32_t es[3] = {1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<void*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+}  // namespace
+
+int tc_supported(int device) {
+  int major = 0, minor = 0;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device);
+  cudaGetLastError();
+  return (major == 10 && minor == 3 && encode_fn() != nullptr) ? 1 : 0;
+}
+
+int tc_tile_rows() { return TI; }
+int tc_tile_cols() { return TJ; }
+
+// Tile list in grouped order: groups of G tile-rows are swept column by
+// column so the CTAs in flight share A and B frames in L2.
+int64_t tc_build_tiles(const OutMap& m, std::vector<int2>& tiles, int64_t& i_base, int64_t& jt_base,
+                       int64_t& i_end, int64_t& jt_end) {
+  if (m.tri) {
+    i_base = m.row_begin;
+    i_end = m.row_end;
+    jt_base = m.row_begin;
+    jt_end = m.n_tgt;
+  } else {
+    i_base = 0;
+    i_end = m.n_ref;
+    jt_base = m.row_begin;
+    jt_end = m.row_end;
+  }
+  tiles.clear();
+  const int64_t Ti = (i_end - i_base + TI - 1) / TI, Tj = (jt_end - jt_base + TJ - 1) / TJ;
+  const int64_t G = 8;
+  for (int64_t g0 = 0; g0 < Ti; g0 += G) {
+    for (int64_t tj = 0; tj < Tj; ++tj) {
+      for (int64_t ti = g0; ti < std::min(Ti, g0 + G); ++ti) {
+        if (m.tri) {
+          const int64_t ilo = i_base + ti * TI;
+          const int64_t jhi = jt_base + tj * TJ + TJ - 1;
+          if (jhi <= ilo) continue;  // no pair with target > reference
+        }
+        tiles.push_back(make_int2((int)ti, (int)tj));
+      }
+    }
+  }
+  return (int64_t)tiles.size();
+}
+
+cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
+  std::vector<int2> tiles;
+  int64_t i_base, jt_base, i_end, jt_end;
+  const int64_t n = tc_build_tiles(L.map, tiles, i_base, jt_base, i_end, jt_end);
+  if (n == 0) return cudaSuccess;
+  if (!L.tile_buf || n > L.tile_cap) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemcpyAsync(L.tile_buf, tiles.data(), sizeof(int2) * n, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  // The copy reads `tiles` asynchronously from pageable memory; cudaMemcpyAsync
+  // from pageable memory returns after the source has been consumed.
+  CUtensorMap mAh, mAl, mBh, mBl;
+  if (!make_map(&mAh, L.hi, L.F, L.Np, TI) || !make_map(&mAl, L.lo, L.F, L.Np, TI) ||
+      !make_map(&mBh, L.hi, L.F, L.Np, TJ) || !make_map(&mBl, L.lo, L.F, L.Np, TJ))
+    return cudaErrorInvalidValue;
+  TcParams P{};
+  P.tiles = (const int2*)L.tile_buf;
+  P.n_tiles = n;
+  P.i_base = i_base;
+  P.jt_base = jt_base;
+  P.i_end = i_end;
+  P.jt_end = jt_end;
+  P.tgt0 = L.tgt0;
+  P.nk = (L.N + KA - 1) / KA;
+  P.inv_scale2 = L.inv_scale2;
+  P.terms = L.terms;
+  P.map = L.map;
+  P.flags = L.flags;
+  P.err = L.dev_error;
+  e = cudaFuncSetAttribute(k_pairs_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+  if (e != cudaSuccess) return e;
+  const int grid = (int)std::min<int64_t>(n, L.num_sms > 0 ? L.num_sms : 148);
+  k_pairs_tc<<<grid, THREADS, SMEM_BYTES, st>>>(mAh, mAl, mBh, mBl, P);
+  return cudaGetLastError();
+}
+
+int64_t tc_max_tiles(const OutMap& m) {
+  int64_t ni, nj;
+  if (m.tri) {
+    ni = m.row_end - m.row_begin;
+    nj = m.n_tgt - m.row_begin;
+  } else {
+    ni = m.n_ref;
+    nj = m.row_end - m.row_begin;
+  }
+  return ((ni + TI - 1) / TI) * ((nj + TJ - 1) / TJ);
+}
+
 }  // namespace gbr

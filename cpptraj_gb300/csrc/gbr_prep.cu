@@ -17,6 +17,8 @@
 //   k_ref_terms    S_ba, its antisymmetric combos and sum w |r_a - r_b|^2.
 #include <cuda_fp16.h>
 
+#include <vector>
+
 #include "gbr_common.cuh"
 #include "gbr_internal.h"
 
@@ -268,28 +270,19 @@ __global__ void __launch_bounds__(kPrepThreads) k_align(FrameSrc<T> src, int64_t
   }
 }
 
-// FP32 plane [F][3][Np] -> FP16 hi/lo planes [F][4][Np] (scaled by `scale`,
-// a power of two), component 3 zero.  The FP32 plane is overwritten with the
-// value the hi/lo pair represents, so per-frame terms match the contraction.
-__global__ void k_split_f16(float* plane, int64_t F, int Np, float scale, __half* hi, __half* lo) {
-  const int64_t total = F * (int64_t)Np;
+// FP32 plane [F][3][Np] -> FP16 hi/lo planes [F][3][Np] scaled by `scale` (a
+// power of two).  The FP32 plane is overwritten with the value hi + lo
+// represents, so the per-frame terms match what the contraction reads.
+__global__ void k_split_f16(float* plane, int64_t total, float scale, __half* hi, __half* lo) {
   const float inv = 1.0f / scale;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
        t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t f = t / Np;
-    const int a = (int)(t - f * Np);
-#pragma unroll
-    for (int p = 0; p < 3; ++p) {
-      float* src = plane + (size_t)f * 3 * Np + (size_t)p * Np + a;
-      const float v = *src * scale;
-      const __half h = __float2half_rn(v);
-      const __half l = __float2half_rn(v - __half2float(h));
-      hi[(size_t)f * 4 * Np + (size_t)p * Np + a] = h;
-      lo[(size_t)f * 4 * Np + (size_t)p * Np + a] = l;
-      *src = (__half2float(h) + __half2float(l)) * inv;
-    }
-    hi[(size_t)f * 4 * Np + 3 * (size_t)Np + a] = __float2half_rn(0.0f);
-    lo[(size_t)f * 4 * Np + 3 * (size_t)Np + a] = __float2half_rn(0.0f);
+    const float v = plane[t] * scale;
+    const __half h = __float2half_rn(v);
+    const __half l = __float2half_rn(v - __half2float(h));
+    hi[t] = h;
+    lo[t] = l;
+    plane[t] = (__half2float(h) + __half2float(l)) * inv;
   }
 }
 
@@ -325,10 +318,13 @@ __global__ void __launch_bounds__(kPrepThreads) k_frame_terms(const float* plane
   }
 }
 
-// S_ba, SA_ba, SSd_ab for every reference pair; one block per (b, a).
+// Reference-pair table (kRefPairStride floats per b*K + a): the exact FP64
+// rotation U_ab taking r_b onto r_a, SU_ab = U_ab S_ba, its antisymmetric
+// combos and sum w |r_a - U_ab r_b|^2.  No-fit mode keeps U = I.
 __global__ void __launch_bounds__(kPrepThreads) k_ref_terms(const double* refs, int N, int K, const double* w,
-                                                            float* S, float* SA, float* SSd) {
+                                                            int nofit, float* RP) {
   __shared__ double red[32 * 10];
+  __shared__ double Us[9];
   const int b = blockIdx.x / K, a = blockIdx.x % K;
   const double* rb = refs + (size_t)b * 3 * N;
   const double* ra = refs + (size_t)a * 3 * N;
@@ -340,18 +336,95 @@ __global__ void __launch_bounds__(kPrepThreads) k_ref_terms(const double* refs, 
     v[0] += wa * b0 * a0; v[1] += wa * b0 * a1; v[2] += wa * b0 * a2;
     v[3] += wa * b1 * a0; v[4] += wa * b1 * a1; v[5] += wa * b1 * a2;
     v[6] += wa * b2 * a0; v[7] += wa * b2 * a1; v[8] += wa * b2 * a2;
-    const double d0 = a0 - b0, d1 = a1 - b1, d2 = a2 - b2;
-    v[9] += wa * (d0 * d0 + d1 * d1 + d2 * d2);
+    v[9] += wa * (b0 * b0 + b1 * b1 + b2 * b2 + a0 * a0 + a1 * a1 + a2 * a2);
   }
   block_sum_f64<10>(v, red);
   if (threadIdx.x == 0) {
-    float* Sb = S + (size_t)blockIdx.x * 9;
-    for (int q = 0; q < 9; ++q) Sb[q] = (float)v[q];
-    SA[blockIdx.x * 3 + 0] = (float)(v[5] - v[7]);
-    SA[blockIdx.x * 3 + 1] = (float)(v[6] - v[2]);
-    SA[blockIdx.x * 3 + 2] = (float)(v[1] - v[3]);
-    SSd[a * K + b] = (float)v[9];
+    double U[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    if (a != b && !nofit) qcp_lambda_rot(v, 0.5 * v[9], U);
+    for (int k = 0; k < 9; ++k) Us[k] = U[k];
   }
+  __syncthreads();
+  // SS_ab = sum w |r_a - U r_b|^2, accumulated directly (no cancellation).
+  double e[1] = {0.0};
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const double wa = w ? w[i] : 1.0;
+    const double b0 = rb[3 * i], b1 = rb[3 * i + 1], b2 = rb[3 * i + 2];
+    const double d0 = ra[3 * i] - (Us[0] * b0 + Us[1] * b1 + Us[2] * b2);
+    const double d1 = ra[3 * i + 1] - (Us[3] * b0 + Us[4] * b1 + Us[5] * b2);
+    const double d2 = ra[3 * i + 2] - (Us[6] * b0 + Us[7] * b1 + Us[8] * b2);
+    e[0] += wa * (d0 * d0 + d1 * d1 + d2 * d2);
+  }
+  block_sum_f64<1>(e, red);
+  if (threadIdx.x == 0) {
+    double SU[9];
+    for (int p = 0; p < 3; ++p)
+      for (int q = 0; q < 3; ++q)
+        SU[p * 3 + q] = Us[p * 3] * v[q] + Us[p * 3 + 1] * v[3 + q] + Us[p * 3 + 2] * v[6 + q];
+    float* o = RP + (size_t)blockIdx.x * kRefPairStride;
+    for (int k = 0; k < 9; ++k) o[k] = (float)Us[k];
+    for (int k = 0; k < 9; ++k) o[9 + k] = (float)SU[k];
+    o[18] = (float)(SU[5] - SU[7]);
+    o[19] = (float)(SU[6] - SU[2]);
+    o[20] = (float)(SU[1] - SU[3]);
+    o[21] = (float)((a == b) ? 0.0 : e[0]);
+    o[22] = 0.f;
+    o[23] = 0.f;
+  }
+}
+
+__global__ void k_absmax(const float* x, int64_t n, unsigned* out_bits) {
+  float m = 0.0f;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(x[t]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out_bits, __float_as_uint(m));
+}
+
+// Mean of the operand plane over the frames of each reference:
+// mean[k][c] = sum_{f in ref k} plane[f][c] / count_k, c over [0, 3*Np).
+__global__ void k_ref_mean(const float* plane, int64_t cols, const int* order, const int* offsets,
+                           float* mean) {
+  const int k = blockIdx.y;
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  const int lo = offsets[k], hi = offsets[k + 1];
+  double s = 0.0;
+  for (int n = lo; n < hi; ++n) s += (double)plane[(size_t)order[n] * cols + c];
+  mean[(size_t)k * cols + c] = (hi > lo) ? (float)(s / (double)(hi - lo)) : 0.0f;
+}
+
+// p_f -= mean[a(f)] (the residual relative to the refined reference).
+__global__ void k_shift(float* plane, int64_t F, int64_t cols, const int* assign, const float* mean) {
+  const int64_t total = F * cols;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = t / cols, c = t - f * cols;
+    plane[t] -= mean[(size_t)assign[f] * cols + c];
+  }
+}
+
+// r_k += mean_k / sqrt(w) (FP64), and the derived sqrt(w) r_k, sum w |r_k|^2.
+__global__ void __launch_bounds__(kPrepThreads) k_ref_update(double* refs, float* swr, double* Eref,
+                                                             const float* mean, const double* w, int N, int Np) {
+  __shared__ double red[32];
+  const int k = blockIdx.x;
+  double* r = refs + (size_t)k * 3 * N;
+  const float* m = mean + (size_t)k * 3 * Np;
+  double e = 0.0;
+  for (int a = threadIdx.x; a < N; a += blockDim.x) {
+    const double wa = w ? w[a] : 1.0;
+    const double sw = sqrt(wa);
+    for (int p = 0; p < 3; ++p) {
+      if (sw > 0.0) r[3 * a + p] += (double)m[(size_t)p * Np + a] / sw;
+      swr[((size_t)k * N + a) * 3 + p] = (float)(sw * r[3 * a + p]);
+    }
+    e += wa * (r[3 * a] * r[3 * a] + r[3 * a + 1] * r[3 * a + 1] + r[3 * a + 2] * r[3 * a + 2]);
+  }
+  double ev[1] = {e};
+  block_sum_f64<1>(ev, red);
+  if (threadIdx.x == 0) Eref[k] = ev[0];
 }
 
 // ---------------------------------------------------------------------------
@@ -402,6 +475,39 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
   k_align<T><<<grid, kPrepThreads, 0, st>>>(src, F, A.Np, A.cen, A.w, A.refs, A.assign, A.nofit, A.rot,
                                             A.plane, A.pmax_bits);
   ++launches;
+  // Refine every reference to the mean of its superposed frames: residuals
+  // shrink to each frame's own fluctuation.  Frames are grouped by reference
+  // with a host-side counting sort of the assignment.
+  {
+    std::vector<int> asg(F), order(F), offsets(K + 1, 0);
+    cudaMemcpyAsync(asg.data(), A.assign, sizeof(int) * F, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    for (int64_t f = 0; f < F; ++f) offsets[asg[f] + 1]++;
+    for (int k = 0; k < K; ++k) offsets[k + 1] += offsets[k];
+    std::vector<int> fill(offsets.begin(), offsets.end() - 1);
+    for (int64_t f = 0; f < F; ++f) order[fill[asg[f]]++] = (int)f;
+    cudaMemcpyAsync(A.order, order.data(), sizeof(int) * F, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(A.offsets, offsets.data(), sizeof(int) * (K + 1), cudaMemcpyHostToDevice, st);
+    const int64_t cols = 3 * (int64_t)A.Np;
+    dim3 g1((unsigned)((cols + 255) / 256), (unsigned)K);
+    k_ref_mean<<<g1, 256, 0, st>>>(A.plane, cols, A.order, A.offsets, A.mean);
+    const int g2 = (int)std::min<int64_t>((F * cols + 255) / 256, 152 * 16);
+    k_shift<<<g2, 256, 0, st>>>(A.plane, F, cols, A.assign, A.mean);
+    k_ref_update<<<K, kPrepThreads, 0, st>>>(A.refs, A.swr, A.Eref, A.mean, A.w, A.N, A.Np);
+    launches += 3;
+    // The copies above read host vectors that go out of scope: finish them.
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+  }
+  // max |p| after the shift (for the FP16 split scale)
+  cudaMemsetAsync(A.pmax_bits, 0, sizeof(unsigned), st);
+  {
+    const int64_t total = F * 3 * (int64_t)A.Np;
+    const int g3 = (int)std::min<int64_t>((total + 255) / 256, 152 * 16);
+    k_absmax<<<g3, 256, 0, st>>>(A.plane, total, A.pmax_bits);
+    ++launches;
+  }
   o.launches = launches;
   return cudaGetLastError();
 }
@@ -411,18 +517,18 @@ cudaError_t run_prep(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
 }
 
 cudaError_t run_split_f16(float* plane, int64_t F, int Np, float scale, void* hi, void* lo, cudaStream_t st) {
-  const int64_t total = F * (int64_t)Np;
+  const int64_t total = F * 3 * (int64_t)Np;
   const int grid = (int)std::min<int64_t>((total + 255) / 256, 152 * 16);
-  k_split_f16<<<grid, 256, 0, st>>>(plane, F, Np, scale, (__half*)hi, (__half*)lo);
+  k_split_f16<<<grid, 256, 0, st>>>(plane, total, scale, (__half*)hi, (__half*)lo);
   return cudaGetLastError();
 }
 
 cudaError_t run_terms(const float* plane, int64_t F, int Np, int N, const float* swr, int K, float* nrm,
-                      float* P, float* trP, const double* refs, const double* w, float* S, float* SA,
-                      float* SSd, cudaStream_t st) {
+                      float* P, float* trP, const double* refs, const double* w, int nofit, float* RP,
+                      cudaStream_t st) {
   const int grid = (int)std::min<int64_t>(F, 152 * 8);
   k_frame_terms<<<grid, kPrepThreads, 0, st>>>(plane, F, Np, N, swr, K, nrm, P, trP);
-  k_ref_terms<<<K * K, kPrepThreads, 0, st>>>(refs, N, K, w, S, SA, SSd);
+  k_ref_terms<<<K * K, kPrepThreads, 0, st>>>(refs, N, K, w, nofit, RP);
   return cudaGetLastError();
 }
 

@@ -136,7 +136,7 @@ typedef struct gbr_stats {
 int gbr_get_stats(const gbr_handle *h, gbr_stats *out);
 
 /* Tuning knobs (mostly for tests and benchmarks).  Keys:
- *   GBR_OPT_TAU          reference-selection radius in Angstrom (default 4.0)
+ *   GBR_OPT_TAU          reference-selection radius in Angstrom (default 6.0)
  *   GBR_OPT_MAX_REFS     maximum pre-alignment references (1..64, default 32)
  *   GBR_OPT_TOL          per-pair error target in Angstrom (default 5e-5)
  *   GBR_OPT_TIMING       1 = record per-kernel device times in gbr_stats

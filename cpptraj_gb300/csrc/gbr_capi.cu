@@ -399,7 +399,11 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     terms.K = K;
     terms.W = (float)Wsum;
     terms.tol = (float)h->tol;
-    terms.gemm_coef = tc ? 2.4e-7f : 1.2e-7f;
+    // FP32: 3-sigma random walk of half-ulp roundings (x2 margin).  TC: the
+    // FP16 hi+lo split represents each product to ~2^-22 (taken coherent),
+    // and tensor-memory accumulation is given four times the FP32 allowance.
+    terms.gem_s = tc ? 6.0e-7f : 1.2e-7f;
+    terms.gem_c = tc ? 4.8e-7f : 1.2e-7f;
     terms.epi_coef = 8e-7f;
     terms.sqrtN = std::sqrt((float)N);
     terms.nofit = nofit;

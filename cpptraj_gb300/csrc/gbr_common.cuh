@@ -165,7 +165,10 @@ struct FrameTerms {
   int K;
   float W;            // total weight
   float tol;          // per-pair tolerance (Angstrom)
-  float gemm_coef;    // contraction error coefficient (times sqrt(N)*sqrt(n_i n_j))
+  // A-priori bound of the contraction error in tr D (see pair_epilogue):
+  //   gem_s * sqrt(n_i n_j) + gem_c * sqrtN * |tr D|
+  float gem_s;        // sign-random part and the FP16 split (no growth with N)
+  float gem_c;        // consistently-signed accumulation (random walk of roundings)
   float epi_coef;     // epilogue rounding coefficient (times the Rayleigh-quotient terms)
   float sqrtN;
   int nofit;
@@ -328,7 +331,11 @@ static __device__ __noinline__ float pair_epilogue(const float D[9], int64_t i, 
       for (int q = 0; q < 3; ++q)
         Y[p * 3 + q] = U[p * 3] * X[q] + U[p * 3 + 1] * X[3 + q] + U[p * 3 + 2] * X[6 + q];
   }
-  const float gem = t.gemm_coef * t.sqrtN * sqrtf(fmaxf(ni, 0.0f) * fmaxf(nj, 0.0f));
+  // Contraction error: products of uncorrelated residuals sum with random
+  // signs (error ~ eps*sqrt(n_i n_j), independent of N), correlated ones with
+  // one sign (rounding errors random-walk: ~ eps*sqrt(N)*|tr D|).
+  const float gem = t.gem_s * sqrtf(fmaxf(ni, 0.0f) * fmaxf(nj, 0.0f)) +
+                    t.gem_c * t.sqrtN * fabsf(D[0] + D[4] + D[8]);
   if (t.nofit) {
     // RMSD_NoFit: sum w |x_i - x_j|^2 / W = 2*G00/W (references are not rotated).
     const float r = sqrtf(fmaxf(2.0f * G00 / W, 0.0f));
@@ -379,7 +386,7 @@ static __device__ __noinline__ float pair_epilogue(const float D[9], int64_t i, 
                      fabsf(t11) + 2.f * (fabsf(q1 * q2 * G12) + fabsf(q1 * q3 * G13) + fabsf(q2 * q3 * G23))) /
                     qq;
   const float r = sqrtf(fmaxf(2.0f * rq / W, 0.0f));
-  const float err = t.epi_coef * mag + 3.0f * gem;
+  const float err = t.epi_coef * mag + 2.0f * gem;
   *flag = !(err <= t.tol * W * fmaxf(r, 1e-3f));
   return r;
 }

@@ -84,6 +84,26 @@ def clustered(seed: int, n_frame: int, n_atom: int, n_centroid: int = 20, sigma:
     return np.ascontiguousarray(X.astype(dtype)), labels
 
 
+def md_like(seed: int, n_frame: int, n_atom: int, amp: float = 1.0, tau: float = 50.0,
+            dtype=np.float32, weighted: bool = False):
+    """Time-correlated trajectory: chain + an Ornstein-Uhlenbeck displacement
+    field (stationary amplitude ``amp`` per coordinate, correlation time
+    ``tau`` frames), each frame rotated and translated.  Consecutive frames
+    are near-duplicates, the hard case for cancellation in E0 - lambda."""
+    rng = np.random.default_rng(seed)
+    chain = random_walk(rng, n_atom)
+    a = np.exp(-1.0 / tau)
+    u = rng.standard_normal((n_atom, 3)) * amp
+    X = np.empty((n_frame, n_atom, 3))
+    for f in range(n_frame):
+        u = a * u + np.sqrt(1 - a * a) * amp * rng.standard_normal((n_atom, 3))
+        X[f] = chain + u
+    R = random_rotations(rng, n_frame)
+    X = np.einsum("fij,faj->fai", R, X) + rng.uniform(-20.0, 20.0, (n_frame, 1, 3))
+    m = masses(rng, n_atom) if weighted else None
+    return np.ascontiguousarray(X.astype(dtype)), m
+
+
 # Named workloads ---------------------------------------------------------------------------
 
 def workload_c0(seed: int = 0, n_frame: int = 500, n_atom: int = 304):

@@ -1,0 +1,152 @@
+// gbr_backward.cu -- gradient of L = sum_{i<j} g_ij RMSD_ij with respect to
+// every coordinate (K4).  cpptraj has no gradient of RMSD; this follows from
+// the envelope theorem: at the optimal rotation T (taking x'_j onto x'_i)
+//   dRMSD_ij/dx'_i[a] = w_a (x'_i[a] - T x'_j[a]) / (W RMSD_ij)
+//   dRMSD_ij/dx'_j[a] = w_a (x'_j[a] - T^T x'_i[a]) / (W RMSD_ij)
+// and centring contributes nothing because sum_a w_a (x'_i - T x'_j) = 0.
+// With x'_f = r + d_f (one pre-alignment reference) and c_fh = g_fh / RMSD_fh:
+//   dL/dx'_f[a] = (w_a / W) [ E_f r[a] + C_f d_f[a] - sum_h c_fh T_fh d_h[a] ]
+//   E_f = sum_h c_fh (I - T_fh),  C_f = sum_h c_fh.
+// The pair kernel (gbr_pair_fp32.cu, backward mode) recomputes every RMSD and
+// rotation and writes c*T blocks; here the blocks are symmetrised, the sum
+// over h runs as an FP32 GEMM Z = B * plane (plane = sqrt(w) d), and the
+// result is rotated back into each frame's original orientation,
+// dL/dx_f = R_f^T dL/dx'_f.
+#include "gbr_common.cuh"
+#include "gbr_internal.h"
+
+namespace gbr {
+
+namespace {
+
+// B := B + B^T for a square n x n matrix (in place), 32 x 32 tile pairs.
+__global__ void k_symmetrize(float* B, int64_t n) {
+  __shared__ float t1[32][33], t2[32][33];
+  const int64_t tiles = (n + 31) / 32;
+  // blockIdx.x enumerates tile pairs (ti <= tj)
+  const int64_t l = blockIdx.x;
+  const double b = 2.0 * (double)tiles + 1.0;
+  int64_t ti = (int64_t)((b - sqrt(b * b - 8.0 * (double)l)) * 0.5);
+  auto cum = [&](int64_t x) { return x * tiles - x * (x - 1) / 2; };
+  while (ti > 0 && cum(ti) > l) --ti;
+  while (cum(ti + 1) <= l) ++ti;
+  const int64_t tj = ti + (l - cum(ti));
+  const int x = threadIdx.x, y0 = threadIdx.y;  // 32 x 8 threads
+  for (int y = y0; y < 32; y += 8) {
+    const int64_t r1 = ti * 32 + y, c1 = tj * 32 + x;
+    const int64_t r2 = tj * 32 + y, c2 = ti * 32 + x;
+    t1[y][x] = (r1 < n && c1 < n) ? B[r1 * n + c1] : 0.f;
+    t2[y][x] = (r2 < n && c2 < n) ? B[r2 * n + c2] : 0.f;
+  }
+  __syncthreads();
+  for (int y = y0; y < 32; y += 8) {
+    const int64_t r1 = ti * 32 + y, c1 = tj * 32 + x;
+    const int64_t r2 = tj * 32 + y, c2 = ti * 32 + x;
+    if (ti == tj) {
+      if (r1 < n && c1 < n) B[r1 * n + c1] = t1[y][x] + t1[x][y];
+    } else {
+      if (r1 < n && c1 < n) B[r1 * n + c1] = t1[y][x] + t2[x][y];
+      if (r2 < n && c2 < n) B[r2 * n + c2] = t2[y][x] + t1[x][y];
+    }
+  }
+}
+
+// C[M x N] = A[M x K] * Bm[K x N], FP32, row-major.  128 x 128 tiles, 8-deep
+// K slabs, 256 threads with 8 x 8 outputs each.
+constexpr int GM = 128, GN = 128, GK = 8;
+__global__ void __launch_bounds__(256) k_sgemm(int64_t M, int64_t N, int64_t K, const float* __restrict__ A,
+                                               int64_t lda, const float* __restrict__ Bm, int64_t ldb,
+                                               float* __restrict__ C, int64_t ldc) {
+  __shared__ __align__(16) float As[GK][GM + 4];
+  __shared__ __align__(16) float Bs[GK][GN + 4];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int64_t m0 = (int64_t)blockIdx.y * GM, n0 = (int64_t)blockIdx.x * GN;
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+  const int ar = tid >> 1, ac = (tid & 1) * 4;   // A tile: 128 rows x 8 cols
+  const int br = tid >> 5, bc = (tid & 31) * 4;  // B tile: 8 rows x 128 cols
+  for (int64_t k0 = 0; k0 < K; k0 += GK) {
+    float av[4], bv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t r = m0 + ar, c = k0 + ac + u;
+      av[u] = (r < M && c < K) ? A[r * lda + c] : 0.f;
+      const int64_t rb = k0 + br, cb = n0 + bc + u;
+      bv[u] = (rb < K && cb < N) ? Bm[rb * ldb + cb] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 4; ++u) As[ac + u][ar] = av[u];
+    *reinterpret_cast<float4*>(&Bs[br][bc]) = make_float4(bv[0], bv[1], bv[2], bv[3]);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < GK; ++k) {
+      const float4 a0 = *reinterpret_cast<const float4*>(&As[k][ty * 4]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&As[k][64 + ty * 4]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[k][tx * 4]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&Bs[k][64 + tx * 4]);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int64_t r = m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
+    if (r >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int64_t c = n0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
+      if (c < N) C[r * ldc + c] = acc[i][j];
+    }
+  }
+}
+
+// dL/dx_f[a] = R_f^T (w_a E_f r[a] + sqrt(w_a) (C_f p_f[a] - Z_f[a])) / W
+__global__ void k_grad_final(int64_t F, int N, int Np, const float* E, const float* Cs, const double* rot,
+                             const double* r, const double* w, double W, const float* plane, const float* Z,
+                             float* grad) {
+  const int64_t total = F * (int64_t)N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = t / N;
+    const int a = (int)(t - f * N);
+    const double wa = w ? w[a] : 1.0;
+    const double sw = sqrt(wa);
+    const float* Ef = E + f * 9;
+    const double r0 = r[3 * a], r1 = r[3 * a + 1], r2 = r[3 * a + 2];
+    const double cf = Cs[f];
+    double gp[3];
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+      const double er = (double)Ef[p * 3] * r0 + (double)Ef[p * 3 + 1] * r1 + (double)Ef[p * 3 + 2] * r2;
+      const size_t row = (size_t)(3 * f + p);
+      gp[p] = (wa * er + sw * (cf * (double)plane[row * Np + a] - (double)Z[row * Np + a])) / W;
+    }
+    const double* R = rot + 9 * f;
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+      grad[t * 3 + q] = (float)(R[q] * gp[0] + R[3 + q] * gp[1] + R[6 + q] * gp[2]);
+  }
+}
+}  // namespace
+
+cudaError_t run_backward_tail(const BackwardTail& T, cudaStream_t st) {
+  const int64_t n = 3 * T.F;
+  const int64_t tiles = (n + 31) / 32;
+  k_symmetrize<<<(unsigned)(tiles * (tiles + 1) / 2), dim3(32, 8), 0, st>>>(T.B, n);
+  dim3 grid((unsigned)((T.Np + GN - 1) / GN), (unsigned)((n + GM - 1) / GM));
+  k_sgemm<<<grid, 256, 0, st>>>(n, T.Np, n, T.B, n, T.plane, T.Np, T.Z, T.Np);
+  const int64_t total = T.F * (int64_t)T.N;
+  const int g = (int)std::min<int64_t>((total + 255) / 256, 152 * 16);
+  k_grad_final<<<g, 256, 0, st>>>(T.F, T.N, T.Np, T.E, T.C, T.rot, T.ref0, T.w, T.W, T.plane, T.Z, T.grad);
+  return cudaGetLastError();
+}
+
+}  // namespace gbr

@@ -399,13 +399,14 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     terms.K = K;
     terms.W = (float)Wsum;
     terms.tol = (float)h->tol;
-    // FP32: 3-sigma random walk of half-ulp roundings (x2 margin).  TC: the
-    // FP16 hi+lo split represents each product to ~2^-22 (taken coherent),
-    // and tensor-memory accumulation is given four times the FP32 allowance.
+    // FP32 FMA accumulation: 3-sigma random walk of half-ulp roundings (x2
+    // margin), ~1.2e-7 sqrt(N) |tr D|.  Tensor memory: the FP16 hi+lo split
+    // represents each product to ~2^-22 (taken coherent), and accumulation
+    // measured on correlated frames behaves like truncation, about
+    // eps/2 per add over 3N/16 adds: ~5.6e-9 N |tr D|, bounded with x2 margin.
     terms.gem_s = tc ? 6.0e-7f : 1.2e-7f;
-    terms.gem_c = tc ? 4.8e-7f : 1.2e-7f;
+    terms.gem_c = tc ? 1.2e-8f * (float)N : 1.2e-7f * std::sqrt((float)N);
     terms.epi_coef = 8e-7f;
-    terms.sqrtN = std::sqrt((float)N);
     terms.nofit = nofit;
     if ((e = run_terms(pa.plane, F, Np, N, pa.swr, K, (float*)terms.nrm, (float*)terms.P, (float*)terms.trP,
                        pa.refs, d_w, nofit, (float*)terms.RP, st)) != cudaSuccess)
@@ -518,8 +519,194 @@ int gbr_allpairs_batched(gbr_handle* h, int32_t n_traj, const float* const* xyz,
 int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t n_atom, const double* mass,
                       const float* g, float* grad_xyz, float* rmsd_out) {
   if (!h) return GBR_ERR_ARG;
-  (void)xyz; (void)n_frame; (void)n_atom; (void)mass; (void)g; (void)grad_xyz; (void)rmsd_out;
-  return h->fail(GBR_ERR_UNSUPPORTED, "backward not built yet");
+  h->err.clear();
+  h->stats = gbr_stats{};
+  const auto t_start = std::chrono::steady_clock::now();
+  if (!xyz || !grad_xyz) return h->fail(GBR_ERR_ARG, "backward: xyz and grad_xyz must not be NULL");
+  if (n_atom < 1) return h->fail(GBR_ERR_ARG, "n_atom must be >= 1");
+  if (n_frame < 0 || n_frame > 60000) return h->fail(GBR_ERR_ARG, "backward supports 0..60000 frames");
+  if (cudaSetDevice(h->device) != cudaSuccess) return h->cuda_fail(cudaGetLastError(), "cudaSetDevice");
+  cudaStream_t st = h->stream;
+  const int N = n_atom;
+  const int64_t F = n_frame;
+  std::vector<double> w_h;
+  double Wsum = (double)N;
+  if (mass) {
+    w_h.resize(N);
+    if (cudaMemcpy(w_h.data(), mass, sizeof(double) * N, cudaMemcpyDefault) != cudaSuccess)
+      return h->cuda_fail(cudaGetLastError(), "reading mass");
+    Wsum = 0.0;
+    for (double v : w_h) Wsum += v;
+  }
+  if (Wsum < 1e-14) return h->fail(GBR_ERR_ZERO_MASS, "total mass %g is below 1e-14 (divide by zero)", Wsum);
+  const bool xyz_dev = is_device_ptr(xyz), grad_dev = is_device_ptr(grad_xyz);
+  const bool g_dev = g ? is_device_ptr(g) : false;
+  const bool r_dev = rmsd_out ? is_device_ptr(rmsd_out) : false;
+  const int64_t npairs = F * (F - 1) / 2;
+  if (F < 2) {
+    if (grad_dev) cudaMemsetAsync(grad_xyz, 0, sizeof(float) * 3 * N * F, st);
+    else std::memset(grad_xyz, 0, sizeof(float) * 3 * N * F);
+    cudaStreamSynchronize(st);
+    return GBR_OK;
+  }
+  const int Np = (N + 63) / 64 * 64;
+  auto layout = [&](Arena& A, void** p) {
+    p[0] = xyz_dev ? nullptr : A.take<float>((size_t)F * 3 * N);
+    p[1] = A.take<double>(N);                       // w
+    p[2] = A.take<double>(3 * F);                   // cen
+    p[3] = A.take<int64_t>(1);                      // fsel
+    p[4] = A.take<float>(1);                        // dmax
+    p[5] = A.take<float>(F);                        // dist
+    p[6] = A.take<int>(F);                          // assign
+    p[7] = A.take<double>(3 * (size_t)N);           // refs (one)
+    p[8] = A.take<float>(3 * (size_t)N);            // swr
+    p[9] = A.take<double>(1);                       // Eref
+    p[10] = A.take<double>(9 * (size_t)F);          // rot
+    p[11] = A.take<float>((size_t)F * 3 * Np);      // plane
+    p[12] = A.take<unsigned>(1);                    // pmax
+    p[13] = A.take<int>(F);                         // order
+    p[14] = A.take<int>(2);                         // offsets
+    p[15] = A.take<float>(3 * (size_t)Np);          // mean
+    p[16] = A.take<float>(F);                       // nrm
+    p[17] = A.take<float>(9 * (size_t)F);           // P
+    p[18] = A.take<float>(F);                       // trP
+    p[19] = A.take<float>(kRefPairStride);          // reference-pair table
+    p[20] = A.take<float>((size_t)9 * F * F);       // B
+    p[21] = A.take<float>(9 * (size_t)F);           // E
+    p[22] = A.take<float>(F);                       // C
+    p[23] = A.take<float>((size_t)3 * F * Np);      // Z
+    p[24] = (g && !g_dev) ? A.take<float>(npairs) : nullptr;
+    p[25] = (rmsd_out && !r_dev) ? A.take<float>(npairs) : nullptr;
+    p[26] = grad_dev ? nullptr : A.take<float>((size_t)F * 3 * N);
+    p[27] = A.take<unsigned long long>(1);          // flag count (unused list)
+  };
+  void* P[28];
+  Arena sizing;
+  layout(sizing, P);
+  if (!h->reserve(sizing.off + 256))
+    return h->fail(GBR_ERR_NOMEM, "cannot allocate %.2f GB of device workspace", (sizing.off + 256) / 1e9);
+  Arena A{h->ws, 0};
+  layout(A, P);
+  cudaError_t e;
+  const float* d_xyz = xyz_dev ? xyz : (const float*)P[0];
+  if (!xyz_dev) cudaMemcpyAsync(P[0], xyz, sizeof(float) * 3 * N * F, cudaMemcpyDefault, st);
+  double* d_w = mass ? (double*)P[1] : nullptr;
+  if (mass) cudaMemcpyAsync(d_w, w_h.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st);
+  const float* d_g = g ? (g_dev ? g : (const float*)P[24]) : nullptr;
+  if (g && !g_dev) cudaMemcpyAsync(P[24], g, sizeof(float) * npairs, cudaMemcpyDefault, st);
+  float* d_rmsd = rmsd_out ? (r_dev ? rmsd_out : (float*)P[25]) : nullptr;
+  float* d_grad = grad_dev ? grad_xyz : (float*)P[26];
+  if (h->timing) cudaEventRecord(h->ev[0], st);
+
+  PrepArgs pa{};
+  pa.dtype_f64 = 0;
+  pa.ref = d_xyz;
+  pa.n_ref = F;
+  pa.F = F;
+  pa.N = N;
+  pa.Np = Np;
+  pa.cmass_ref = pa.cmass_tgt = pa.w = d_w;
+  pa.Wsum = Wsum;
+  pa.tau = 1e30;
+  pa.max_refs = 1;
+  pa.cen = (double*)P[2];
+  pa.fsel = (int64_t*)P[3];
+  pa.dmax = (float*)P[4];
+  pa.dist = (float*)P[5];
+  pa.assign = (int*)P[6];
+  pa.refs = (double*)P[7];
+  pa.swr = (float*)P[8];
+  pa.Eref = (double*)P[9];
+  pa.rot = (double*)P[10];
+  pa.plane = (float*)P[11];
+  pa.pmax_bits = (unsigned*)P[12];
+  pa.order = (int*)P[13];
+  pa.offsets = (int*)P[14];
+  pa.mean = (float*)P[15];
+  PrepOut po;
+  if ((e = run_prep(pa, po, st)) != cudaSuccess) return h->cuda_fail(e, "prep");
+  int launches = po.launches;
+  FrameTerms terms{};
+  terms.assign = pa.assign;
+  terms.nrm = (float*)P[16];
+  terms.P = (float*)P[17];
+  terms.trP = (float*)P[18];
+  terms.RP = (float*)P[19];
+  terms.K = 1;
+  terms.W = (float)Wsum;
+  terms.tol = (float)h->tol;
+  terms.gem_s = 1.2e-7f;
+  terms.gem_c = 1.2e-7f * std::sqrt((float)N);
+  terms.epi_coef = 8e-7f;
+  terms.nofit = 0;
+  if ((e = run_terms(pa.plane, F, Np, N, pa.swr, 1, (float*)terms.nrm, (float*)terms.P, (float*)terms.trP,
+                     pa.refs, d_w, 0, (float*)terms.RP, st)) != cudaSuccess)
+    return h->cuda_fail(e, "frame terms");
+  launches += 2;
+  float* B = (float*)P[20];
+  cudaMemsetAsync(B, 0, sizeof(float) * 9 * F * F, st);
+  cudaMemsetAsync(P[21], 0, sizeof(float) * 9 * F, st);
+  cudaMemsetAsync(P[22], 0, sizeof(float) * F, st);
+  if (h->timing) cudaEventRecord(h->ev[1], st);
+  PairLaunch L{};
+  L.bwd.B = B;
+  L.bwd.ldB = 3 * F;
+  L.bwd.E = (float*)P[21];
+  L.bwd.C = (float*)P[22];
+  L.bwd.g = d_g;
+  L.bwd.rmsd = d_rmsd;
+  L.plane = pa.plane;
+  L.Np = Np;
+  L.N = N;
+  L.tgt0 = 0;
+  L.terms = terms;
+  OutMap map{};
+  map.n_ref = F;
+  map.n_tgt = F;
+  map.tri = 1;
+  map.row_begin = 0;
+  map.row_end = F;
+  L.map = map;
+  L.flags = FlagList{nullptr, (unsigned long long*)P[27], 0};
+  L.tiles = make_tiles(map, 64, 64);
+  if ((e = run_pairs_fp32(L, st)) != cudaSuccess) return h->cuda_fail(e, "backward pair kernel");
+  if (h->timing) cudaEventRecord(h->ev[2], st);
+  BackwardTail T{};
+  T.F = F;
+  T.N = N;
+  T.Np = Np;
+  T.B = B;
+  T.plane = pa.plane;
+  T.Z = (float*)P[23];
+  T.E = (float*)P[21];
+  T.C = (float*)P[22];
+  T.rot = pa.rot;
+  T.ref0 = pa.refs;
+  T.w = d_w;
+  T.W = Wsum;
+  T.grad = d_grad;
+  if ((e = run_backward_tail(T, st)) != cudaSuccess) return h->cuda_fail(e, "backward tail");
+  launches += 4;
+  if (h->timing) cudaEventRecord(h->ev[3], st);
+  if (!grad_dev) cudaMemcpyAsync(grad_xyz, d_grad, sizeof(float) * 3 * N * F, cudaMemcpyDefault, st);
+  if (rmsd_out && !r_dev) cudaMemcpyAsync(rmsd_out, d_rmsd, sizeof(float) * npairs, cudaMemcpyDefault, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return h->cuda_fail(e, "backward");
+  h->stats.pairs = npairs;
+  h->stats.n_refs = 1;
+  h->stats.precision = GBR_PREC_FP32;
+  h->stats.kernel_launches = launches;
+  if (h->timing) {
+    float a = 0, b = 0, c = 0;
+    cudaEventElapsedTime(&a, h->ev[0], h->ev[1]);
+    cudaEventElapsedTime(&b, h->ev[1], h->ev[2]);
+    cudaEventElapsedTime(&c, h->ev[2], h->ev[3]);
+    h->stats.ms_prep = a;
+    h->stats.ms_pairs = b;
+    h->stats.ms_fixup = c;
+  }
+  h->stats.ms_total =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+  return GBR_OK;
 }
 
 }  // extern "C"

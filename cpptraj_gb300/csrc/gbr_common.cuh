@@ -166,11 +166,12 @@ struct FrameTerms {
   float W;            // total weight
   float tol;          // per-pair tolerance (Angstrom)
   // A-priori bound of the contraction error in tr D (see pair_epilogue):
-  //   gem_s * sqrt(n_i n_j) + gem_c * sqrtN * |tr D|
+  //   gem_s * sqrt(n_i n_j) + gem_c * |tr D|
   float gem_s;        // sign-random part and the FP16 split (no growth with N)
-  float gem_c;        // consistently-signed accumulation (random walk of roundings)
+  float gem_c;        // consistently-signed accumulation, already scaled by N:
+                      //   FP32 FMA (round to nearest): random walk, ~sqrt(N)
+                      //   tensor memory (measured to behave like truncation): ~N
   float epi_coef;     // epilogue rounding coefficient (times the Rayleigh-quotient terms)
-  float sqrtN;
   int nofit;
 };
 
@@ -278,8 +279,11 @@ __device__ inline void qcp_vec_f32(const float M[9], float E0, float q[4]) {
 //   G00 = 1/2 sum w |x'_i - U_ab x'_j|^2
 //       = 1/2 (SS_ab + n_i + n_j) + trP_ia - <U,P_ib> - <U,P_ja^T> + trP_jb - tr(U D_ji)
 // (for a == b: U = I and G00 = 1/2 (n_i + n_j) - tr D_ji).
+// qout (optional) receives the unit quaternion (QCP convention) of the
+// optimal superposition of x'_j onto x'_i, i.e. x'_i ~ R(q)^T x'_j with R(q)
+// the rotation matrix QCP builds from q; only meaningful when t.K == 1.
 static __device__ __noinline__ float pair_epilogue(const float D[9], int64_t i, int64_t j, const FrameTerms& t,
-                                                   bool* flag) {
+                                                   bool* flag, float* qout = nullptr) {
   const int K = t.K;
   const int a = (K > 1) ? __ldg(t.assign + i) : 0;
   const int b = (K > 1) ? __ldg(t.assign + j) : 0;
@@ -334,8 +338,7 @@ static __device__ __noinline__ float pair_epilogue(const float D[9], int64_t i, 
   // Contraction error: products of uncorrelated residuals sum with random
   // signs (error ~ eps*sqrt(n_i n_j), independent of N), correlated ones with
   // one sign (rounding errors random-walk: ~ eps*sqrt(N)*|tr D|).
-  const float gem = t.gem_s * sqrtf(fmaxf(ni, 0.0f) * fmaxf(nj, 0.0f)) +
-                    t.gem_c * t.sqrtN * fabsf(D[0] + D[4] + D[8]);
+  const float gem = t.gem_s * sqrtf(fmaxf(ni, 0.0f) * fmaxf(nj, 0.0f)) + t.gem_c * fabsf(D[0] + D[4] + D[8]);
   if (t.nofit) {
     // RMSD_NoFit: sum w |x_i - x_j|^2 / W = 2*G00/W (references are not rotated).
     const float r = sqrtf(fmaxf(2.0f * G00 / W, 0.0f));
@@ -388,6 +391,11 @@ static __device__ __noinline__ float pair_epilogue(const float D[9], int64_t i, 
   const float r = sqrtf(fmaxf(2.0f * rq / W, 0.0f));
   const float err = t.epi_coef * mag + 2.0f * gem;
   *flag = !(err <= t.tol * W * fmaxf(r, 1e-3f));
+  if (qout) {
+    const float inv = rsqrtf(qq);
+    const float sgn = (q0 < 0.0f) ? -inv : inv;
+    qout[0] = q0 * sgn; qout[1] = q1 * sgn; qout[2] = q2 * sgn; qout[3] = q3 * sgn;
+  }
   return r;
 }
 

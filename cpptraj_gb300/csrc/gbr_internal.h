@@ -64,7 +64,18 @@ struct TileSpace {
 
 TileSpace make_tiles(const OutMap& m, int bm, int bn);
 
+// Backward-mode outputs of the FP32 pair kernel (nullptr B = forward mode).
+struct BwdArgs {
+  float* B;          // [3F][3F], upper pair blocks c*T (row 3i+p, column 3j+q, i < j)
+  int64_t ldB;       // 3F
+  float* E;          // [F][9] sum_h c_fh (I - T_fh)
+  float* C;          // [F]    sum_h c_fh
+  const float* g;    // TRI upstream weights (nullptr = 1)
+  float* rmsd;       // TRI forward values (nullptr = not stored)
+};
+
 struct PairLaunch {
+  BwdArgs bwd;
   const float* plane;  // FP32 plane [F][3][Np]
   int Np, N;
   int64_t tgt0;        // set index of target frame 0
@@ -96,6 +107,23 @@ struct TcLaunch {
 cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st);
 int tc_supported(int device);
 int64_t tc_max_tiles(const OutMap& m);
+
+// Backward tail: symmetrise B, Z = B * plane, assemble and rotate the gradient.
+struct BackwardTail {
+  int64_t F;
+  int N, Np;
+  float* B;            // [3F][3F]
+  const float* plane;  // [F][3][Np]  (= [3F][Np])
+  float* Z;            // [3F][Np]
+  const float* E;      // [F][9]
+  const float* C;      // [F]
+  const double* rot;   // [F][9] pre-alignment rotations
+  const double* ref0;  // [N][3] the (single) pre-alignment reference
+  const double* w;     // masses or nullptr
+  double W;
+  float* grad;         // [F][N][3]
+};
+cudaError_t run_backward_tail(const BackwardTail& T, cudaStream_t st);
 
 // Direct FP64 recomputation (flagged pairs or every pair).
 struct ExactLaunch {

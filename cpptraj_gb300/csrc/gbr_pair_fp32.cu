@@ -51,6 +51,7 @@ __device__ __forceinline__ void load_slab(float* dst, const float* plane, int64_
   }
 }
 
+template <bool BWD>
 __global__ void __launch_bounds__(THREADS, 1) k_pairs_fp32(PairLaunch L) {
   extern __shared__ __align__(16) float smem[];
   const int tid = threadIdx.x;
@@ -149,22 +150,86 @@ __global__ void __launch_bounds__(THREADS, 1) k_pairs_fp32(PairLaunch L) {
     }
   __syncthreads();
 
+  if constexpr (!BWD) {
 #pragma unroll 1
-  for (int r = 0; r < (BM * BN) / THREADS; ++r) {
-    const int fast = tid & 63, slow = (tid >> 6) + 4 * r;
-    const int il = tri ? slow : fast, jl = tri ? fast : slow;
-    const int64_t i = i0 + il, jt = jt0 + jl;
-    if (i >= i_end || jt >= jt_end) continue;
-    const int64_t idx = out_index(L.map, i, jt);
-    if (idx < 0) continue;
-    const int slot = tri ? (il * BN + jl) : (jl * BM + il);
-    float D[9];
+    for (int r = 0; r < (BM * BN) / THREADS; ++r) {
+      const int fast = tid & 63, slow = (tid >> 6) + 4 * r;
+      const int il = tri ? slow : fast, jl = tri ? fast : slow;
+      const int64_t i = i0 + il, jt = jt0 + jl;
+      if (i >= i_end || jt >= jt_end) continue;
+      const int64_t idx = out_index(L.map, i, jt);
+      if (idx < 0) continue;
+      const int slot = tri ? (il * BN + jl) : (jl * BM + il);
+      float D[9];
 #pragma unroll
-    for (int c = 0; c < 9; ++c) D[c] = Ds[slot * 9 + c];
-    bool flag = false;
-    const float rm = pair_epilogue(D, i, L.tgt0 + jt, L.terms, &flag);
-    if (flag) flag_pair(L.flags, i, jt);
-    L.map.out[idx] = rm;
+      for (int c = 0; c < 9; ++c) D[c] = Ds[slot * 9 + c];
+      bool flag = false;
+      const float rm = pair_epilogue(D, i, L.tgt0 + jt, L.terms, &flag);
+      if (flag) flag_pair(L.flags, i, jt);
+      L.map.out[idx] = rm;
+    }
+  } else {
+    // Backward epilogue (one frame set, TRI).  For pair (i < j) with weight
+    // c = g_ij / RMSD_ij and T = rotation taking x'_j onto x'_i:
+    //   B[3i+p][3j+q] = c T[p][q]   (the lower block is added by transposition later)
+    //   E_i += c (I - T),  E_j += c (I - T^T),  C_i += c,  C_j += c.
+    // I - T comes straight from the quaternion, so it is accurate when T ~ I.
+    __shared__ float Erow[BM][10], Ecol[BN][10];
+    for (int k = tid; k < BM * 10; k += THREADS) (&Erow[0][0])[k] = 0.f;
+    for (int k = tid; k < BN * 10; k += THREADS) (&Ecol[0][0])[k] = 0.f;
+    __syncthreads();
+    const BwdArgs& bw = L.bwd;
+#pragma unroll 1
+    for (int r = 0; r < (BM * BN) / THREADS; ++r) {
+      const int jl = tid & 63, il = (tid >> 6) + 4 * r;
+      const int64_t i = i0 + il, j = jt0 + jl;
+      if (i >= i_end || j >= jt_end || !(j > i)) continue;
+      const int slot = il * BN + jl;
+      float D[9];
+#pragma unroll
+      for (int c = 0; c < 9; ++c) D[c] = Ds[slot * 9 + c];
+      bool flag = false;
+      float q[4];
+      const float rm = pair_epilogue(D, i, j, L.terms, &flag, q);
+      const int64_t t = tri_index(L.map.n_ref, i, j);
+      if (bw.rmsd) bw.rmsd[t] = rm;
+      const float gij = bw.g ? bw.g[t] : 1.0f;
+      const float c = (rm > 1e-6f) ? gij / rm : 0.0f;
+      const float a = q[0], x = q[1], y = q[2], z = q[3];
+      // QCP rotation R(q) (row-major); T = R^T.
+      const float R0 = a * a + x * x - y * y - z * z, R1 = 2.f * (x * y + a * z), R2 = 2.f * (z * x - a * y);
+      const float R3 = 2.f * (x * y - a * z), R4 = a * a - x * x + y * y - z * z, R5 = 2.f * (y * z + a * x);
+      const float R6 = 2.f * (z * x + a * y), R7 = 2.f * (y * z - a * x), R8 = a * a - x * x - y * y + z * z;
+      float* Bi = bw.B + (size_t)(3 * i) * bw.ldB + 3 * j;
+      Bi[0] = c * R0; Bi[1] = c * R3; Bi[2] = c * R6;
+      Bi += bw.ldB;
+      Bi[0] = c * R1; Bi[1] = c * R4; Bi[2] = c * R7;
+      Bi += bw.ldB;
+      Bi[0] = c * R2; Bi[1] = c * R5; Bi[2] = c * R8;
+      const float d00 = 2.f * (y * y + z * z), d11 = 2.f * (x * x + z * z), d22 = 2.f * (x * x + y * y);
+      // E_i += c (I - R^T);  E_j += c (I - R)
+      atomicAdd(&Erow[il][0], c * d00); atomicAdd(&Erow[il][1], -c * R3); atomicAdd(&Erow[il][2], -c * R6);
+      atomicAdd(&Erow[il][3], -c * R1); atomicAdd(&Erow[il][4], c * d11); atomicAdd(&Erow[il][5], -c * R7);
+      atomicAdd(&Erow[il][6], -c * R2); atomicAdd(&Erow[il][7], -c * R5); atomicAdd(&Erow[il][8], c * d22);
+      atomicAdd(&Erow[il][9], c);
+      atomicAdd(&Ecol[jl][0], c * d00); atomicAdd(&Ecol[jl][1], -c * R1); atomicAdd(&Ecol[jl][2], -c * R2);
+      atomicAdd(&Ecol[jl][3], -c * R3); atomicAdd(&Ecol[jl][4], c * d11); atomicAdd(&Ecol[jl][5], -c * R5);
+      atomicAdd(&Ecol[jl][6], -c * R6); atomicAdd(&Ecol[jl][7], -c * R7); atomicAdd(&Ecol[jl][8], c * d22);
+      atomicAdd(&Ecol[jl][9], c);
+    }
+    __syncthreads();
+    for (int k = tid; k < BM * 10; k += THREADS) {
+      const int fl = k / 10, e = k % 10;
+      const int64_t f = i0 + fl;
+      const float v = Erow[fl][e];
+      if (f < i_end && v != 0.f) atomicAdd(e < 9 ? &bw.E[f * 9 + e] : &bw.C[f], v);
+    }
+    for (int k = tid; k < BN * 10; k += THREADS) {
+      const int fl = k / 10, e = k % 10;
+      const int64_t f = jt0 + fl;
+      const float v = Ecol[fl][e];
+      if (f < jt_end && v != 0.f) atomicAdd(e < 9 ? &bw.E[f * 9 + e] : &bw.C[f], v);
+    }
   }
 }
 }  // namespace
@@ -198,9 +263,16 @@ TileSpace make_tiles(const OutMap& m, int bm, int bn) {
 
 cudaError_t run_pairs_fp32(const PairLaunch& L, cudaStream_t st) {
   if (L.tiles.count == 0) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(k_pairs_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-  if (e != cudaSuccess) return e;
-  k_pairs_fp32<<<(unsigned)L.tiles.count, THREADS, SMEM_BYTES, st>>>(L);
+  cudaError_t e;
+  if (L.bwd.B) {
+    e = cudaFuncSetAttribute(k_pairs_fp32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    k_pairs_fp32<true><<<(unsigned)L.tiles.count, THREADS, SMEM_BYTES, st>>>(L);
+  } else {
+    e = cudaFuncSetAttribute(k_pairs_fp32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    k_pairs_fp32<false><<<(unsigned)L.tiles.count, THREADS, SMEM_BYTES, st>>>(L);
+  }
   return cudaGetLastError();
 }
 

@@ -56,6 +56,13 @@ def lib():
                                     ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                     ctypes.c_void_p, ctypes.c_int]
         L.orc_max_threads.restype = ctypes.c_int
+        L.orc_grad_f64.restype = ctypes.c_int
+        L.orc_grad_f64.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        L.orc_fd_f64.restype = ctypes.c_double
+        L.orc_fd_f64.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p,
+                                 ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                 ctypes.c_int]
         _lib = L
     return _lib
 
@@ -174,3 +181,25 @@ def pairs_f64(xyz, pi, pj, mass=None, mode=FIT, nthreads=0, use_reference_code=F
 
 def tri_index(n, i, j):
     return n * i - ((i + 1) * i) // 2 + j - i - 1
+
+
+def grad_f64(xyz, mass=None, g=None, nthreads=0):
+    """Analytic FP64 gradient of L = sum_{i<j} g_ij RMSD_ij (xyz float32)."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float32)
+    if mass is not None:
+        mass = np.ascontiguousarray(mass, dtype=np.float64)
+    if g is not None:
+        g = np.ascontiguousarray(g, dtype=np.float32)
+    out = np.zeros(xyz.shape, np.float64)
+    lib().orc_grad_f64(_p(xyz), xyz.shape[0], xyz.shape[1], _p(mass), _p(g), _p(out), nthreads)
+    return out
+
+
+def fd_f64(xyz, f, a, p, h=1e-3, mass=None, g=None, nthreads=0):
+    """Central finite difference dL/dxyz[f, a, p] with step h (FP64 arithmetic)."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float32)
+    if mass is not None:
+        mass = np.ascontiguousarray(mass, dtype=np.float64)
+    if g is not None:
+        g = np.ascontiguousarray(g, dtype=np.float32)
+    return lib().orc_fd_f64(_p(xyz), xyz.shape[0], xyz.shape[1], _p(mass), _p(g), f, a, p, h, nthreads)

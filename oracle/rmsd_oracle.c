@@ -415,3 +415,180 @@ int orc_max_threads(void) {
   return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------------ */
+/* Gradient oracle (cpptraj has no RMSD gradient; these are the checks for  */
+/* gbr_rmsd_backward).  L = sum_{i<j} g_ij RMSD_ij over one frame set.       */
+/* ------------------------------------------------------------------------ */
+
+/* Optimal proper rotation R (row-major) with R*t ~ r for centred t, r, from */
+/* the QCP key matrix's top eigenvector (Newton on the quartic, then the     */
+/* adjugate column of largest norm).  Returns lambda.                        */
+static double qcp_rotation(const double *A, double E0, double *R) {
+  double xx = A[0], xy = A[1], xz = A[2], yx = A[3], yy = A[4], yz = A[5], zx = A[6], zy = A[7], zz = A[8];
+  double K[16] = {xx + yy + zz, yz - zy, zx - xz, xy - yx,
+                  yz - zy, xx - yy - zz, xy + yx, zx + xz,
+                  zx - xz, xy + yx, -xx + yy - zz, yz + zy,
+                  xy - yx, zx + xz, yz + zy, -xx - yy + zz};
+  /* largest eigenvalue by Newton on det(K - l I) starting from E0 */
+  double xx2 = xx * xx, yy2 = yy * yy, zz2 = zz * zz, xy2 = xy * xy, yz2 = yz * yz, xz2 = xz * xz;
+  double yx2 = yx * yx, zy2 = zy * zy, zx2 = zx * zx;
+  double c2 = -2.0 * (xx2 + yy2 + zz2 + xy2 + yx2 + xz2 + zx2 + yz2 + zy2);
+  double c1 = 8.0 * (xx * yz * zy + yy * zx * xz + zz * xy * yx - xx * yy * zz - yz * zx * xy - zy * yx * xz);
+  double t1 = 2.0 * (yz * zy - yy * zz), t2 = yy2 + zz2 - xx2 + yz2 + zy2, t3 = xy2 + xz2 - yx2 - zx2;
+  double pxz = xz + zx, pyz = yz + zy, pxy = xy + yx, myz = yz - zy, mxz = xz - zx, mxy = xy - yx;
+  double pxx = xx + yy, mxx = xx - yy;
+  double c0 = t3 * t3 + (t2 + t1) * (t2 - t1)
+            + (-pxz * myz + mxy * (mxx - zz)) * (-mxz * pyz + mxy * (mxx + zz))
+            + (-pxz * pyz - pxy * (pxx - zz)) * (-mxz * myz - pxy * (pxx + zz))
+            + (pxy * pyz + pxz * (mxx + zz)) * (-mxy * myz + pxz * (pxx + zz))
+            + (pxy * myz + mxz * (mxx - zz)) * (-mxy * pyz + mxz * (pxx - zz));
+  double lam = E0;
+  for (int it = 0; it < 100; ++it) {
+    double prev = lam, l2 = lam * lam, b = (l2 + c2) * lam, a = b + c1;
+    double den = 2.0 * l2 * lam + b + a;
+    if (den == 0.0) break;
+    lam -= (a * lam + c0) / den;
+    if (fabs(lam - prev) < fabs(1e-14 * lam)) break;
+  }
+  double q[4] = {1, 0, 0, 0}, best = -1.0;
+  for (int col = 0; col < 4; ++col) {
+    double c[4];
+    for (int r = 0; r < 4; ++r) {
+      int rr[3], cc[3], nr = 0, nc = 0;
+      for (int k = 0; k < 4; ++k) {
+        if (k != r) rr[nr++] = k;
+        if (k != col) cc[nc++] = k;
+      }
+      double m[9];
+      for (int u = 0; u < 3; ++u)
+        for (int v = 0; v < 3; ++v) m[3 * u + v] = K[rr[u] * 4 + cc[v]] - ((rr[u] == cc[v]) ? lam : 0.0);
+      double det = m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+                   m[2] * (m[3] * m[7] - m[4] * m[6]);
+      c[r] = ((r + col) & 1) ? -det : det;
+    }
+    double n2 = c[0] * c[0] + c[1] * c[1] + c[2] * c[2] + c[3] * c[3];
+    if (n2 > best) { best = n2; memcpy(q, c, sizeof q); }
+  }
+  double inv = 1.0 / sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  double a = q[0] * inv, b = q[1] * inv, c = q[2] * inv, d = q[3] * inv;
+  /* QCP's matrix for q, transposed so that R * t ~ r */
+  R[0] = a * a + b * b - c * c - d * d; R[3] = 2 * (b * c + a * d); R[6] = 2 * (d * b - a * c);
+  R[1] = 2 * (b * c - a * d); R[4] = a * a - b * b + c * c - d * d; R[7] = 2 * (c * d + a * b);
+  R[2] = 2 * (d * b + a * c); R[5] = 2 * (c * d - a * b); R[8] = a * a - b * b - c * c + d * d;
+  return lam;
+}
+
+static void centre_copy(const float *src, int n, const double *mass, double *dst) {
+  for (int k = 0; k < 3 * n; ++k) dst[k] = (double)src[k];
+  double c[3];
+  orc_center(dst, n, mass, c);
+  for (int a = 0; a < n; ++a) { dst[3 * a] -= c[0]; dst[3 * a + 1] -= c[1]; dst[3 * a + 2] -= c[2]; }
+}
+
+/* Analytic FP64 gradient: grad[f][a][p] (double), xyz float32. */
+int orc_grad_f64(const float *xyz, int64_t F, int n, const double *mass, const float *g, double *grad,
+                 int nthreads) {
+  double W = 0.0;
+  for (int a = 0; a < n; ++a) W += mass ? mass[a] : 1.0;
+  memset(grad, 0, sizeof(double) * 3 * (size_t)n * F);
+  double *Y = (double *)malloc(sizeof(double) * 3 * (size_t)n * F);
+  for (int64_t f = 0; f < F; ++f) centre_copy(xyz + (size_t)f * 3 * n, n, mass, Y + (size_t)f * 3 * n);
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel
+#endif
+  {
+    double *acc = (double *)calloc(3 * (size_t)n * F, sizeof(double));
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic)
+#endif
+    for (int64_t i = 0; i < F; ++i) {
+      const double *yi = Y + (size_t)i * 3 * n;
+      for (int64_t j = i + 1; j < F; ++j) {
+        const double *yj = Y + (size_t)j * 3 * n;
+        double A[9] = {0}, ss = 0.0;
+        for (int a = 0; a < n; ++a) {
+          double w = mass ? mass[a] : 1.0;
+          for (int p = 0; p < 3; ++p)
+            for (int q = 0; q < 3; ++q) A[3 * p + q] += w * yj[3 * a + p] * yi[3 * a + q];
+          for (int p = 0; p < 3; ++p) ss += w * (yi[3 * a + p] * yi[3 * a + p] + yj[3 * a + p] * yj[3 * a + p]);
+        }
+        double R[9];
+        qcp_rotation(A, 0.5 * ss, R);
+        /* residuals e = y_i - R y_j, rmsd from them */
+        double s2 = 0.0;
+        for (int a = 0; a < n; ++a) {
+          double w = mass ? mass[a] : 1.0;
+          for (int p = 0; p < 3; ++p) {
+            double e = yi[3 * a + p] - (R[3 * p] * yj[3 * a] + R[3 * p + 1] * yj[3 * a + 1] + R[3 * p + 2] * yj[3 * a + 2]);
+            s2 += w * e * e;
+          }
+        }
+        double rmsd = sqrt(s2 / W);
+        if (!(rmsd > 1e-12)) continue;
+        double gij = g ? (double)g[orc_tri_index(F, i, j)] : 1.0;
+        double c = gij / (W * rmsd);
+        double *gi = acc + (size_t)i * 3 * n, *gj = acc + (size_t)j * 3 * n;
+        for (int a = 0; a < n; ++a) {
+          double w = mass ? mass[a] : 1.0;
+          double e[3];
+          for (int p = 0; p < 3; ++p)
+            e[p] = yi[3 * a + p] - (R[3 * p] * yj[3 * a] + R[3 * p + 1] * yj[3 * a + 1] + R[3 * p + 2] * yj[3 * a + 2]);
+          for (int p = 0; p < 3; ++p) {
+            gi[3 * a + p] += c * w * e[p];
+            gj[3 * a + p] -= c * w * (R[p] * e[0] + R[3 + p] * e[1] + R[6 + p] * e[2]);
+          }
+        }
+      }
+    }
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+    for (size_t k = 0; k < 3 * (size_t)n * F; ++k) grad[k] += acc[k];
+    free(acc);
+  }
+  free(Y);
+  return 0;
+}
+
+/* Central finite difference of L with respect to xyz[f][a][p]: only the pairs */
+/* containing frame f change.  All arithmetic in FP64.                          */
+double orc_fd_f64(const float *xyz, int64_t F, int n, const double *mass, const float *g, int64_t f, int a,
+                  int p, double h, int nthreads) {
+  double total = 0.0;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel reduction(+ : total)
+#endif
+  {
+    double *R = (double *)malloc(sizeof(double) * 3 * (size_t)n);
+    double *T = (double *)malloc(sizeof(double) * 3 * (size_t)n);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 16)
+#endif
+    for (int64_t o = 0; o < F; ++o) {
+      if (o == f) continue;
+      double gw = g ? (double)g[o < f ? orc_tri_index(F, o, f) : orc_tri_index(F, f, o)] : 1.0;
+      double val[2];
+      for (int s = 0; s < 2; ++s) {
+        for (int k = 0; k < 3 * n; ++k) R[k] = (double)xyz[(size_t)o * 3 * n + k];
+        for (int k = 0; k < 3 * n; ++k) T[k] = (double)xyz[(size_t)f * 3 * n + k];
+        T[3 * a + p] += (s == 0) ? h : -h;
+        double c[3];
+        orc_center(R, n, mass, c);
+        for (int b = 0; b < n; ++b) { R[3 * b] -= c[0]; R[3 * b + 1] -= c[1]; R[3 * b + 2] -= c[2]; }
+        double A[9], E0;
+        double W = target_moments(R, T, n, mass, A, &E0);
+        double Rm[9];
+        double lam = qcp_rotation(A, E0, Rm);
+        double e = E0 - lam;
+        val[s] = (e < 0.0) ? 0.0 : sqrt(2.0 * e / W);
+      }
+      total += gw * (val[0] - val[1]) / (2.0 * h);
+    }
+    free(R);
+    free(T);
+  }
+  return total;
+}

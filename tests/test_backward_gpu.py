@@ -1,0 +1,67 @@
+"""Backward (gbr_rmsd_backward and the torch.autograd.Function) against the
+FP64 oracle gradient and central finite differences (h = 1e-3 Angstrom).
+Tolerance: 1e-5 relative (normwise against the FP64 gradient, and per
+coordinate against finite differences where |dL/dx| is not tiny)."""
+import numpy as np
+import pytest
+
+import oracle
+from cpptraj_gb300 import gbrmsd, synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def h():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    hd = gbrmsd.Handle(0)
+    yield hd
+    hd.close()
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+def test_gradient_matches_fp64(h, weighted):
+    X, m = synth.trajectory(4, 96, 180, 1.0, 1.0, np.float32, weighted)
+    rng = np.random.default_rng(1)
+    g = rng.uniform(0.5, 1.5, 96 * 95 // 2).astype(np.float32)
+    grad = h.backward(X, mass=m, g=g)
+    ref = oracle.grad_f64(X, mass=m, g=g)
+    err = np.abs(grad - ref).max() / np.abs(ref).max()
+    assert err <= 1e-5, err
+
+
+def test_gradient_matches_finite_differences(h):
+    X, m = synth.trajectory(40, 128, 300, 1.0, 1.0, np.float32, False)
+    grad = h.backward(X)
+    rng = np.random.default_rng(2)
+    gmax = np.abs(grad).max()
+    worst = 0.0
+    for _ in range(64):
+        f, a, p = int(rng.integers(0, 128)), int(rng.integers(0, 300)), int(rng.integers(0, 3))
+        fd = oracle.fd_f64(X, f, a, p, 1e-3)
+        worst = max(worst, abs(grad[f, a, p] - fd) / max(abs(fd), 1e-3 * gmax))
+    assert worst <= 1e-5, worst
+
+
+def test_forward_output_of_backward(h):
+    X, _ = synth.trajectory(41, 70, 90, 0.5, 1.5, np.float32, False)
+    r = np.zeros(70 * 69 // 2, np.float32)
+    h.backward(X, rmsd_out=r)
+    ref = oracle.allpairs_f64(X)
+    assert np.abs(r - ref).max() <= 1e-4
+
+
+def test_autograd_function():
+    torch = pytest.importorskip("torch")
+    from cpptraj_gb300.torch_ext import allpairs_rmsd
+    X, _ = synth.trajectory(42, 64, 120, 1.0, 1.0, np.float32, False)
+    x = torch.from_numpy(X).cuda().requires_grad_(True)
+    tri = allpairs_rmsd(x, precision="fp32")
+    w = torch.linspace(0.5, 1.5, tri.numel(), device="cuda")
+    (tri * w).sum().backward()
+    ref = oracle.grad_f64(X, g=w.cpu().numpy())
+    err = np.abs(x.grad.cpu().numpy() - ref).max() / np.abs(ref).max()
+    assert err <= 1e-5, err
+    np.testing.assert_allclose(tri.detach().cpu().numpy(), oracle.allpairs_f64(X), atol=1e-4)

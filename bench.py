@@ -39,7 +39,30 @@ def parse():
     ap.add_argument("--frames", type=int, default=N_FRAME)
     ap.add_argument("--atoms", type=int, default=N_ATOM)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--profile", action="store_true",
+                    help="warm up, then run exactly one all-pairs call (for ncu); prints stats only")
     return ap.parse_args()
+
+
+def main_profile(args):
+    """--warmup calls then one call of the workload, nothing else on the GPU."""
+    import torch
+
+    from cpptraj_gb300 import gbrmsd
+
+    X, m = make_workload(args.frames, args.atoms, 1)
+    pairs = X.shape[0] * (X.shape[0] - 1) // 2
+    h = gbrmsd.Handle(0)
+    prec = "tc" if args.precision == "auto" else args.precision
+    dX = torch.from_numpy(X).cuda()
+    out = torch.empty(pairs, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        h.allpairs(dX, tgt_mass=m, precision=prec, out=out)
+    torch.cuda.synchronize()
+    h.set_option(gbrmsd.OPT_TIMING, 1)
+    h.allpairs(dX, tgt_mass=m, precision=prec, out=out)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_call": h.stats(), "frames": X.shape[0], "atoms": X.shape[1], "precision": prec}))
 
 
 def dist_env():
@@ -192,6 +215,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return main_reference(args)
+    if args.profile:
+        return main_profile(args)
     import torch
     import torch.distributed as dist
 

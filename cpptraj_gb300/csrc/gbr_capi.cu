@@ -266,7 +266,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     p[10] = A.take<float>((size_t)Kmax * 3 * N);  // swr
     p[11] = A.take<double>(Kmax);                 // Eref
     p[12] = need_planes ? A.take<float>((size_t)F * 3 * Np) : nullptr;  // plane
-    p[13] = A.take<unsigned>(1);                                        // pmax
+    p[13] = A.take<float>(F);                                           // per-frame 1/scale
     p[14] = A.take<float>(F);                                           // nrm
     p[15] = A.take<float>((size_t)F * Kmax * 9);                        // P
     p[16] = A.take<float>((size_t)F * Kmax);                            // trP
@@ -281,8 +281,11 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     p[25] = A.take<int>(1);                                             // device error flag
     p[26] = tc ? A.take<int2>(tc_tiles) : nullptr;                      // tile list
     p[27] = need_planes ? A.take<float>((size_t)Kmax * 3 * Np) : nullptr;  // reference means
+    p[28] = need_planes ? A.take<float>((size_t)Kmax * 64 * 3 * Np) : nullptr;  // chunk sums
+    p[29] = A.take<double>(N);                                                 // sqrt(w)
+    p[30] = A.take<float>(N);                                                  // sqrt(w), FP32
   };
-  void* P[28];
+  void* P[31];
   Arena sizing;
   layout(sizing, P);
   if (!h->reserve(sizing.off + 256))
@@ -337,10 +340,12 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
   pa.Eref = (double*)P[11];
   pa.rot = nullptr;
   pa.plane = (float*)P[12];
-  pa.pmax_bits = (unsigned*)P[13];
   pa.order = (int*)P[18];
   pa.offsets = (int*)P[19];
   pa.mean = (float*)P[27];
+  pa.partial = (float*)P[28];
+  pa.sqw = (double*)P[29];
+  pa.sqwf = (float*)P[30];
 
   ExactLaunch ex{};
   ex.dtype_f64 = pa.dtype_f64;
@@ -375,21 +380,6 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     if ((e = run_prep(pa, po, st)) != cudaSuccess) return h->cuda_fail(e, "prep");
     launches += po.launches;
     K = po.K;
-    float scale = 1.0f;
-    if (tc) {
-      unsigned bits = 0;
-      cudaMemcpyAsync(&bits, pa.pmax_bits, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
-      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return h->cuda_fail(e, "prep sync");
-      float pmax;
-      std::memcpy(&pmax, &bits, sizeof pmax);
-      // Largest power of two keeping max |p| * scale <= 2^14 (FP16 max 65504).
-      int ex2 = 0;
-      if (pmax > 0.0f && std::isfinite(pmax)) std::frexp(pmax, &ex2);
-      scale = std::ldexp(1.0f, 14 - ex2);
-      if ((e = run_split_f16(pa.plane, F, Np, scale, P[23], P[24], st)) != cudaSuccess)
-        return h->cuda_fail(e, "split");
-      ++launches;
-    }
     FrameTerms terms{};
     terms.assign = pa.assign;
     terms.nrm = (float*)P[14];
@@ -408,9 +398,28 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     terms.gem_c = tc ? 1.2e-8f * (float)N : 1.2e-7f * std::sqrt((float)N);
     terms.epi_coef = 8e-7f;
     terms.nofit = nofit;
-    if ((e = run_terms(pa.plane, F, Np, N, pa.swr, K, (float*)terms.nrm, (float*)terms.P, (float*)terms.trP,
-                       pa.refs, d_w, nofit, (float*)terms.RP, st)) != cudaSuccess)
-      return h->cuda_fail(e, "frame terms");
+    FinishArgs fa{};
+    fa.plane = pa.plane;
+    fa.F = F;
+    fa.N = N;
+    fa.Np = Np;
+    fa.K = K;
+    fa.mean = pa.mean;
+    fa.assign = pa.assign;
+    fa.swr = pa.swr;
+    fa.tc = tc;
+    fa.hi = P[23];
+    fa.lo = P[24];
+    fa.inv_scale = (float*)P[13];
+    fa.write_plane = !tc;
+    fa.nrm = (float*)terms.nrm;
+    fa.P = (float*)terms.P;
+    fa.trP = (float*)terms.trP;
+    fa.refs = pa.refs;
+    fa.w = d_w;
+    fa.nofit = nofit;
+    fa.RP = (float*)terms.RP;
+    if ((e = run_finish(fa, st)) != cudaSuccess) return h->cuda_fail(e, "finish");
     launches += 2;
     FlagList fl{(int2*)P[20], (unsigned long long*)P[21], flag_cap};
     if (h->timing) cudaEventRecord(h->ev[1], st);
@@ -424,7 +433,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
       L.Np = Np;
       L.N = N;
       L.tgt0 = tgt0;
-      L.inv_scale2 = 1.0f / (scale * scale);
+      L.inv_scale = (const float*)P[13];
       L.terms = terms;
       L.map = map;
       L.flags = fl;
@@ -563,7 +572,7 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
     p[9] = A.take<double>(1);                       // Eref
     p[10] = A.take<double>(9 * (size_t)F);          // rot
     p[11] = A.take<float>((size_t)F * 3 * Np);      // plane
-    p[12] = A.take<unsigned>(1);                    // pmax
+    p[12] = A.take<float>(F);                       // per-frame 1/scale (unused)
     p[13] = A.take<int>(F);                         // order
     p[14] = A.take<int>(2);                         // offsets
     p[15] = A.take<float>(3 * (size_t)Np);          // mean
@@ -579,8 +588,11 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
     p[25] = (rmsd_out && !r_dev) ? A.take<float>(npairs) : nullptr;
     p[26] = grad_dev ? nullptr : A.take<float>((size_t)F * 3 * N);
     p[27] = A.take<unsigned long long>(1);          // flag count (unused list)
+    p[28] = A.take<float>((size_t)64 * 3 * Np);     // chunk sums
+    p[29] = A.take<double>(N);                      // sqrt(w)
+    p[30] = A.take<float>(N);                       // sqrt(w), FP32
   };
-  void* P[28];
+  void* P[31];
   Arena sizing;
   layout(sizing, P);
   if (!h->reserve(sizing.off + 256))
@@ -619,10 +631,12 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   pa.Eref = (double*)P[9];
   pa.rot = (double*)P[10];
   pa.plane = (float*)P[11];
-  pa.pmax_bits = (unsigned*)P[12];
   pa.order = (int*)P[13];
   pa.offsets = (int*)P[14];
   pa.mean = (float*)P[15];
+  pa.partial = (float*)P[28];
+  pa.sqw = (double*)P[29];
+  pa.sqwf = (float*)P[30];
   PrepOut po;
   if ((e = run_prep(pa, po, st)) != cudaSuccess) return h->cuda_fail(e, "prep");
   int launches = po.launches;
@@ -639,9 +653,26 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   terms.gem_c = 1.2e-7f * std::sqrt((float)N);
   terms.epi_coef = 8e-7f;
   terms.nofit = 0;
-  if ((e = run_terms(pa.plane, F, Np, N, pa.swr, 1, (float*)terms.nrm, (float*)terms.P, (float*)terms.trP,
-                     pa.refs, d_w, 0, (float*)terms.RP, st)) != cudaSuccess)
-    return h->cuda_fail(e, "frame terms");
+  FinishArgs fa{};
+  fa.plane = pa.plane;
+  fa.F = F;
+  fa.N = N;
+  fa.Np = Np;
+  fa.K = 1;
+  fa.mean = pa.mean;
+  fa.assign = pa.assign;
+  fa.swr = pa.swr;
+  fa.tc = 0;
+  fa.write_plane = 1;
+  fa.inv_scale = (float*)P[12];
+  fa.nrm = (float*)terms.nrm;
+  fa.P = (float*)terms.P;
+  fa.trP = (float*)terms.trP;
+  fa.refs = pa.refs;
+  fa.w = d_w;
+  fa.nofit = 0;
+  fa.RP = (float*)terms.RP;
+  if ((e = run_finish(fa, st)) != cudaSuccess) return h->cuda_fail(e, "finish");
   launches += 2;
   float* B = (float*)P[20];
   cudaMemsetAsync(B, 0, sizeof(float) * 9 * F * F, st);

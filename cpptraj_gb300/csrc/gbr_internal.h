@@ -36,11 +36,37 @@ struct PrepArgs {
   double* Eref;    // [max_refs]
   double* rot;     // [F][9] or nullptr
   float* plane;    // [F][3][Np]
-  unsigned* pmax_bits;
   int* order;      // [F] frames grouped by reference
   int* offsets;    // [max_refs + 1]
   float* mean;     // [max_refs][3][Np]
+  float* partial;  // [max_refs][64][3][Np] chunk sums for the means
+  double* sqw;     // [N] sqrt of the weights
+  float* sqwf;     // [N] the same in FP32
 };
+
+// Last per-frame pass: shift to the refined references, optional FP16 split
+// with per-frame scales, per-frame terms n/P/trP, reference-pair table.
+struct FinishArgs {
+  float* plane;
+  int64_t F;
+  int N, Np, K;
+  const float* mean;
+  const int* assign;
+  const float* swr;
+  int tc;
+  void* hi;
+  void* lo;
+  float* inv_scale;   // [F] 1/scale per frame (tensor path)
+  int write_plane;    // keep the shifted FP32 plane (FP32 pair kernel, backward)
+  float* nrm;
+  float* P;
+  float* trP;
+  const double* refs;
+  const double* w;
+  int nofit;
+  float* RP;
+};
+cudaError_t run_finish(const FinishArgs& A, cudaStream_t st);
 
 struct PrepOut {
   int K = 1;
@@ -48,10 +74,7 @@ struct PrepOut {
 };
 
 cudaError_t run_prep(const PrepArgs& A, PrepOut& o, cudaStream_t st);
-cudaError_t run_split_f16(float* plane, int64_t F, int Np, float scale, void* hi, void* lo, cudaStream_t st);
-cudaError_t run_terms(const float* plane, int64_t F, int Np, int N, const float* swr, int K, float* nrm,
-                      float* P, float* trP, const double* refs, const double* w, int nofit, float* RP,
-                      cudaStream_t st);
+
 
 // Tiles of the pair space: rows = reference frames, cols = target frames.
 struct TileSpace {
@@ -96,7 +119,7 @@ struct TcLaunch {
   int64_t F;
   int Np, N;
   int64_t tgt0;
-  float inv_scale2;  // 1 / scale^2
+  const float* inv_scale;  // [F] per-frame 1/scale of the FP16 split
   FrameTerms terms;
   OutMap map;
   FlagList flags;

@@ -6,9 +6,9 @@
 // with the residual contraction D_ji = sum_a p_j[a] p_i[a]^T run on the
 // 5th-generation tensor cores.
 //
-// Operands.  p = sqrt(w)*d is split into FP16 hi + lo (scaled by a power of
-// two); hi*hi + lo*hi + hi*lo is accumulated in FP32 in tensor memory, which
-// reproduces the products to ~2^-22 relative.  The planes are [F][3][Np]
+// Operands.  p = sqrt(w)*d is split into FP16 hi + lo (scaled per frame by a
+// power of two, undone in the epilogue); hi*hi + lo*hi + hi*lo is accumulated
+// in FP32 in tensor memory, which reproduces the products to ~2^-22 relative.  The planes are [F][3][Np]
 // FP16 (atoms contiguous), so one 3-D TMA box (64 atoms, 3 components, n
 // frames) lands in shared memory as (frame, component) rows of 128 bytes with
 // the 128-byte swizzle the UMMA K-major descriptor expects.
@@ -76,7 +76,7 @@ struct TcParams {
   int64_t i_end, jt_end;
   int64_t tgt0;
   int nk;             // 64-atom stages per tile
-  float inv_scale2;
+  const float* inv_scale;  // per-frame 1/scale of the FP16 split
   FrameTerms terms;
   OutMap map;
   FlagList flags;
@@ -331,11 +331,12 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (i >= P.i_end || jt >= P.jt_end) continue;
             const int64_t idx = out_index(P.map, i, jt);
             if (idx < 0) continue;
+            const float sc = __ldg(P.inv_scale + i) * __ldg(P.inv_scale + P.tgt0 + jt);
             float D[9];
 #pragma unroll
             for (int pj = 0; pj < 3; ++pj)
 #pragma unroll
-              for (int pi = 0; pi < 3; ++pi) D[pj * 3 + pi] = st[(3 * il + pi) * ST_STRIDE + 3 * jl + pj] * P.inv_scale2;
+              for (int pi = 0; pi < 3; ++pi) D[pj * 3 + pi] = st[(3 * il + pi) * ST_STRIDE + 3 * jl + pj] * sc;
             bool flag = false;
             const float r = pair_epilogue(D, i, P.tgt0 + jt, P.terms, &flag);
             if (flag) flag_pair(P.flags, i, jt);
@@ -454,7 +455,7 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
   P.jt_end = jt_end;
   P.tgt0 = L.tgt0;
   P.nk = (L.N + KA - 1) / KA;
-  P.inv_scale2 = L.inv_scale2;
+  P.inv_scale = L.inv_scale;
   P.terms = L.terms;
   P.map = L.map;
   P.flags = L.flags;

@@ -62,6 +62,7 @@ struct gbr_handle {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   int num_sms = 0;
   int tc_ok = 0;
+  int tc_variant = 1;
 
   int fail(int code, const char* fmt, ...) {
     char buf[512];
@@ -151,6 +152,10 @@ int gbr_set_option(gbr_handle* h, int key, double value) {
       return GBR_OK;
     case GBR_OPT_TIMING:
       h->timing = value != 0.0;
+      return GBR_OK;
+    case GBR_OPT_TC_PIPELINE:
+      if (value != 0.0 && value != 1.0) return h->fail(GBR_ERR_ARG, "tc pipeline must be 0 or 1");
+      h->tc_variant = (int)value;
       return GBR_OK;
   }
   return h->fail(GBR_ERR_ARG, "unknown option %d", key);
@@ -439,6 +444,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
       L.flags = fl;
       L.dev_error = (int*)P[25];
       L.num_sms = h->num_sms;
+      L.variant = h->tc_variant;
       if ((e = run_pairs_tc(L, st)) != cudaSuccess) return h->cuda_fail(e, "tensor-core pair kernel");
     } else {
       PairLaunch L{};

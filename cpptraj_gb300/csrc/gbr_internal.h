@@ -126,6 +126,7 @@ struct TcLaunch {
   TileSpace tiles;
   int* dev_error;    // set non-zero when a bounded wait gives up
   int num_sms;
+  int variant;       // 0: 64-atom stages (128B swizzle, 2 stages); 1: 32-atom stages (64B swizzle, 4 stages)
 };
 cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st);
 int tc_supported(int device);

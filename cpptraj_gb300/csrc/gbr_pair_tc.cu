@@ -44,13 +44,21 @@ constexpr int TI = 42;                 // reference frames per tile
 constexpr int TJ = 64;                 // target frames per tile
 constexpr int UM = 128;                // MMA M
 constexpr int UN = 3 * TJ;             // MMA N = 192
-constexpr int KA = 64;                 // atoms per stage (128-byte FP16 rows)
-constexpr int STAGES = 2;
-constexpr int A_BYTES = UM * 128;      // 16384 (TMA writes 126 rows)
-constexpr int B_BYTES = UN * 128;      // 24576
-constexpr int A_TX = 3 * TI * 128;     // bytes one A box delivers
-constexpr int B_TX = UN * 128;
-constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+// Pipeline configurations: KA atoms per stage, rows of 2*KA bytes with the
+// matching swizzle (128 B or 64 B), STAGES stages of shared memory.
+template <int KA_>
+struct Pipe {
+  static constexpr int KA = KA_;
+  static constexpr int ROW = 2 * KA;                       // bytes per (frame, component) row
+  static constexpr int STAGES = (KA == 64) ? 2 : 4;
+  static constexpr int A_BYTES = UM * ROW;                 // TMA writes 126 of the 128 rows
+  static constexpr int B_BYTES = UN * ROW;
+  static constexpr int A_TX = 3 * TI * ROW;
+  static constexpr int B_TX = UN * ROW;
+  static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+  static constexpr uint32_t SBO = 8 * ROW;                 // 8-row core-matrix groups
+  static constexpr uint64_t LAYOUT = (KA == 64) ? 2ull : 4ull;  // SWIZZLE_128B : SWIZZLE_64B
+};
 constexpr int EPI_WARPS = 8;
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
 constexpr int CH_TGT = 16;             // target frames per epilogue chunk
@@ -58,7 +66,7 @@ constexpr int CH_COLS = 3 * CH_TGT;    // 48 accumulator columns
 constexpr int ST_STRIDE = CH_COLS + 1;
 constexpr int STAGING_BYTES = 128 * ST_STRIDE * 4;
 constexpr int BAR_BYTES = 128;
-constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + 2 * STAGING_BYTES + BAR_BYTES;
+constexpr int SMEM_BYTES = 1024 + 2 * (2 * UM * 128 + 2 * UN * 128) + 2 * STAGING_BYTES + BAR_BYTES;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t ACC_STRIDE = 256;
 constexpr long long TIMEOUT_CYCLES = 4000000000LL;
@@ -139,14 +147,15 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
-// UMMA shared-memory descriptor: K-major, 128-byte swizzle, 8-row groups
-// 1024 bytes apart (SBO), version bits 46-48 = 0b001.
+// UMMA shared-memory descriptor: K-major, swizzled rows (128 B or 64 B),
+// 8-row groups SBO bytes apart, version bits 46-48 = 0b001, layout in 61-63.
+template <class PP>
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   uint64_t d = 0;
   d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)(1024u >> 4) << 32;
+  d |= (uint64_t)(PP::SBO >> 4) << 32;
   d |= 1ull << 46;
-  d |= 2ull << 61;
+  d |= PP::LAYOUT << 61;
   return d;
 }
 
@@ -182,20 +191,23 @@ __device__ __forceinline__ void named_sync(int id, int n) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
 
+template <class PP>
 __global__ void __launch_bounds__(THREADS, 1)
     k_pairs_tc(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
                const TcParams P) {
+  constexpr int STAGES = PP::STAGES, KA = PP::KA, STAGE_BYTES = PP::STAGE_BYTES, A_BYTES = PP::A_BYTES,
+                B_BYTES = PP::B_BYTES, A_TX = PP::A_TX, B_TX = PP::B_TX;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* stage_base = smem;
   float* staging = (float*)(smem + STAGES * STAGE_BYTES);
   uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES + 2 * STAGING_BYTES);
-  // bars: full[2] empty[2] accfull[2] accempty[2] done[1]; then the TMEM address.
-  uint32_t* tmem_slot = (uint32_t*)(bars + 12);
-  volatile int* grp_ok = (volatile int*)(bars + 13);  // two ints, one per epilogue warpgroup
-  const uint32_t full0 = smem_u32(bars + 0), empty0 = smem_u32(bars + 2), accf0 = smem_u32(bars + 4),
-                 acce0 = smem_u32(bars + 6), done = smem_u32(bars + 8);
+  // bars: full[4] empty[4] accfull[2] accempty[2] done[1]; then the TMEM address.
+  uint32_t* tmem_slot = (uint32_t*)(bars + 14);
+  volatile int* grp_ok = (volatile int*)(bars + 15);  // two ints, one per epilogue warpgroup
+  const uint32_t full0 = smem_u32(bars + 0), empty0 = smem_u32(bars + 4), accf0 = smem_u32(bars + 8),
+                 acce0 = smem_u32(bars + 10), done = smem_u32(bars + 12);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
@@ -272,9 +284,9 @@ __global__ void __launch_bounds__(THREADS, 1)
           const uint32_t sb = smem_u32(stage_base + s * STAGE_BYTES);
 #pragma unroll
           for (int kk = 0; kk < KA / 16; ++kk) {
-            const uint64_t ah = smem_desc(sb + kk * 32), al = smem_desc(sb + A_BYTES + kk * 32);
-            const uint64_t bh = smem_desc(sb + 2 * A_BYTES + kk * 32);
-            const uint64_t bl = smem_desc(sb + 2 * A_BYTES + B_BYTES + kk * 32);
+            const uint64_t ah = smem_desc<PP>(sb + kk * 32), al = smem_desc<PP>(sb + A_BYTES + kk * 32);
+            const uint64_t bh = smem_desc<PP>(sb + 2 * A_BYTES + kk * 32);
+            const uint64_t bl = smem_desc<PP>(sb + 2 * A_BYTES + B_BYTES + kk * 32);
             umma_f16(d, ah, bh, (kc | kk) != 0);
             umma_f16(d, al, bh, 1u);
             umma_f16(d, ah, bl, 1u);
@@ -375,16 +387,16 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-bool make_map(CUtensorMap* m, const void* base, int64_t F, int Np, int box_frames) {
+bool make_map(CUtensorMap* m, const void* base, int64_t F, int Np, int box_frames, int ka) {
   auto fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[3] = {(cuuint64_t)Np, 3, (cuuint64_t)F};
   cuuint64_t strides[2] = {(cuuint64_t)Np * 2, (cuuint64_t)Np * 2 * 3};
-  cuuint32_t box[3] = {(cuuint32_t)KA, 3, (cuuint32_t)box_frames};
+  cuuint32_t box[3] = {(cuuint32_t)ka, 3, (cuuint32_t)box_frames};
   cuuint32_t es[3] = {1, 1, 1};
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<void*>(base), dims, strides, box, es,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+            CU_TENSOR_MAP_INTERLEAVE_NONE, ka == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 }  // namespace
 
@@ -442,9 +454,10 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
   if (e != cudaSuccess) return e;
   // The copy reads `tiles` asynchronously from pageable memory; cudaMemcpyAsync
   // from pageable memory returns after the source has been consumed.
+  const int ka = (L.variant == 1) ? 32 : 64;
   CUtensorMap mAh, mAl, mBh, mBl;
-  if (!make_map(&mAh, L.hi, L.F, L.Np, TI) || !make_map(&mAl, L.lo, L.F, L.Np, TI) ||
-      !make_map(&mBh, L.hi, L.F, L.Np, TJ) || !make_map(&mBl, L.lo, L.F, L.Np, TJ))
+  if (!make_map(&mAh, L.hi, L.F, L.Np, TI, ka) || !make_map(&mAl, L.lo, L.F, L.Np, TI, ka) ||
+      !make_map(&mBh, L.hi, L.F, L.Np, TJ, ka) || !make_map(&mBl, L.lo, L.F, L.Np, TJ, ka))
     return cudaErrorInvalidValue;
   TcParams P{};
   P.tiles = (const int2*)L.tile_buf;
@@ -454,16 +467,22 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
   P.i_end = i_end;
   P.jt_end = jt_end;
   P.tgt0 = L.tgt0;
-  P.nk = (L.N + KA - 1) / KA;
+  P.nk = (L.N + ka - 1) / ka;
   P.inv_scale = L.inv_scale;
   P.terms = L.terms;
   P.map = L.map;
   P.flags = L.flags;
   P.err = L.dev_error;
-  e = cudaFuncSetAttribute(k_pairs_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-  if (e != cudaSuccess) return e;
   const int grid = (int)std::min<int64_t>(n, L.num_sms > 0 ? L.num_sms : 148);
-  k_pairs_tc<<<grid, THREADS, SMEM_BYTES, st>>>(mAh, mAl, mBh, mBl, P);
+  if (ka == 64) {
+    e = cudaFuncSetAttribute(k_pairs_tc<Pipe<64>>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    k_pairs_tc<Pipe<64>><<<grid, THREADS, SMEM_BYTES, st>>>(mAh, mAl, mBh, mBl, P);
+  } else {
+    e = cudaFuncSetAttribute(k_pairs_tc<Pipe<32>>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    k_pairs_tc<Pipe<32>><<<grid, THREADS, SMEM_BYTES, st>>>(mAh, mAl, mBh, mBl, P);
+  }
   return cudaGetLastError();
 }
 

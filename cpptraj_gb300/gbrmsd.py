@@ -21,7 +21,7 @@ GBR_F32, GBR_F64 = 0, 1
 FIT, NOFIT = 0, 1
 TRI, FULL = 0, 1
 PREC_FP32, PREC_TC, PREC_FP64 = 0, 1, 2
-OPT_TAU, OPT_MAX_REFS, OPT_TOL, OPT_TIMING = 0, 1, 2, 3
+OPT_TAU, OPT_MAX_REFS, OPT_TOL, OPT_TIMING, OPT_TC_PIPELINE = 0, 1, 2, 3, 4
 
 PRECISIONS = {"fp32": PREC_FP32, "tc": PREC_TC, "fp64": PREC_FP64}
 MODES = {"fit": FIT, "nofit": NOFIT}
@@ -237,3 +237,4 @@ def default_handle(device: int = 0) -> Handle:
     if h is None:
         h = _default[device] = Handle(device)
     return h
+

@@ -193,3 +193,14 @@ def test_tc_matches_fp32_closely(h):
     a = run(h, X, tgt_mass=m, precision="fp32")
     b = run(h, X, tgt_mass=m, precision="tc")
     assert np.abs(a - b).max() <= TOL
+
+
+@pytest.mark.parametrize("pipeline", [0, 1])
+@pytest.mark.parametrize("F,N", [(67, 129), (300, 2000), (129, 31), (2, 65)])
+def test_tc_pipeline_variants(h, pipeline, F, N):
+    X, m = synth.trajectory(F * 7 + N, F, N, 0.1, 3.0, np.float32, True)
+    h.set_option(gbrmsd.OPT_TC_PIPELINE, pipeline)
+    try:
+        _check(h, X, m, "tc")
+    finally:
+        h.set_option(gbrmsd.OPT_TC_PIPELINE, 1)

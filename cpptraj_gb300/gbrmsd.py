@@ -28,7 +28,8 @@ MODES = {"fit": FIT, "nofit": NOFIT}
 
 #: Every symbol include/gbrmsd.h declares.
 EXPORTED = ("gbr_create", "gbr_destroy", "gbr_last_error", "gbr_allpairs", "gbr_output_count",
-            "gbr_allpairs_batched", "gbr_rmsd_backward", "gbr_get_stats", "gbr_set_option", "gbr_set_stream")
+            "gbr_allpairs_batched", "gbr_rmsd_backward", "gbr_get_stats", "gbr_set_option", "gbr_set_stream",
+            "gbr_allpairs_fp64_static")
 
 
 class GbrError(RuntimeError):
@@ -81,6 +82,8 @@ def load():
         L.gbr_set_option.argtypes = [vp, ci, cd]
         L.gbr_set_stream.restype = ci
         L.gbr_set_stream.argtypes = [vp, vp]
+        L.gbr_allpairs_fp64_static.restype = ci
+        L.gbr_allpairs_fp64_static.argtypes = [vp, ci, i64, i32, vp, ci, vp, vp]
         _lib = L
         return L
 
@@ -238,3 +241,18 @@ def default_handle(device: int = 0) -> Handle:
         h = _default[device] = Handle(device)
     return h
 
+
+def allpairs_fp64_static(xyz, mass=None, mode="fit", out=None, stream=None):
+    """gbr_allpairs_fp64_static: FP64 all-pairs RMSD with no allocation inside
+    the library.  xyz, mass and out must be CUDA tensors; returns out."""
+    import torch
+
+    L = load()
+    F, N = int(xyz.shape[0]), int(xyz.shape[1])
+    if out is None:
+        out = torch.empty(max(F * (F - 1) // 2, 0), dtype=torch.float32, device=xyz.device)
+    m = MODES[mode] if isinstance(mode, str) else mode
+    rc = L.gbr_allpairs_fp64_static(_ptr(xyz), _dtype_code(xyz), F, N, _ptr(mass), m, _ptr(out), stream)
+    if rc != GBR_OK:
+        raise GbrError(rc, "gbr_allpairs_fp64_static failed")
+    return out

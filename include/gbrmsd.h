@@ -120,6 +120,24 @@ int gbr_allpairs_batched(gbr_handle *h, int32_t n_traj, const float *const *xyz,
 int gbr_rmsd_backward(gbr_handle *h, const float *xyz, int64_t n_frame, int32_t n_atom,
                       const double *mass, const float *g, float *grad_xyz, float *rmsd_out);
 
+/* All-pairs RMSD that allocates nothing.  No counterpart in the reference:
+ * cpptraj's loops allocate host frames per thread; this entry point exists for
+ * callers that cannot call cudaMalloc at all -- code running while a CUDA
+ * graph is captured, processes whose device memory belongs to a fixed pool,
+ * and plugins loaded after start-up.  It computes the same triangle as
+ * gbr_allpairs(..., GBR_TRI, GBR_PREC_FP64, ...) -- every pair directly in
+ * FP64 -- for one frame set: xyz (dtype GBR_F32/GBR_F64), mass (NULL =
+ * unweighted) and out (n_frame*(n_frame-1)/2 floats) must all be device
+ * memory; stream may be NULL (legacy default stream).  Its only scratch is a
+ * fixed 32 MiB __device__ array in this library (held by every GPU that loads
+ * it until the process exits): frame counts needing more (above ~1.39 million
+ * frames) are rejected with GBR_ERR_NOMEM.  The first call on a device looks
+ * the array's address up (make it before any stream capture).  Calls share
+ * the array, so calls that overlap on the GPU race.  Returns a gbr_status;
+ * there is no handle and no message text. */
+int gbr_allpairs_fp64_static(const void *xyz, int dtype, int64_t n_frame, int32_t n_atom,
+                             const double *mass, int mode, float *out, void *stream);
+
 /* Per-call statistics of the last gbr_allpairs / batched / backward call. */
 typedef struct gbr_stats {
   int64_t pairs;          /* pairs computed                                      */

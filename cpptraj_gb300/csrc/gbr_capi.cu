@@ -17,78 +17,10 @@
 #include <vector>
 
 #include "../../include/gbrmsd.h"
+#include "gbr_handle.h"
 #include "gbr_internal.h"
 
 using namespace gbr;
-
-namespace {
-
-struct Arena {
-  char* base = nullptr;
-  size_t off = 0;
-  template <class T>
-  T* take(size_t n) {
-    off = (off + 255) & ~size_t(255);
-    T* p = reinterpret_cast<T*>(base ? base + off : nullptr);
-    off += n * sizeof(T);
-    return p;
-  }
-};
-
-bool is_device_ptr(const void* p) {
-  if (!p) return false;
-  cudaPointerAttributes at{};
-  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
-}
-
-}  // namespace
-
-struct gbr_handle {
-  int device = 0;
-  cudaStream_t stream = nullptr;      // stream in use
-  cudaStream_t own_stream = nullptr;  // created with the handle
-  std::string err;
-  gbr_stats stats{};
-  double tau = 6.0;
-  int max_refs = 32;
-  double tol = 5e-5;
-  bool timing = false;
-  char* ws = nullptr;
-  size_t ws_cap = 0;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  int num_sms = 0;
-  int tc_ok = 0;
-  int tc_variant = 1;
-
-  int fail(int code, const char* fmt, ...) {
-    char buf[512];
-    va_list ap;
-    va_start(ap, fmt);
-    vsnprintf(buf, sizeof buf, fmt, ap);
-    va_end(ap);
-    err = buf;
-    return code;
-  }
-  int cuda_fail(cudaError_t e, const char* where) {
-    return fail(GBR_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
-  }
-  bool reserve(size_t bytes) {
-    if (bytes <= ws_cap) return true;
-    if (ws) cudaFree(ws);
-    ws = nullptr;
-    ws_cap = 0;
-    if (cudaMalloc(&ws, bytes) != cudaSuccess) {
-      cudaGetLastError();
-      return false;
-    }
-    ws_cap = bytes;
-    return true;
-  }
-};
 
 extern "C" {
 
@@ -117,6 +49,7 @@ void gbr_destroy(gbr_handle* h) {
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   if (h->ws) cudaFree(h->ws);
+  h->release_batch();
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
 }
@@ -497,37 +430,6 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
   }
   h->stats.ms_total =
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
-  return GBR_OK;
-}
-
-int gbr_allpairs_batched(gbr_handle* h, int32_t n_traj, const float* const* xyz, const int64_t* n_frames,
-                         const int32_t* n_atoms, const double* const* mass, int mode, int precision,
-                         float* const* out) {
-  if (!h) return GBR_ERR_ARG;
-  if (n_traj < 0 || (n_traj > 0 && (!xyz || !n_frames || !n_atoms || !out)))
-    return h->fail(GBR_ERR_ARG, "batched: null array argument");
-  gbr_stats total{};
-  total.precision = precision;
-  const auto t0 = std::chrono::steady_clock::now();
-  for (int32_t t = 0; t < n_traj; ++t) {
-    const double* m = mass ? mass[t] : nullptr;
-    const int rc = gbr_allpairs(h, xyz[t], nullptr, GBR_F32, n_frames[t], n_frames[t], n_atoms[t], m, m, mode,
-                                GBR_TRI, precision, out[t], 0, -1);
-    if (rc != GBR_OK) {
-      std::string msg = "trajectory " + std::to_string(t) + ": " + h->err;
-      h->err = msg;
-      return rc;
-    }
-    total.pairs += h->stats.pairs;
-    total.pairs_fixed += h->stats.pairs_fixed;
-    total.n_refs = std::max(total.n_refs, h->stats.n_refs);
-    total.kernel_launches += h->stats.kernel_launches;
-    total.ms_prep += h->stats.ms_prep;
-    total.ms_pairs += h->stats.ms_pairs;
-    total.ms_fixup += h->stats.ms_fixup;
-  }
-  total.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-  h->stats = total;
   return GBR_OK;
 }
 

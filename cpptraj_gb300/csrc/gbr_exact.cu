@@ -46,7 +46,9 @@ __global__ void __launch_bounds__(256) k_exact(ExactLaunch L) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t k = warp; k < L.count; k += nwarps) {
+  int64_t count = L.count;
+  if (L.dev_count) count = (int64_t)min((unsigned long long)L.count, *L.dev_count);
+  for (int64_t k = warp; k < count; k += nwarps) {
     int64_t i, jt;
     if (L.list) {
       const int2 p = L.list[k];
@@ -100,7 +102,9 @@ __global__ void __launch_bounds__(256) k_exact(ExactLaunch L) {
 cudaError_t run_exact(const ExactLaunch& L, cudaStream_t st) {
   if (L.count <= 0) return cudaSuccess;
   const int64_t warps_needed = L.count;
-  const int grid = (int)std::min<int64_t>((warps_needed + 7) / 8, 152 * 32);
+  // With a device-side count the true length is unknown here: use a grid
+  // that covers the capacity up to a few waves and loop inside.
+  const int grid = (int)std::min<int64_t>((warps_needed + 7) / 8, L.dev_count ? 152 * 8 : 152 * 32);
   if (L.dtype_f64)
     k_exact<double><<<grid, 256, 0, st>>>(L);
   else

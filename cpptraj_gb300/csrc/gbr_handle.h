@@ -1,0 +1,142 @@
+// gbr_handle.h -- the library handle and small host helpers shared by the
+// C-ABI files (gbr_capi.cu, gbr_batch.cu).  Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/gbrmsd.h"
+#include "gbr_internal.h"
+
+namespace gbr {
+
+// Sub-allocator over one device buffer: a sizing pass (base == nullptr)
+// followed by a carving pass with the same sequence of take() calls.
+struct Arena {
+  char* base = nullptr;
+  size_t off = 0;
+  template <class T>
+  T* take(size_t n) {
+    off = (off + 255) & ~size_t(255);
+    T* p = reinterpret_cast<T*>(base ? base + off : nullptr);
+    off += n * sizeof(T);
+    return p;
+  }
+};
+
+inline bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+inline bool is_pinned_or_device(const void* p) {
+  if (!p) return true;
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type != cudaMemoryTypeUnregistered;
+}
+
+}  // namespace gbr
+
+struct gbr_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;      // stream in use
+  cudaStream_t own_stream = nullptr;  // created with the handle
+  std::string err;
+  gbr_stats stats{};
+  double tau = 6.0;
+  int max_refs = 32;
+  double tol = 5e-5;
+  bool timing = false;
+  char* ws = nullptr;
+  size_t ws_cap = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  int num_sms = 0;
+  int tc_ok = 0;
+  int tc_variant = 1;
+  // batched path: auxiliary streams, fork/join events, pinned staging,
+  // the captured graph of the last batch signature, the autotuner table
+  static constexpr int kAux = 8;
+  cudaStream_t aux[kAux] = {};
+  cudaEvent_t fork = nullptr, join[kAux] = {};
+  void* pinned = nullptr;
+  size_t pinned_cap = 0;
+  std::vector<unsigned long long> graph_sig;
+  cudaGraphExec_t graph_exec = nullptr;
+  int graph_launches = 0;
+  bool last_batch_graph = false;
+  std::map<std::pair<int, int>, int> tuned;  // (log2 F, log2 N) -> kernel choice
+
+  int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    err = buf;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* where) {
+    return fail(GBR_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+  }
+  bool reserve(size_t bytes) {
+    if (bytes <= ws_cap) return true;
+    if (graph_exec) {  // a captured graph points into the old workspace
+      cudaGraphExecDestroy(graph_exec);
+      graph_exec = nullptr;
+      graph_sig.clear();
+    }
+    if (ws) cudaFree(ws);
+    ws = nullptr;
+    ws_cap = 0;
+    if (cudaMalloc(&ws, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    ws_cap = bytes;
+    return true;
+  }
+  bool reserve_pinned(size_t bytes) {
+    if (bytes <= pinned_cap) return true;
+    if (pinned) cudaFreeHost(pinned);
+    pinned = nullptr;
+    pinned_cap = 0;
+    if (cudaHostAlloc(&pinned, bytes, cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    pinned_cap = bytes;
+    return true;
+  }
+  bool ensure_aux() {
+    if (fork) return true;
+    for (int s = 0; s < kAux; ++s) {
+      if (cudaStreamCreateWithFlags(&aux[s], cudaStreamNonBlocking) != cudaSuccess) return false;
+      if (cudaEventCreateWithFlags(&join[s], cudaEventDisableTiming) != cudaSuccess) return false;
+    }
+    return cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) == cudaSuccess;
+  }
+  void release_batch() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    graph_exec = nullptr;
+    for (int s = 0; s < kAux; ++s) {
+      if (aux[s]) cudaStreamDestroy(aux[s]);
+      if (join[s]) cudaEventDestroy(join[s]);
+    }
+    if (fork) cudaEventDestroy(fork);
+    if (pinned) cudaFreeHost(pinned);
+  }
+};

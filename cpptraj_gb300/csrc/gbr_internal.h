@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <vector>
 
 #include "gbr_common.cuh"
 
@@ -127,7 +128,13 @@ struct TcLaunch {
   int* dev_error;    // set non-zero when a bounded wait gives up
   int num_sms;
   int variant;       // 0: 64-atom stages (128B swizzle, 2 stages); 1: 32-atom stages (64B swizzle, 4 stages)
+  int64_t ready_tiles;  // > 0: tile_buf already holds this many tiles (no host build or copy)
 };
+// Tile list of the tensor-core kernel for this map (host side).
+struct TcTileInfo {
+  int64_t i_base, jt_base, i_end, jt_end;
+};
+int64_t tc_build_tile_list(const OutMap& m, std::vector<int2>& tiles, TcTileInfo& info);
 cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st);
 int tc_supported(int device);
 int64_t tc_max_tiles(const OutMap& m);
@@ -164,6 +171,8 @@ struct ExactLaunch {
   OutMap map;
   const int2* list;   // pairs (i, jt) or nullptr => every pair of the map
   int64_t count;      // pairs in list (or total pairs when list == nullptr)
+  const unsigned long long* dev_count;  // non-null: the list length is read on the device,
+                                        // clamped to `count` (the list capacity)
 };
 cudaError_t run_exact(const ExactLaunch& L, cudaStream_t st);
 

@@ -444,16 +444,31 @@ int64_t tc_build_tiles(const OutMap& m, std::vector<int2>& tiles, int64_t& i_bas
   return (int64_t)tiles.size();
 }
 
+int64_t tc_build_tile_list(const OutMap& m, std::vector<int2>& tiles, TcTileInfo& info) {
+  return tc_build_tiles(m, tiles, info.i_base, info.jt_base, info.i_end, info.jt_end);
+}
+
 cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
   std::vector<int2> tiles;
   int64_t i_base, jt_base, i_end, jt_end;
-  const int64_t n = tc_build_tiles(L.map, tiles, i_base, jt_base, i_end, jt_end);
-  if (n == 0) return cudaSuccess;
-  if (!L.tile_buf || n > L.tile_cap) return cudaErrorInvalidValue;
-  cudaError_t e = cudaMemcpyAsync(L.tile_buf, tiles.data(), sizeof(int2) * n, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return e;
-  // The copy reads `tiles` asynchronously from pageable memory; cudaMemcpyAsync
-  // from pageable memory returns after the source has been consumed.
+  int64_t n;
+  cudaError_t e = cudaSuccess;
+  if (L.ready_tiles > 0) {
+    // The caller uploaded the list already (batched / graph-captured path).
+    TcTileInfo info;
+    std::vector<int2> none;
+    tc_build_tiles(L.map, none, info.i_base, info.jt_base, info.i_end, info.jt_end);
+    i_base = info.i_base; jt_base = info.jt_base; i_end = info.i_end; jt_end = info.jt_end;
+    n = L.ready_tiles;
+  } else {
+    n = tc_build_tiles(L.map, tiles, i_base, jt_base, i_end, jt_end);
+    if (n == 0) return cudaSuccess;
+    if (!L.tile_buf || n > L.tile_cap) return cudaErrorInvalidValue;
+    e = cudaMemcpyAsync(L.tile_buf, tiles.data(), sizeof(int2) * n, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    // The copy reads `tiles` asynchronously from pageable memory; cudaMemcpyAsync
+    // from pageable memory returns after the source has been consumed.
+  }
   const int ka = (L.variant == 1) ? 32 : 64;
   CUtensorMap mAh, mAl, mBh, mBl;
   if (!make_map(&mAh, L.hi, L.F, L.Np, TI, ka) || !make_map(&mAl, L.lo, L.F, L.Np, TI, ka) ||

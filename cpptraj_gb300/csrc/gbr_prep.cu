@@ -525,9 +525,14 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
   cudaMemsetAsync(A.fsel, 0, sizeof(int64_t), st);
   k_make_ref<T><<<1, kPrepThreads, 0, st>>>(src, A.fsel, A.cen, A.w, A.assign, 0, 0, A.nofit, A.refs, A.swr,
                                             A.Eref);
-  k_ref_dist<T><<<grid, kPrepThreads, 0, st>>>(src, F, A.cen, sqwf, A.Wsum, A.swr, A.Eref, 0, A.nofit, A.dist,
-                                               A.assign);
-  launches += 2;
+  if (A.max_refs > 1) {
+    k_ref_dist<T><<<grid, kPrepThreads, 0, st>>>(src, F, A.cen, sqwf, A.Wsum, A.swr, A.Eref, 0, A.nofit, A.dist,
+                                                 A.assign);
+    ++launches;
+  } else {
+    cudaMemsetAsync(A.assign, 0, sizeof(int) * F, st);  // one reference: every frame uses it
+  }
+  ++launches;
   int K = 1;
   while (K < A.max_refs && F > 1) {
     k_argmax<<<1, 1024, 0, st>>>(A.dist, F, A.dmax, A.fsel);

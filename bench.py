@@ -41,7 +41,139 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--profile", action="store_true",
                     help="warm up, then run exactly one all-pairs call (for ncu); prints stats only")
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4"],
+                    help="c1 = the headline metric; c2/c3/c4 print secondary lines for the other configs")
     return ap.parse_args()
+
+
+def _gpu_time(fn, steps, warmup):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(steps):
+        fn()
+    ev1.record()
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / steps
+
+
+def main_c2(args):
+    """Clustering pairwise cache: 50,000 frames x 500 atoms around 20 centroids, TRI in HBM."""
+    import torch
+
+    import oracle
+    from cpptraj_gb300 import gbrmsd, synth
+
+    X, labels = synth.workload_c2()
+    F, N = X.shape[0], X.shape[1]
+    pairs = F * (F - 1) // 2
+    h = gbrmsd.Handle(0)
+    h.set_stream(torch.cuda.current_stream().cuda_stream)
+    h.set_option(gbrmsd.OPT_TIMING, 1)
+    dX = torch.from_numpy(X).cuda()
+    out = torch.empty(pairs, dtype=torch.float32, device="cuda")
+    res = {}
+    for prec in ("tc", "fp32"):
+        ms = _gpu_time(lambda: h.allpairs(dX, precision=prec, out=out), max(1, args.steps // 2), 1)
+        st = h.stats()
+        rng = np.random.default_rng(0)
+        pi = rng.integers(0, F - 1, 2000)
+        pj = np.array([rng.integers(i + 1, F) for i in pi])
+        ref = oracle.pairs_f64(X, pi, pj)
+        idx = F * pi - ((pi + 1) * pi) // 2 + pj - pi - 1
+        got = out[torch.from_numpy(idx).cuda()].cpu().numpy().astype(np.float64)
+        same = labels[pi] == labels[pj]
+        res[prec] = {"pairs_per_s": pairs / (ms / 1e3), "ms_per_call": ms, "kernel_ms": st["ms_pairs"],
+                     "prep_ms": st["ms_prep"], "fixup_ms": st["ms_fixup"], "pairs_fixed": st["pairs_fixed"],
+                     "n_refs": st["n_refs"], "max_abs_err_A": float(np.abs(got - ref).max()),
+                     "mean_rmsd_same_centroid": float(got[same].mean()),
+                     "mean_rmsd_other_centroid": float(got[~same].mean())}
+    print(json.dumps({"workload": f"c2 clustering cache, {F} frames x {N} atoms, 20 centroids, TRI {pairs} "
+                                  f"pairs ({pairs * 4 / 1e9:.2f} GB) in HBM", "results": res}), flush=True)
+
+
+def main_c3(args):
+    """256 independent trajectories (frames U[100,4000], atoms U[50,3000]), mass-weighted, one batched call."""
+    import torch
+
+    import oracle
+    from cpptraj_gb300 import gbrmsd, synth
+
+    batch = synth.workload_c3()
+    h = gbrmsd.Handle(0)
+    h.set_stream(torch.cuda.current_stream().cuda_stream)
+    import ctypes
+    n = len(batch)
+    dX = [torch.from_numpy(X).cuda() for X, _ in batch]
+    dm = [torch.from_numpy(m).cuda() for _, m in batch]
+    outs = [torch.empty(X.shape[0] * (X.shape[0] - 1) // 2, device="cuda") for X, _ in batch]
+    P = ctypes.c_void_p * n
+    xyz = P(*[x.data_ptr() for x in dX])
+    nf = (ctypes.c_int64 * n)(*[X.shape[0] for X, _ in batch])
+    na = (ctypes.c_int32 * n)(*[X.shape[1] for X, _ in batch])
+    ms_ = P(*[m.data_ptr() for m in dm])
+    op = P(*[o.data_ptr() for o in outs])
+    pairs = sum(X.shape[0] * (X.shape[0] - 1) // 2 for X, _ in batch)
+    flops = sum(18 * X.shape[1] * X.shape[0] * (X.shape[0] - 1) // 2 for X, _ in batch)
+    res = {}
+    for prec in ("tc", "fp32"):
+        p = gbrmsd.PRECISIONS[prec]
+
+        def call():
+            h._check(h.lib.gbr_allpairs_batched(h.h, n, ctypes.cast(xyz, ctypes.c_void_p),
+                                                ctypes.cast(nf, ctypes.c_void_p), ctypes.cast(na, ctypes.c_void_p),
+                                                ctypes.cast(ms_, ctypes.c_void_p), gbrmsd.FIT, p,
+                                                ctypes.cast(op, ctypes.c_void_p)))
+        import time as _t
+        t0 = _t.perf_counter()
+        call()  # autotune unseen shape buckets + capture the graph
+        torch.cuda.synchronize()
+        first_ms = 1e3 * (_t.perf_counter() - t0)
+        ms = _gpu_time(call, max(2, args.steps), 1)
+        st = h.stats()
+        errs = []
+        for t in (0, 1, 2):
+            X, m = batch[t]
+            ref = oracle.allpairs_f64(X, tgt_mass=m)
+            errs.append(float(np.abs(outs[t].cpu().numpy() - ref).max()))
+        res[prec] = {"pairs_per_s": pairs / (ms / 1e3), "ms_per_call": ms, "first_call_ms": first_ms,
+                     "algorithmic_tflops": flops / (ms / 1e3) / 1e12, "kernel_launches": st["kernel_launches"],
+                     "pairs_fixed": st["pairs_fixed"], "max_abs_err_A_first3": max(errs)}
+    print(json.dumps({"workload": f"c3 batch of {n} trajectories, {pairs} pairs, {flops / 1e12:.2f} TFLOP "
+                                  f"algorithmic", "results": res}), flush=True)
+
+
+def main_c4(args):
+    """Gradient of sum_{i<j} RMSD_ij, 4,096 frames x 1,000 atoms, FP32 with FD check on 64 coordinates."""
+    import torch
+
+    import oracle
+    from cpptraj_gb300 import gbrmsd, synth
+
+    X, _ = synth.workload_c4()
+    F, N = X.shape[0], X.shape[1]
+    h = gbrmsd.Handle(0)
+    h.set_stream(torch.cuda.current_stream().cuda_stream)
+    h.set_option(gbrmsd.OPT_TIMING, 1)
+    dX = torch.from_numpy(X).cuda()
+    grad = torch.empty_like(dX)
+    out = torch.empty(F * (F - 1) // 2, device="cuda")
+    fwd_ms = _gpu_time(lambda: h.allpairs(dX, precision="tc", out=out), 3, 2)
+    bwd_ms = _gpu_time(lambda: h.backward(dX, grad=grad), max(2, args.steps // 2), 1)
+    st = h.stats()
+    g = grad.cpu().numpy()
+    rng = np.random.default_rng(4)
+    worst, gmax = 0.0, float(np.abs(g).max())
+    for _ in range(64):
+        f, a, p = int(rng.integers(0, F)), int(rng.integers(0, N)), int(rng.integers(0, 3))
+        fd = oracle.fd_f64(X, f, a, p, 1e-3)
+        worst = max(worst, abs(g[f, a, p] - fd) / max(abs(fd), 1e-3 * gmax))
+    print(json.dumps({"workload": f"c4 gradient of sum RMSD, {F} frames x {N} atoms",
+                      "forward_tc_ms": fwd_ms, "backward_ms": bwd_ms, "backward_stats": st,
+                      "fd_check": {"coordinates": 64, "h": 1e-3, "max_rel_err": worst}}), flush=True)
 
 
 def main_profile(args):
@@ -217,6 +349,8 @@ def main():
         return main_reference(args)
     if args.profile:
         return main_profile(args)
+    if args.workload != "c1":
+        return {"c2": main_c2, "c3": main_c3, "c4": main_c4}[args.workload](args)
     import torch
     import torch.distributed as dist
 

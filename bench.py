@@ -170,7 +170,7 @@ def main_c4(args):
     for _ in range(64):
         f, a, p = int(rng.integers(0, F)), int(rng.integers(0, N)), int(rng.integers(0, 3))
         fd = oracle.fd_f64(X, f, a, p, 1e-3)
-        worst = max(worst, abs(g[f, a, p] - fd) / max(abs(fd), 1e-3 * gmax))
+        worst = max(worst, float(abs(float(g[f, a, p]) - fd) / max(abs(fd), 1e-3 * gmax)))
     print(json.dumps({"workload": f"c4 gradient of sum RMSD, {F} frames x {N} atoms",
                       "forward_tc_ms": fwd_ms, "backward_ms": bwd_ms, "backward_stats": st,
                       "fd_check": {"coordinates": 64, "h": 1e-3, "max_rel_err": worst}}), flush=True)

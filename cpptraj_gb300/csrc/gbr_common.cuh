@@ -144,6 +144,31 @@ __device__ inline double qcp_lambda_rot(const double A[9], double E0, double R[9
   return lam;
 }
 
+// Proper rotation (row-major, FP64) of the quaternion q, oriented as
+// qcp_lambda_rot's R: R * t best matches r for the covariance QCP was given.
+// q is normalised here in FP64, so R is orthogonal to FP64 rounding whatever
+// precision q came from.  A zero or non-finite q gives the identity.
+__device__ inline void rotation_from_quat(const float qf[4], double R[9]) {
+  double a0 = qf[0], a1 = qf[1], a2 = qf[2], a3 = qf[3];
+  const double n2 = a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3;
+  if (!(n2 > 0.0) || !isfinite(n2)) {
+    a0 = 1.0; a1 = a2 = a3 = 0.0;
+  } else {
+    const double inv = 1.0 / sqrt(n2);
+    a0 *= inv; a1 *= inv; a2 *= inv; a3 *= inv;
+  }
+  const double aa = a0 * a0, bb = a1 * a1, cc = a2 * a2, dd = a3 * a3;
+  R[0] = aa + bb - cc - dd;
+  R[3] = 2.0 * (a1 * a2 + a0 * a3);
+  R[6] = 2.0 * (a3 * a1 - a0 * a2);
+  R[1] = 2.0 * (a1 * a2 - a0 * a3);
+  R[4] = aa - bb + cc - dd;
+  R[7] = 2.0 * (a2 * a3 + a0 * a1);
+  R[2] = 2.0 * (a3 * a1 + a0 * a2);
+  R[5] = 2.0 * (a2 * a3 - a0 * a1);
+  R[8] = aa - bb - cc + dd;
+}
+
 // --------------------------------------------------------------------------
 // Per-pair data and the FP32 epilogue.
 // --------------------------------------------------------------------------

@@ -280,7 +280,17 @@ __global__ void __launch_bounds__(kPrepThreads) k_align(FrameSrc<T> src, int64_t
 #pragma unroll
       for (int q = 0; q < 10; ++q) v[q] = h[q];
       warp_sum_f64<10>(v);
-      if (lane == 0) qcp_lambda_rot(v, 0.5 * v[9], R);
+      if (lane == 0) {
+        // Any exact rotation keeps every pairwise RMSD; the optimal one only
+        // makes d small.  So the eigenvector comes from FP32 QCP and the
+        // rotation is built (orthogonal to FP64 rounding) from it.
+        float M[9], q[4] = {1.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int k = 0; k < 9; ++k) M[k] = (float)v[k];
+        const float E0 = (float)(0.5 * v[9]);
+        if (E0 > 0.0f) qcp_vec_f32(M, E0, q);
+        rotation_from_quat(q, R);
+      }
 #pragma unroll
       for (int q = 0; q < 9; ++q) R[q] = __shfl_sync(0xffffffffu, R[q], 0);
     }

@@ -73,7 +73,9 @@ def test_batched_host_matches_oracle(h, precision, mode):
         ref = oracle.allpairs_f64(X, tgt_mass=m, mode=oracle.FIT if mode == "fit" else oracle.NOFIT)
         assert o.size == ref.size
         if ref.size:
-            assert np.abs(o - ref).max() <= (2e-6 if precision == "fp64" else TOL)
+            # FP64 mode: FP64 arithmetic, then the float32 store (half an ulp of the value)
+            tol = 2e-6 + 6e-8 * np.abs(ref) if precision == "fp64" else TOL
+            assert np.all(np.abs(o - ref) <= tol)
 
 
 @pytest.mark.parametrize("precision", ["fp32", "tc"])

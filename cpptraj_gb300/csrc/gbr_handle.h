@@ -79,6 +79,9 @@ struct gbr_handle {
   int graph_launches = 0;
   bool last_batch_graph = false;
   std::map<std::pair<int, int>, int> tuned;  // (log2 F, log2 N) -> kernel choice
+  // device buffer for results that leave through the host (cluster-matrix files)
+  float* outbuf = nullptr;
+  size_t outbuf_cap = 0;
 
   int fail(int code, const char* fmt, ...) {
     char buf[512];
@@ -129,7 +132,20 @@ struct gbr_handle {
     }
     return cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) == cudaSuccess;
   }
+  bool reserve_out(size_t floats) {
+    if (floats <= outbuf_cap) return true;
+    if (outbuf) cudaFree(outbuf);
+    outbuf = nullptr;
+    outbuf_cap = 0;
+    if (cudaMalloc(&outbuf, floats * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    outbuf_cap = floats;
+    return true;
+  }
   void release_batch() {
+    if (outbuf) cudaFree(outbuf);
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     graph_exec = nullptr;
     for (int s = 0; s < kAux; ++s) {

@@ -29,6 +29,7 @@ MODES = {"fit": FIT, "nofit": NOFIT}
 #: Every symbol include/gbrmsd.h declares.
 EXPORTED = ("gbr_create", "gbr_destroy", "gbr_last_error", "gbr_allpairs", "gbr_output_count",
             "gbr_allpairs_batched", "gbr_rmsd_backward", "gbr_get_stats", "gbr_set_option", "gbr_set_stream",
+            "gbr_write_cmatrix",
             "gbr_allpairs_fp64_static")
 
 
@@ -82,6 +83,8 @@ def load():
         L.gbr_set_option.argtypes = [vp, ci, cd]
         L.gbr_set_stream.restype = ci
         L.gbr_set_stream.argtypes = [vp, vp]
+        L.gbr_write_cmatrix.restype = ci
+        L.gbr_write_cmatrix.argtypes = [vp, ctypes.c_char_p, vp, ci, i64, i32, vp, ci, ci, vp, i64, i64]
         L.gbr_allpairs_fp64_static.restype = ci
         L.gbr_allpairs_fp64_static.argtypes = [vp, ci, i64, i32, vp, ci, vp, vp]
         _lib = L
@@ -214,6 +217,23 @@ class Handle:
                                            ctypes.cast(op, ctypes.c_void_p))
         self._check(rc)
         return [o[: int(t.shape[0]) * (int(t.shape[0]) - 1) // 2] for o, t in zip(outs, trajs)]
+
+    def write_cmatrix(self, path, xyz, mass=None, mode="fit", precision="tc", frame_to_idx=None, sieve=1):
+        """Pairwise cache of one frame set straight to a cpptraj binary
+        cluster-matrix file (CTM version 2)."""
+        n_frame, n_atom = int(xyz.shape[0]), int(xyz.shape[1])
+        if mass is not None and isinstance(mass, np.ndarray):
+            mass = np.ascontiguousarray(mass, dtype=np.float64)
+        f2i = None
+        n_orig = n_frame
+        if frame_to_idx is not None:
+            f2i = np.ascontiguousarray(frame_to_idx, dtype=np.int32)
+            n_orig = len(f2i)
+        m = MODES[mode] if isinstance(mode, str) else mode
+        p = PRECISIONS[precision] if isinstance(precision, str) else precision
+        rc = self.lib.gbr_write_cmatrix(self.h, os.fsencode(path), _ptr(xyz), _dtype_code(xyz), n_frame, n_atom,
+                                        _ptr(mass), m, p, _ptr(f2i), n_orig, int(sieve))
+        self._check(rc)
 
     def backward(self, xyz, mass=None, g=None, grad=None, rmsd_out=None):
         """dL/dxyz for L = sum_{i<j} g_ij RMSD_ij (float32 frames)."""

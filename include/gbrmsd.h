@@ -14,6 +14,8 @@
  *                        (src/Frame.cpp:1279-1307).
  *   gbr_allpairs_batched <- the same loop run over many independent COORDS
  *                        sets, one rms2d per set.
+ *   gbr_write_cmatrix <- the pairwise-cache fill plus Cmatrix_Binary::WriteCmatrix
+ *                        (savepairdist) in one call.
  *   gbr_rmsd_backward <- no reference counterpart (cpptraj has no gradient of
  *                        RMSD); dL/dx for L = sum_{i<j} g_ij RMSD_ij.
  *
@@ -65,7 +67,8 @@ enum gbr_status {
   GBR_ERR_NOMEM = 3,      /* device workspace could not be allocated          */
   GBR_ERR_ZERO_MASS = 4,  /* total mass below 1e-14                           */
   GBR_ERR_DEVICE = 5,     /* a kernel reported a device-side error (timeout)  */
-  GBR_ERR_UNSUPPORTED = 6 /* precision/mode not available on this device      */
+  GBR_ERR_UNSUPPORTED = 6, /* precision/mode not available on this device     */
+  GBR_ERR_IO = 7           /* a file could not be opened or written           */
 };
 
 enum gbr_dtype { GBR_F32 = 0, GBR_F64 = 1 };
@@ -112,6 +115,17 @@ int gbr_allpairs_batched(gbr_handle *h, int32_t n_traj, const float *const *xyz,
                          const int64_t *n_frames, const int32_t *n_atoms,
                          const double *const *mass, int mode, int precision,
                          float *const *out);
+
+/* The clustering pairwise cache of one frame set (GBR_TRI, as gbr_allpairs
+ * computes it) written to `path` as cpptraj's binary cluster-matrix file,
+ * version 2 -- the file `savepairdist` writes and `loadpairdist` reads
+ * (Cpptraj::Cluster::Cmatrix_Binary::WriteCmatrix, src/Cluster/Cmatrix_Binary.cpp:141-188).
+ * The n_frame frames are the cached ones in order.  frame_to_idx (length
+ * n_original, entries -1 for sieved-out frames, else the cache row) and sieve
+ * go into the header and trailer; frame_to_idx NULL means no sieve. */
+int gbr_write_cmatrix(gbr_handle *h, const char *path, const void *xyz, int dtype, int64_t n_frame,
+                      int32_t n_atom, const double *mass, int mode, int precision,
+                      const int32_t *frame_to_idx, int64_t n_original, int64_t sieve);
 
 /* Gradient of L = sum_{i<j} g[tri(i,j)] * RMSD_ij (best fit, one set, GBR_F32)
  * with respect to every coordinate.  g NULL means g = 1.  grad_xyz has the

@@ -79,6 +79,9 @@ def ref_lib():
         L.ref_allpairs.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int64,
                                    ctypes.c_int64, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+        L.ref_write_cmatrix.restype = ctypes.c_int
+        L.ref_write_cmatrix.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                        ctypes.c_int64, ctypes.c_int]
         L.ref_pairs_f64.restype = ctypes.c_int
         L.ref_pairs_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                     ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
@@ -203,3 +206,13 @@ def fd_f64(xyz, f, a, p, h=1e-3, mass=None, g=None, nthreads=0):
     if g is not None:
         g = np.ascontiguousarray(g, dtype=np.float32)
     return lib().orc_fd_f64(_p(xyz), xyz.shape[0], xyz.shape[1], _p(mass), _p(g), f, a, p, h, nthreads)
+
+
+def ref_write_cmatrix(path, tri, frame_to_idx, sieve):
+    """Write a pairwise cache with cpptraj's own Cmatrix_Binary writer (oracle/_ref)."""
+    tri = np.ascontiguousarray(tri, dtype=np.float32)
+    f2i = np.ascontiguousarray(frame_to_idx, dtype=np.int32)
+    nrows = int((f2i >= 0).sum())
+    rc = ref_lib().ref_write_cmatrix(path.encode(), _p(tri), _p(f2i), len(f2i), nrows, int(sieve))
+    if rc != 0:
+        raise RuntimeError("reference cmatrix writer failed")

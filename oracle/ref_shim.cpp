@@ -10,6 +10,9 @@
 // QuaternionRMSD_CenteredRef.
 #include <cstdint>
 #include <vector>
+#include "Cluster/Cframes.h"
+#include "Cluster/Cmatrix_Binary.h"
+#include "FileName.h"
 #include "Frame.h"
 #include "QuaternionRMSD.h"
 #ifdef _OPENMP
@@ -84,4 +87,15 @@ extern "C" int ref_pairs_f64(const void* xyz, int dtype, int n_atom, const doubl
     out[k] = (mode == 1) ? A.RMSD_NoFit(B, use_mass) : A.RMSD(B, use_mass);
   }
   return 0;
+}
+
+// The pairwise cache written by cpptraj's own binary cluster-matrix writer
+// (Cpptraj::Cluster::Cmatrix_Binary::WriteCmatrix, src/Cluster/Cmatrix_Binary.cpp:141-188).
+// frame_to_idx[k] is the cache row of original frame k, or -1 when sieved out.
+extern "C" int ref_write_cmatrix(const char* path, const float* tri, const int* frame_to_idx, int64_t n_original,
+                                 int64_t nrows, int sieve) {
+  Cpptraj::Cluster::Cframes f2i;
+  for (int64_t k = 0; k < n_original; ++k) f2i.push_back(frame_to_idx[k]);
+  Cpptraj::Cluster::Cmatrix_Binary w;
+  return w.WriteCmatrix(FileName(path), tri, f2i, (size_t)nrows, sieve);
 }

@@ -16,6 +16,12 @@ Run in a container where the reference tree is mounted (default
    `make -C oracle ref`) on seeded synthetic frames, for fit/nofit/qrmsd with
    and without mass weighting.  This pins the restatement where the reference
    tree is absent.
+3. tz2_cluster_cmatrix.npz -- the pairwise cache of test/Test_Cluster's first
+   unit (`cluster C1 :2-10 ... nofit savepairdist ... pairdist Cmatrix.cmatrix`
+   on all 101 tz2 frames): distances from cpptraj's own Metric_RMS arithmetic
+   (frame f1 as target, RMSD_NoFit against f2) and the file bytes from its own
+   Cmatrix_Binary::WriteCmatrix, for the full cache and for a regular sieve of
+   3 (frames 0, 3, 6, ... kept).
 """
 from __future__ import annotations
 
@@ -168,6 +174,45 @@ def make_ref_pairs():
     print("ref_pairs.npz:", len(pi), "pairs")
 
 
+def make_cluster_cmatrix():
+    sys.path.insert(0, ROOT)
+    import tempfile
+
+    import oracle
+
+    oracle.build(with_ref=True)
+    test = os.path.join(REF, "test")
+    natom, names, mass, respt = read_parm7(os.path.join(test, "tz2.parm7"))
+    res = residue_of_atom(natom, respt)
+    frames = read_crd(os.path.join(test, "tz2.crd"), natom)
+    sel = residue_mask(res, 2, 10)
+    X = np.ascontiguousarray(frames[:, sel].astype(np.float32))
+    out = {"xyz": X}
+
+    def cache(kept):
+        n = len(kept)
+        f1, f2 = np.triu_indices(n, 1)
+        # Metric_RMS::FrameDist(f1, f2): frm1 (f1) is the target, RMSD_NoFit against frm2
+        d = oracle.pairs_f64(X, kept[f2], kept[f1], mode=oracle.NOFIT, use_reference_code=True)
+        return d.astype(np.float32)
+
+    for tag, step in (("full", 1), ("sieve3", 3)):
+        F = X.shape[0]
+        kept = np.arange(0, F, step)
+        f2i = np.full(F, -1, np.int32)
+        f2i[kept] = np.arange(len(kept), dtype=np.int32)
+        tri = cache(kept)
+        with tempfile.TemporaryDirectory() as td:
+            path = os.path.join(td, "c.cmatrix")
+            oracle.ref_write_cmatrix(path, tri, f2i, step)
+            out[f"ctm_{tag}"] = np.frombuffer(open(path, "rb").read(), dtype=np.uint8)
+        out[f"f2i_{tag}"] = f2i
+        out[f"tri_{tag}"] = tri
+    np.savez_compressed(os.path.join(HERE, "tz2_cluster_cmatrix.npz"), **out)
+    print("tz2_cluster_cmatrix.npz:", X.shape, {k: v.shape for k, v in out.items() if k.startswith("ctm")})
+
+
 if __name__ == "__main__":
     make_tz2()
     make_ref_pairs()
+    make_cluster_cmatrix()

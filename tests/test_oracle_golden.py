@@ -101,3 +101,22 @@ def test_full_row_ranges_are_target_rows(refp):
     assert full.size == 10 * 14
     parts = [oracle.allpairs(A, B, tgt_mass=m, row_begin=a, row_end=b) for a, b in ((0, 3), (3, 14))]
     assert np.array_equal(np.concatenate(parts), full)
+
+
+def test_cluster_cmatrix_fixture_matches_oracle():
+    # the cached distances in the reference-written file are the oracle's nofit RMSDs
+    z = np.load(os.path.join(GOLD, "tz2_cluster_cmatrix.npz"))
+    for tag in ("full", "sieve3"):
+        f2i = z[f"f2i_{tag}"]
+        kept = np.nonzero(f2i >= 0)[0]
+        raw = z[f"ctm_{tag}"].tobytes()
+        assert raw[:4] == b"CTM\x02"
+        n_orig, nrows, sieve = np.frombuffer(raw[4:28], dtype=np.int64)
+        assert (n_orig, nrows) == (len(f2i), len(kept))
+        n = nrows * (nrows - 1) // 2
+        tri = np.frombuffer(raw[28:28 + 4 * n], dtype=np.float32)
+        mine = oracle.allpairs(np.ascontiguousarray(z["xyz"][kept]), mode=oracle.NOFIT)
+        np.testing.assert_allclose(tri, mine, rtol=0, atol=1e-6)
+        if sieve != 1:
+            flags = raw[28 + 4 * n:]
+            assert flags == b"".join(b"T" if v < 0 else b"F" for v in f2i)

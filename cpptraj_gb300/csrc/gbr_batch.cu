@@ -73,6 +73,7 @@ struct Prob {
   float* sqwf = nullptr;
   int* order = nullptr;
   int* offsets = nullptr;
+  void* scratch = nullptr;
 };
 
 void layout_prob(Arena& A, Prob& p, bool host_in, bool host_out) {
@@ -89,7 +90,7 @@ void layout_prob(Arena& A, Prob& p, bool host_in, bool host_out) {
   p.refs = A.take<double>(3 * N);
   p.swr = A.take<float>(3 * N);
   p.Eref = A.take<double>(1);
-  p.plane = planes ? A.take<float>(F * 3 * Np) : nullptr;
+  p.plane = (planes && !tc) ? A.take<float>(F * 3 * Np) : nullptr;
   p.inv_scale = A.take<float>(F);
   p.nrm = A.take<float>(F);
   p.P = A.take<float>(9 * F);
@@ -106,6 +107,7 @@ void layout_prob(Arena& A, Prob& p, bool host_in, bool host_out) {
   p.sqwf = A.take<float>(N);
   p.order = A.take<int>(F);
   p.offsets = A.take<int>(2);
+  p.scratch = planes ? A.take<char>(prep_scratch_bytes(p.F, p.N, 1)) : nullptr;
 }
 
 OutMap tri_map(const Prob& p, float* out) {
@@ -164,6 +166,7 @@ cudaError_t enqueue_prob(gbr_handle* h, Prob& p, int mode, bool host_in, bool ho
   pa.partial = p.partial;
   pa.sqw = p.sqw;
   pa.sqwf = p.sqwf;
+  pa.scratch = p.scratch;
   PrepOut po;
   if ((e = run_prep(pa, po, st)) != cudaSuccess) return e;
   nl += po.launches;
@@ -201,6 +204,7 @@ cudaError_t enqueue_prob(gbr_handle* h, Prob& p, int mode, bool host_in, bool ho
     terms.epi_coef = 8e-7f;
     terms.nofit = nofit;
     FinishArgs fa{};
+    fa.prep = &pa;
     fa.plane = p.plane;
     fa.F = p.F;
     fa.N = p.N;

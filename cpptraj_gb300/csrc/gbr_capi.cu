@@ -203,7 +203,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     p[9] = A.take<double>((size_t)Kmax * 3 * N);  // refs
     p[10] = A.take<float>((size_t)Kmax * 3 * N);  // swr
     p[11] = A.take<double>(Kmax);                 // Eref
-    p[12] = need_planes ? A.take<float>((size_t)F * 3 * Np) : nullptr;  // plane
+    p[12] = (need_planes && !tc) ? A.take<float>((size_t)F * 3 * Np) : nullptr;  // FP32 plane
     p[13] = A.take<float>(F);                                           // per-frame 1/scale
     p[14] = A.take<float>(F);                                           // nrm
     p[15] = A.take<float>((size_t)F * Kmax * 9);                        // P
@@ -222,8 +222,9 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     p[28] = need_planes ? A.take<float>((size_t)Kmax * 64 * 3 * Np) : nullptr;  // chunk sums
     p[29] = A.take<double>(N);                                                 // sqrt(w)
     p[30] = A.take<float>(N);                                                  // sqrt(w), FP32
+    p[31] = need_planes ? A.take<char>(prep_scratch_bytes(F, N, Kmax)) : nullptr;  // prep tables
   };
-  void* P[31];
+  void* P[32];
   Arena sizing;
   layout(sizing, P);
   if (!h->reserve(sizing.off + 256))
@@ -284,6 +285,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
   pa.partial = (float*)P[28];
   pa.sqw = (double*)P[29];
   pa.sqwf = (float*)P[30];
+  pa.scratch = P[31];
 
   ExactLaunch ex{};
   ex.dtype_f64 = pa.dtype_f64;
@@ -337,6 +339,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     terms.epi_coef = 8e-7f;
     terms.nofit = nofit;
     FinishArgs fa{};
+    fa.prep = &pa;
     fa.plane = pa.plane;
     fa.F = F;
     fa.N = N;
@@ -499,8 +502,9 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
     p[28] = A.take<float>((size_t)64 * 3 * Np);     // chunk sums
     p[29] = A.take<double>(N);                      // sqrt(w)
     p[30] = A.take<float>(N);                       // sqrt(w), FP32
+    p[31] = A.take<char>(prep_scratch_bytes(F, N, 1));  // prep tables
   };
-  void* P[31];
+  void* P[32];
   Arena sizing;
   layout(sizing, P);
   if (!h->reserve(sizing.off + 256))
@@ -545,6 +549,7 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   pa.partial = (float*)P[28];
   pa.sqw = (double*)P[29];
   pa.sqwf = (float*)P[30];
+  pa.scratch = P[31];
   PrepOut po;
   if ((e = run_prep(pa, po, st)) != cudaSuccess) return h->cuda_fail(e, "prep");
   int launches = po.launches;
@@ -562,6 +567,7 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   terms.epi_coef = 8e-7f;
   terms.nofit = 0;
   FinishArgs fa{};
+  fa.prep = &pa;
   fa.plane = pa.plane;
   fa.F = F;
   fa.N = N;

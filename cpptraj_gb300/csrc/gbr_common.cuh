@@ -219,8 +219,9 @@ __device__ __forceinline__ float solve_sym3(float a00, float a01, float a02, flo
   return det;
 }
 
-// FP32 QCP eigenvector of the key matrix of M (scaled by 1/E0).
-__device__ inline void qcp_vec_f32(const float M[9], float E0, float q[4]) {
+// FP32 QCP eigenvector of the key matrix of M (scaled by 1/E0).  When
+// lam_rel is given it receives the largest eigenvalue divided by E0.
+__device__ inline void qcp_vec_f32(const float M[9], float E0, float q[4], float* lam_rel = nullptr) {
   const float s = 1.0f / E0;
   const float xx = M[0] * s, xy = M[1] * s, xz = M[2] * s, yx = M[3] * s, yy = M[4] * s,
               yz = M[5] * s, zx = M[6] * s, zy = M[7] * s, zz = M[8] * s;
@@ -291,6 +292,7 @@ __device__ inline void qcp_vec_f32(const float M[9], float E0, float q[4]) {
   }
   if (!(bn > 0.0f)) { best[0] = 1.0f; best[1] = best[2] = best[3] = 0.0f; }
   q[0] = best[0]; q[1] = best[1]; q[2] = best[2]; q[3] = best[3];
+  if (lam_rel) *lam_rel = lam;
 }
 
 // The pair epilogue.  D[pj*3+pi] = sum p_j[pj] p_i[pi] (target j first).

@@ -43,11 +43,30 @@ struct PrepArgs {
   float* partial;  // [max_refs][64][3][Np] chunk sums for the means
   double* sqw;     // [N] sqrt of the weights
   float* sqwf;     // [N] the same in FP32
+  void* scratch;   // prep_scratch_bytes(F, N, max_refs) bytes (PrepScratch)
 };
+
+// Further per-call prep buffers, carved from PrepArgs::scratch.
+struct PrepScratch {
+  float* wf;       // [N] weights in FP32 (centring masses of target frames)
+  float* wfl;      // [N] w - wf (the low part)
+  float* cmf_ref;  // [N] centring masses of reference frames in FP32
+  float* cmfl_ref; // [N] their low parts
+  double* scal;    // [4] max sqrt(w), sum w, sum of reference centring masses
+  float2* refhl;   // [Kmax][N][3] references as hi + lo floats
+  double* sr;      // [Kmax][3] sum_a w_a r_k,a
+  float* rmax;     // [Kmax] max_a |r_k,a|
+  float4* quat;    // [F] superposition quaternion onto the assigned reference
+  float* ymax;     // [F] upper bound of max_a |y_a| (centred frame)
+  float* ftab;     // [F][24] rotation hi/lo (9 + 9), R c hi/lo (3 + 3)
+};
+size_t prep_scratch_bytes(int64_t F, int N, int Kmax);
+PrepScratch prep_carve(void* base, int64_t F, int N, int Kmax);
 
 // Last per-frame pass: shift to the refined references, optional FP16 split
 // with per-frame scales, per-frame terms n/P/trP, reference-pair table.
 struct FinishArgs {
+  const PrepArgs* prep;  // the prep call of the same frames (sources, tables)
   float* plane;
   int64_t F;
   int N, Np, K;

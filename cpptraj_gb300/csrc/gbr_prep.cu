@@ -1,26 +1,33 @@
 // gbr_prep.cu -- per-frame passes that run before the pair contraction (K1).
 //
-// Every per-frame pass runs one warp per frame (8 frames per 256-thread
-// block, many frames in flight per SM) with FP32 per-lane partial sums and an
-// FP64 warp reduction; the per-frame 3x3 solves run on lane 0 in FP64.
+// GB300's FP64 rate is a small fraction of its FP32 rate, so nothing here does
+// FP64 arithmetic per atom per frame.  Per-atom work is FP32; where a value
+// must be exact to well below FP32 rounding of the raw coordinates (the
+// superposed residual p = sqrt(w)(R y - r)), it is evaluated as a compensated
+// dot product (Dot2 of Ogita, Rump and Oishi, "Accurate sum and dot product",
+// SIAM J. Sci. Comput. 26(6), 2005) over FP32 hi/lo splits of the FP64
+// rotation, translation and reference.  FP64 is kept for O(1)-per-frame and
+// O(N)-per-reference work.
 //
-//   k_centroid     centre of each frame: Frame::CenterOnOrigin / the target
-//                  centring of Frame::RMSD_CenteredRef (src/Frame.cpp:1043-1055,
-//                  1142-1171); reference frames use the reference masses.
-//   k_make_ref     builds pre-alignment reference k from one frame, superposed
-//                  onto an existing reference so all references share an
-//                  orientation.
-//   k_ref_dist     fit (or no-fit) RMSD of every frame to reference k, keeping
-//                  the nearest reference per frame (greedy k-centre selection).
-//   k_align        superposes every frame onto its reference with an exact FP64
-//                  rotation and writes p = sqrt(w)*(R y - r) (FP32, [F][3][Np]).
-//   k_ref_mean_*   mean of p over each reference's frames (two fixed-order stages).
-//   k_ref_update   moves each reference to the mean of its frames.
-//   k_finish       p -= mean; for the tensor path splits p into FP16 hi/lo with
-//                  a per-frame power-of-two scale; n_f and P_fc from the exact
-//                  operand values the contraction will read.
+// Passes over the coordinates (one warp per frame, 8 frames per block):
+//   k_scan<FIRST>  FIRST: the frame centre (Frame::CenterOnOrigin / the target
+//                  centring of Frame::RMSD_CenteredRef, src/Frame.cpp:1043-1055,
+//                  1142-1171), a bound of the centred extent, and the fit to
+//                  reference 0.  Later: the fit to reference k of the greedy
+//                  k-centre choice.  The fit gives the distance and the FP32
+//                  QCP quaternion; a frame keeps the nearest reference.
+//   k_rot          one thread per frame: exact FP64 rotation from the
+//                  quaternion, R c, and their hi/lo FP32 splits.
+//   k_sample_sum   mean residual d = R y - r over the first kSample frames of
+//                  each reference (fixed chunks, fixed order).
+//   k_ref_update   moves each reference to that mean: residuals shrink to each
+//                  frame's own fluctuation.
+//   k_build        p = sqrt(w)(R y - r_a) by Dot2; the FP16 hi/lo split with a
+//                  per-frame power-of-two scale (tensor path) or the FP32
+//                  plane; n_f = |p|^2 and P_fc = sum p (sqrt(w) r_c)^T from the
+//                  exact operand values the contraction reads.
 //   k_ref_terms    per reference pair: exact rotation U_ab, U_ab S_ba, and
-//                  sum w |r_a - U_ab r_b|^2.
+//                  sum w |r_a - U_ab r_b|^2 (O(N) per pair of references).
 #include <cuda_fp16.h>
 
 #include <vector>
@@ -43,45 +50,200 @@ struct FrameSrc {
 
 constexpr int kPrepThreads = 256;
 constexpr int kWarps = kPrepThreads / 32;
+constexpr int kSample = 2048;      // frames per reference that set its refined mean
+constexpr int kMeanChunks = 64;    // fixed partition of those frames
+constexpr int kFtab = 24;          // floats per frame in the rotation table
+
+static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+size_t prep_scratch_bytes(int64_t F, int N, int Kmax) {
+  size_t b = 0;
+  b += align256(sizeof(float) * N) * 4;
+  b += align256(sizeof(double) * 4);
+  b += align256(sizeof(float2) * (size_t)Kmax * 3 * N);
+  b += align256(sizeof(double) * 3 * Kmax);
+  b += align256(sizeof(float) * Kmax);
+  b += align256(sizeof(float4) * F);
+  b += align256(sizeof(float) * F);
+  b += align256(sizeof(float) * kFtab * F);
+  return b;
+}
+
+PrepScratch prep_carve(void* base, int64_t F, int N, int Kmax) {
+  char* p = (char*)base;
+  PrepScratch s;
+  auto take = [&](size_t bytes) {
+    char* r = p;
+    p += align256(bytes);
+    return (void*)r;
+  };
+  s.wf = (float*)take(sizeof(float) * N);
+  s.wfl = (float*)take(sizeof(float) * N);
+  s.cmf_ref = (float*)take(sizeof(float) * N);
+  s.cmfl_ref = (float*)take(sizeof(float) * N);
+  s.scal = (double*)take(sizeof(double) * 4);
+  s.refhl = (float2*)take(sizeof(float2) * (size_t)Kmax * 3 * N);
+  s.sr = (double*)take(sizeof(double) * 3 * Kmax);
+  s.rmax = (float*)take(sizeof(float) * Kmax);
+  s.quat = (float4*)take(sizeof(float4) * F);
+  s.ymax = (float*)take(sizeof(float) * F);
+  s.ftab = (float*)take(sizeof(float) * kFtab * F);
+  return s;
+}
 
 template <int NV>
-__device__ __forceinline__ void warp_sum_f64(double (&v)[NV]) {
+__device__ __forceinline__ void warp_sum_f32(float (&v)[NV]) {
 #pragma unroll
   for (int k = 0; k < NV; ++k)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
 }
 
-// Largest eigenvalue of the QCP key matrix only (Newton from E0, FP64).
-__device__ inline double qcp_lambda(const double A[9], double E0) {
-  const double xx = A[0], xy = A[1], xz = A[2], yx = A[3], yy = A[4], yz = A[5], zx = A[6],
-               zy = A[7], zz = A[8];
-  const double xx2 = xx * xx, yy2 = yy * yy, zz2 = zz * zz, xy2 = xy * xy, yz2 = yz * yz,
-               xz2 = xz * xz, yx2 = yx * yx, zy2 = zy * zy, zx2 = zx * zx;
-  const double c2 = -2.0 * (xx2 + yy2 + zz2 + xy2 + yx2 + xz2 + zx2 + yz2 + zy2);
-  const double c1 = 8.0 * (xx * yz * zy + yy * zx * xz + zz * xy * yx - xx * yy * zz - yz * zx * xy -
-                           zy * yx * xz);
-  const double t1 = 2.0 * (yz * zy - yy * zz);
-  const double t2 = yy2 + zz2 - xx2 + yz2 + zy2;
-  const double t3 = xy2 + xz2 - yx2 - zx2;
-  const double pxz = xz + zx, pyz = yz + zy, pxy = xy + yx, myz = yz - zy, mxz = xz - zx,
-               mxy = xy - yx, pxx = xx + yy, mxx = xx - yy;
-  const double c0 = t3 * t3 + (t2 + t1) * (t2 - t1) +
-                    (-pxz * myz + mxy * (mxx - zz)) * (-mxz * pyz + mxy * (mxx + zz)) +
-                    (-pxz * pyz - pxy * (pxx - zz)) * (-mxz * myz - pxy * (pxx + zz)) +
-                    (pxy * pyz + pxz * (mxx + zz)) * (-mxy * myz + pxz * (pxx + zz)) +
-                    (pxy * myz + mxz * (mxx - zz)) * (-mxy * pyz + mxz * (pxx - zz));
-  double lam = E0;
-  for (int it = 0; it < 50; ++it) {
-    const double prev = lam, l2 = lam * lam, b = (l2 + c2) * lam, a = b + c1;
-    const double den = 2.0 * l2 * lam + b + a;
-    if (den == 0.0) break;
-    lam -= (a * lam + c0) / den;
-    if (fabs(lam - prev) < fabs(1e-11 * lam)) break;
-  }
-  return lam;
+// Error-free transformations (Knuth's TwoSum; TwoProduct by FMA).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+  p = a * b;
+  e = fmaf(a, b, -p);
 }
 
+// One atom's coordinates as FP32 hi + lo (lo = 0 for FP32 input).
+__device__ __forceinline__ void load_atom(const float* x, int a, float (&h)[3], float (&l)[3]) {
+  h[0] = x[3 * a]; h[1] = x[3 * a + 1]; h[2] = x[3 * a + 2];
+  l[0] = l[1] = l[2] = 0.0f;
+}
+__device__ __forceinline__ void load_atom(const double* x, int a, float (&h)[3], float (&l)[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double v = x[3 * a + k];
+    h[k] = (float)v;
+    l[k] = (float)(v - (double)h[k]);
+  }
+}
+
+// Per-warp staging of FP32 frames: a chunk of kChunkAtoms atoms (AoS, 3
+// floats each) is read with 16-byte loads -- the unaligned head and tail of
+// the chunk with scalar loads, so nothing outside the frame is touched -- and
+// lanes then take their atoms (stride 3 floats: no bank conflicts) from shared
+// memory.  buf holds kStage floats, 16-byte aligned.
+constexpr int kChunkAtoms = 128;
+constexpr int kStage = 3 * kChunkAtoms + 4;
+__device__ __forceinline__ const float* stage_chunk(const float* x, int N, int a0, float* buf, int lane) {
+  const float* src = x + 3 * (size_t)a0;
+  const int n = 3 * (min(a0 + kChunkAtoms, N) - a0);
+  int head = (int)((16u - ((unsigned)(uintptr_t)src & 15u)) & 15u) >> 2;  // floats before a 16-byte boundary
+  if (head > n) head = n;
+  const int nv = (n - head) >> 2;
+  const int tail0 = head + 4 * nv;
+  float* dst = buf + ((4 - head) & 3);  // dst + head is 16-byte aligned
+  const float4* v4 = reinterpret_cast<const float4*>(src + head);
+  float4 t[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const int j = lane + 32 * i;
+    if (j < nv) t[i] = __ldg(v4 + j);
+  }
+  if (lane < head) dst[lane] = src[lane];
+  if (lane < n - tail0) dst[tail0 + lane] = src[tail0 + lane];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const int j = lane + 32 * i;
+    if (j < nv) *reinterpret_cast<float4*>(dst + head + 4 * j) = t[i];
+  }
+  __syncwarp();
+  return dst;
+}
+
+// Coordinates of atom a as FP32 hi + lo: from the staged chunk (FP32 input)
+// or from global memory (FP64 input).
+__device__ __forceinline__ void fetch_atom(const float* x, const float* xs, int a, int a0, float (&h)[3],
+                                           float (&l)[3]) {
+  (void)x;
+  const float* p = xs + 3 * (a - a0);
+  h[0] = p[0]; h[1] = p[1]; h[2] = p[2];
+  l[0] = l[1] = l[2] = 0.0f;
+}
+__device__ __forceinline__ void fetch_atom(const double* x, const float* xs, int a, int a0, float (&h)[3],
+                                           float (&l)[3]) {
+  (void)xs;
+  (void)a0;
+  load_atom(x, a, h, l);
+}
+template <typename T>
+__device__ __forceinline__ const float* stage_frame_chunk(const T* x, int N, int a0, float* buf, int lane) {
+  if constexpr (sizeof(T) == 4) return stage_chunk((const float*)x, N, a0, buf, lane);
+  (void)x; (void)N; (void)a0; (void)lane;
+  return buf;
+}
+
+// Row k of R x - t - r, with R, t, r given as FP32 hi + lo: Dot2 over the
+// hi products and the subtractions, lo terms into the compensation.  The
+// result is as accurate as if computed in twice FP32 precision and rounded.
+__device__ __forceinline__ float dot2_row(const float* Rh, const float* Rl, float th, float tl,
+                                          const float (&xh)[3], const float (&xl)[3], float rh, float rl) {
+  float s, c, p, e, q;
+  two_prod(Rh[0], xh[0], s, c);
+  two_prod(Rh[1], xh[1], p, e);
+  two_sum(s, p, s, q);
+  c += q + e;
+  two_prod(Rh[2], xh[2], p, e);
+  two_sum(s, p, s, q);
+  c += q + e;
+  two_sum(s, -th, s, q);
+  c += q;
+  two_sum(s, -rh, s, q);
+  c += q;
+  c += fmaf(Rl[0], xh[0], fmaf(Rl[1], xh[1], fmaf(Rl[2], xh[2], -tl - rl)));
+  c += fmaf(Rh[0], xl[0], fmaf(Rh[1], xl[1], Rh[2] * xl[2]));
+  return s + c;
+}
+
+// Weights in the forms the passes read; scal = {max sqrt(w), sum w, sum of
+// the reference centring masses}.  One block.
+__global__ void __launch_bounds__(kPrepThreads) k_weights(const double* w, const double* cmass_ref, int N,
+                                                          double* sqw, float* sqwf, float* wf, float* wfl,
+                                                          float* cmf_ref, float* cmfl_ref, double* scal) {
+  __shared__ double red[32 * 3];
+  double v[3] = {0.0, 0.0, 0.0};
+  double mx = 0.0;
+  for (int a = threadIdx.x; a < N; a += blockDim.x) {
+    const double wa = w ? w[a] : 1.0;
+    const double ca = cmass_ref ? cmass_ref[a] : 1.0;
+    const double s = sqrt(wa);
+    if (w) {
+      sqw[a] = s;
+      sqwf[a] = (float)s;
+      wf[a] = (float)wa;
+      wfl[a] = (float)(wa - (double)wf[a]);
+    }
+    if (cmass_ref) {
+      cmf_ref[a] = (float)ca;
+      cmfl_ref[a] = (float)(ca - (double)cmf_ref[a]);
+    }
+    mx = fmax(mx, s);
+    v[0] += wa;
+    v[1] += ca;
+  }
+  // max via the sum helper's layout: reduce max separately in shared memory
+  __shared__ double smx[kPrepThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) smx[threadIdx.x >> 5] = mx;
+  block_sum_f64<3>(v, red);
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) m = fmax(m, smx[k]);
+    scal[0] = m;
+    scal[1] = v[0];
+    scal[2] = v[1];
+    scal[3] = 0.0;
+  }
+}
+
+// FP64-accumulated centres (the FP64 checking mode only).
 template <typename T>
 __global__ void __launch_bounds__(kPrepThreads) k_centroid(FrameSrc<T> src, int64_t F,
                                                            const double* cmass_ref,
@@ -90,16 +252,18 @@ __global__ void __launch_bounds__(kPrepThreads) k_centroid(FrameSrc<T> src, int6
   for (int64_t f = blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5); f < F; f += (int64_t)gridDim.x * kWarps) {
     const T* x = src.frame(f);
     const double* m = (f < src.n_ref) ? cmass_ref : cmass_tgt;
-    float s0 = 0.f, s1 = 0.f, s2 = 0.f, sm = 0.f;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
     for (int a = lane; a < src.N; a += 32) {
-      const float w = m ? (float)m[a] : 1.0f;
-      s0 += w * (float)x[3 * a];
-      s1 += w * (float)x[3 * a + 1];
-      s2 += w * (float)x[3 * a + 2];
-      sm += w;
+      const double w = m ? m[a] : 1.0;
+      v[0] += w * (double)x[3 * a];
+      v[1] += w * (double)x[3 * a + 1];
+      v[2] += w * (double)x[3 * a + 2];
+      v[3] += w;
     }
-    double v[4] = {s0, s1, s2, sm};
-    warp_sum_f64<4>(v);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
     if (lane == 0) {
       double wt = m ? v[3] : (double)src.N;
       if (m && wt == 0.0) {  // zero total mass: centre at the origin, as VCenterOfMass does
@@ -113,23 +277,51 @@ __global__ void __launch_bounds__(kPrepThreads) k_centroid(FrameSrc<T> src, int6
   }
 }
 
-// Reference k := frame f centred (and superposed onto reference `parent` when
-// fitting and parent >= 0).  Also writes sqrt(w)*r_k in FP32 and sum w |r_k|^2.
+// Reference k := frame *fsel centred (and superposed onto reference `parent`
+// when fitting and use_parent).  Reference 0 is built before any centre is
+// known and centres its frame itself (FP64, one block).  Writes the FP64
+// reference, sqrt(w) r (FP32), r as hi + lo floats, sum w |r|^2, sum w r and
+// max |r|.
 template <typename T>
 __global__ void __launch_bounds__(kPrepThreads) k_make_ref(FrameSrc<T> src, const int64_t* fsel,
-                                                           const double* cen, const double* w,
-                                                           const int* assign, int k, int use_parent,
-                                                           int nofit, double* refs, float* swr,
-                                                           double* Eref) {
+                                                           const double* cen, const double* cmass_ref,
+                                                           const double* cmass_tgt, const double* w,
+                                                           const int* assign, int k, int use_parent, int nofit,
+                                                           double* refs, float* swr, float2* refhl,
+                                                           double* Eref, double* sr, float* rmax) {
   __shared__ double red[32 * 10];
   __shared__ double Rs[9];
+  __shared__ double cs[3];
+  __shared__ float smx[kWarps];
   const int N = src.N;
   const int64_t f = *fsel;
   const T* x = src.frame(f);
-  const double c0 = cen[3 * f], c1 = cen[3 * f + 1], c2 = cen[3 * f + 2];
-  double* rk = refs + (size_t)k * 3 * N;
   if (threadIdx.x < 9) Rs[threadIdx.x] = (threadIdx.x % 4 == 0) ? 1.0 : 0.0;
+  if (nofit || use_parent) {
+    if (threadIdx.x < 3) cs[threadIdx.x] = nofit ? 0.0 : cen[3 * f + threadIdx.x];
+  } else {
+    const double* m = (f < src.n_ref) ? cmass_ref : cmass_tgt;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int a = threadIdx.x; a < N; a += blockDim.x) {
+      const double wm = m ? m[a] : 1.0;
+      v[0] += wm * (double)x[3 * a];
+      v[1] += wm * (double)x[3 * a + 1];
+      v[2] += wm * (double)x[3 * a + 2];
+      v[3] += wm;
+    }
+    block_sum_f64<4>(v, red);
+    if (threadIdx.x == 0) {
+      double wt = m ? v[3] : (double)N;
+      if (m && wt == 0.0) {
+        wt = 1.0;
+        v[0] = v[1] = v[2] = 0.0;
+      }
+      for (int q = 0; q < 3; ++q) cs[q] = v[q] / wt;
+    }
+  }
   __syncthreads();
+  const double c0 = cs[0], c1 = cs[1], c2 = cs[2];
+  double* rk = refs + (size_t)k * 3 * N;
   const int parent = use_parent ? assign[f] : -1;
   if (!nofit && parent >= 0) {
     const double* rp = refs + (size_t)parent * 3 * N;
@@ -151,73 +343,219 @@ __global__ void __launch_bounds__(kPrepThreads) k_make_ref(FrameSrc<T> src, cons
     }
     __syncthreads();
   }
-  double e = 0.0;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  float mx = 0.0f;
   for (int a = threadIdx.x; a < N; a += blockDim.x) {
     const double wa = w ? w[a] : 1.0;
     const double y0 = (double)x[3 * a] - c0, y1 = (double)x[3 * a + 1] - c1, y2 = (double)x[3 * a + 2] - c2;
-    const double r0 = Rs[0] * y0 + Rs[1] * y1 + Rs[2] * y2;
-    const double r1 = Rs[3] * y0 + Rs[4] * y1 + Rs[5] * y2;
-    const double r2 = Rs[6] * y0 + Rs[7] * y1 + Rs[8] * y2;
-    rk[3 * a] = r0; rk[3 * a + 1] = r1; rk[3 * a + 2] = r2;
+    double r[3];
+    r[0] = Rs[0] * y0 + Rs[1] * y1 + Rs[2] * y2;
+    r[1] = Rs[3] * y0 + Rs[4] * y1 + Rs[5] * y2;
+    r[2] = Rs[6] * y0 + Rs[7] * y1 + Rs[8] * y2;
     const double sw = sqrt(wa);
-    float* s = swr + ((size_t)k * N + a) * 3;
-    s[0] = (float)(sw * r0); s[1] = (float)(sw * r1); s[2] = (float)(sw * r2);
-    e += wa * (r0 * r0 + r1 * r1 + r2 * r2);
+    for (int p = 0; p < 3; ++p) {
+      rk[3 * a + p] = r[p];
+      swr[((size_t)k * N + a) * 3 + p] = (float)(sw * r[p]);
+      const float rh = (float)r[p];
+      refhl[((size_t)k * N + a) * 3 + p] = make_float2(rh, (float)(r[p] - (double)rh));
+      acc[1 + p] += wa * r[p];
+    }
+    const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    acc[0] += wa * r2;
+    mx = fmaxf(mx, (float)sqrt(r2));
   }
-  double ev[1] = {e};
-  block_sum_f64<1>(ev, red);
-  if (threadIdx.x == 0) Eref[k] = ev[0];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) smx[threadIdx.x >> 5] = mx;
+  block_sum_f64<4>(acc, red);
+  if (threadIdx.x == 0) {
+    float m = 0.0f;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) m = fmaxf(m, smx[q]);
+    Eref[k] = acc[0];
+    sr[3 * k] = acc[1];
+    sr[3 * k + 1] = acc[2];
+    sr[3 * k + 2] = acc[3];
+    rmax[k] = m;
+  }
 }
 
-// Distance of every frame to reference k; keeps the minimum and its index.
-template <typename T>
-__global__ void __launch_bounds__(kPrepThreads) k_ref_dist(FrameSrc<T> src, int64_t F, const double* cen,
-                                                           const float* sqwf, double Wsum, const float* swr,
-                                                           const double* Eref, int k, int nofit, float* dist,
-                                                           int* assign) {
+struct ScanArgs {
+  const float* cm_ref;  // centring masses of reference frames (FP32, nullptr = geometric)
+  const float* cm_tgt;  // centring masses of target frames
+  const float* cml_ref; // low parts of those masses (exact mass = cm + cml)
+  const float* cml_tgt;
+  const float* wf;      // fit weights (FP32) or nullptr; read only when they differ from cm_ref
+  int cm_ref_is_w;      // reference frames centre with the fit weights
+  const double* scal;   // [1] sum w (or N), [2] sum of reference centring masses
+  const float* sqwf;    // sqrt(w) or nullptr
+  const float* swr;     // sqrt(w) r_k, [N][3]
+  const double* sr;     // sum w r_k, [3]
+  const double* Eref;   // &Eref[k]
+  double Wsum;
+  int k, nofit;
+  double* cen;
+  float* dist;
+  int* assign;
+  float4* quat;
+  float* ymax;
+};
+
+// FIRST: centre + extent + fit to reference 0 in one read of the frame.  The
+// sums use u = x - x0 (x0 = the frame's first atom) so FP32 accumulates
+// quantities of the size of the molecule, not of its absolute position:
+//   c = x0 + sum cm u / sum cm
+//   sum w y r^T = sum w u r^T - (c - x0) (sum w r)^T
+//   sum w |y|^2 = sum w |u|^2 - 2 (c - x0).sum w u + W |c - x0|^2
+// Later passes (reference k > 0) centre with the known c directly.
+template <typename T, bool FIRST>
+__global__ void __launch_bounds__(kPrepThreads) k_scan(FrameSrc<T> src, int64_t F, ScanArgs s) {
+  __shared__ __align__(16) float sbuf[kWarps][kStage];
   const int N = src.N, lane = threadIdx.x & 31;
-  const float* rk = swr + (size_t)k * 3 * N;  // sqrt(w) r_k
+  const bool fit = !s.nofit;
   for (int64_t f = blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5); f < F; f += (int64_t)gridDim.x * kWarps) {
     const T* x = src.frame(f);
-    const float c0 = (float)cen[3 * f], c1 = (float)cen[3 * f + 1], c2 = (float)cen[3 * f + 2];
-    float h[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int a = lane; a < N; a += 32) {
-      const float sw = sqwf ? sqwf[a] : 1.0f;
-      const float y0 = sw * ((float)x[3 * a] - c0), y1 = sw * ((float)x[3 * a + 1] - c1),
-                  y2 = sw * ((float)x[3 * a + 2] - c2);
-      const float r0 = rk[3 * a], r1 = rk[3 * a + 1], r2 = rk[3 * a + 2];
-      if (nofit) {
-        const float d0 = y0 - r0, d1 = y1 - r1, d2 = y2 - r2;
-        h[9] += d0 * d0 + d1 * d1 + d2 * d2;
-      } else {
-        h[0] += y0 * r0; h[1] += y0 * r1; h[2] += y0 * r2;
-        h[3] += y1 * r0; h[4] += y1 * r1; h[5] += y1 * r2;
-        h[6] += y2 * r0; h[7] += y2 * r1; h[8] += y2 * r2;
-        h[9] += y0 * y0 + y1 * y1 + y2 * y2;
-      }
+    const bool in_ref = f < src.n_ref;
+    const float* cm = in_ref ? s.cm_ref : s.cm_tgt;
+    const float* cml = in_ref ? s.cml_ref : s.cml_tgt;
+    const bool same_w = in_ref ? (s.cm_ref_is_w != 0) : true;
+    float o0, o1, o2;  // origin of the sums: x0 (FIRST) or the centre
+    if (FIRST) {
+      o0 = (float)x[0]; o1 = (float)x[1]; o2 = (float)x[2];
+      if (!fit) o0 = o1 = o2 = 0.0f;
+    } else {
+      o0 = (float)s.cen[3 * f]; o1 = (float)s.cen[3 * f + 1]; o2 = (float)s.cen[3 * f + 2];
     }
-    double v[10];
+    // v: 0-8 sum w u r^T, 9 sum w|u|^2 (fit) or sum |sqrt(w)x - sqrt(w)r|^2,
+    //    10-12 sum cm u, 13-15 sum w u (weights differing from cm).
+    // The centre sums (10-12) are compensated: ce holds their error terms, so
+    // the centre is exact to ~FP32^2 (u = x - x0 and cm*u by error-free
+    // transformations, the running sums by TwoSum).
+    float v[16], ce[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
-    for (int q = 0; q < 10; ++q) v[q] = h[q];
-    warp_sum_f64<10>(v);
-    if (lane == 0) {
-      double d2;
-      if (nofit) {
-        d2 = v[9] / Wsum;
+    for (int q = 0; q < 16; ++q) v[q] = 0.0f;
+    float umax = 0.0f;
+    for (int a0 = 0; a0 < N; a0 += kChunkAtoms) {
+     const float* xs = stage_frame_chunk<T>(x, N, a0, sbuf[threadIdx.x >> 5], lane);
+#pragma unroll 2
+     for (int kk = 0; kk < kChunkAtoms / 32; ++kk) {
+      const int a = a0 + lane + 32 * kk;
+      if (a >= N) break;
+      const float sw = s.sqwf ? s.sqwf[a] : 1.0f;
+      float xh[3], xl[3], u[3], ue[3];
+      fetch_atom(x, xs, a, a0, xh, xl);
+      two_sum(xh[0], -o0, u[0], ue[0]);
+      two_sum(xh[1], -o1, u[1], ue[1]);
+      two_sum(xh[2], -o2, u[2], ue[2]);
+      ue[0] += xl[0]; ue[1] += xl[1]; ue[2] += xl[2];
+      const float u0 = u[0], u1 = u[1], u2 = u[2];
+      const float r0 = s.swr[3 * a], r1 = s.swr[3 * a + 1], r2 = s.swr[3 * a + 2];
+      const float y0 = sw * u0, y1 = sw * u1, y2 = sw * u2;
+      if (fit) {
+        v[0] += y0 * r0; v[1] += y0 * r1; v[2] += y0 * r2;
+        v[3] += y1 * r0; v[4] += y1 * r1; v[5] += y1 * r2;
+        v[6] += y2 * r0; v[7] += y2 * r1; v[8] += y2 * r2;
+        v[9] += y0 * y0 + y1 * y1 + y2 * y2;
       } else {
-        const double E0 = 0.5 * (v[9] + Eref[k]);
-        d2 = 2.0 * (E0 - qcp_lambda(v, E0)) / Wsum;
+        const float d0 = y0 - r0, d1 = y1 - r1, d2 = y2 - r2;
+        v[9] += d0 * d0 + d1 * d1 + d2 * d2;
+      }
+      if (FIRST) {
+        if (fit) {
+          const float c = cm ? cm[a] : 1.0f;
+          const float cl = cm ? cml[a] : 0.0f;
+#pragma unroll
+          for (int p = 0; p < 3; ++p) {
+            float pt, pe, q;
+            two_prod(c, u[p], pt, pe);
+            two_sum(v[10 + p], pt, v[10 + p], q);
+            ce[p] += q + fmaf(c, ue[p], fmaf(cl, u[p], pe));
+          }
+          if (!same_w) {
+            const float wa = s.wf ? s.wf[a] : 1.0f;
+            v[13] += wa * u0; v[14] += wa * u1; v[15] += wa * u2;
+          }
+        }
+        umax = fmaxf(umax, u0 * u0 + u1 * u1 + u2 * u2);
+      }
+     }
+     __syncwarp();
+    }
+    if (FIRST && fit) {
+      // compensated cross-lane sum of the centre terms
+#pragma unroll
+      for (int p = 0; p < 3; ++p)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float so = __shfl_xor_sync(0xffffffffu, v[10 + p], o);
+          const float eo = __shfl_xor_sync(0xffffffffu, ce[p], o);
+          float q;
+          two_sum(v[10 + p], so, v[10 + p], q);
+          ce[p] += eo + q;
+        }
+#pragma unroll
+      for (int q = 0; q < 9; ++q)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+#pragma unroll
+      for (int q = 9; q < 10; ++q)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+#pragma unroll
+      for (int q = 13; q < 16; ++q)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+    } else {
+      warp_sum_f32<16>(v);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) umax = fmaxf(umax, __shfl_xor_sync(0xffffffffu, umax, o));
+    if (lane == 0) {
+      double d2 = 0.0;
+      float q[4] = {1.0f, 0.0f, 0.0f, 0.0f};
+      if (!fit) {
+        d2 = (double)v[9] / s.Wsum;
+        if (FIRST) {
+          s.cen[3 * f] = s.cen[3 * f + 1] = s.cen[3 * f + 2] = 0.0;
+          s.ymax[f] = sqrtf(umax) * (1.0f + 1e-6f);
+        }
+      } else {
+        double del[3] = {0.0, 0.0, 0.0};
+        if (FIRST) {
+          const double Wc = (in_ref && !s.cm_ref_is_w) ? s.scal[2] : s.scal[1];
+          for (int p = 0; p < 3; ++p) {
+            const double xo = (p == 0) ? o0 : (p == 1) ? o1 : o2;
+            const double sum = (double)v[10 + p] + (double)ce[p];
+            del[p] = (Wc != 0.0) ? sum / Wc : -xo;  // zero mass: centre at the origin
+            s.cen[3 * f + p] = xo + del[p];
+          }
+          s.ymax[f] = (float)((sqrt((double)umax) + sqrt(del[0] * del[0] + del[1] * del[1] + del[2] * del[2])) *
+                              (1.0 + 1e-6));
+        }
+        double su[3];
+        for (int p = 0; p < 3; ++p) su[p] = same_w ? (double)v[10 + p] + (double)ce[p] : (double)v[13 + p];
+        float M[9];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) M[3 * i + j] = (float)((double)v[3 * i + j] - del[i] * s.sr[j]);
+        const double Ey = (double)v[9] - 2.0 * (del[0] * su[0] + del[1] * su[1] + del[2] * su[2]) +
+                          s.Wsum * (del[0] * del[0] + del[1] * del[1] + del[2] * del[2]);
+        const double E0 = 0.5 * (Ey + *s.Eref);
+        if (E0 > 0.0) {
+          float lr = 1.0f;
+          qcp_vec_f32(M, (float)E0, q, &lr);
+          d2 = 2.0 * E0 * (1.0 - (double)lr) / s.Wsum;
+        }
       }
       const float d = (float)sqrt(fmax(d2, 0.0));
-      if (k == 0 || d < dist[f]) {
-        dist[f] = d;
-        assign[f] = k;
+      if (s.k == 0 || d < s.dist[f]) {
+        s.dist[f] = d;
+        s.assign[f] = s.k;
+        s.quat[f] = make_float4(q[0], q[1], q[2], q[3]);
       }
     }
   }
 }
 
-// Single-block argmax of dist[0..F): out_val, out_idx.
+// Single-block argmax of dist[0..F): out_val, out_idx (lowest index on ties).
 __global__ void k_argmax(const float* dist, int64_t F, float* out_val, int64_t* out_idx) {
   __shared__ float sv[1024];
   __shared__ int64_t si[1024];
@@ -247,137 +585,258 @@ __global__ void k_argmax(const float* dist, int64_t F, float* out_val, int64_t* 
   }
 }
 
-// Superpose every frame onto its reference (exact FP64 rotation) and write
-// p = sqrt(w) * (R y - r_a) as the FP32 operand plane (zero past N).
-template <typename T>
-__global__ void __launch_bounds__(kPrepThreads) k_align(FrameSrc<T> src, int64_t F, int Np,
-                                                        const double* cen, const float* sqwf,
-                                                        const double* sqw, const double* refs,
-                                                        const float* swr, const int* assign, int nofit,
-                                                        double* rot, float* plane) {
-  const int N = src.N, lane = threadIdx.x & 31;
-  for (int64_t f = blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5); f < F; f += (int64_t)gridDim.x * kWarps) {
-    const T* x = src.frame(f);
-    const int a_ref = assign[f];
-    const double* ra = refs + (size_t)a_ref * 3 * N;
-    const float* rs = swr + (size_t)a_ref * 3 * N;
-    const double c0 = cen[3 * f], c1 = cen[3 * f + 1], c2 = cen[3 * f + 2];
+// One thread per frame: the exact (FP64-orthogonal) rotation of the frame's
+// quaternion, t = R c, and both split into FP32 hi + lo.  No-fit: R = I, t = 0.
+__global__ void k_rot(int64_t F, const float4* quat, const double* cen, int nofit, float* ftab, double* rot) {
+  for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < F; f += (int64_t)gridDim.x * blockDim.x) {
     double R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     if (!nofit) {
-      float h[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-      const float fc0 = (float)c0, fc1 = (float)c1, fc2 = (float)c2;
-      for (int a = lane; a < N; a += 32) {
-        const float sw = sqwf ? sqwf[a] : 1.0f;
-        const float y0 = sw * ((float)x[3 * a] - fc0), y1 = sw * ((float)x[3 * a + 1] - fc1),
-                    y2 = sw * ((float)x[3 * a + 2] - fc2);
-        const float r0 = rs[3 * a], r1 = rs[3 * a + 1], r2 = rs[3 * a + 2];
-        h[0] += y0 * r0; h[1] += y0 * r1; h[2] += y0 * r2;
-        h[3] += y1 * r0; h[4] += y1 * r1; h[5] += y1 * r2;
-        h[6] += y2 * r0; h[7] += y2 * r1; h[8] += y2 * r2;
-        h[9] += y0 * y0 + y1 * y1 + y2 * y2 + r0 * r0 + r1 * r1 + r2 * r2;
-      }
-      double v[10];
-#pragma unroll
-      for (int q = 0; q < 10; ++q) v[q] = h[q];
-      warp_sum_f64<10>(v);
-      if (lane == 0) {
-        // Any exact rotation keeps every pairwise RMSD; the optimal one only
-        // makes d small.  So the eigenvector comes from FP32 QCP and the
-        // rotation is built (orthogonal to FP64 rounding) from it.
-        float M[9], q[4] = {1.f, 0.f, 0.f, 0.f};
-#pragma unroll
-        for (int k = 0; k < 9; ++k) M[k] = (float)v[k];
-        const float E0 = (float)(0.5 * v[9]);
-        if (E0 > 0.0f) qcp_vec_f32(M, E0, q);
-        rotation_from_quat(q, R);
-      }
-#pragma unroll
-      for (int q = 0; q < 9; ++q) R[q] = __shfl_sync(0xffffffffu, R[q], 0);
+      const float4 q4 = quat[f];
+      const float q[4] = {q4.x, q4.y, q4.z, q4.w};
+      rotation_from_quat(q, R);
     }
-    if (lane < 9 && rot) rot[9 * f + lane] = R[lane];
-    float* pl = plane + (size_t)f * 3 * Np;
-    for (int a = lane; a < Np; a += 32) {
-      float p0 = 0.f, p1 = 0.f, p2 = 0.f;
-      if (a < N) {
-        const double y0 = (double)x[3 * a] - c0, y1 = (double)x[3 * a + 1] - c1, y2 = (double)x[3 * a + 2] - c2;
-        const double sw = sqw ? sqw[a] : 1.0;
-        p0 = (float)(sw * (R[0] * y0 + R[1] * y1 + R[2] * y2 - ra[3 * a]));
-        p1 = (float)(sw * (R[3] * y0 + R[4] * y1 + R[5] * y2 - ra[3 * a + 1]));
-        p2 = (float)(sw * (R[6] * y0 + R[7] * y1 + R[8] * y2 - ra[3 * a + 2]));
-      }
-      pl[a] = p0;
-      pl[Np + a] = p1;
-      pl[2 * Np + a] = p2;
+    const double c0 = cen[3 * f], c1 = cen[3 * f + 1], c2 = cen[3 * f + 2];
+    double t[3];
+    for (int k = 0; k < 3; ++k) t[k] = R[3 * k] * c0 + R[3 * k + 1] * c1 + R[3 * k + 2] * c2;
+    float* o = ftab + (size_t)kFtab * f;
+    for (int k = 0; k < 9; ++k) {
+      const float h = (float)R[k];
+      o[k] = h;
+      o[9 + k] = (float)(R[k] - (double)h);
     }
+    for (int k = 0; k < 3; ++k) {
+      const float h = (float)t[k];
+      o[18 + k] = h;
+      o[21 + k] = (float)(t[k] - (double)h);
+    }
+    if (rot)
+      for (int k = 0; k < 9; ++k) rot[9 * f + k] = R[k];
   }
 }
 
-// p -= mean[a(f)]; then, for the tensor path, split p into FP16 hi + lo with
-// a per-frame scale s_f = 2^(14 - e), e = exponent of max |p| (so hi stays
-// below 2^15), and use the value hi + lo represents from here on.  Writes
-// n_f = sum |p|^2 and P_fc = sum p (sqrt(w) r_c)^T for every reference c.
-__global__ void __launch_bounds__(kPrepThreads) k_finish(float* plane, int64_t F, int Np, int N, const float* mean,
-                                                         const int* assign, int K, const float* swr, int tc,
-                                                         __half* hi, __half* lo, float* inv_scale,
-                                                         int write_plane, float* nrm, float* P, float* trP) {
-  const int lane = threadIdx.x & 31;
+// The frame's rotation table, loaded by lanes 0-23 and shared by shuffles.
+struct FrameTable {
+  float Rh[9], Rl[9], th[3], tl[3];
+};
+__device__ __forceinline__ void load_table(const float* ftab, int64_t f, int lane, FrameTable& T) {
+  const float v = (lane < kFtab) ? ftab[(size_t)kFtab * f + lane] : 0.0f;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    T.Rh[k] = __shfl_sync(0xffffffffu, v, k);
+    T.Rl[k] = __shfl_sync(0xffffffffu, v, 9 + k);
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    T.th[k] = __shfl_sync(0xffffffffu, v, 18 + k);
+    T.tl[k] = __shfl_sync(0xffffffffu, v, 21 + k);
+  }
+}
+
+// Sum of d = R y - r_k (unweighted) over the first kSample frames of
+// reference k, split into kMeanChunks fixed chunks: grid (atoms, chunk, k).
+// Frames of reference k are order[offsets[k] ...] (order == nullptr: every
+// frame, in index order).
+template <typename T>
+__global__ void __launch_bounds__(128) k_sample_sum(FrameSrc<T> src, int64_t F, int Np, const float* ftab,
+                                                    const int* order, const int* offsets, const float2* refhl,
+                                                    float* partial) {
+  const int k = blockIdx.z, ch = blockIdx.y, N = src.N;
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= Np) return;
+  const int64_t lo = offsets ? offsets[k] : 0;
+  const int64_t cnt = std::min<int64_t>((offsets ? (int64_t)offsets[k + 1] : F) - lo, (int64_t)kSample);
+  const int64_t per = (cnt + kMeanChunks - 1) / kMeanChunks;
+  const int64_t b0 = ch * per, b1 = std::min<int64_t>(cnt, b0 + per);
+  float s[3] = {0.0f, 0.0f, 0.0f};
+  if (a < N) {
+    float rh[3], rl[3];
+    for (int p = 0; p < 3; ++p) {
+      const float2 r = refhl[((size_t)k * N + a) * 3 + p];
+      rh[p] = r.x;
+      rl[p] = r.y;
+    }
+    for (int64_t n = b0; n < b1; ++n) {
+      const int64_t f = order ? order[lo + n] : lo + n;
+      const float* tb = ftab + (size_t)kFtab * f;
+      float xh[3], xl[3];
+      load_atom(src.frame(f), a, xh, xl);
+#pragma unroll
+      for (int p = 0; p < 3; ++p) s[p] += dot2_row(tb + 3 * p, tb + 9 + 3 * p, tb[18 + p], tb[21 + p], xh, xl, rh[p], rl[p]);
+    }
+  }
+  for (int p = 0; p < 3; ++p) partial[(((size_t)k * kMeanChunks + ch) * 3 + p) * Np + a] = s[p];
+}
+
+// r_k += mean d over its sample (FP64 over the chunk sums, fixed order), and
+// the derived sqrt(w) r_k and hi/lo r_k; grid (atoms / 128, reference).
+// rmax[k] only grows (atomicMax on the non-negative float bits), so it stays
+// an upper bound of |r_k|.  Eref and sr describe the unrefined references
+// and are not read after this point.
+__global__ void __launch_bounds__(128) k_ref_update(double* refs, float* swr, float2* refhl, float* rmax,
+                                                    const float* partial, const int* offsets, int64_t F,
+                                                    const double* w, int N, int Np) {
+  __shared__ float smx[4];
+  const int k = blockIdx.y;
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t cnt = std::min<int64_t>((offsets ? (int64_t)(offsets[k + 1] - offsets[k]) : F), (int64_t)kSample);
+  float mx = 0.0f;
+  if (a < N) {
+    double* r = refs + (size_t)k * 3 * N;
+    const double wa = w ? w[a] : 1.0;
+    const double sw = sqrt(wa);
+    double rr[3];
+    for (int p = 0; p < 3; ++p) {
+      double sum = 0.0;
+      for (int ch = 0; ch < kMeanChunks; ++ch)
+        sum += (double)partial[(((size_t)k * kMeanChunks + ch) * 3 + p) * Np + a];
+      rr[p] = r[3 * a + p] + ((cnt > 0) ? sum / (double)cnt : 0.0);
+      r[3 * a + p] = rr[p];
+      swr[((size_t)k * N + a) * 3 + p] = (float)(sw * rr[p]);
+      const float h = (float)rr[p];
+      refhl[((size_t)k * N + a) * 3 + p] = make_float2(h, (float)(rr[p] - (double)h));
+    }
+    mx = (float)sqrt(rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2]) * (1.0f + 1e-6f);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) smx[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const float m = fmaxf(fmaxf(smx[0], smx[1]), fmaxf(smx[2], smx[3]));
+    atomicMax(reinterpret_cast<int*>(rmax + k), __float_as_int(m));
+  }
+}
+
+struct BuildArgs {
+  const float* ftab;
+  const int* assign;
+  const float2* refhl;
+  const float* sqwf;    // sqrt(w) or nullptr
+  const float* ymax;    // [F] bound of max |y|
+  const float* rmax;    // [K] bound of max |r_k|
+  const double* scal;   // [0] max sqrt(w)
+  const float* swr;     // [K][N][3] sqrt(w) r_c
+  int K, Np;
+  int tc;
+  __half* hi;
+  __half* lo;
+  float* inv_scale;
+  int write_plane;
+  float* plane;
+  float* nrm;
+  float* P;
+  float* trP;
+};
+
+// Final operands, one warp per frame.  p = sqrt(w)(R y - r_a) by Dot2.  The
+// tensor path stores p*s as FP16 hi + lo, s = 2^(14 - e) with 2^e above the
+// bound sqrt(w)max (max|y| + max|r_a|) >= max|p| (so |hi| < 2^15; a loose
+// bound only lowers the floor of the smallest representable residual, far
+// below FP32 rounding), and continues with the value hi + lo represents.
+// n_f = sum |p|^2 and P_fc = sum p (sqrt(w) r_c)^T use those exact operands.
+template <typename T>
+__global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int64_t F, BuildArgs b) {
+  __shared__ __align__(16) float sbuf[kWarps][kStage];
+  const int N = src.N, Np = b.Np, lane = threadIdx.x & 31;
+  const float sqwmax = (float)b.scal[0];
   for (int64_t f = blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5); f < F; f += (int64_t)gridDim.x * kWarps) {
-    float* pl = plane + (size_t)f * 3 * Np;
-    const float* mu = mean + (size_t)assign[f] * 3 * Np;
+    const T* x = src.frame(f);
+    const int ra = b.assign[f];
+    FrameTable Tb;
+    load_table(b.ftab, f, lane, Tb);
     float scale = 1.0f, inv = 1.0f;
-    if (tc) {
-      float m = 0.0f;
-      for (int a = lane; a < N; a += 32)
-#pragma unroll
-        for (int p = 0; p < 3; ++p) m = fmaxf(m, fabsf(pl[p * Np + a] - mu[p * Np + a]));
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (b.tc) {
+      const float B = sqwmax * (b.ymax[f] + b.rmax[ra]) * (1.0f + 1e-6f);
       int e = 0;
-      if (m > 0.0f) frexpf(m, &e);
+      if (B > 0.0f && isfinite(B)) frexpf(B, &e);
+      e = max(-100, min(100, e));
       scale = ldexpf(1.0f, 14 - e);
       inv = ldexpf(1.0f, e - 14);
-      if (lane == 0) inv_scale[f] = inv;
+      if (lane == 0) b.inv_scale[f] = inv;
     }
-    // pass over atoms: final operand values, written planes, n_f
-    float n = 0.0f;
-    for (int a = lane; a < Np; a += 32) {
+    const float2* rr = b.refhl + (size_t)ra * 3 * N;
+    const float* r0 = b.swr;  // reference 0 for the fused P term
+    const size_t base = (size_t)f * 3 * Np;
+    float acc[10];
+#pragma unroll
+    for (int q = 0; q < 10; ++q) acc[q] = 0.0f;
+    for (int a0 = 0; a0 < N; a0 += kChunkAtoms) {
+      const float* xs = stage_frame_chunk<T>(x, N, a0, sbuf[threadIdx.x >> 5], lane);
+#pragma unroll 2
+      for (int kk = 0; kk < kChunkAtoms / 32; ++kk) {
+        const int a = a0 + lane + 32 * kk;
+        if (a >= N) break;
+        float xh[3], xl[3], v[3];
+        fetch_atom(x, xs, a, a0, xh, xl);
+        const float sw = b.sqwf ? b.sqwf[a] : 1.0f;
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+          const float2 r = rr[3 * a + p];
+          v[p] = sw * dot2_row(Tb.Rh + 3 * p, Tb.Rl + 3 * p, Tb.th[p], Tb.tl[p], xh, xl, r.x, r.y);
+        }
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+          if (b.tc) {
+            const float t = v[p] * scale;
+            const __half h = __float2half_rn(t);
+            const __half l = __float2half_rn(t - __half2float(h));
+            b.hi[base + (size_t)p * Np + a] = h;
+            b.lo[base + (size_t)p * Np + a] = l;
+            v[p] = (__half2float(h) + __half2float(l)) * inv;
+          }
+          if (b.write_plane) b.plane[base + (size_t)p * Np + a] = v[p];
+          acc[9] += v[p] * v[p];
+        }
+        const float c0 = r0[3 * a], c1 = r0[3 * a + 1], c2 = r0[3 * a + 2];
+        acc[0] += v[0] * c0; acc[1] += v[0] * c1; acc[2] += v[0] * c2;
+        acc[3] += v[1] * c0; acc[4] += v[1] * c1; acc[5] += v[1] * c2;
+        acc[6] += v[2] * c0; acc[7] += v[2] * c1; acc[8] += v[2] * c2;
+      }
+      __syncwarp();
+    }
+    // zero padding [N, Np)
+    for (int a = N + lane; a < Np; a += 32) {
 #pragma unroll
       for (int p = 0; p < 3; ++p) {
-        float v = (a < N) ? pl[p * Np + a] - mu[p * Np + a] : 0.0f;
-        if (tc) {
-          const float t = v * scale;
-          const __half h = __float2half_rn(t);
-          const __half l = __float2half_rn(t - __half2float(h));
-          hi[(size_t)f * 3 * Np + (size_t)p * Np + a] = h;
-          lo[(size_t)f * 3 * Np + (size_t)p * Np + a] = l;
-          v = (__half2float(h) + __half2float(l)) * inv;
+        if (b.tc) {
+          b.hi[base + (size_t)p * Np + a] = __float2half_rn(0.0f);
+          b.lo[base + (size_t)p * Np + a] = __float2half_rn(0.0f);
         }
-        if (write_plane || tc) pl[p * Np + a] = v;
-        n += v * v;
+        if (b.write_plane) b.plane[base + (size_t)p * Np + a] = 0.0f;
       }
     }
-    double nv[1] = {n};
-    warp_sum_f64<1>(nv);
-    if (lane == 0) nrm[f] = (float)nv[0];
+    warp_sum_f32<10>(acc);
+    if (lane == 0) {
+      b.nrm[f] = acc[9];
+      float* Pf = b.P + (size_t)f * b.K * 9;
+      for (int q = 0; q < 9; ++q) Pf[q] = acc[q];
+      b.trP[(size_t)f * b.K] = acc[0] + acc[4] + acc[8];
+    }
+    // P against the other references: read the operands back (this lane's own
+    // writes, same atom mapping).
     __syncwarp();
-    for (int c = 0; c < K; ++c) {
-      const float* rc = swr + (size_t)c * N * 3;
-      float h[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-      for (int a = lane; a < N; a += 32) {
-        const float p0 = pl[a], p1 = pl[Np + a], p2 = pl[2 * Np + a];
-        const float r0 = rc[3 * a], r1 = rc[3 * a + 1], r2 = rc[3 * a + 2];
-        h[0] += p0 * r0; h[1] += p0 * r1; h[2] += p0 * r2;
-        h[3] += p1 * r0; h[4] += p1 * r1; h[5] += p1 * r2;
-        h[6] += p2 * r0; h[7] += p2 * r1; h[8] += p2 * r2;
-      }
-      double v[9];
+    for (int c = 1; c < b.K; ++c) {
+      const float* rc = b.swr + (size_t)c * N * 3;
+      float h9[9];
 #pragma unroll
-      for (int q = 0; q < 9; ++q) v[q] = h[q];
-      warp_sum_f64<9>(v);
+      for (int q = 0; q < 9; ++q) h9[q] = 0.0f;
+      for (int a = lane; a < N; a += 32) {
+        float v[3];
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+          const size_t i = base + (size_t)p * Np + a;
+          v[p] = b.tc ? (__half2float(b.hi[i]) + __half2float(b.lo[i])) * inv : b.plane[i];
+        }
+        const float c0 = rc[3 * a], c1 = rc[3 * a + 1], c2 = rc[3 * a + 2];
+        h9[0] += v[0] * c0; h9[1] += v[0] * c1; h9[2] += v[0] * c2;
+        h9[3] += v[1] * c0; h9[4] += v[1] * c1; h9[5] += v[1] * c2;
+        h9[6] += v[2] * c0; h9[7] += v[2] * c1; h9[8] += v[2] * c2;
+      }
+      warp_sum_f32<9>(h9);
       if (lane == 0) {
-        float* Pf = P + ((size_t)f * K + c) * 9;
-        for (int q = 0; q < 9; ++q) Pf[q] = (float)v[q];
-        trP[(size_t)f * K + c] = (float)(v[0] + v[4] + v[8]);
+        float* Pf = b.P + ((size_t)f * b.K + c) * 9;
+        for (int q = 0; q < 9; ++q) Pf[q] = h9[q];
+        b.trP[(size_t)f * b.K + c] = h9[0] + h9[4] + h9[8];
       }
     }
   }
@@ -438,111 +897,62 @@ __global__ void __launch_bounds__(kPrepThreads) k_ref_terms(const double* refs, 
   }
 }
 
-__global__ void k_sqrt(const double* w, double* sqw, float* sqwf, int n) {
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a < n) {
-    const double v = sqrt(w[a]);
-    sqw[a] = v;
-    sqwf[a] = (float)v;
-  }
-}
-
-// Frames grouped by reference when every frame has reference 0.
-__global__ void k_iota(int* order, int* offsets, int64_t F) {
-  for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < F; f += (int64_t)gridDim.x * blockDim.x)
-    order[f] = (int)f;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    offsets[0] = 0;
-    offsets[1] = (int)F;
-  }
-}
-
-// Mean of the operand plane over the frames of each reference, in two
-// deterministic stages: partial sums over chunks of a reference's frame list
-// (grid.y = chunk, grid.z = reference), then a fixed-order sum of the chunks.
-constexpr int kMeanChunks = 64;
-__global__ void k_ref_mean_partial(const float* plane, int64_t cols, const int* order, const int* offsets,
-                                   float* partial) {
-  const int k = blockIdx.z, ch = blockIdx.y;
-  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c >= cols) return;
-  const int lo = offsets[k], hi = offsets[k + 1];
-  const int per = (hi - lo + kMeanChunks - 1) / kMeanChunks;
-  const int a = lo + ch * per, b = min(hi, a + per);
-  float s = 0.0f;
-  for (int n = a; n < b; ++n) s += plane[(size_t)order[n] * cols + c];
-  partial[((size_t)k * kMeanChunks + ch) * cols + c] = s;
-}
-__global__ void k_ref_mean_final(const float* partial, int64_t cols, const int* offsets, float* mean) {
-  const int k = blockIdx.y;
-  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c >= cols) return;
-  const int cnt = offsets[k + 1] - offsets[k];
-  double s = 0.0;
-  for (int ch = 0; ch < kMeanChunks; ++ch) s += (double)partial[((size_t)k * kMeanChunks + ch) * cols + c];
-  mean[(size_t)k * cols + c] = (cnt > 0) ? (float)(s / (double)cnt) : 0.0f;
-}
-
-// r_k += mean_k / sqrt(w) (FP64), and the derived sqrt(w) r_k, sum w |r_k|^2.
-__global__ void __launch_bounds__(kPrepThreads) k_ref_update(double* refs, float* swr, double* Eref,
-                                                             const float* mean, const double* w, int N, int Np) {
-  __shared__ double red[32];
-  const int k = blockIdx.x;
-  double* r = refs + (size_t)k * 3 * N;
-  const float* m = mean + (size_t)k * 3 * Np;
-  double e = 0.0;
-  for (int a = threadIdx.x; a < N; a += blockDim.x) {
-    const double wa = w ? w[a] : 1.0;
-    const double sw = sqrt(wa);
-    for (int p = 0; p < 3; ++p) {
-      if (sw > 0.0) r[3 * a + p] += (double)m[(size_t)p * Np + a] / sw;
-      swr[((size_t)k * N + a) * 3 + p] = (float)(sw * r[3 * a + p]);
-    }
-    e += wa * (r[3 * a] * r[3 * a] + r[3 * a + 1] * r[3 * a + 1] + r[3 * a + 2] * r[3 * a + 2]);
-  }
-  double ev[1] = {e};
-  block_sum_f64<1>(ev, red);
-  if (threadIdx.x == 0) Eref[k] = ev[0];
-}
-
 // ---------------------------------------------------------------------------
 // Host driver for the prep passes.
 // ---------------------------------------------------------------------------
+static int prep_grid(int64_t F) { return (int)std::min<int64_t>((F + kWarps - 1) / kWarps, 152 * 16); }
+
 template <typename T>
 static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
   FrameSrc<T> src{(const T*)A.ref, (const T*)(A.tgt ? A.tgt : A.ref), A.n_ref, A.N};
   const int64_t F = A.F;
-  const int grid = (int)std::min<int64_t>((F + kWarps - 1) / kWarps, 152 * 16);
+  const int N = A.N;
+  const int grid = prep_grid(F);
   int launches = 0;
-  if (A.nofit) {
-    cudaMemsetAsync(A.cen, 0, sizeof(double) * 3 * F, st);
-  } else {
-    k_centroid<T><<<grid, kPrepThreads, 0, st>>>(src, F, A.cmass_ref, A.cmass_tgt, A.cen);
-    ++launches;
-  }
   if (A.centroid_only) {
+    if (A.nofit) {
+      cudaMemsetAsync(A.cen, 0, sizeof(double) * 3 * F, st);
+    } else {
+      k_centroid<T><<<grid, kPrepThreads, 0, st>>>(src, F, A.cmass_ref, A.cmass_tgt, A.cen);
+      ++launches;
+    }
     o.K = 0;
     o.launches = launches;
     return cudaGetLastError();
   }
-  if (A.w) {
-    k_sqrt<<<(A.N + 255) / 256, 256, 0, st>>>(A.w, A.sqw, A.sqwf, A.N);
-    ++launches;
-  }
-  const float* sqwf = A.w ? A.sqwf : nullptr;
-  const double* sqw = A.w ? A.sqw : nullptr;
-  // Greedy k-centre choice of pre-alignment references.
-  cudaMemsetAsync(A.fsel, 0, sizeof(int64_t), st);
-  k_make_ref<T><<<1, kPrepThreads, 0, st>>>(src, A.fsel, A.cen, A.w, A.assign, 0, 0, A.nofit, A.refs, A.swr,
-                                            A.Eref);
-  if (A.max_refs > 1) {
-    k_ref_dist<T><<<grid, kPrepThreads, 0, st>>>(src, F, A.cen, sqwf, A.Wsum, A.swr, A.Eref, 0, A.nofit, A.dist,
-                                                 A.assign);
-    ++launches;
-  } else {
-    cudaMemsetAsync(A.assign, 0, sizeof(int) * F, st);  // one reference: every frame uses it
-  }
+  const PrepScratch S = prep_carve(A.scratch, F, N, A.max_refs);
+  const bool ref_distinct = A.cmass_ref != nullptr && A.cmass_ref != A.w;
+  k_weights<<<1, kPrepThreads, 0, st>>>(A.w, ref_distinct ? A.cmass_ref : nullptr, N, A.sqw, A.sqwf, S.wf,
+                                        S.wfl, S.cmf_ref, S.cmfl_ref, S.scal);
   ++launches;
+  ScanArgs sa{};
+  sa.cm_tgt = A.w ? S.wf : nullptr;
+  sa.cml_tgt = A.w ? S.wfl : nullptr;
+  sa.cm_ref = ref_distinct ? S.cmf_ref : sa.cm_tgt;
+  sa.cml_ref = ref_distinct ? S.cmfl_ref : sa.cml_tgt;
+  sa.wf = A.w ? S.wf : nullptr;
+  sa.cm_ref_is_w = !ref_distinct;
+  sa.scal = S.scal;
+  sa.sqwf = A.w ? A.sqwf : nullptr;
+  sa.Wsum = A.Wsum;
+  sa.nofit = A.nofit;
+  sa.cen = A.cen;
+  sa.dist = A.dist;
+  sa.assign = A.assign;
+  sa.quat = S.quat;
+  sa.ymax = S.ymax;
+  // Reference 0 from frame 0, then centres + fit to it in one pass.
+  cudaMemsetAsync(A.fsel, 0, sizeof(int64_t), st);
+  k_make_ref<T><<<1, kPrepThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w, A.assign, 0, 0,
+                                            A.nofit, A.refs, A.swr, S.refhl, A.Eref, S.sr, S.rmax);
+  sa.k = 0;
+  sa.swr = A.swr;
+  sa.sr = S.sr;
+  sa.Eref = A.Eref;
+  k_scan<T, true><<<grid, kPrepThreads, 0, st>>>(src, F, sa);
+  launches += 2;
+  // Greedy k-centre: add the farthest frame as a reference while it is
+  // farther than tau from every reference.
   int K = 1;
   while (K < A.max_refs && F > 1) {
     k_argmax<<<1, 1024, 0, st>>>(A.dist, F, A.dmax, A.fsel);
@@ -552,45 +962,44 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return e;
     if (!(dmax > A.tau)) break;
-    k_make_ref<T><<<1, kPrepThreads, 0, st>>>(src, A.fsel, A.cen, A.w, A.assign, K, 1, A.nofit, A.refs, A.swr,
-                                              A.Eref);
-    k_ref_dist<T><<<grid, kPrepThreads, 0, st>>>(src, F, A.cen, sqwf, A.Wsum, A.swr, A.Eref, K, A.nofit, A.dist,
-                                                 A.assign);
+    k_make_ref<T><<<1, kPrepThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w, A.assign, K, 1,
+                                              A.nofit, A.refs, A.swr, S.refhl, A.Eref, S.sr, S.rmax);
+    sa.k = K;
+    sa.swr = A.swr + (size_t)K * 3 * N;
+    sa.sr = S.sr + 3 * K;
+    sa.Eref = A.Eref + K;
+    k_scan<T, false><<<grid, kPrepThreads, 0, st>>>(src, F, sa);
     launches += 2;
     ++K;
   }
   o.K = K;
-  k_align<T><<<grid, kPrepThreads, 0, st>>>(src, F, A.Np, A.cen, sqwf, sqw, A.refs, A.swr, A.assign, A.nofit,
-                                            A.rot, A.plane);
+  k_rot<<<(int)std::min<int64_t>((F + 255) / 256, 1024), 256, 0, st>>>(F, S.quat, A.cen, A.nofit, S.ftab, A.rot);
   ++launches;
-  // Refine every reference to the mean of its superposed frames: residuals
-  // shrink to each frame's own fluctuation.  With several references the
-  // frames are grouped by reference with a host-side counting sort.
-  if (K == 1) {
-    k_iota<<<(int)std::min<int64_t>((F + 255) / 256, 1024), 256, 0, st>>>(A.order, A.offsets, F);
-    ++launches;
-  } else {
-    std::vector<int> asg(F), order(F), offsets(K + 1, 0);
+  // Frames grouped by reference (host counting sort) when there are several.
+  const int* order = nullptr;
+  const int* offsets = nullptr;
+  if (K > 1) {
+    std::vector<int> asg(F), ord(F), offs(K + 1, 0);
     cudaMemcpyAsync(asg.data(), A.assign, sizeof(int) * F, cudaMemcpyDeviceToHost, st);
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return e;
-    for (int64_t f = 0; f < F; ++f) offsets[asg[f] + 1]++;
-    for (int k = 0; k < K; ++k) offsets[k + 1] += offsets[k];
-    std::vector<int> fill(offsets.begin(), offsets.end() - 1);
-    for (int64_t f = 0; f < F; ++f) order[fill[asg[f]]++] = (int)f;
-    cudaMemcpyAsync(A.order, order.data(), sizeof(int) * F, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(A.offsets, offsets.data(), sizeof(int) * (K + 1), cudaMemcpyHostToDevice, st);
+    for (int64_t f = 0; f < F; ++f) offs[asg[f] + 1]++;
+    for (int k = 0; k < K; ++k) offs[k + 1] += offs[k];
+    std::vector<int> fill(offs.begin(), offs.end() - 1);
+    for (int64_t f = 0; f < F; ++f) ord[fill[asg[f]]++] = (int)f;
+    cudaMemcpyAsync(A.order, ord.data(), sizeof(int) * F, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(A.offsets, offs.data(), sizeof(int) * (K + 1), cudaMemcpyHostToDevice, st);
     // the copies read host vectors that go out of scope: finish them here
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return e;
+    order = A.order;
+    offsets = A.offsets;
   }
-  const int64_t cols = 3 * (int64_t)A.Np;
-  dim3 g1((unsigned)((cols + 255) / 256), (unsigned)kMeanChunks, (unsigned)K);
-  k_ref_mean_partial<<<g1, 256, 0, st>>>(A.plane, cols, A.order, A.offsets, A.partial);
-  dim3 g1b((unsigned)((cols + 255) / 256), (unsigned)K);
-  k_ref_mean_final<<<g1b, 256, 0, st>>>(A.partial, cols, A.offsets, A.mean);
-  k_ref_update<<<K, kPrepThreads, 0, st>>>(A.refs, A.swr, A.Eref, A.mean, A.w, A.N, A.Np);
-  launches += 3;
+  dim3 gs((unsigned)((A.Np + 127) / 128), (unsigned)kMeanChunks, (unsigned)K);
+  k_sample_sum<T><<<gs, 128, 0, st>>>(src, F, A.Np, S.ftab, order, offsets, S.refhl, A.partial);
+  k_ref_update<<<dim3((unsigned)((N + 127) / 128), (unsigned)K), 128, 0, st>>>(A.refs, A.swr, S.refhl, S.rmax,
+                                                                             A.partial, offsets, F, A.w, N, A.Np);
+  launches += 2;
   o.launches = launches;
   return cudaGetLastError();
 }
@@ -599,13 +1008,38 @@ cudaError_t run_prep(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
   return A.dtype_f64 ? prep_impl<double>(A, o, st) : prep_impl<float>(A, o, st);
 }
 
-cudaError_t run_finish(const FinishArgs& A, cudaStream_t st) {
-  const int grid = (int)std::min<int64_t>((A.F + kWarps - 1) / kWarps, 152 * 16);
-  k_finish<<<grid, kPrepThreads, 0, st>>>(A.plane, A.F, A.Np, A.N, A.mean, A.assign, A.K, A.swr, A.tc,
-                                          (__half*)A.hi, (__half*)A.lo, A.inv_scale, A.write_plane, A.nrm, A.P,
-                                          A.trP);
-  k_ref_terms<<<A.K * A.K, kPrepThreads, 0, st>>>(A.refs, A.N, A.K, A.w, A.nofit, A.RP);
+template <typename T>
+static cudaError_t finish_impl(const FinishArgs& fa, cudaStream_t st) {
+  const PrepArgs& A = *fa.prep;
+  FrameSrc<T> src{(const T*)A.ref, (const T*)(A.tgt ? A.tgt : A.ref), A.n_ref, A.N};
+  const PrepScratch S = prep_carve(A.scratch, A.F, A.N, A.max_refs);
+  BuildArgs b{};
+  b.ftab = S.ftab;
+  b.assign = A.assign;
+  b.refhl = S.refhl;
+  b.sqwf = A.w ? A.sqwf : nullptr;
+  b.ymax = S.ymax;
+  b.rmax = S.rmax;
+  b.scal = S.scal;
+  b.swr = A.swr;
+  b.K = fa.K;
+  b.Np = A.Np;
+  b.tc = fa.tc;
+  b.hi = (__half*)fa.hi;
+  b.lo = (__half*)fa.lo;
+  b.inv_scale = fa.inv_scale;
+  b.write_plane = fa.write_plane || !fa.tc;
+  b.plane = fa.plane;
+  b.nrm = fa.nrm;
+  b.P = fa.P;
+  b.trP = fa.trP;
+  k_build<T><<<prep_grid(A.F), kPrepThreads, 0, st>>>(src, A.F, b);
+  k_ref_terms<<<fa.K * fa.K, kPrepThreads, 0, st>>>(A.refs, A.N, fa.K, A.w, A.nofit, fa.RP);
   return cudaGetLastError();
+}
+
+cudaError_t run_finish(const FinishArgs& A, cudaStream_t st) {
+  return A.prep->dtype_f64 ? finish_impl<double>(A, st) : finish_impl<float>(A, st);
 }
 
 }  // namespace gbr

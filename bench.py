@@ -39,6 +39,8 @@ def parse():
     ap.add_argument("--frames", type=int, default=N_FRAME)
     ap.add_argument("--atoms", type=int, default=N_ATOM)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--tc-pipeline", type=int, default=None, choices=[0, 1, 2],
+                    help="tensor-core kernel shape (GBR_OPT_TC_PIPELINE); default: the library's")
     ap.add_argument("--profile", action="store_true",
                     help="warm up, then run exactly one all-pairs call (for ncu); prints stats only")
     ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4"],
@@ -71,6 +73,7 @@ def main_c2(args):
     F, N = X.shape[0], X.shape[1]
     pairs = F * (F - 1) // 2
     h = gbrmsd.Handle(0)
+    _apply_pipeline(h, args)
     h.set_stream(torch.cuda.current_stream().cuda_stream)
     h.set_option(gbrmsd.OPT_TIMING, 1)
     dX = torch.from_numpy(X).cuda()
@@ -104,6 +107,7 @@ def main_c3(args):
 
     batch = synth.workload_c3()
     h = gbrmsd.Handle(0)
+    _apply_pipeline(h, args)
     h.set_stream(torch.cuda.current_stream().cuda_stream)
     import ctypes
     n = len(batch)
@@ -156,6 +160,7 @@ def main_c4(args):
     X, _ = synth.workload_c4()
     F, N = X.shape[0], X.shape[1]
     h = gbrmsd.Handle(0)
+    _apply_pipeline(h, args)
     h.set_stream(torch.cuda.current_stream().cuda_stream)
     h.set_option(gbrmsd.OPT_TIMING, 1)
     dX = torch.from_numpy(X).cuda()
@@ -185,6 +190,7 @@ def main_profile(args):
     X, m = make_workload(args.frames, args.atoms, 1)
     pairs = X.shape[0] * (X.shape[0] - 1) // 2
     h = gbrmsd.Handle(0)
+    _apply_pipeline(h, args)
     prec = "tc" if args.precision == "auto" else args.precision
     dX = torch.from_numpy(X).cuda()
     out = torch.empty(pairs, dtype=torch.float32, device="cuda")
@@ -253,6 +259,12 @@ class Clocks:
         loaded = [s for s in sm if mx and s > 0.5 * mx] or sm
         return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": mx,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _apply_pipeline(h, args):
+    from cpptraj_gb300 import gbrmsd
+    if getattr(args, "tc_pipeline", None) is not None:
+        h.set_option(gbrmsd.OPT_TC_PIPELINE, args.tc_pipeline)
 
 
 def make_workload(frames, atoms, seed):
@@ -365,6 +377,7 @@ def main():
     F, N = X.shape[0], X.shape[1]
     pairs = F * (F - 1) // 2
     h = gbrmsd.Handle(local)
+    _apply_pipeline(h, args)
     h.set_option(gbrmsd.OPT_TIMING, 1)
     stream = torch.cuda.current_stream(dev)
     h.set_stream(stream.cuda_stream)

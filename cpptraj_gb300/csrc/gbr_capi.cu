@@ -87,7 +87,7 @@ int gbr_set_option(gbr_handle* h, int key, double value) {
       h->timing = value != 0.0;
       return GBR_OK;
     case GBR_OPT_TC_PIPELINE:
-      if (value != 0.0 && value != 1.0) return h->fail(GBR_ERR_ARG, "tc pipeline must be 0 or 1");
+      if (value != 0.0 && value != 1.0 && value != 2.0) return h->fail(GBR_ERR_ARG, "tc pipeline must be 0, 1 or 2");
       h->tc_variant = (int)value;
       return GBR_OK;
   }
@@ -286,6 +286,10 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
   pa.sqw = (double*)P[29];
   pa.sqwf = (float*)P[30];
   pa.scratch = P[31];
+  // With several references, a whole triangle is computed over frames laid
+  // out grouped by reference (tiles then share their references, whose terms
+  // the tensor-core epilogue stages per tile); outputs map back to frames.
+  pa.sort_frames = (map.tri && row_begin == 0 && row_end == n_ref) ? 1 : 0;
 
   ExactLaunch ex{};
   ex.dtype_f64 = pa.dtype_f64;
@@ -320,8 +324,13 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     if ((e = run_prep(pa, po, st)) != cudaSuccess) return h->cuda_fail(e, "prep");
     launches += po.launches;
     K = po.K;
+    OutMap pmap = map;  // the pair kernels' view: sorted positions when po.sorted
     FrameTerms terms{};
     terms.assign = pa.assign;
+    if (po.sorted) {
+      pmap.perm = pa.order;
+      terms.assign = prep_carve(pa.scratch, F, N, Kmax).assign_pos;
+    }
     terms.nrm = (float*)P[14];
     terms.P = (float*)P[15];
     terms.trP = (float*)P[16];
@@ -340,6 +349,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     terms.nofit = nofit;
     FinishArgs fa{};
     fa.prep = &pa;
+    fa.sorted = po.sorted;
     fa.plane = pa.plane;
     fa.F = F;
     fa.N = N;
@@ -376,7 +386,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
       L.tgt0 = tgt0;
       L.inv_scale = (const float*)P[13];
       L.terms = terms;
-      L.map = map;
+      L.map = pmap;
       L.flags = fl;
       L.dev_error = (int*)P[25];
       L.num_sms = h->num_sms;
@@ -389,9 +399,9 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
       L.N = N;
       L.tgt0 = tgt0;
       L.terms = terms;
-      L.map = map;
+      L.map = pmap;
       L.flags = fl;
-      L.tiles = make_tiles(map, 64, 64);
+      L.tiles = make_tiles(pmap, 64, 64);
       if ((e = run_pairs_fp32(L, st)) != cudaSuccess) return h->cuda_fail(e, "fp32 pair kernel");
     }
     ++launches;

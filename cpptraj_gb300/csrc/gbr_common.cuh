@@ -309,30 +309,34 @@ __device__ inline void qcp_vec_f32(const float M[9], float E0, float q[4], float
 // qout (optional) receives the unit quaternion (QCP convention) of the
 // optimal superposition of x'_j onto x'_i, i.e. x'_i ~ R(q)^T x'_j with R(q)
 // the rotation matrix QCP builds from q; only meaningful when t.K == 1.
-static __device__ __noinline__ float pair_epilogue(const float D[9], int64_t i, int64_t j, const FrameTerms& t,
-                                                   bool* flag, float* qout = nullptr) {
-  const int K = t.K;
-  const int a = (K > 1) ? __ldg(t.assign + i) : 0;
-  const int b = (K > 1) ? __ldg(t.assign + j) : 0;
-  const float ni = __ldg(t.nrm + i), nj = __ldg(t.nrm + j);
-  const float* Pja = t.P + ((size_t)j * K + a) * 9;
-  const float* Pib = t.P + ((size_t)i * K + b) * 9;
-  const float* rp = t.RP + (size_t)(b * K + a) * kRefPairStride;
+struct F9 {
+  float v[9];
+};
+
+// Solver part of the epilogue with every per-frame term given (by value, so
+// nothing goes through local memory at the call): P_ja, P_ib, trPia / trPjb
+// (read only when a != b), rp the reference-pair entry of (a, b).
+static __device__ __noinline__ float pair_solve(const F9 Dv, float ni, float nj, const F9 Pjav, const F9 Pibv,
+                                                float trPia, float trPjb, const float* rp, bool same,
+                                                const FrameTerms& t, bool* flag, float* qout = nullptr) {
+  const float* D = Dv.v;
+  const float* Pja = Pjav.v;
+  const float* Pib = Pibv.v;
   const float W = t.W;
   // X = P_ja + P_ib^T + D_ji
   float X[9];
-  X[0] = __ldg(Pja + 0) + __ldg(Pib + 0) + D[0];
-  X[1] = __ldg(Pja + 1) + __ldg(Pib + 3) + D[1];
-  X[2] = __ldg(Pja + 2) + __ldg(Pib + 6) + D[2];
-  X[3] = __ldg(Pja + 3) + __ldg(Pib + 1) + D[3];
-  X[4] = __ldg(Pja + 4) + __ldg(Pib + 4) + D[4];
-  X[5] = __ldg(Pja + 5) + __ldg(Pib + 7) + D[5];
-  X[6] = __ldg(Pja + 6) + __ldg(Pib + 2) + D[6];
-  X[7] = __ldg(Pja + 7) + __ldg(Pib + 5) + D[7];
-  X[8] = __ldg(Pja + 8) + __ldg(Pib + 8) + D[8];
+  X[0] = Pja[0] + Pib[0] + D[0];
+  X[1] = Pja[1] + Pib[3] + D[1];
+  X[2] = Pja[2] + Pib[6] + D[2];
+  X[3] = Pja[3] + Pib[1] + D[3];
+  X[4] = Pja[4] + Pib[4] + D[4];
+  X[5] = Pja[5] + Pib[7] + D[5];
+  X[6] = Pja[6] + Pib[2] + D[6];
+  X[7] = Pja[7] + Pib[5] + D[7];
+  X[8] = Pja[8] + Pib[8] + D[8];
   float G00, g00mag;
   float Y[9];
-  if (a == b) {
+  if (same) {
     const float trD = D[0] + D[4] + D[8];
     const float h = 0.5f * (ni + nj);
     G00 = h - trD;
@@ -348,11 +352,10 @@ static __device__ __noinline__ float pair_epilogue(const float D[9], int64_t i, 
     for (int p = 0; p < 3; ++p)
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
-        uPib += U[p * 3 + q] * __ldg(Pib + p * 3 + q);
-        uPjaT += U[p * 3 + q] * __ldg(Pja + q * 3 + p);
+        uPib += U[p * 3 + q] * Pib[p * 3 + q];
+        uPjaT += U[p * 3 + q] * Pja[q * 3 + p];
         trUD += U[p * 3 + q] * D[q * 3 + p];
       }
-    const float trPia = __ldg(t.trP + i * K + a), trPjb = __ldg(t.trP + j * K + b);
     const float h = 0.5f * (__ldg(rp + 21) + ni + nj);
     G00 = h + trPia - uPib - uPjaT + trPjb - trUD;
     g00mag = h + fabsf(trPia) + fabsf(uPib) + fabsf(uPjaT) + fabsf(trPjb) + fabsf(trUD);
@@ -426,6 +429,31 @@ static __device__ __noinline__ float pair_epilogue(const float D[9], int64_t i, 
   return r;
 }
 
+// The pair epilogue with its per-frame terms read from global memory.
+static __device__ __forceinline__ float pair_epilogue(const float D[9], int64_t i, int64_t j, const FrameTerms& t,
+                                                      bool* flag, float* qout = nullptr) {
+  const int K = t.K;
+  const int a = (K > 1) ? __ldg(t.assign + i) : 0;
+  const int b = (K > 1) ? __ldg(t.assign + j) : 0;
+  const float ni = __ldg(t.nrm + i), nj = __ldg(t.nrm + j);
+  const float* Pja = t.P + ((size_t)j * K + a) * 9;
+  const float* Pib = t.P + ((size_t)i * K + b) * 9;
+  const float* rp = t.RP + (size_t)(b * K + a) * kRefPairStride;
+  F9 dv, pja, pib;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    dv.v[k] = D[k];
+    pja.v[k] = __ldg(Pja + k);
+    pib.v[k] = __ldg(Pib + k);
+  }
+  float trPia = 0.0f, trPjb = 0.0f;
+  if (a != b) {
+    trPia = __ldg(t.trP + i * K + a);
+    trPjb = __ldg(t.trP + j * K + b);
+  }
+  return pair_solve(dv, ni, nj, pja, pib, trPia, trPjb, rp, a == b, t, flag, qout);
+}
+
 __host__ __device__ inline int64_t tri_index(int64_t n, int64_t i, int64_t j) {
   return n * i - ((i + 1) * i) / 2 + j - i - 1;
 }
@@ -440,6 +468,8 @@ struct OutMap {
   int64_t row_begin;  // TRI: ref rows; FULL: target rows
   int64_t row_end;
   int64_t base;       // TRI: tri_index of the first element of row_begin
+  const int* perm;    // TRI over reference-sorted positions: position -> frame
+                      // (whole triangle only; nullptr = positions are frames)
 };
 
 // i: reference frame (0..n_ref), jt: target frame (0..n_tgt).  Returns -1 if
@@ -447,6 +477,13 @@ struct OutMap {
 __device__ __forceinline__ int64_t out_index(const OutMap& m, int64_t i, int64_t jt) {
   if (m.tri) {
     if (!(jt > i) || i < m.row_begin || i >= m.row_end || jt >= m.n_tgt) return -1;
+    if (m.perm) {
+      int64_t a = m.perm[i], b = m.perm[jt];
+      if (a > b) {
+        const int64_t c = a; a = b; b = c;
+      }
+      return tri_index(m.n_ref, a, b);
+    }
     return tri_index(m.n_ref, i, jt) - m.base;
   }
   if (i >= m.n_ref || jt < m.row_begin || jt >= m.row_end) return -1;
@@ -459,7 +496,17 @@ struct FlagList {
   unsigned long long cap;
 };
 
-__device__ __forceinline__ void flag_pair(const FlagList& fl, int64_t i, int64_t jt) {
+// Records a pair for the FP64 re-check, as (reference frame, target frame)
+// of the caller's numbering (sorted positions mapped back through m.perm).
+__device__ __forceinline__ void flag_pair(const FlagList& fl, const OutMap& m, int64_t i, int64_t jt) {
+  if (m.perm) {
+    int64_t a = m.perm[i], b = m.perm[jt];
+    if (a > b) {
+      const int64_t c = a; a = b; b = c;
+    }
+    i = a;
+    jt = b;
+  }
   const unsigned long long k = atomicAdd(fl.count, 1ull);
   if (k < fl.cap) fl.pairs[k] = make_int2((int)i, (int)jt);
 }

@@ -44,6 +44,7 @@ struct PrepArgs {
   double* sqw;     // [N] sqrt of the weights
   float* sqwf;     // [N] the same in FP32
   void* scratch;   // prep_scratch_bytes(F, N, max_refs) bytes (PrepScratch)
+  int sort_frames; // with several references: lay operands out grouped by reference
 };
 
 // Further per-call prep buffers, carved from PrepArgs::scratch.
@@ -59,6 +60,8 @@ struct PrepScratch {
   float4* quat;    // [F] superposition quaternion onto the assigned reference
   float* ymax;     // [F] upper bound of max_a |y_a| (centred frame)
   float* ftab;     // [F][24] rotation hi/lo (9 + 9), R c hi/lo (3 + 3)
+  int* pos;        // [F] frame -> position when frames are laid out sorted by reference
+  int* assign_pos; // [F] reference of the frame at each position
 };
 size_t prep_scratch_bytes(int64_t F, int N, int Kmax);
 PrepScratch prep_carve(void* base, int64_t F, int N, int Kmax);
@@ -67,6 +70,7 @@ PrepScratch prep_carve(void* base, int64_t F, int N, int Kmax);
 // with per-frame scales, per-frame terms n/P/trP, reference-pair table.
 struct FinishArgs {
   const PrepArgs* prep;  // the prep call of the same frames (sources, tables)
+  int sorted;            // PrepOut::sorted of that call
   float* plane;
   int64_t F;
   int N, Np, K;
@@ -91,6 +95,7 @@ cudaError_t run_finish(const FinishArgs& A, cudaStream_t st);
 struct PrepOut {
   int K = 1;
   int launches = 0;
+  int sorted = 0;  // operands and per-frame terms are at sorted positions (PrepScratch::pos)
 };
 
 cudaError_t run_prep(const PrepArgs& A, PrepOut& o, cudaStream_t st);
@@ -146,14 +151,15 @@ struct TcLaunch {
   TileSpace tiles;
   int* dev_error;    // set non-zero when a bounded wait gives up
   int num_sms;
-  int variant;       // 0: 64-atom stages (128B swizzle, 2 stages); 1: 32-atom stages (64B swizzle, 4 stages)
+  int variant;       // 0: 64-atom stages (128B swizzle, 2 stages); 1: 32-atom stages (64B swizzle, 4 stages);
+                     // 2: pairs of SMs (cta_group::2, 32-atom stages, 6 stages)
   int64_t ready_tiles;  // > 0: tile_buf already holds this many tiles (no host build or copy)
 };
 // Tile list of the tensor-core kernel for this map (host side).
 struct TcTileInfo {
   int64_t i_base, jt_base, i_end, jt_end;
 };
-int64_t tc_build_tile_list(const OutMap& m, std::vector<int2>& tiles, TcTileInfo& info);
+int64_t tc_build_tile_list(const OutMap& m, std::vector<int2>& tiles, TcTileInfo& info, int variant = 1);
 cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st);
 int tc_supported(int device);
 int64_t tc_max_tiles(const OutMap& m);

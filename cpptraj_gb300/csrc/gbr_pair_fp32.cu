@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_pairs_fp32(PairLaunch L) {
       for (int c = 0; c < 9; ++c) D[c] = Ds[slot * 9 + c];
       bool flag = false;
       const float rm = pair_epilogue(D, i, L.tgt0 + jt, L.terms, &flag);
-      if (flag) flag_pair(L.flags, i, jt);
+      if (flag) flag_pair(L.flags, L.map, i, jt);
       L.map.out[idx] = rm;
     }
   } else {

@@ -59,14 +59,24 @@ struct Pipe {
   static constexpr uint32_t SBO = 8 * ROW;                 // 8-row core-matrix groups
   static constexpr uint64_t LAYOUT = (KA == 64) ? 2ull : 4ull;  // SWIZZLE_128B : SWIZZLE_64B
 };
-constexpr int EPI_WARPS = 8;
+constexpr int EPI_WARPS = 16;          // four groups of four warps (one per TMEM lane quadrant)
+constexpr int EPI_GROUPS = EPI_WARPS / 4;
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
-constexpr int CH_TGT = 16;             // target frames per epilogue chunk
-constexpr int CH_COLS = 3 * CH_TGT;    // 48 accumulator columns
+constexpr int CH_TGT = 8;              // target frames per epilogue chunk
+constexpr int CH_COLS = 3 * CH_TGT;    // 24 accumulator columns
 constexpr int ST_STRIDE = CH_COLS + 1;
 constexpr int STAGING_BYTES = 128 * ST_STRIDE * 4;
+// Per-tile frame terms staged in shared memory, two buffers.  With A the
+// reference (pre-alignment) of the tile's first reference frame and B that of
+// its first target frame, each frame slot holds n, 1/scale, its reference,
+// trP against its own reference, and P against B (reference frames) or A
+// (target frames): everything a pair with references (A, B) reads.
+constexpr int TERM_STRIDE = 13;
+constexpr int TERM_FLOATS = ((TI + TJ) * TERM_STRIDE + 3) & ~3;
+constexpr int EPI_BYTES = EPI_GROUPS * STAGING_BYTES + 2 * TERM_FLOATS * 4;
 constexpr int BAR_BYTES = 128;
-constexpr int SMEM_BYTES = 1024 + 2 * (2 * UM * 128 + 2 * UN * 128) + 2 * STAGING_BYTES + BAR_BYTES;
+constexpr int SMEM_BYTES = 1024 + 2 * (2 * UM * 128 + 2 * UN * 128) + EPI_BYTES + BAR_BYTES;
+static_assert(SMEM_BYTES <= 232448, "one-SM kernel shared memory");
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t ACC_STRIDE = 256;
 constexpr long long TIMEOUT_CYCLES = 4000000000LL;
@@ -185,10 +195,153 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 #pragma unroll
   for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = __uint_as_float(r[k]);
+}
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 __device__ __forceinline__ void named_sync(int id, int n) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t caddr) {
+  asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(caddr) : "memory");
+}
+
+// Epilogue warps (2 .. 2 + EPI_WARPS): for tiles t0, t0 + tstep, ... wait for
+// the accumulator, stage the tile's frame terms (one reference), read the
+// 128 x 192 FP32 block from tensor memory in 24-column chunks (group g takes
+// chunks g, g + 4, ...), and run the per-pair solve.  The reference frames of
+// a tile start at i_base + ti * ti_frames + i_off.  acce_bar is the address
+// the warps arrive on when the buffer is free (remote: CTA 0 of a pair).
+__device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_base, float* staging, float* terms,
+                                               volatile int* okf, uint32_t accf0, uint32_t acce_bar, bool remote,
+                                               int64_t t0, int64_t tstep, int ti_frames, int i_off, int warp,
+                                               int lane) {
+  const int e = warp - 2;
+  const int g = e >> 2;
+  const int q = warp & 3;               // TMEM lane quadrant this warp may access
+  const int row = 32 * q + lane;        // accumulator row = (reference frame, component)
+  const int tid = (e & 3) * 32 + lane;  // 0..127 within the group
+  const int etid = e * 32 + lane;       // 0..511
+  float* st = staging + g * (128 * ST_STRIDE);
+  const bool tri = P.map.tri;
+  const int K = P.terms.K;
+  uint32_t it = 0;
+  for (int64_t t = t0; t < P.n_tiles; t += tstep, ++it) {
+    const uint32_t b = it & 1u, aph = (it >> 1) & 1u;
+    const int2 tl = P.tiles[t];
+    const int64_t i0 = P.i_base + (int64_t)tl.x * ti_frames + i_off;
+    const int64_t jt0 = P.jt_base + (int64_t)tl.y * TJ;
+    float* T = terms + b * TERM_FLOATS;
+    // Loads overlap the MMAs of this tile; buffer b was last read two tiles
+    // ago, before every group passed the previous tile's barrier.
+    const int A = (K > 1 && i0 < P.i_end) ? __ldg(P.terms.assign + i0) : 0;
+    const int B = (K > 1 && jt0 < P.jt_end) ? __ldg(P.terms.assign + P.tgt0 + jt0) : 0;
+    for (int x = etid; x < (TI + TJ) * TERM_STRIDE; x += EPI_WARPS * 32) {
+      const int sl = x / TERM_STRIDE, k = x - sl * TERM_STRIDE;
+      int64_t f;
+      bool valid;
+      int other;
+      if (sl < TI) {
+        f = i0 + sl;
+        valid = f < P.i_end;
+        other = B;
+      } else {
+        const int64_t jt = jt0 + (sl - TI);
+        f = P.tgt0 + jt;
+        valid = jt < P.jt_end;
+        other = A;
+      }
+      float v = 0.0f;
+      if (valid) {
+        if (k == 0) {
+          v = __ldg(P.terms.nrm + f);
+        } else if (k == 1) {
+          v = __ldg(P.inv_scale + f);
+        } else if (k == 2) {
+          v = __int_as_float(K > 1 ? __ldg(P.terms.assign + f) : 0);
+        } else if (k == 3) {
+          v = (K > 1) ? __ldg(P.terms.trP + f * K + __ldg(P.terms.assign + f)) : 0.0f;
+        } else {
+          v = __ldg(P.terms.P + (f * K + other) * 9 + (k - 4));
+        }
+      }
+      T[x] = v;
+    }
+    // One thread waits; the verdict is shared so every epilogue thread takes
+    // the same path through the named barriers.
+    if (etid == 0) okf[b] = mbar_wait(accf0 + 8 * b, aph, P.err, 5) ? 1 : 0;
+    named_sync(1 + EPI_GROUPS, EPI_WARPS * 32);
+    const bool ok = okf[b] != 0;
+    if (ok) {
+      tc_fence_after();
+      for (int c = g; c < TJ / CH_TGT; c += EPI_GROUPS) {
+        float v[CH_COLS];
+        const uint32_t taddr = tmem_base + ((uint32_t)(32 * q) << 16) + b * ACC_STRIDE + c * CH_COLS;
+        tmem_ld16(taddr, v);
+        tmem_ld8(taddr + 16, v + 16);
+        tmem_wait_ld();
+#pragma unroll
+        for (int k = 0; k < CH_COLS; ++k) st[row * ST_STRIDE + k] = v[k];
+        named_sync(1 + g, 128);
+        const int64_t jc0 = jt0 + (int64_t)c * CH_TGT;
+#pragma unroll 1
+        for (int p = tid; p < TI * CH_TGT; p += 128) {
+          const int il = tri ? p / CH_TGT : p % TI;
+          const int jl = tri ? p % CH_TGT : p / TI;
+          const int64_t i = i0 + il, jt = jc0 + jl;
+          if (i >= P.i_end || jt >= P.jt_end) continue;
+          const int64_t idx = out_index(P.map, i, jt);
+          if (idx < 0) continue;
+          bool flag = false;
+          float r;
+          const float* Ti = T + il * TERM_STRIDE;
+          const float* Tj = T + (TI + c * CH_TGT + jl) * TERM_STRIDE;
+          if (__float_as_int(Ti[2]) == A && __float_as_int(Tj[2]) == B) {
+            const float sc = Ti[1] * Tj[1];
+            F9 D, pja, pib;
+#pragma unroll
+            for (int pj = 0; pj < 3; ++pj)
+#pragma unroll
+              for (int pi = 0; pi < 3; ++pi) D.v[pj * 3 + pi] = st[(3 * il + pi) * ST_STRIDE + 3 * jl + pj] * sc;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+              pja.v[k] = Tj[4 + k];
+              pib.v[k] = Ti[4 + k];
+            }
+            r = pair_solve(D, Ti[0], Tj[0], pja, pib, Ti[3], Tj[3], P.terms.RP + (size_t)(B * K + A) * kRefPairStride,
+                           A == B, P.terms, &flag);
+          } else {
+            const float sc = __ldg(P.inv_scale + i) * __ldg(P.inv_scale + P.tgt0 + jt);
+            float D[9];
+#pragma unroll
+            for (int pj = 0; pj < 3; ++pj)
+#pragma unroll
+              for (int pi = 0; pi < 3; ++pi) D[pj * 3 + pi] = st[(3 * il + pi) * ST_STRIDE + 3 * jl + pj] * sc;
+            r = pair_epilogue(D, i, P.tgt0 + jt, P.terms, &flag);
+          }
+          if (flag) flag_pair(P.flags, P.map, i, jt);
+          P.map.out[idx] = r;
+        }
+        named_sync(1 + g, 128);
+      }
+    }
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) {
+      if (remote)
+        mbar_arrive_remote(acce_bar + 8 * b);
+      else
+        mbar_arrive(acce_bar + 8 * b);
+    }
+    if (!ok) break;
+  }
 }
 
 template <class PP>
@@ -202,10 +355,11 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* stage_base = smem;
   float* staging = (float*)(smem + STAGES * STAGE_BYTES);
-  uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES + 2 * STAGING_BYTES);
+  float* terms = (float*)(smem + STAGES * STAGE_BYTES + EPI_GROUPS * STAGING_BYTES);
+  uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES + EPI_BYTES);
   // bars: full[4] empty[4] accfull[2] accempty[2] done[1]; then the TMEM address.
   uint32_t* tmem_slot = (uint32_t*)(bars + 14);
-  volatile int* grp_ok = (volatile int*)(bars + 15);  // two ints, one per epilogue warpgroup
+  volatile int* okf = (volatile int*)(bars + 15);  // accumulator verdicts, one per buffer
   const uint32_t full0 = smem_u32(bars + 0), empty0 = smem_u32(bars + 4), accf0 = smem_u32(bars + 8),
                  acce0 = smem_u32(bars + 10), done = smem_u32(bars + 12);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -303,65 +457,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
   } else {
     // ---------------- epilogue ----------------
-    const int e = warp - 2;
-    const int g = e >> 2;                 // warpgroup 0/1
-    const int q = warp & 3;               // TMEM lane quadrant this warp may access
-    const int row = 32 * q + lane;        // accumulator row = (ref frame, component)
-    const int tid = (e & 3) * 32 + lane;  // 0..127 within the warpgroup
-    float* st = staging + g * (128 * ST_STRIDE);
-    const bool tri = P.map.tri;
-    uint32_t it = 0;
-    bool ok = true;
-    for (int64_t t = blockIdx.x; t < P.n_tiles; t += gridDim.x, ++it) {
-      const uint32_t b = it & 1u, aph = (it >> 1) & 1u;
-      // One thread per warpgroup waits; the verdict is shared so that every
-      // thread of the group takes the same path through the named barriers.
-      if (tid == 0) grp_ok[g] = mbar_wait(accf0 + 8 * b, aph, P.err, 5) ? 1 : 0;
-      named_sync(1 + g, 128);
-      ok = grp_ok[g] != 0;
-      const int2 tl = P.tiles[t];
-      const int64_t i0 = P.i_base + (int64_t)tl.x * TI;
-      const int64_t jt0 = P.jt_base + (int64_t)tl.y * TJ;
-      if (ok) {
-        tc_fence_after();
-        for (int c = g; c < TJ / CH_TGT; c += 2) {
-          float v[CH_COLS];
-          const uint32_t taddr = tmem_base + ((uint32_t)(32 * q) << 16) + b * ACC_STRIDE + c * CH_COLS;
-          tmem_ld16(taddr, v);
-          tmem_ld16(taddr + 16, v + 16);
-          tmem_ld16(taddr + 32, v + 32);
-          tmem_wait_ld();
-#pragma unroll
-          for (int k = 0; k < CH_COLS; ++k) st[row * ST_STRIDE + k] = v[k];
-          named_sync(1 + g, 128);
-          const int64_t jc0 = jt0 + (int64_t)c * CH_TGT;
-#pragma unroll 1
-          for (int p = tid; p < TI * CH_TGT; p += 128) {
-            const int il = tri ? p / CH_TGT : p % TI;
-            const int jl = tri ? p % CH_TGT : p / TI;
-            const int64_t i = i0 + il, jt = jc0 + jl;
-            if (i >= P.i_end || jt >= P.jt_end) continue;
-            const int64_t idx = out_index(P.map, i, jt);
-            if (idx < 0) continue;
-            const float sc = __ldg(P.inv_scale + i) * __ldg(P.inv_scale + P.tgt0 + jt);
-            float D[9];
-#pragma unroll
-            for (int pj = 0; pj < 3; ++pj)
-#pragma unroll
-              for (int pi = 0; pi < 3; ++pi) D[pj * 3 + pi] = st[(3 * il + pi) * ST_STRIDE + 3 * jl + pj] * sc;
-            bool flag = false;
-            const float r = pair_epilogue(D, i, P.tgt0 + jt, P.terms, &flag);
-            if (flag) flag_pair(P.flags, i, jt);
-            P.map.out[idx] = r;
-          }
-          named_sync(1 + g, 128);
-        }
-      }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(acce0 + 8 * b);
-      if (!ok) break;
-    }
+    epilogue_tiles(P, tmem_base, staging, terms, okf, accf0, acce0, false, blockIdx.x, gridDim.x, TI, 0, warp, lane);
   }
 
   tc_fence_before();
@@ -370,6 +466,225 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (warp == 1) {
     __syncwarp();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pair-of-SMs variant (tcgen05 cta_group::2).  A cluster of two CTAs shares
+// one 256 x 192 MMA: CTA r holds reference frames i0 + 42 r .. +42 (its own
+// 128-row A, rows 126-127 unused) and target frames j0 + 32 r .. +32 (half of
+// B, 96 rows); the MMA issued by CTA 0 reads A from each CTA and B from both,
+// and writes each CTA's 128 x 192 block into that CTA's tensor memory.  Per
+// SM this halves the B bytes loaded by TMA and read from shared memory,
+// which (with the three split products) is what limits the one-SM kernel.
+//   full[s]  in CTA 0: both producers arrive (expect_tx of their own bytes)
+//            and both CTAs' TMA copies complete_tx on it.
+//   empty[s] in each CTA: CTA 0's commit arrives on both (multicast).
+//   accf[b]  in each CTA: CTA 0's commit arrives on both.
+//   acce[b]  in CTA 0: the epilogue warps of both CTAs arrive.
+// ---------------------------------------------------------------------------
+constexpr int TI2 = 2 * TI;            // reference frames per cluster tile (84)
+constexpr int TJH = TJ / 2;            // target frames per CTA half of B (32)
+constexpr int UM2 = 256;
+constexpr int UNH = 3 * TJH;           // 96 B rows per CTA
+constexpr int KA2 = 32;                // atoms per stage (64-byte rows, 64B swizzle)
+constexpr int ROW2 = 2 * KA2;
+constexpr int STAGES2 = 5;
+constexpr int A2_BYTES = UM * ROW2;    // 8 KB (per CTA: 128 rows)
+constexpr int BH_BYTES = UNH * ROW2;   // 6 KB
+constexpr int A2_TX = 3 * TI * ROW2;
+constexpr int BH_TX = UNH * ROW2;
+constexpr int STAGE2_BYTES = 2 * A2_BYTES + 2 * BH_BYTES;
+constexpr int BAR2_BYTES = 256;
+constexpr int SMEM2_BYTES = 1024 + STAGES2 * STAGE2_BYTES + EPI_BYTES + BAR2_BYTES;
+static_assert(SMEM2_BYTES <= 232448, "pair kernel shared memory");
+static_assert(STAGE2_BYTES % 1024 == 0 && A2_BYTES % 1024 == 0 && BH_BYTES % 1024 == 0, "swizzle alignment");
+constexpr uint32_t IDESC2 = (1u << 4) | ((uint32_t)(UN >> 3) << 17) | ((uint32_t)(UM2 >> 4) << 24);
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t mapa_rank(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// Relaxed: the producer publishes no data of its own (the bytes arrive by
+// TMA complete_tx); a release at cluster scope here costs about one
+// round trip per stage and halves the kernel's speed.
+__device__ __forceinline__ void mbar_expect_tx_remote(uint32_t caddr, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.relaxed.cluster.shared::cluster.b64 _, [%0], %1;" ::"r"(caddr), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void tma_load_3d_pair(uint32_t dst, const CUtensorMap* map, int x, int y, int z,
+                                                 uint32_t bar_caddr) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+      "%4}], [%5];" ::"r"(dst),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(bar_caddr)
+      : "memory");
+}
+__device__ __forceinline__ void umma_f16_pair(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(IDESC2), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit_pair(uint32_t bar) {
+  const uint16_t mask = 0x3;
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
+      "h"(mask)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit_pair_local(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ uint64_t smem_desc64(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((8 * ROW2) >> 4) << 32;
+  d |= 1ull << 46;
+  d |= 4ull << 61;  // SWIZZLE_64B
+  return d;
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_pairs_tc2(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
+                const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
+                const TcParams P) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* stage_base = smem;
+  float* staging = (float*)(smem + STAGES2 * STAGE2_BYTES);
+  float* terms = (float*)(smem + STAGES2 * STAGE2_BYTES + EPI_GROUPS * STAGING_BYTES);
+  uint64_t* bars = (uint64_t*)(smem + STAGES2 * STAGE2_BYTES + EPI_BYTES);
+  // bars: full[STAGES2] empty[STAGES2] accf[2] acce[2] done; TMEM address; verdicts.
+  constexpr int kFull = 0, kEmpty = STAGES2, kAccf = 2 * STAGES2, kAcce = 2 * STAGES2 + 2, kDone = 2 * STAGES2 + 4;
+  uint32_t* tmem_slot = (uint32_t*)(bars + kDone + 1);
+  volatile int* okf = (volatile int*)(bars + kDone + 2);
+  const uint32_t full0 = smem_u32(bars + kFull), empty0 = smem_u32(bars + kEmpty), accf0 = smem_u32(bars + kAccf),
+                 acce0 = smem_u32(bars + kAcce), done = smem_u32(bars + kDone);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t rank = cluster_rank();
+  const int64_t cluster = blockIdx.x >> 1, n_clusters = gridDim.x >> 1;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES2; ++s) {
+      mbar_init(full0 + 8 * s, 2);   // one expect_tx arrival per CTA (used in CTA 0)
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(accf0 + 8 * b, 1);
+      mbar_init(acce0 + 8 * b, 2 * EPI_WARPS);  // used in CTA 0
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&tmAh) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&tmAl) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&tmBh) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&tmBl) : "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  cluster_sync_all();  // barriers of both CTAs initialised before any remote arrive
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------- TMA producer (both CTAs) ----------------
+    if (lane == 0) {
+      int s = 0;
+      uint32_t ph = 0;
+      bool ok = true;
+      int last_par[STAGES2];
+      for (int k = 0; k < STAGES2; ++k) last_par[k] = -1;
+      for (int64_t t = cluster; t < P.n_tiles && ok; t += n_clusters) {
+        const int2 tl = P.tiles[t];
+        const int iz = (int)(P.i_base + (int64_t)tl.x * TI2 + (int64_t)rank * TI);
+        const int jz = (int)(P.tgt0 + P.jt_base + (int64_t)tl.y * TJ + (int64_t)rank * TJH);
+        for (int kc = 0; kc < P.nk; ++kc) {
+          if (!mbar_wait(empty0 + 8 * s, ph ^ 1u, P.err, 11)) { ok = false; break; }
+          const uint32_t fb = mapa_rank(full0 + 8 * s, 0);
+          if (rank == 0)
+            mbar_expect_tx(full0 + 8 * s, 2 * A2_TX + 2 * BH_TX);
+          else
+            mbar_expect_tx_remote(fb, 2 * A2_TX + 2 * BH_TX);
+          const uint32_t sb = smem_u32(stage_base + s * STAGE2_BYTES);
+          tma_load_3d_pair(sb, &tmAh, kc * KA2, 0, iz, fb);
+          tma_load_3d_pair(sb + A2_BYTES, &tmAl, kc * KA2, 0, iz, fb);
+          tma_load_3d_pair(sb + 2 * A2_BYTES, &tmBh, kc * KA2, 0, jz, fb);
+          tma_load_3d_pair(sb + 2 * A2_BYTES + BH_BYTES, &tmBl, kc * KA2, 0, jz, fb);
+          last_par[s] = (int)ph;
+          if (++s == STAGES2) { s = 0; ph ^= 1u; }
+        }
+      }
+      // CTA 0 sees every copy of both CTAs complete on its full barriers.
+      if (rank == 0)
+        for (int k = 0; k < STAGES2; ++k)
+          if (last_par[k] >= 0) mbar_wait_quiet(full0 + 8 * k, (uint32_t)last_par[k]);
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer (CTA 0 only) ----------------
+    if (lane == 0 && rank == 0) {
+      int s = 0;
+      uint32_t ph = 0;
+      uint32_t it = 0;
+      bool ok = true;
+      for (int64_t t = cluster; t < P.n_tiles && ok; t += n_clusters, ++it) {
+        const uint32_t b = it & 1u, aph = (it >> 1) & 1u;
+        if (!mbar_wait(acce0 + 8 * b, aph ^ 1u, P.err, 12)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t d = tmem_base + b * ACC_STRIDE;
+        for (int kc = 0; kc < P.nk; ++kc) {
+          if (!mbar_wait(full0 + 8 * s, ph, P.err, 13)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t sb = smem_u32(stage_base + s * STAGE2_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < KA2 / 16; ++kk) {
+            const uint64_t ah = smem_desc64(sb + kk * 32), al = smem_desc64(sb + A2_BYTES + kk * 32);
+            const uint64_t bh = smem_desc64(sb + 2 * A2_BYTES + kk * 32);
+            const uint64_t bl = smem_desc64(sb + 2 * A2_BYTES + BH_BYTES + kk * 32);
+            umma_f16_pair(d, ah, bh, (kc | kk) != 0);
+            umma_f16_pair(d, al, bh, 1u);
+            umma_f16_pair(d, ah, bl, 1u);
+          }
+          umma_commit_pair(empty0 + 8 * s);  // frees stage s in both CTAs
+          if (++s == STAGES2) { s = 0; ph ^= 1u; }
+        }
+        if (!ok) break;
+        umma_commit_pair(accf0 + 8 * b);
+      }
+      umma_commit_pair_local(done);
+      mbar_wait_quiet(done, 0);
+    }
+  } else {
+    // ---------------- epilogue (both CTAs) ----------------
+    epilogue_tiles(P, tmem_base, staging, terms, okf, accf0, mapa_rank(acce0, 0), true, cluster, n_clusters, TI2,
+                   (int)rank * TI, warp, lane);
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  cluster_sync_all();  // CTA 0's MMAs (writing both CTAs' tensor memory) have retired
+  tc_fence_after();
+  if (warp == 1) {
+    __syncwarp();
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS)
                  : "memory");
   }
 }
@@ -414,7 +729,7 @@ int tc_tile_cols() { return TJ; }
 // Tile list in grouped order: groups of G tile-rows are swept column by
 // column so the CTAs in flight share A and B frames in L2.
 int64_t tc_build_tiles(const OutMap& m, std::vector<int2>& tiles, int64_t& i_base, int64_t& jt_base,
-                       int64_t& i_end, int64_t& jt_end) {
+                       int64_t& i_end, int64_t& jt_end, int ti_frames = TI) {
   if (m.tri) {
     i_base = m.row_begin;
     i_end = m.row_end;
@@ -427,13 +742,13 @@ int64_t tc_build_tiles(const OutMap& m, std::vector<int2>& tiles, int64_t& i_bas
     jt_end = m.row_end;
   }
   tiles.clear();
-  const int64_t Ti = (i_end - i_base + TI - 1) / TI, Tj = (jt_end - jt_base + TJ - 1) / TJ;
+  const int64_t Ti = (i_end - i_base + ti_frames - 1) / ti_frames, Tj = (jt_end - jt_base + TJ - 1) / TJ;
   const int64_t G = 8;
   for (int64_t g0 = 0; g0 < Ti; g0 += G) {
     for (int64_t tj = 0; tj < Tj; ++tj) {
       for (int64_t ti = g0; ti < std::min(Ti, g0 + G); ++ti) {
         if (m.tri) {
-          const int64_t ilo = i_base + ti * TI;
+          const int64_t ilo = i_base + ti * ti_frames;
           const int64_t jhi = jt_base + tj * TJ + TJ - 1;
           if (jhi <= ilo) continue;  // no pair with target > reference
         }
@@ -444,8 +759,39 @@ int64_t tc_build_tiles(const OutMap& m, std::vector<int2>& tiles, int64_t& i_bas
   return (int64_t)tiles.size();
 }
 
-int64_t tc_build_tile_list(const OutMap& m, std::vector<int2>& tiles, TcTileInfo& info) {
-  return tc_build_tiles(m, tiles, info.i_base, info.jt_base, info.i_end, info.jt_end);
+int64_t tc_build_tile_list(const OutMap& m, std::vector<int2>& tiles, TcTileInfo& info, int variant) {
+  return tc_build_tiles(m, tiles, info.i_base, info.jt_base, info.i_end, info.jt_end, variant == 2 ? TI2 : TI);
+}
+
+// Launch of the pair-of-SMs kernel: clusters of two CTAs, as many clusters
+// as can be resident at once (one CTA per SM), at most one per tile.
+static cudaError_t launch_pair_kernel(const CUtensorMap& mAh, const CUtensorMap& mAl, const CUtensorMap& mBh,
+                                      const CUtensorMap& mBl, const TcParams& P, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(k_pairs_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_BYTES);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(THREADS, 1, 1);
+  cfg.dynamicSmemBytes = SMEM2_BYTES;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  static int max_clusters = 0;
+  if (max_clusters == 0) {
+    cfg.gridDim = dim3(2 * 76, 1, 1);
+    int n = 0;
+    e = cudaOccupancyMaxActiveClusters(&n, k_pairs_tc2, &cfg);
+    if (e != cudaSuccess) return e;
+    if (n < 1) return cudaErrorInvalidConfiguration;
+    max_clusters = n;
+  }
+  const int64_t nc = std::min<int64_t>(P.n_tiles, (int64_t)max_clusters);
+  cfg.gridDim = dim3((unsigned)(2 * nc), 1, 1);
+  return cudaLaunchKernelEx(&cfg, k_pairs_tc2, mAh, mAl, mBh, mBl, P);
 }
 
 cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
@@ -453,15 +799,17 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
   int64_t i_base, jt_base, i_end, jt_end;
   int64_t n;
   cudaError_t e = cudaSuccess;
+  const bool pair = (L.variant == 2);
+  const int ti_frames = pair ? TI2 : TI;
   if (L.ready_tiles > 0) {
     // The caller uploaded the list already (batched / graph-captured path).
     TcTileInfo info;
     std::vector<int2> none;
-    tc_build_tiles(L.map, none, info.i_base, info.jt_base, info.i_end, info.jt_end);
+    tc_build_tiles(L.map, none, info.i_base, info.jt_base, info.i_end, info.jt_end, ti_frames);
     i_base = info.i_base; jt_base = info.jt_base; i_end = info.i_end; jt_end = info.jt_end;
     n = L.ready_tiles;
   } else {
-    n = tc_build_tiles(L.map, tiles, i_base, jt_base, i_end, jt_end);
+    n = tc_build_tiles(L.map, tiles, i_base, jt_base, i_end, jt_end, ti_frames);
     if (n == 0) return cudaSuccess;
     if (!L.tile_buf || n > L.tile_cap) return cudaErrorInvalidValue;
     e = cudaMemcpyAsync(L.tile_buf, tiles.data(), sizeof(int2) * n, cudaMemcpyHostToDevice, st);
@@ -469,10 +817,11 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
     // The copy reads `tiles` asynchronously from pageable memory; cudaMemcpyAsync
     // from pageable memory returns after the source has been consumed.
   }
-  const int ka = (L.variant == 1) ? 32 : 64;
+  const int ka = (L.variant == 0) ? 64 : 32;
+  const int bj = pair ? TJH : TJ;
   CUtensorMap mAh, mAl, mBh, mBl;
   if (!make_map(&mAh, L.hi, L.F, L.Np, TI, ka) || !make_map(&mAl, L.lo, L.F, L.Np, TI, ka) ||
-      !make_map(&mBh, L.hi, L.F, L.Np, TJ, ka) || !make_map(&mBl, L.lo, L.F, L.Np, TJ, ka))
+      !make_map(&mBh, L.hi, L.F, L.Np, bj, ka) || !make_map(&mBl, L.lo, L.F, L.Np, bj, ka))
     return cudaErrorInvalidValue;
   TcParams P{};
   P.tiles = (const int2*)L.tile_buf;
@@ -488,6 +837,11 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
   P.map = L.map;
   P.flags = L.flags;
   P.err = L.dev_error;
+  if (pair) {
+    e = launch_pair_kernel(mAh, mAl, mBh, mBl, P, st);
+    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+  }
   const int grid = (int)std::min<int64_t>(n, L.num_sms > 0 ? L.num_sms : 148);
   if (ka == 64) {
     e = cudaFuncSetAttribute(k_pairs_tc<Pipe<64>>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);

@@ -66,6 +66,7 @@ size_t prep_scratch_bytes(int64_t F, int N, int Kmax) {
   b += align256(sizeof(float4) * F);
   b += align256(sizeof(float) * F);
   b += align256(sizeof(float) * kFtab * F);
+  b += align256(sizeof(int) * F) * 2;
   return b;
 }
 
@@ -88,6 +89,8 @@ PrepScratch prep_carve(void* base, int64_t F, int N, int Kmax) {
   s.quat = (float4*)take(sizeof(float4) * F);
   s.ymax = (float*)take(sizeof(float) * F);
   s.ftab = (float*)take(sizeof(float) * kFtab * F);
+  s.pos = (int*)take(sizeof(int) * F);
+  s.assign_pos = (int*)take(sizeof(int) * F);
   return s;
 }
 
@@ -726,6 +729,8 @@ struct BuildArgs {
   float* nrm;
   float* P;
   float* trP;
+  const int* pos;       // frame -> position of its operands and terms (nullptr = same)
+  int* assign_pos;      // reference of the frame at each position (with pos)
 };
 
 // Final operands, one warp per frame.  p = sqrt(w)(R y - r_a) by Dot2.  The
@@ -742,6 +747,8 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
   for (int64_t f = blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5); f < F; f += (int64_t)gridDim.x * kWarps) {
     const T* x = src.frame(f);
     const int ra = b.assign[f];
+    const int64_t pf = b.pos ? (int64_t)b.pos[f] : f;  // where this frame's operands go
+    if (b.pos && lane == 0) b.assign_pos[pf] = ra;
     FrameTable Tb;
     load_table(b.ftab, f, lane, Tb);
     float scale = 1.0f, inv = 1.0f;
@@ -752,11 +759,11 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
       e = max(-100, min(100, e));
       scale = ldexpf(1.0f, 14 - e);
       inv = ldexpf(1.0f, e - 14);
-      if (lane == 0) b.inv_scale[f] = inv;
+      if (lane == 0) b.inv_scale[pf] = inv;
     }
     const float2* rr = b.refhl + (size_t)ra * 3 * N;
     const float* r0 = b.swr;  // reference 0 for the fused P term
-    const size_t base = (size_t)f * 3 * Np;
+    const size_t base = (size_t)pf * 3 * Np;
     float acc[10];
 #pragma unroll
     for (int q = 0; q < 10; ++q) acc[q] = 0.0f;
@@ -807,10 +814,10 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
     }
     warp_sum_f32<10>(acc);
     if (lane == 0) {
-      b.nrm[f] = acc[9];
-      float* Pf = b.P + (size_t)f * b.K * 9;
+      b.nrm[pf] = acc[9];
+      float* Pf = b.P + (size_t)pf * b.K * 9;
       for (int q = 0; q < 9; ++q) Pf[q] = acc[q];
-      b.trP[(size_t)f * b.K] = acc[0] + acc[4] + acc[8];
+      b.trP[(size_t)pf * b.K] = acc[0] + acc[4] + acc[8];
     }
     // P against the other references: read the operands back (this lane's own
     // writes, same atom mapping).
@@ -834,9 +841,9 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
       }
       warp_sum_f32<9>(h9);
       if (lane == 0) {
-        float* Pf = b.P + ((size_t)f * b.K + c) * 9;
+        float* Pf = b.P + ((size_t)pf * b.K + c) * 9;
         for (int q = 0; q < 9; ++q) Pf[q] = h9[q];
-        b.trP[(size_t)f * b.K + c] = h9[0] + h9[4] + h9[8];
+        b.trP[(size_t)pf * b.K + c] = h9[0] + h9[4] + h9[8];
       }
     }
   }
@@ -989,6 +996,13 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
     for (int64_t f = 0; f < F; ++f) ord[fill[asg[f]]++] = (int)f;
     cudaMemcpyAsync(A.order, ord.data(), sizeof(int) * F, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(A.offsets, offs.data(), sizeof(int) * (K + 1), cudaMemcpyHostToDevice, st);
+    std::vector<int> pos;
+    if (A.sort_frames) {
+      pos.resize(F);
+      for (int64_t p = 0; p < F; ++p) pos[ord[p]] = (int)p;
+      cudaMemcpyAsync(S.pos, pos.data(), sizeof(int) * F, cudaMemcpyHostToDevice, st);
+      o.sorted = 1;
+    }
     // the copies read host vectors that go out of scope: finish them here
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return e;
@@ -1033,6 +1047,8 @@ static cudaError_t finish_impl(const FinishArgs& fa, cudaStream_t st) {
   b.nrm = fa.nrm;
   b.P = fa.P;
   b.trP = fa.trP;
+  b.pos = fa.sorted ? S.pos : nullptr;
+  b.assign_pos = S.assign_pos;
   k_build<T><<<prep_grid(A.F), kPrepThreads, 0, st>>>(src, A.F, b);
   k_ref_terms<<<fa.K * fa.K, kPrepThreads, 0, st>>>(A.refs, A.N, fa.K, A.w, A.nofit, fa.RP);
   return cudaGetLastError();

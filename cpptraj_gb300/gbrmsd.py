@@ -22,6 +22,8 @@ FIT, NOFIT = 0, 1
 TRI, FULL = 0, 1
 PREC_FP32, PREC_TC, PREC_FP64 = 0, 1, 2
 OPT_TAU, OPT_MAX_REFS, OPT_TOL, OPT_TIMING, OPT_TC_PIPELINE = 0, 1, 2, 3, 4
+#: The library's default tensor-core kernel shape (pairs of SMs).
+TC_PIPELINE_DEFAULT = 2
 
 PRECISIONS = {"fp32": PREC_FP32, "tc": PREC_TC, "fp64": PREC_FP64}
 MODES = {"fit": FIT, "nofit": NOFIT}

@@ -172,8 +172,9 @@ int gbr_get_stats(const gbr_handle *h, gbr_stats *out);
  *   GBR_OPT_MAX_REFS     maximum pre-alignment references (1..64, default 32)
  *   GBR_OPT_TOL          per-pair error target in Angstrom (default 5e-5)
  *   GBR_OPT_TIMING       1 = record per-kernel device times in gbr_stats
- *   GBR_OPT_TC_PIPELINE  tensor-core stage shape: 0 = 64-atom stages x 2,
- *                        1 = 32-atom stages x 4 (default 1)
+ *   GBR_OPT_TC_PIPELINE  tensor-core kernel shape: 0 = one SM, 64-atom stages x 2,
+ *                        1 = one SM, 32-atom stages x 4, 2 = pairs of SMs
+ *                        sharing one 256-row MMA, 32-atom stages x 5 (default 2)
  */
 enum gbr_option { GBR_OPT_TAU = 0, GBR_OPT_MAX_REFS = 1, GBR_OPT_TOL = 2, GBR_OPT_TIMING = 3,
                   GBR_OPT_TC_PIPELINE = 4 };

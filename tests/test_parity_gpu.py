@@ -113,6 +113,28 @@ def test_clustered_frames(h, precision):
     assert h.stats()["n_refs"] >= 2
 
 
+@pytest.mark.parametrize("pipeline", [1, 2])
+@pytest.mark.parametrize("precision", ["fp32", "tc"])
+def test_clustered_sorted_layout(h, pipeline, precision):
+    # frames from 12 interleaved centroids: a whole triangle is computed over
+    # frames re-ordered by reference, a row range over the original order
+    X, _ = synth.clustered(5, 700, 300, 12, 0.8)
+    ref = oracle.allpairs_f64(X)
+    h.set_option(gbrmsd.OPT_TC_PIPELINE, pipeline)
+    try:
+        out = run(h, X, precision=precision)
+        st = h.stats()
+        assert st["n_refs"] >= 2
+        assert np.abs(out - ref).max() <= TOL
+        assert st["pairs_fixed"] <= st["pairs"] // 100, st
+        part = run(h, X, precision=precision, row_begin=100, row_end=400)
+        lo = 100 * 700 - 100 * 101 // 2
+        hi = 400 * 700 - 400 * 401 // 2
+        assert np.abs(part - ref[lo:hi]).max() <= TOL
+    finally:
+        h.set_option(gbrmsd.OPT_TC_PIPELINE, gbrmsd.TC_PIPELINE_DEFAULT)
+
+
 @pytest.mark.parametrize("precision", _precisions())
 def test_nofit(h, precision):
     X, m = synth.trajectory(8, 130, 77, 0.2, 2.0, np.float32, True)
@@ -195,12 +217,37 @@ def test_tc_matches_fp32_closely(h):
     assert np.abs(a - b).max() <= TOL
 
 
-@pytest.mark.parametrize("pipeline", [0, 1])
-@pytest.mark.parametrize("F,N", [(67, 129), (300, 2000), (129, 31), (2, 65)])
+@pytest.mark.parametrize("pipeline", [0, 1, 2])
+@pytest.mark.parametrize("F,N", [(67, 129), (300, 2000), (129, 31), (2, 65), (171, 200)])
 def test_tc_pipeline_variants(h, pipeline, F, N):
     X, m = synth.trajectory(F * 7 + N, F, N, 0.1, 3.0, np.float32, True)
     h.set_option(gbrmsd.OPT_TC_PIPELINE, pipeline)
     try:
         _check(h, X, m, "tc")
+        st = h.stats()
+        # the contraction itself must be right: the FP64 re-check may only
+        # touch the odd pair, not stand in for the tensor-core result
+        assert st["pairs_fixed"] <= max(1, st["pairs"] // 100), st
     finally:
-        h.set_option(gbrmsd.OPT_TC_PIPELINE, 1)
+        h.set_option(gbrmsd.OPT_TC_PIPELINE, gbrmsd.TC_PIPELINE_DEFAULT)
+
+
+@pytest.mark.parametrize("pipeline", [1, 2])
+def test_tc_pipeline_full_and_rows(h, pipeline):
+    R, m = synth.trajectory(77, 130, 257, 0.1, 3.0, np.float32, True)
+    T, _ = synth.trajectory(78, 201, 257, 0.1, 3.0, np.float32, True)
+    ref = oracle.allpairs_f64(R, T, tgt_mass=m).reshape(201, 130)
+    tri_ref = oracle.allpairs_f64(R, tgt_mass=m)
+    h.set_option(gbrmsd.OPT_TC_PIPELINE, pipeline)
+    try:
+        full = run(h, R, T, tgt_mass=m, precision="tc").reshape(201, 130)
+        assert np.abs(full - ref).max() <= TOL
+        assert h.stats()["pairs_fixed"] <= 201 * 130 // 100
+        part = run(h, R, T, tgt_mass=m, precision="tc", row_begin=37, row_end=161).reshape(124, 130)
+        assert np.abs(part - ref[37:161]).max() <= TOL
+        tri = run(h, R, tgt_mass=m, precision="tc", row_begin=50, row_end=120)
+        lo = 50 * 130 - 50 * 51 // 2
+        hi = 120 * 130 - 120 * 121 // 2
+        assert np.abs(tri - tri_ref[lo:hi]).max() <= TOL
+    finally:
+        h.set_option(gbrmsd.OPT_TC_PIPELINE, gbrmsd.TC_PIPELINE_DEFAULT)

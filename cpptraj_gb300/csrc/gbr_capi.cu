@@ -22,6 +22,10 @@
 
 using namespace gbr;
 
+namespace {
+constexpr int kMaxBands = 8;  // output row bands whose copies overlap the contraction
+}
+
 extern "C" {
 
 gbr_handle* gbr_create(int device) {
@@ -212,7 +216,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     p[18] = A.take<int>(F);                                             // frames by reference
     p[19] = A.take<int>(Kmax + 1);                                      // offsets
     p[20] = A.take<int2>(flag_cap);                                     // flagged
-    p[21] = A.take<unsigned long long>(1);                              // count
+    p[21] = A.take<unsigned long long>(kMaxBands);                      // counts (one per band)
     p[22] = out_dev ? nullptr : A.take<float>(n_out);                   // out staging
     p[23] = tc ? A.take<__half_raw>((size_t)F * 3 * Np) : nullptr;      // hi
     p[24] = tc ? A.take<__half_raw>((size_t)F * 3 * Np) : nullptr;      // lo
@@ -238,8 +242,34 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
   // ---- stage inputs ----
   const void* d_ref = ref_dev ? ref_xyz : P[0];
   const void* d_tgt = tgt_xyz ? (tgt_dev ? tgt_xyz : P[1]) : nullptr;
-  if (!ref_dev) cudaMemcpyAsync(P[0], ref_xyz, esz * 3 * (size_t)N * n_ref, cudaMemcpyDefault, st);
-  if (tgt_xyz && !tgt_dev) cudaMemcpyAsync(P[1], tgt_xyz, esz * 3 * (size_t)N * n_tgt, cudaMemcpyDefault, st);
+  // Pinned host inputs of some size travel in chunks on the copy stream; the
+  // first prep pass starts on each chunk as it lands.
+  const size_t in_bytes = esz * 3 * (size_t)N * (size_t)F;
+  const bool chunk_in = need_planes && (!ref_dev || (tgt_xyz && !tgt_dev)) && in_bytes >= (32u << 20) &&
+                        is_pinned_or_device(ref_xyz) && (!tgt_xyz || is_pinned_or_device(tgt_xyz)) &&
+                        h->ensure_xfer();
+  int n_chunks = 0;
+  int64_t chunk_end[8];
+  if (chunk_in) {
+    cudaEventRecord(h->xev[h->kXev - 1], st);  // the copies follow earlier work on the caller's stream
+    cudaStreamWaitEvent(h->xfer, h->xev[h->kXev - 1], 0);
+    auto add_chunks = [&](const void* src, void* dst, int64_t set0, int64_t nf, bool dev, int parts) {
+      for (int c = 0; c < parts; ++c) {
+        const int64_t a = nf * c / parts, b = nf * (c + 1) / parts;
+        if (b <= a) continue;
+        if (!dev)
+          cudaMemcpyAsync((char*)dst + esz * 3 * (size_t)N * a, (const char*)src + esz * 3 * (size_t)N * a,
+                          esz * 3 * (size_t)N * (b - a), cudaMemcpyHostToDevice, h->xfer);
+        cudaEventRecord(h->xev[n_chunks], h->xfer);
+        chunk_end[n_chunks++] = set0 + b;
+      }
+    };
+    add_chunks(ref_xyz, P[0], 0, n_ref, ref_dev, tgt_xyz ? 4 : 8);
+    if (tgt_xyz) add_chunks(tgt_xyz, P[1], n_ref, n_tgt, tgt_dev, 4);
+  } else {
+    if (!ref_dev) cudaMemcpyAsync(P[0], ref_xyz, esz * 3 * (size_t)N * n_ref, cudaMemcpyDefault, st);
+    if (tgt_xyz && !tgt_dev) cudaMemcpyAsync(P[1], tgt_xyz, esz * 3 * (size_t)N * n_tgt, cudaMemcpyDefault, st);
+  }
   double* d_w = tgt_mass ? (double*)P[2] : nullptr;
   double* d_wref = nullptr;
   if (tgt_mass) {
@@ -249,7 +279,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
       cudaMemcpyAsync(d_wref, wref_h.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st);
     }
   }
-  cudaMemsetAsync(P[21], 0, sizeof(unsigned long long), st);
+  cudaMemsetAsync(P[21], 0, sizeof(unsigned long long) * kMaxBands, st);
   cudaMemsetAsync(P[25], 0, sizeof(int), st);
 
   map.out = out_dev ? out : (float*)P[22];
@@ -290,6 +320,11 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
   // out grouped by reference (tiles then share their references, whose terms
   // the tensor-core epilogue stages per tile); outputs map back to frames.
   pa.sort_frames = (map.tri && row_begin == 0 && row_end == n_ref) ? 1 : 0;
+  pa.n_chunks = n_chunks;
+  for (int c = 0; c < n_chunks; ++c) {
+    pa.chunk_end[c] = chunk_end[c];
+    pa.chunk_ev[c] = h->xev[c];
+  }
 
   ExactLaunch ex{};
   ex.dtype_f64 = pa.dtype_f64;
@@ -372,60 +407,150 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     fa.RP = (float*)terms.RP;
     if ((e = run_finish(fa, st)) != cudaSuccess) return h->cuda_fail(e, "finish");
     launches += 2;
-    FlagList fl{(int2*)P[20], (unsigned long long*)P[21], flag_cap};
-    if (h->timing) cudaEventRecord(h->ev[1], st);
-    if (tc) {
-      TcLaunch L{};
-      L.hi = P[23];
-      L.lo = P[24];
-      L.tile_buf = P[26];
-      L.tile_cap = tc_tiles;
-      L.F = F;
-      L.Np = Np;
-      L.N = N;
-      L.tgt0 = tgt0;
-      L.inv_scale = (const float*)P[13];
-      L.terms = terms;
-      L.map = pmap;
-      L.flags = fl;
-      L.dev_error = (int*)P[25];
-      L.num_sms = h->num_sms;
-      L.variant = h->tc_variant;
-      if ((e = run_pairs_tc(L, st)) != cudaSuccess) return h->cuda_fail(e, "tensor-core pair kernel");
-    } else {
+    // One launch of the pair kernel over the rows of map m.
+    auto launch_pairs = [&](const OutMap& m, const FlagList& f) -> cudaError_t {
+      if (tc) {
+        TcLaunch L{};
+        L.hi = P[23];
+        L.lo = P[24];
+        L.tile_buf = P[26];
+        L.tile_cap = tc_tiles;
+        L.F = F;
+        L.Np = Np;
+        L.N = N;
+        L.tgt0 = tgt0;
+        L.inv_scale = (const float*)P[13];
+        L.terms = terms;
+        L.map = m;
+        L.flags = f;
+        L.dev_error = (int*)P[25];
+        L.num_sms = h->num_sms;
+        L.variant = h->tc_variant;
+        return run_pairs_tc(L, st);
+      }
       PairLaunch L{};
       L.plane = pa.plane;
       L.Np = Np;
       L.N = N;
       L.tgt0 = tgt0;
       L.terms = terms;
-      L.map = pmap;
-      L.flags = fl;
-      L.tiles = make_tiles(pmap, 64, 64);
-      if ((e = run_pairs_fp32(L, st)) != cudaSuccess) return h->cuda_fail(e, "fp32 pair kernel");
-    }
-    ++launches;
-    if (h->timing) cudaEventRecord(h->ev[2], st);
-    cudaMemcpyAsync(&nflag, P[21], sizeof nflag, cudaMemcpyDeviceToHost, st);
+      L.map = m;
+      L.flags = f;
+      L.tiles = make_tiles(m, 64, 64);
+      return run_pairs_fp32(L, st);
+    };
+    if (h->timing) cudaEventRecord(h->ev[1], st);
+    // A large result bound for pinned host memory leaves in row bands: each
+    // band's pairs are computed and checked (FP64 re-check of its flagged
+    // pairs, list length read on the device), then copied on the copy stream
+    // while the next band computes.
+    const bool band_out = !out_dev && !po.sorted && is_pinned_or_device(out) &&
+                          (size_t)n_out * sizeof(float) >= (32u << 20) && h->ensure_xfer();
     int derr = 0;
-    cudaMemcpyAsync(&derr, P[25], sizeof derr, cudaMemcpyDeviceToHost, st);
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return h->cuda_fail(e, "pair kernel");
-    if (derr != 0)
-      return h->fail(GBR_ERR_DEVICE, "pair kernel reported device error %d (bounded wait expired)", derr);
-    if (nflag > 0) {
-      if (nflag <= flag_cap) {
-        ex.list = (const int2*)P[20];
-        ex.count = (int64_t)nflag;
-      } else {
-        ex.list = nullptr;  // too many: recompute everything exactly
-        ex.count = n_out;
-      }
-      if ((e = run_exact(ex, st)) != cudaSuccess) return h->cuda_fail(e, "fix-up kernel");
+    if (!band_out) {
+      FlagList fl{(int2*)P[20], (unsigned long long*)P[21], flag_cap};
+      if ((e = launch_pairs(pmap, fl)) != cudaSuccess) return h->cuda_fail(e, "pair kernel launch");
       ++launches;
+      if (h->timing) cudaEventRecord(h->ev[2], st);
+      cudaMemcpyAsync(&nflag, P[21], sizeof nflag, cudaMemcpyDeviceToHost, st);
+      cudaMemcpyAsync(&derr, P[25], sizeof derr, cudaMemcpyDeviceToHost, st);
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return h->cuda_fail(e, "pair kernel");
+      if (derr != 0)
+        return h->fail(GBR_ERR_DEVICE, "pair kernel reported device error %d (bounded wait expired)", derr);
+      if (nflag > 0) {
+        if (nflag <= flag_cap) {
+          ex.list = (const int2*)P[20];
+          ex.count = (int64_t)nflag;
+        } else {
+          ex.list = nullptr;  // too many: recompute everything exactly
+          ex.count = n_out;
+        }
+        if ((e = run_exact(ex, st)) != cudaSuccess) return h->cuda_fail(e, "fix-up kernel");
+        ++launches;
+      }
+      if (h->timing) cudaEventRecord(h->ev[3], st);
+      if (!out_dev) cudaMemcpyAsync(out, map.out, sizeof(float) * n_out, cudaMemcpyDefault, st);
+    } else {
+      // Band boundaries: equal pair counts, aligned to the kernel's tile rows.
+      const int64_t align = tc ? 84 : 64;
+      const int nb = kMaxBands - 2;
+      std::vector<int64_t> cut{row_begin};
+      const int64_t total = n_out;
+      int64_t acc = 0;
+      for (int64_t r = row_begin; r < row_end && (int)cut.size() < nb; ++r) {
+        acc += map.tri ? (n_ref - 1 - r) : n_ref;
+        const int64_t r1 = r + 1;
+        if (acc * nb >= total * (int64_t)cut.size() && (r1 - row_begin) % align == 0 && r1 < row_end) cut.push_back(r1);
+      }
+      cut.push_back(row_end);
+      const int nbands = (int)cut.size() - 1;
+      const unsigned long long capb = flag_cap / (unsigned long long)nbands;
+      unsigned long long* counts = (unsigned long long*)P[21];
+      for (int b = 0; b < nbands; ++b) {
+        const int64_t rb = cut[b], re = cut[b + 1];
+        const int64_t cnt = gbr_output_count(n_ref, n_tgt, out_kind, rb, re);
+        if (cnt <= 0) continue;
+        OutMap mb = map;
+        mb.row_begin = rb;
+        mb.row_end = re;
+        int64_t off;
+        if (map.tri) {
+          mb.base = (rb < n_ref - 1) ? tri_index(n_ref, rb, rb + 1) : 0;
+          off = mb.base - map.base;
+        } else {
+          off = (rb - row_begin) * n_ref;
+        }
+        mb.out = map.out + off;
+        FlagList fb{(int2*)P[20] + (size_t)b * capb, counts + b, capb};
+        if ((e = launch_pairs(mb, fb)) != cudaSuccess) return h->cuda_fail(e, "pair kernel launch");
+        ExactLaunch exb = ex;
+        exb.map = mb;
+        exb.list = fb.pairs;
+        exb.count = (int64_t)capb;
+        exb.dev_count = counts + b;
+        if ((e = run_exact(exb, st)) != cudaSuccess) return h->cuda_fail(e, "fix-up kernel");
+        launches += 2;
+        cudaEventRecord(h->xev[8 + b], st);
+        cudaStreamWaitEvent(h->xfer, h->xev[8 + b], 0);
+        cudaMemcpyAsync(out + off, mb.out, sizeof(float) * cnt, cudaMemcpyDeviceToHost, h->xfer);
+      }
+      if (h->timing) {
+        cudaEventRecord(h->ev[2], st);
+        cudaEventRecord(h->ev[3], st);
+      }
+      std::vector<unsigned long long> cnts(nbands);
+      cudaMemcpyAsync(cnts.data(), counts, sizeof(unsigned long long) * nbands, cudaMemcpyDeviceToHost, st);
+      cudaMemcpyAsync(&derr, P[25], sizeof derr, cudaMemcpyDeviceToHost, st);
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return h->cuda_fail(e, "pair kernel");
+      if (derr != 0) {
+        cudaStreamSynchronize(h->xfer);
+        return h->fail(GBR_ERR_DEVICE, "pair kernel reported device error %d (bounded wait expired)", derr);
+      }
+      bool overflow = false;
+      for (int b = 0; b < nbands; ++b) {
+        nflag += cnts[b];
+        overflow |= cnts[b] > capb;
+      }
+      if (overflow) {
+        // a band flagged more pairs than its list holds: recompute everything
+        // exactly and send the whole result again
+        cudaEventRecord(h->xev[h->kXev - 2], h->xfer);
+        cudaStreamWaitEvent(st, h->xev[h->kXev - 2], 0);
+        ex.list = nullptr;
+        ex.count = n_out;
+        if ((e = run_exact(ex, st)) != cudaSuccess) return h->cuda_fail(e, "fix-up kernel");
+        ++launches;
+        cudaMemcpyAsync(out, map.out, sizeof(float) * n_out, cudaMemcpyDeviceToHost, st);
+        nflag = (unsigned long long)n_out;
+      }
     }
   }
-  if (h->timing) cudaEventRecord(h->ev[3], st);
-  if (!out_dev) cudaMemcpyAsync(out, map.out, sizeof(float) * n_out, cudaMemcpyDefault, st);
+  if (h->timing && !need_planes) cudaEventRecord(h->ev[3], st);
+  if (!need_planes && !out_dev) cudaMemcpyAsync(out, map.out, sizeof(float) * n_out, cudaMemcpyDefault, st);
+  if (h->xfer) {  // the copy stream's work belongs to this call
+    cudaEventRecord(h->xev[h->kXev - 3], h->xfer);
+    cudaStreamWaitEvent(st, h->xev[h->kXev - 3], 0);
+  }
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return h->cuda_fail(e, "call");
   h->stats.pairs = n_out;
   h->stats.pairs_fixed = (int64_t)std::min<unsigned long long>(nflag, (unsigned long long)n_out);

@@ -82,6 +82,10 @@ struct gbr_handle {
   // device buffer for results that leave through the host (cluster-matrix files)
   float* outbuf = nullptr;
   size_t outbuf_cap = 0;
+  // copies that overlap one call's compute (input chunks in, output bands out)
+  cudaStream_t xfer = nullptr;
+  static constexpr int kXev = 24;
+  cudaEvent_t xev[kXev] = {};
 
   int fail(int code, const char* fmt, ...) {
     char buf[512];
@@ -132,6 +136,16 @@ struct gbr_handle {
     }
     return cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) == cudaSuccess;
   }
+  bool ensure_xfer() {
+    if (xfer) return true;
+    if (cudaStreamCreateWithFlags(&xfer, cudaStreamNonBlocking) != cudaSuccess) {
+      xfer = nullptr;
+      return false;
+    }
+    for (auto& e : xev)
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
+    return true;
+  }
   bool reserve_out(size_t floats) {
     if (floats <= outbuf_cap) return true;
     if (outbuf) cudaFree(outbuf);
@@ -154,5 +168,8 @@ struct gbr_handle {
     }
     if (fork) cudaEventDestroy(fork);
     if (pinned) cudaFreeHost(pinned);
+    if (xfer) cudaStreamDestroy(xfer);
+    for (auto& e : xev)
+      if (e) cudaEventDestroy(e);
   }
 };

@@ -45,6 +45,11 @@ struct PrepArgs {
   float* sqwf;     // [N] the same in FP32
   void* scratch;   // prep_scratch_bytes(F, N, max_refs) bytes (PrepScratch)
   int sort_frames; // with several references: lay operands out grouped by reference
+  // Inputs arriving in chunks (host copies overlapping the first pass):
+  // frames [chunk_end[c-1], chunk_end[c]) are usable once chunk_ev[c] completes.
+  int n_chunks;
+  int64_t chunk_end[8];
+  cudaEvent_t chunk_ev[8];
 };
 
 // Further per-call prep buffers, carved from PrepArgs::scratch.

@@ -182,6 +182,66 @@ __device__ __forceinline__ const float* stage_frame_chunk(const T* x, int N, int
   return buf;
 }
 
+// Software-pipelined form of the staging: chunk_load issues the 16-byte
+// loads of a chunk into registers, chunk_store moves them to shared memory.
+// A warp stores chunk c, issues the loads of chunk c + 1, then computes on
+// chunk c, so the next chunk's global latency overlaps the arithmetic.
+struct ChunkRegs {
+  float4 t[3];
+  float hv, tv;
+  int head, nv, tail0, n;
+};
+__device__ __forceinline__ void chunk_load(const float* x, int N, int a0, int lane, ChunkRegs& c) {
+  const float* src = x + 3 * (size_t)a0;
+  c.n = 3 * (min(a0 + kChunkAtoms, N) - a0);
+  int head = (int)((16u - ((unsigned)(uintptr_t)src & 15u)) & 15u) >> 2;
+  if (head > c.n) head = c.n;
+  c.head = head;
+  c.nv = (c.n - head) >> 2;
+  c.tail0 = head + 4 * c.nv;
+  const float4* v4 = reinterpret_cast<const float4*>(src + head);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const int j = lane + 32 * i;
+    c.t[i] = (j < c.nv) ? __ldg(v4 + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  c.hv = (lane < head) ? src[lane] : 0.0f;
+  c.tv = (lane < c.n - c.tail0) ? src[c.tail0 + lane] : 0.0f;
+}
+__device__ __forceinline__ const float* chunk_store(const ChunkRegs& c, float* buf, int lane) {
+  float* dst = buf + ((4 - c.head) & 3);  // dst + head is 16-byte aligned
+  if (lane < c.head) dst[lane] = c.hv;
+  if (lane < c.n - c.tail0) dst[c.tail0 + lane] = c.tv;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const int j = lane + 32 * i;
+    if (j < c.nv) *reinterpret_cast<float4*>(dst + c.head + 4 * j) = c.t[i];
+  }
+  __syncwarp();
+  return dst;
+}
+// Per-frame driver: calls body(a, a0, xs) for every atom a of the frame, xs
+// the staged chunk holding atom a (FP32 input) or unused (FP64 input).
+template <typename T, class Body>
+__device__ __forceinline__ void for_each_atom(const T* x, int N, float* buf, int lane, Body&& body) {
+  if constexpr (sizeof(T) == 4) {
+    ChunkRegs cr;
+    if (N > 0) chunk_load((const float*)x, N, 0, lane, cr);
+    for (int a0 = 0; a0 < N; a0 += kChunkAtoms) {
+      const float* xs = chunk_store(cr, buf, lane);
+      if (a0 + kChunkAtoms < N) chunk_load((const float*)x, N, a0 + kChunkAtoms, lane, cr);
+#pragma unroll
+      for (int kk = 0; kk < kChunkAtoms / 32; ++kk) {
+        const int a = a0 + lane + 32 * kk;
+        if (a < N) body(a, a0, xs);
+      }
+      __syncwarp();
+    }
+  } else {
+    for (int a = lane; a < N; a += 32) body(a, 0, buf);
+  }
+}
+
 // Row k of R x - t - r, with R, t, r given as FP32 hi + lo: Dot2 over the
 // hi products and the subtractions, lo terms into the compensation.  The
 // result is as accurate as if computed in twice FP32 precision and rounded.
@@ -411,11 +471,11 @@ struct ScanArgs {
 //   sum w |y|^2 = sum w |u|^2 - 2 (c - x0).sum w u + W |c - x0|^2
 // Later passes (reference k > 0) centre with the known c directly.
 template <typename T, bool FIRST>
-__global__ void __launch_bounds__(kPrepThreads) k_scan(FrameSrc<T> src, int64_t F, ScanArgs s) {
+__global__ void __launch_bounds__(kPrepThreads) k_scan(FrameSrc<T> src, int64_t f_begin, int64_t F, ScanArgs s) {
   __shared__ __align__(16) float sbuf[kWarps][kStage];
   const int N = src.N, lane = threadIdx.x & 31;
   const bool fit = !s.nofit;
-  for (int64_t f = blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5); f < F; f += (int64_t)gridDim.x * kWarps) {
+  for (int64_t f = f_begin + blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5); f < F; f += (int64_t)gridDim.x * kWarps) {
     const T* x = src.frame(f);
     const bool in_ref = f < src.n_ref;
     const float* cm = in_ref ? s.cm_ref : s.cm_tgt;
@@ -437,12 +497,7 @@ __global__ void __launch_bounds__(kPrepThreads) k_scan(FrameSrc<T> src, int64_t 
 #pragma unroll
     for (int q = 0; q < 16; ++q) v[q] = 0.0f;
     float umax = 0.0f;
-    for (int a0 = 0; a0 < N; a0 += kChunkAtoms) {
-     const float* xs = stage_frame_chunk<T>(x, N, a0, sbuf[threadIdx.x >> 5], lane);
-#pragma unroll 2
-     for (int kk = 0; kk < kChunkAtoms / 32; ++kk) {
-      const int a = a0 + lane + 32 * kk;
-      if (a >= N) break;
+    for_each_atom<T>(x, N, sbuf[threadIdx.x >> 5], lane, [&](int a, int a0, const float* xs) {
       const float sw = s.sqwf ? s.sqwf[a] : 1.0f;
       float xh[3], xl[3], u[3], ue[3];
       fetch_atom(x, xs, a, a0, xh, xl);
@@ -480,9 +535,7 @@ __global__ void __launch_bounds__(kPrepThreads) k_scan(FrameSrc<T> src, int64_t 
         }
         umax = fmaxf(umax, u0 * u0 + u1 * u1 + u2 * u2);
       }
-     }
-     __syncwarp();
-    }
+    });
     if (FIRST && fit) {
       // compensated cross-lane sum of the centre terms
 #pragma unroll
@@ -740,7 +793,7 @@ struct BuildArgs {
 // below FP32 rounding), and continues with the value hi + lo represents.
 // n_f = sum |p|^2 and P_fc = sum p (sqrt(w) r_c)^T use those exact operands.
 template <typename T>
-__global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int64_t F, BuildArgs b) {
+__global__ void __launch_bounds__(kPrepThreads, 2) k_build(FrameSrc<T> src, int64_t F, BuildArgs b) {
   __shared__ __align__(16) float sbuf[kWarps][kStage];
   const int N = src.N, Np = b.Np, lane = threadIdx.x & 31;
   const float sqwmax = (float)b.scal[0];
@@ -767,12 +820,7 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
     float acc[10];
 #pragma unroll
     for (int q = 0; q < 10; ++q) acc[q] = 0.0f;
-    for (int a0 = 0; a0 < N; a0 += kChunkAtoms) {
-      const float* xs = stage_frame_chunk<T>(x, N, a0, sbuf[threadIdx.x >> 5], lane);
-#pragma unroll 2
-      for (int kk = 0; kk < kChunkAtoms / 32; ++kk) {
-        const int a = a0 + lane + 32 * kk;
-        if (a >= N) break;
+    for_each_atom<T>(x, N, sbuf[threadIdx.x >> 5], lane, [&](int a, int a0, const float* xs) {
         float xh[3], xl[3], v[3];
         fetch_atom(x, xs, a, a0, xh, xl);
         const float sw = b.sqwf ? b.sqwf[a] : 1.0f;
@@ -798,9 +846,7 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
         acc[0] += v[0] * c0; acc[1] += v[0] * c1; acc[2] += v[0] * c2;
         acc[3] += v[1] * c0; acc[4] += v[1] * c1; acc[5] += v[1] * c2;
         acc[6] += v[2] * c0; acc[7] += v[2] * c1; acc[8] += v[2] * c2;
-      }
-      __syncwarp();
-    }
+    });
     // zero padding [N, Np)
     for (int a = N + lane; a < Np; a += 32) {
 #pragma unroll
@@ -948,16 +994,32 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
   sa.assign = A.assign;
   sa.quat = S.quat;
   sa.ymax = S.ymax;
-  // Reference 0 from frame 0, then centres + fit to it in one pass.
+  // Reference 0 from frame 0, then centres + fit to it in one pass (chunk by
+  // chunk when the frames are still arriving).
   cudaMemsetAsync(A.fsel, 0, sizeof(int64_t), st);
+  if (A.n_chunks > 0) cudaStreamWaitEvent(st, A.chunk_ev[0], 0);
   k_make_ref<T><<<1, kPrepThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w, A.assign, 0, 0,
                                             A.nofit, A.refs, A.swr, S.refhl, A.Eref, S.sr, S.rmax);
   sa.k = 0;
   sa.swr = A.swr;
   sa.sr = S.sr;
   sa.Eref = A.Eref;
-  k_scan<T, true><<<grid, kPrepThreads, 0, st>>>(src, F, sa);
-  launches += 2;
+  ++launches;
+  if (A.n_chunks > 0) {
+    int64_t f0 = 0;
+    for (int c = 0; c < A.n_chunks; ++c) {
+      if (c > 0) cudaStreamWaitEvent(st, A.chunk_ev[c], 0);
+      const int64_t f1 = A.chunk_end[c];
+      if (f1 > f0) {
+        k_scan<T, true><<<prep_grid(f1 - f0), kPrepThreads, 0, st>>>(src, f0, f1, sa);
+        ++launches;
+      }
+      f0 = f1;
+    }
+  } else {
+    k_scan<T, true><<<grid, kPrepThreads, 0, st>>>(src, 0, F, sa);
+    ++launches;
+  }
   // Greedy k-centre: add the farthest frame as a reference while it is
   // farther than tau from every reference.
   int K = 1;
@@ -975,7 +1037,7 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
     sa.swr = A.swr + (size_t)K * 3 * N;
     sa.sr = S.sr + 3 * K;
     sa.Eref = A.Eref + K;
-    k_scan<T, false><<<grid, kPrepThreads, 0, st>>>(src, F, sa);
+    k_scan<T, false><<<grid, kPrepThreads, 0, st>>>(src, 0, F, sa);
     launches += 2;
     ++K;
   }

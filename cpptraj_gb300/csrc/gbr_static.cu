@@ -1,10 +1,12 @@
 // gbr_static.cu -- gbr_allpairs_fp64_static: all-pairs RMSD that allocates no
 // memory at all.
 //
-// Some callers cannot call cudaMalloc: code that runs while a CUDA graph is
-// being captured or replayed, host programs whose device memory is owned by a
-// pool they must not grow, and plugins loaded into a process that forbids
-// device allocation after start-up.  For them this entry point computes the
+// Some callers cannot call cudaMalloc: host programs (an MD engine, a
+// visualiser) that reserve the GPU's memory at start-up and hand it out from
+// their own fixed pool, which a library must not grow behind their back; and
+// plugins loaded into such a process, or into one whose latency-critical
+// streams must not be stalled by the device-wide synchronisation that
+// cudaMalloc and cudaFree can cause.  For them this entry point computes the
 // same upper triangle as gbr_allpairs(..., GBR_PREC_FP64) -- every pair
 // directly in FP64 -- from device inputs into a device output, using as
 // scratch only a file-scope __device__ array of fixed size.

@@ -136,9 +136,11 @@ int gbr_rmsd_backward(gbr_handle *h, const float *xyz, int64_t n_frame, int32_t 
 
 /* All-pairs RMSD that allocates nothing.  No counterpart in the reference:
  * cpptraj's loops allocate host frames per thread; this entry point exists for
- * callers that cannot call cudaMalloc at all -- code running while a CUDA
- * graph is captured, processes whose device memory belongs to a fixed pool,
- * and plugins loaded after start-up.  It computes the same triangle as
+ * callers that cannot call cudaMalloc at all -- host programs that reserve the
+ * GPU's memory at start-up and serve it from their own fixed pool, and plugins
+ * loaded into such a process or into one whose latency-critical streams must
+ * not be stalled by the synchronisation cudaMalloc/cudaFree can cause.  It
+ * computes the same triangle as
  * gbr_allpairs(..., GBR_TRI, GBR_PREC_FP64, ...) -- every pair directly in
  * FP64 -- for one frame set: xyz (dtype GBR_F32/GBR_F64), mass (NULL =
  * unweighted) and out (n_frame*(n_frame-1)/2 floats) must all be device

@@ -1,6 +1,7 @@
 """gbr_allpairs_fp64_static: the entry point for callers that cannot
-allocate device memory (graph capture, fixed memory pools, late-loaded
-plugins).  It must give the same triangle as the allocating entry point
+allocate device memory (hosts that serve all device memory from their own
+fixed pool, and plugins loaded into them).  It must give the same triangle as
+the allocating entry point
 gbr_allpairs(..., GBR_PREC_FP64), on two calls in a row that reuse the shared
 scratch array.  This file is collected last so that a failure here leaves
 every other test already run."""

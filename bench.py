@@ -27,6 +27,9 @@ sys.path.insert(0, ROOT)
 METRIC = "RMSD pairs/s, 10k frames x 2k atoms: tensor-core vs plain GPU at 1e-4 Angstrom"
 N_FRAME, N_ATOM = 10000, 2000
 FLOPS_PER_PAIR = 18 * N_ATOM  # 9 products x N atoms x 2 (SURVEY 18*N; split extras not counted)
+# DRAM bytes (read + write) of one k_pairs_tc2 launch on this workload, from an
+# ncu capture of `python bench.py --profile --warmup 2` (profiles/k_pairs_tc2_10000x2000_full.md).
+K2_TRAFFIC_BYTES = {(N_FRAME, N_ATOM): 2.244835e9 + 0.198118e9}
 
 
 def parse():
@@ -210,8 +213,68 @@ def dist_env():
     return ws, rank, local
 
 
+class _NvmlSampler:
+    """Read-only NVML polling (SM clock, max SM clock, power, clock-event
+    reasons) in a background thread, through ctypes on the driver's
+    libnvidia-ml; None when NVML cannot be opened."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, dev_index, period_s=0.005):
+        import ctypes
+        import threading
+        self.ct = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        ok = False
+        try:
+            import torch
+            uuid = str(torch.cuda.get_device_properties(dev_index).uuid)
+            for u in (uuid, "GPU-" + uuid):
+                if self.lib.nvmlDeviceGetHandleByUUID(u.encode(), ctypes.byref(self.h)) == 0:
+                    ok = True
+                    break
+        except Exception:
+            ok = False
+        if not ok and self.lib.nvmlDeviceGetHandleByIndex_v2(dev_index, ctypes.byref(self.h)) != 0:
+            raise RuntimeError("no NVML handle")
+        self.period = period_s
+        self.samples = []
+        self.stop_ev = threading.Event()
+        self.th = threading.Thread(target=self._run, daemon=True)
+        mx = ctypes.c_uint()
+        self.max_mhz = float(mx.value) if self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(mx)) == 0 else None
+        fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None)
+        self.reason_fn = fn or self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def _run(self):
+        ct = self.ct
+        clk, pw, rs = ct.c_uint(), ct.c_uint(), ct.c_ulonglong()
+        while not self.stop_ev.is_set():
+            a = self.lib.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(clk))
+            b = self.lib.nvmlDeviceGetPowerUsage(self.h, ct.byref(pw))
+            c = self.reason_fn(self.h, ct.byref(rs))
+            if a == 0:
+                self.samples.append((float(clk.value), pw.value / 1e3 if b == 0 else None,
+                                     int(rs.value) if c == 0 else 0))
+            self.stop_ev.wait(self.period)
+
+    def start(self):
+        self.th.start()
+
+    def stop(self):
+        self.stop_ev.set()
+        self.th.join(timeout=2)
+        return self.samples
+
+
 class Clocks:
-    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    """SM clocks and clock-event (throttle) reasons sampled during a region:
+    NVML every 5 ms where it opens (the timed regions here last tens of
+    milliseconds), else nvidia-smi every 200 ms."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -220,9 +283,16 @@ class Clocks:
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
+        self.nvml = None
         self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
 
     def start(self):
+        try:
+            self.nvml = _NvmlSampler(self.gpu)
+            self.nvml.start()
+            return
+        except Exception:
+            self.nvml = None
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.fh = open(self.path, "w")
@@ -233,6 +303,20 @@ class Clocks:
             self.proc = None
 
     def stop(self):
+        if self.nvml is not None:
+            smp = self.nvml.stop()
+            mx = self.nvml.max_mhz
+            sm = [c for c, _, _ in smp]
+            reasons = set()
+            for _, _, r in smp:
+                for bit, name in _NvmlSampler.REASONS.items():
+                    if r & bit:
+                        reasons.add(name)
+            pw = [p for _, p, _ in smp if p is not None]
+            loaded = [s for s in sm if mx and s > 0.5 * mx] or sm
+            return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": mx,
+                    "reasons": sorted(reasons), "samples": len(sm), "source": "nvml 5 ms",
+                    "power_w_max": max(pw) if pw else None}
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
         time.sleep(0.25)
@@ -258,7 +342,7 @@ class Clocks:
                     reasons.add(k)
         loaded = [s for s in sm if mx and s > 0.5 * mx] or sm
         return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi 200 ms"}
 
 
 def _apply_pipeline(h, args):
@@ -472,7 +556,9 @@ def main():
                        "max_abs_err_A": err32},
         "speedup_vs_plain_fp32": ms32 / ms,
         "roofline": {"bound": "tensor" if precision == "tc" else "fp32", "achieved": achieved, "peak": peak,
-                     "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                     "unit": "TFLOP/s", "frac": achieved / peak,
+                     "traffic": K2_TRAFFIC_BYTES.get((F, N)) if precision == "tc" else None,
+                     "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
                      "kernel_ms": kern_ms, "flops_per_launch": flops, "peak_kind": peak_desc},
         "e2e": {"value": ws * pairs / (e2e_ms / 1e3), "unit": "pairs/s",
                 "h2d_bytes_per_step": int(hX.numel() * 4 + hm.numel() * 8),

@@ -50,6 +50,10 @@ struct FrameSrc {
 
 constexpr int kPrepThreads = 256;
 constexpr int kWarps = kPrepThreads / 32;
+// Single-block kernels (weights, one reference, reference-pair terms) walk N
+// atoms with FP64 sums; their time is the serial FP64 tail of one thread (a
+// larger block measured slower).
+constexpr int kOneBlockThreads = 256;
 constexpr int kSample = 2048;      // frames per reference that set its refined mean
 constexpr int kMeanChunks = 64;    // fixed partition of those frames
 constexpr int kFtab = 24;          // floats per frame in the rotation table
@@ -127,38 +131,11 @@ __device__ __forceinline__ void load_atom(const double* x, int a, float (&h)[3],
   }
 }
 
-// Per-warp staging of FP32 frames: a chunk of kChunkAtoms atoms (AoS, 3
-// floats each) is read with 16-byte loads -- the unaligned head and tail of
-// the chunk with scalar loads, so nothing outside the frame is touched -- and
-// lanes then take their atoms (stride 3 floats: no bank conflicts) from shared
-// memory.  buf holds kStage floats, 16-byte aligned.
+// Staging of FP32 frames in shared memory: chunks of kChunkAtoms atoms (AoS,
+// 3 floats each), from which lanes take their atoms (stride 3 floats: no bank
+// conflicts).  A stage buffer holds kStage floats, 16-byte aligned.
 constexpr int kChunkAtoms = 128;
 constexpr int kStage = 3 * kChunkAtoms + 4;
-__device__ __forceinline__ const float* stage_chunk(const float* x, int N, int a0, float* buf, int lane) {
-  const float* src = x + 3 * (size_t)a0;
-  const int n = 3 * (min(a0 + kChunkAtoms, N) - a0);
-  int head = (int)((16u - ((unsigned)(uintptr_t)src & 15u)) & 15u) >> 2;  // floats before a 16-byte boundary
-  if (head > n) head = n;
-  const int nv = (n - head) >> 2;
-  const int tail0 = head + 4 * nv;
-  float* dst = buf + ((4 - head) & 3);  // dst + head is 16-byte aligned
-  const float4* v4 = reinterpret_cast<const float4*>(src + head);
-  float4 t[3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    const int j = lane + 32 * i;
-    if (j < nv) t[i] = __ldg(v4 + j);
-  }
-  if (lane < head) dst[lane] = src[lane];
-  if (lane < n - tail0) dst[tail0 + lane] = src[tail0 + lane];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    const int j = lane + 32 * i;
-    if (j < nv) *reinterpret_cast<float4*>(dst + head + 4 * j) = t[i];
-  }
-  __syncwarp();
-  return dst;
-}
 
 // Coordinates of atom a as FP32 hi + lo: from the staged chunk (FP32 input)
 // or from global memory (FP64 input).
@@ -175,72 +152,115 @@ __device__ __forceinline__ void fetch_atom(const double* x, const float* xs, int
   (void)a0;
   load_atom(x, a, h, l);
 }
-template <typename T>
-__device__ __forceinline__ const float* stage_frame_chunk(const T* x, int N, int a0, float* buf, int lane) {
-  if constexpr (sizeof(T) == 4) return stage_chunk((const float*)x, N, a0, buf, lane);
-  (void)x; (void)N; (void)a0; (void)lane;
-  return buf;
+
+// Multistage staging.  Each warp streams the chunks of all its frames --
+// frames f0, f0 + stride, ... below F, chunks in atom order -- through a
+// ring of kPipe shared-memory stages with cp.async
+// (16-byte copies for the aligned body of a chunk, 4-byte copies for its
+// unaligned head and tail, so nothing outside the frame is read).  kPipe - 1
+// chunks are in flight while the warp computes on the oldest, and the stream
+// runs on into the warp's next frame, so the memory latency is covered
+// without holding the data in registers.  Completion is tracked with
+// cp.async groups (one per chunk, empty past the last one): no spin-waits.
+constexpr int kPipe = 3;
+
+__device__ __forceinline__ void cp_async16(float* dst, const float* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Floats before the first 16-byte boundary of a chunk, and where the chunk's
+// element 0 sits in its stage buffer (so that the body lands 16-byte aligned).
+__device__ __forceinline__ int chunk_head(const float* src, int n) {
+  const int head = (int)((16u - ((unsigned)(uintptr_t)src & 15u)) & 15u) >> 2;
+  return head > n ? n : head;
 }
 
-// Software-pipelined form of the staging: chunk_load issues the 16-byte
-// loads of a chunk into registers, chunk_store moves them to shared memory.
-// A warp stores chunk c, issues the loads of chunk c + 1, then computes on
-// chunk c, so the next chunk's global latency overlaps the arithmetic.
-struct ChunkRegs {
-  float4 t[3];
-  float hv, tv;
-  int head, nv, tail0, n;
-};
-__device__ __forceinline__ void chunk_load(const float* x, int N, int a0, int lane, ChunkRegs& c) {
-  const float* src = x + 3 * (size_t)a0;
-  c.n = 3 * (min(a0 + kChunkAtoms, N) - a0);
-  int head = (int)((16u - ((unsigned)(uintptr_t)src & 15u)) & 15u) >> 2;
-  if (head > c.n) head = c.n;
-  c.head = head;
-  c.nv = (c.n - head) >> 2;
-  c.tail0 = head + 4 * c.nv;
-  const float4* v4 = reinterpret_cast<const float4*>(src + head);
+template <typename T>
+struct WarpPipe {
+  FrameSrc<T> src;
+  int64_t f_next, F, stride;  // next frame to issue, end, this warp's frame stride
+  int c_next, nch, issued;    // next chunk of f_next, chunks per frame, chunks issued
+  float* ring;                // kPipe * kStage floats, 16-byte aligned
+
+  __device__ __forceinline__ void init(const FrameSrc<T>& s, int64_t f0, int64_t f_end, int64_t str, float* buf,
+                                       int lane) {
+    src = s;
+    f_next = f0;
+    F = f_end;
+    stride = str;
+    c_next = 0;
+    nch = (s.N + kChunkAtoms - 1) / kChunkAtoms;
+    issued = 0;
+    ring = buf;
+    if constexpr (sizeof(T) == 4) {
 #pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    const int j = lane + 32 * i;
-    c.t[i] = (j < c.nv) ? __ldg(v4 + j) : make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-  c.hv = (lane < head) ? src[lane] : 0.0f;
-  c.tv = (lane < c.n - c.tail0) ? src[c.tail0 + lane] : 0.0f;
-}
-__device__ __forceinline__ const float* chunk_store(const ChunkRegs& c, float* buf, int lane) {
-  float* dst = buf + ((4 - c.head) & 3);  // dst + head is 16-byte aligned
-  if (lane < c.head) dst[lane] = c.hv;
-  if (lane < c.n - c.tail0) dst[c.tail0 + lane] = c.tv;
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    const int j = lane + 32 * i;
-    if (j < c.nv) *reinterpret_cast<float4*>(dst + c.head + 4 * j) = c.t[i];
-  }
-  __syncwarp();
-  return dst;
-}
-// Per-frame driver: calls body(a, a0, xs) for every atom a of the frame, xs
-// the staged chunk holding atom a (FP32 input) or unused (FP64 input).
-template <typename T, class Body>
-__device__ __forceinline__ void for_each_atom(const T* x, int N, float* buf, int lane, Body&& body) {
-  if constexpr (sizeof(T) == 4) {
-    ChunkRegs cr;
-    if (N > 0) chunk_load((const float*)x, N, 0, lane, cr);
-    for (int a0 = 0; a0 < N; a0 += kChunkAtoms) {
-      const float* xs = chunk_store(cr, buf, lane);
-      if (a0 + kChunkAtoms < N) chunk_load((const float*)x, N, a0 + kChunkAtoms, lane, cr);
-#pragma unroll
-      for (int kk = 0; kk < kChunkAtoms / 32; ++kk) {
-        const int a = a0 + lane + 32 * kk;
-        if (a < N) body(a, a0, xs);
-      }
-      __syncwarp();
+      for (int k = 0; k < kPipe - 1; ++k) issue(lane);
     }
-  } else {
-    for (int a = lane; a < N; a += 32) body(a, 0, buf);
   }
-}
+  __device__ __forceinline__ void issue(int lane) {
+    if constexpr (sizeof(T) == 4) {
+      if (f_next < F && nch > 0) {
+        const int N = src.N, a0 = c_next * kChunkAtoms;
+        const float* x = (const float*)src.frame(f_next) + 3 * (size_t)a0;
+        const int n = 3 * (min(a0 + kChunkAtoms, N) - a0);
+        const int head = chunk_head(x, n);
+        const int nv = (n - head) >> 2, tail0 = head + 4 * nv;
+        float* dst = ring + (issued % kPipe) * kStage + ((4 - head) & 3);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const int j = lane + 32 * i;
+          if (j < nv) cp_async16(dst + head + 4 * j, x + head + 4 * j);
+        }
+        if (lane < head) cp_async4(dst + lane, x + lane);
+        if (lane < n - tail0) cp_async4(dst + tail0 + lane, x + tail0 + lane);
+        if (++c_next == nch) {
+          c_next = 0;
+          f_next += stride;
+        }
+      }
+      cp_async_commit();
+      ++issued;
+    }
+  }
+  // body(a, a0, xs) for every atom a of frame f, the next frame of this
+  // warp's stream; xs is the staged chunk holding atom a (FP32 input).
+  template <class Body>
+  __device__ __forceinline__ void for_each_atom(int64_t f, int lane, Body&& body) {
+    const int N = src.N;
+    if constexpr (sizeof(T) == 4) {
+      const float* x = (const float*)src.frame(f);
+      for (int c = 0; c < nch; ++c) {
+        const int a0 = c * kChunkAtoms;
+        const int consumed = issued - (kPipe - 1);
+        cp_async_wait<kPipe - 2>();
+        __syncwarp();
+        const float* cx = x + 3 * (size_t)a0;
+        const int n = 3 * (min(a0 + kChunkAtoms, N) - a0);
+        const float* xs = ring + (consumed % kPipe) * kStage + ((4 - chunk_head(cx, n)) & 3);
+        issue(lane);  // refills the stage consumed one chunk ago
+#pragma unroll
+        for (int kk = 0; kk < kChunkAtoms / 32; ++kk) {
+          const int a = a0 + lane + 32 * kk;
+          if (a < N) body(a, a0, xs);
+        }
+        __syncwarp();
+      }
+    } else {
+      for (int a = lane; a < N; a += 32) body(a, 0, ring);
+    }
+  }
+  __device__ __forceinline__ void drain() {
+    if constexpr (sizeof(T) == 4) cp_async_wait<0>();
+  }
+};
 
 // Row k of R x - t - r, with R, t, r given as FP32 hi + lo: Dot2 over the
 // hi products and the subtractions, lo terms into the compensation.  The
@@ -266,7 +286,7 @@ __device__ __forceinline__ float dot2_row(const float* Rh, const float* Rl, floa
 
 // Weights in the forms the passes read; scal = {max sqrt(w), sum w, sum of
 // the reference centring masses}.  One block.
-__global__ void __launch_bounds__(kPrepThreads) k_weights(const double* w, const double* cmass_ref, int N,
+__global__ void __launch_bounds__(kOneBlockThreads) k_weights(const double* w, const double* cmass_ref, int N,
                                                           double* sqw, float* sqwf, float* wf, float* wfl,
                                                           float* cmf_ref, float* cmfl_ref, double* scal) {
   __shared__ double red[32 * 3];
@@ -291,7 +311,7 @@ __global__ void __launch_bounds__(kPrepThreads) k_weights(const double* w, const
     v[1] += ca;
   }
   // max via the sum helper's layout: reduce max separately in shared memory
-  __shared__ double smx[kPrepThreads / 32];
+  __shared__ double smx[32];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   if ((threadIdx.x & 31) == 0) smx[threadIdx.x >> 5] = mx;
@@ -346,7 +366,7 @@ __global__ void __launch_bounds__(kPrepThreads) k_centroid(FrameSrc<T> src, int6
 // reference, sqrt(w) r (FP32), r as hi + lo floats, sum w |r|^2, sum w r and
 // max |r|.
 template <typename T>
-__global__ void __launch_bounds__(kPrepThreads) k_make_ref(FrameSrc<T> src, const int64_t* fsel,
+__global__ void __launch_bounds__(kOneBlockThreads) k_make_ref(FrameSrc<T> src, const int64_t* fsel,
                                                            const double* cen, const double* cmass_ref,
                                                            const double* cmass_tgt, const double* w,
                                                            const int* assign, int k, int use_parent, int nofit,
@@ -355,7 +375,7 @@ __global__ void __launch_bounds__(kPrepThreads) k_make_ref(FrameSrc<T> src, cons
   __shared__ double red[32 * 10];
   __shared__ double Rs[9];
   __shared__ double cs[3];
-  __shared__ float smx[kWarps];
+  __shared__ float smx[32];
   const int N = src.N;
   const int64_t f = *fsel;
   const T* x = src.frame(f);
@@ -471,11 +491,15 @@ struct ScanArgs {
 //   sum w |y|^2 = sum w |u|^2 - 2 (c - x0).sum w u + W |c - x0|^2
 // Later passes (reference k > 0) centre with the known c directly.
 template <typename T, bool FIRST>
-__global__ void __launch_bounds__(kPrepThreads) k_scan(FrameSrc<T> src, int64_t f_begin, int64_t F, ScanArgs s) {
-  __shared__ __align__(16) float sbuf[kWarps][kStage];
+__global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64_t f_begin, int64_t F, ScanArgs s) {
+  __shared__ __align__(16) float sbuf[kWarps][kPipe * kStage];
   const int N = src.N, lane = threadIdx.x & 31;
   const bool fit = !s.nofit;
-  for (int64_t f = f_begin + blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5); f < F; f += (int64_t)gridDim.x * kWarps) {
+  const int64_t f_first = f_begin + blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5);
+  const int64_t f_stride = (int64_t)gridDim.x * kWarps;
+  WarpPipe<T> pipe;
+  pipe.init(src, f_first, F, f_stride, sbuf[threadIdx.x >> 5], lane);
+  for (int64_t f = f_first; f < F; f += f_stride) {
     const T* x = src.frame(f);
     const bool in_ref = f < src.n_ref;
     const float* cm = in_ref ? s.cm_ref : s.cm_tgt;
@@ -497,7 +521,7 @@ __global__ void __launch_bounds__(kPrepThreads) k_scan(FrameSrc<T> src, int64_t 
 #pragma unroll
     for (int q = 0; q < 16; ++q) v[q] = 0.0f;
     float umax = 0.0f;
-    for_each_atom<T>(x, N, sbuf[threadIdx.x >> 5], lane, [&](int a, int a0, const float* xs) {
+    pipe.for_each_atom(f, lane, [&](int a, int a0, const float* xs) {
       const float sw = s.sqwf ? s.sqwf[a] : 1.0f;
       float xh[3], xl[3], u[3], ue[3];
       fetch_atom(x, xs, a, a0, xh, xl);
@@ -609,6 +633,7 @@ __global__ void __launch_bounds__(kPrepThreads) k_scan(FrameSrc<T> src, int64_t 
       }
     }
   }
+  pipe.drain();
 }
 
 // Single-block argmax of dist[0..F): out_val, out_idx (lowest index on ties).
@@ -793,11 +818,15 @@ struct BuildArgs {
 // below FP32 rounding), and continues with the value hi + lo represents.
 // n_f = sum |p|^2 and P_fc = sum p (sqrt(w) r_c)^T use those exact operands.
 template <typename T>
-__global__ void __launch_bounds__(kPrepThreads, 2) k_build(FrameSrc<T> src, int64_t F, BuildArgs b) {
-  __shared__ __align__(16) float sbuf[kWarps][kStage];
+__global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int64_t F, BuildArgs b) {
+  __shared__ __align__(16) float sbuf[kWarps][kPipe * kStage];
   const int N = src.N, Np = b.Np, lane = threadIdx.x & 31;
   const float sqwmax = (float)b.scal[0];
-  for (int64_t f = blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5); f < F; f += (int64_t)gridDim.x * kWarps) {
+  const int64_t f_first = blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5);
+  const int64_t f_stride = (int64_t)gridDim.x * kWarps;
+  WarpPipe<T> pipe;
+  pipe.init(src, f_first, F, f_stride, sbuf[threadIdx.x >> 5], lane);
+  for (int64_t f = f_first; f < F; f += f_stride) {
     const T* x = src.frame(f);
     const int ra = b.assign[f];
     const int64_t pf = b.pos ? (int64_t)b.pos[f] : f;  // where this frame's operands go
@@ -820,7 +849,7 @@ __global__ void __launch_bounds__(kPrepThreads, 2) k_build(FrameSrc<T> src, int6
     float acc[10];
 #pragma unroll
     for (int q = 0; q < 10; ++q) acc[q] = 0.0f;
-    for_each_atom<T>(x, N, sbuf[threadIdx.x >> 5], lane, [&](int a, int a0, const float* xs) {
+    pipe.for_each_atom(f, lane, [&](int a, int a0, const float* xs) {
         float xh[3], xl[3], v[3];
         fetch_atom(x, xs, a, a0, xh, xl);
         const float sw = b.sqwf ? b.sqwf[a] : 1.0f;
@@ -893,12 +922,13 @@ __global__ void __launch_bounds__(kPrepThreads, 2) k_build(FrameSrc<T> src, int6
       }
     }
   }
+  pipe.drain();
 }
 
 // Reference-pair table (kRefPairStride floats per b*K + a): the exact FP64
 // rotation U_ab taking r_b onto r_a, SU_ab = U_ab S_ba, its antisymmetric
 // combos and sum w |r_a - U_ab r_b|^2.  No-fit mode keeps U = I.
-__global__ void __launch_bounds__(kPrepThreads) k_ref_terms(const double* refs, int N, int K, const double* w,
+__global__ void __launch_bounds__(kOneBlockThreads) k_ref_terms(const double* refs, int N, int K, const double* w,
                                                             int nofit, float* RP) {
   __shared__ double red[32 * 10];
   __shared__ double Us[9];
@@ -953,7 +983,15 @@ __global__ void __launch_bounds__(kPrepThreads) k_ref_terms(const double* refs, 
 // ---------------------------------------------------------------------------
 // Host driver for the prep passes.
 // ---------------------------------------------------------------------------
-static int prep_grid(int64_t F) { return (int)std::min<int64_t>((F + kWarps - 1) / kWarps, 152 * 16); }
+// Blocks for a warp-per-frame pass over F frames: one wave of per_sm resident
+// blocks on each of GB300's 152 SMs at most.  The cp.async-pipelined passes
+// (k_scan, k_build) are persistent: each warp streams several frames, so the
+// pipeline fills once per warp rather than once per frame.
+static int prep_grid(int64_t F, int per_sm = 16) {
+  return (int)std::min<int64_t>((F + kWarps - 1) / kWarps, 152 * per_sm);
+}
+constexpr int kScanBlocksPerSM = 4;   // k_scan: __launch_bounds__(kPrepThreads, 4)
+constexpr int kBuildBlocksPerSM = 3;  // k_build: __launch_bounds__(kPrepThreads, 3)
 
 template <typename T>
 static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
@@ -975,7 +1013,7 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
   }
   const PrepScratch S = prep_carve(A.scratch, F, N, A.max_refs);
   const bool ref_distinct = A.cmass_ref != nullptr && A.cmass_ref != A.w;
-  k_weights<<<1, kPrepThreads, 0, st>>>(A.w, ref_distinct ? A.cmass_ref : nullptr, N, A.sqw, A.sqwf, S.wf,
+  k_weights<<<1, kOneBlockThreads, 0, st>>>(A.w, ref_distinct ? A.cmass_ref : nullptr, N, A.sqw, A.sqwf, S.wf,
                                         S.wfl, S.cmf_ref, S.cmfl_ref, S.scal);
   ++launches;
   ScanArgs sa{};
@@ -998,7 +1036,7 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
   // chunk when the frames are still arriving).
   cudaMemsetAsync(A.fsel, 0, sizeof(int64_t), st);
   if (A.n_chunks > 0) cudaStreamWaitEvent(st, A.chunk_ev[0], 0);
-  k_make_ref<T><<<1, kPrepThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w, A.assign, 0, 0,
+  k_make_ref<T><<<1, kOneBlockThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w, A.assign, 0, 0,
                                             A.nofit, A.refs, A.swr, S.refhl, A.Eref, S.sr, S.rmax);
   sa.k = 0;
   sa.swr = A.swr;
@@ -1011,13 +1049,13 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
       if (c > 0) cudaStreamWaitEvent(st, A.chunk_ev[c], 0);
       const int64_t f1 = A.chunk_end[c];
       if (f1 > f0) {
-        k_scan<T, true><<<prep_grid(f1 - f0), kPrepThreads, 0, st>>>(src, f0, f1, sa);
+        k_scan<T, true><<<prep_grid(f1 - f0, kScanBlocksPerSM), kPrepThreads, 0, st>>>(src, f0, f1, sa);
         ++launches;
       }
       f0 = f1;
     }
   } else {
-    k_scan<T, true><<<grid, kPrepThreads, 0, st>>>(src, 0, F, sa);
+    k_scan<T, true><<<prep_grid(F, kScanBlocksPerSM), kPrepThreads, 0, st>>>(src, 0, F, sa);
     ++launches;
   }
   // Greedy k-centre: add the farthest frame as a reference while it is
@@ -1031,13 +1069,13 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return e;
     if (!(dmax > A.tau)) break;
-    k_make_ref<T><<<1, kPrepThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w, A.assign, K, 1,
+    k_make_ref<T><<<1, kOneBlockThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w, A.assign, K, 1,
                                               A.nofit, A.refs, A.swr, S.refhl, A.Eref, S.sr, S.rmax);
     sa.k = K;
     sa.swr = A.swr + (size_t)K * 3 * N;
     sa.sr = S.sr + 3 * K;
     sa.Eref = A.Eref + K;
-    k_scan<T, false><<<grid, kPrepThreads, 0, st>>>(src, 0, F, sa);
+    k_scan<T, false><<<prep_grid(F, kScanBlocksPerSM), kPrepThreads, 0, st>>>(src, 0, F, sa);
     launches += 2;
     ++K;
   }
@@ -1111,8 +1149,8 @@ static cudaError_t finish_impl(const FinishArgs& fa, cudaStream_t st) {
   b.trP = fa.trP;
   b.pos = fa.sorted ? S.pos : nullptr;
   b.assign_pos = S.assign_pos;
-  k_build<T><<<prep_grid(A.F), kPrepThreads, 0, st>>>(src, A.F, b);
-  k_ref_terms<<<fa.K * fa.K, kPrepThreads, 0, st>>>(A.refs, A.N, fa.K, A.w, A.nofit, fa.RP);
+  k_build<T><<<prep_grid(A.F, kBuildBlocksPerSM), kPrepThreads, 0, st>>>(src, A.F, b);
+  k_ref_terms<<<fa.K * fa.K, kOneBlockThreads, 0, st>>>(A.refs, A.N, fa.K, A.w, A.nofit, fa.RP);
   return cudaGetLastError();
 }
 

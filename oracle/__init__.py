@@ -18,7 +18,7 @@ LIB = os.path.join(HERE, "librmsd_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libcpptraj_rmsd_ref.so")
 REF_SRC = "/root/reference/src"
 
-FIT, NOFIT, QCP = 0, 1, 2
+FIT, NOFIT, QCP, DME = 0, 1, 2, 3
 TRI, FULL = 0, 1
 
 _lib = None

@@ -40,7 +40,8 @@ Frame make(int n, const double* mass) {
 }
 }  // namespace
 
-// mode: 0 = fit (RMSD_CenteredRef), 1 = nofit, 2 = qrmsd.  Same argument meaning
+// mode: 0 = fit (RMSD_CenteredRef), 1 = nofit, 2 = qrmsd, 3 = dme (DISTRMSD,
+// reference not centred, src/Analysis_Rms2d.cpp:265-278).  Same argument meaning
 // as orc_allpairs in rmsd_oracle.c.
 extern "C" int ref_allpairs(const void* ref_xyz, const void* tgt_xyz, int dtype, int64_t n_ref,
                             int64_t n_tgt, int n_atom, const double* ref_mass, const double* tgt_mass,
@@ -59,13 +60,14 @@ extern "C" int ref_allpairs(const void* ref_xyz, const void* tgt_xyz, int dtype,
 #endif
     for (int64_t i = 0; i < n_ref; ++i) {
       fill(R, ref_xyz, dtype, i, n_atom);
-      if (mode != 1) R.CenterOnOrigin(use_mass);
+      if (mode == 0 || mode == 2) R.CenterOnOrigin(use_mass);
       int64_t j0 = (out_kind == 0) ? i + 1 : 0;
       for (int64_t j = j0; j < n_tgt; ++j) {
         fill(T, tgt_xyz, dtype, j, n_atom);
         double r;
         if (mode == 0) r = T.RMSD_CenteredRef(R, use_mass);
         else if (mode == 1) r = T.RMSD_NoFit(R, use_mass);
+        else if (mode == 3) r = T.DISTRMSD(R);
         else r = QuaternionRMSD_CenteredRef(R, T, use_mass);
         int64_t idx = (out_kind == 0) ? tri(n_ref, i, j) : j * n_ref + i;
         out[idx] = (float)r;
@@ -84,7 +86,7 @@ extern "C" int ref_pairs_f64(const void* xyz, int dtype, int n_atom, const doubl
   for (int64_t k = 0; k < npairs; ++k) {
     fill(A, xyz, dtype, pi[k], n_atom);
     fill(B, xyz, dtype, pj[k], n_atom);
-    out[k] = (mode == 1) ? A.RMSD_NoFit(B, use_mass) : A.RMSD(B, use_mass);
+    out[k] = (mode == 1) ? A.RMSD_NoFit(B, use_mass) : (mode == 3) ? A.DISTRMSD(B) : A.RMSD(B, use_mass);
   }
   return 0;
 }

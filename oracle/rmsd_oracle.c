@@ -10,6 +10,7 @@
  *   - Matrix_3x3::Diagonalize        src/Matrix_3x3.cpp:110-211 (cyclic Jacobi)
  *   - Matrix_3x3::Diagonalize_Sort   src/Matrix_3x3.cpp:219-280
  *   - Frame::RMSD_NoFit              src/Frame.cpp:1279-1307
+ *   - Frame::DISTRMSD                src/Frame.cpp:1313-1344 (rms2d `dme`)
  *   - Frame::CenterOnOrigin          src/Frame.cpp:1043-1055, Frame.h:373-391
  *   - QCPRot::FastCalcRMSDAndRotation src/qcprot.cpp:167-246 (RMSD part) and
  *     do_quaternion_rmsd              src/QuaternionRMSD.cpp:25-120
@@ -37,7 +38,7 @@
 #define ORC_JACOBI_SWEEPS 50
 
 enum { ORC_F32 = 0, ORC_F64 = 1 };
-enum { ORC_FIT = 0, ORC_NOFIT = 1, ORC_QCP = 2 };
+enum { ORC_FIT = 0, ORC_NOFIT = 1, ORC_QCP = 2, ORC_DME = 3 };
 enum { ORC_TRI = 0, ORC_FULL = 1 };
 
 /* ------------------------------------------------------------------------ */
@@ -252,6 +253,37 @@ double orc_rmsd_nofit(const double *ref, const double *tgt, int n, const double 
   return sqrt(s / W);
 }
 
+/* Distance RMSD (Frame::DISTRMSD, src/Frame.cpp:1313-1344): over atom pairs
+ * a < b (a outer, b inner), the squared difference of the target's and the
+ * reference's a-b distances, summed in that order; sqrt(sum / (N^2 - N)/2).
+ * No masses, no centring.  N = 1 gives 0/0, as in the reference. */
+double orc_rmsd_dme(const double *ref, const double *tgt, int n) {
+  const double nd = (double)((n * n) - n) / 2.0;
+  double sum = 0.0;
+  for (int a = 0; a < n - 1; ++a) {
+    for (int b = a + 1; b < n; ++b) {
+      double x = tgt[3 * a] - tgt[3 * b], y = tgt[3 * a + 1] - tgt[3 * b + 1], z = tgt[3 * a + 2] - tgt[3 * b + 2];
+      const double dt = sqrt(x * x + y * y + z * z);
+      x = ref[3 * a] - ref[3 * b]; y = ref[3 * a + 1] - ref[3 * b + 1]; z = ref[3 * a + 2] - ref[3 * b + 2];
+      const double dr = sqrt(x * x + y * y + z * z);
+      const double d = dt - dr;
+      sum += d * d;
+    }
+  }
+  return sqrt(sum / nd);
+}
+
+static double pair_value(int mode, const double *R, const double *T, int n, const double *mass) {
+  if (mode == ORC_FIT) return orc_rmsd_centered_ref(R, T, n, mass);
+  if (mode == ORC_QCP) return orc_rmsd_qcp(R, T, n, mass);
+  if (mode == ORC_DME) return orc_rmsd_dme(R, T, n);
+  return orc_rmsd_nofit(R, T, n, mass);
+}
+
+/* Calculate_2D centres the reference frame for fit and qrmsd only
+ * (src/Analysis_Rms2d.cpp:265-266). */
+static int centres_ref(int mode) { return mode == ORC_FIT || mode == ORC_QCP; }
+
 /* ------------------------------------------------------------------------ */
 /* All-pairs driver with Calculate_2D semantics.                             */
 /*   rows = reference frames (nref), columns = target frames (ntgt).         */
@@ -302,7 +334,7 @@ int orc_allpairs(const void *ref_xyz, const void *tgt_xyz, int dtype, int64_t n_
 #endif
     for (int64_t i = i_begin; i < i_end; ++i) {
       load_frame(ref_xyz, dtype, i, n_atom, R);
-      if (mode != ORC_NOFIT) {
+      if (centres_ref(mode)) {
         double c[3];
         orc_center(R, n_atom, ref_mass, c);
         for (int a = 0; a < n_atom; ++a) {
@@ -312,10 +344,7 @@ int orc_allpairs(const void *ref_xyz, const void *tgt_xyz, int dtype, int64_t n_
       int64_t j0 = (out_kind == ORC_TRI) ? i + 1 : j_lo;
       for (int64_t j = j0; j < j_hi; ++j) {
         load_frame(tgt_xyz, dtype, j, n_atom, T);
-        double r;
-        if (mode == ORC_FIT) r = orc_rmsd_centered_ref(R, T, n_atom, tgt_mass);
-        else if (mode == ORC_QCP) r = orc_rmsd_qcp(R, T, n_atom, tgt_mass);
-        else r = orc_rmsd_nofit(R, T, n_atom, tgt_mass);
+        const double r = pair_value(mode, R, T, n_atom, tgt_mass);
         if (r < 0.0) err |= 2;
         int64_t idx = (out_kind == ORC_TRI) ? orc_tri_index(n_ref, i, j) - base : (j - row_begin) * n_ref + i;
         out[idx] = (float)r;
@@ -346,7 +375,7 @@ int orc_allpairs_f64(const void *ref_xyz, const void *tgt_xyz, int dtype, int64_
 #endif
     for (int64_t i = 0; i < n_ref; ++i) {
       load_frame(ref_xyz, dtype, i, n_atom, R);
-      if (mode != ORC_NOFIT) {
+      if (centres_ref(mode)) {
         double c[3];
         orc_center(R, n_atom, ref_mass, c);
         for (int a = 0; a < n_atom; ++a) {
@@ -356,10 +385,7 @@ int orc_allpairs_f64(const void *ref_xyz, const void *tgt_xyz, int dtype, int64_
       int64_t j0 = (out_kind == ORC_TRI) ? i + 1 : 0;
       for (int64_t j = j0; j < n_tgt; ++j) {
         load_frame(tgt_xyz, dtype, j, n_atom, T);
-        double r;
-        if (mode == ORC_FIT) r = orc_rmsd_centered_ref(R, T, n_atom, tgt_mass);
-        else if (mode == ORC_QCP) r = orc_rmsd_qcp(R, T, n_atom, tgt_mass);
-        else r = orc_rmsd_nofit(R, T, n_atom, tgt_mass);
+        const double r = pair_value(mode, R, T, n_atom, tgt_mass);
         if (r < 0.0) err |= 2;
         int64_t idx = (out_kind == ORC_TRI) ? orc_tri_index(n_ref, i, j) : j * n_ref + i;
         out[idx] = r;
@@ -388,17 +414,14 @@ int orc_pairs_f64(const void *xyz, int dtype, int n_atom, const double *mass, in
     for (int64_t k = 0; k < npairs; ++k) {
       load_frame(xyz, dtype, pi[k], n_atom, R);
       load_frame(xyz, dtype, pj[k], n_atom, T);
-      if (mode != ORC_NOFIT) {
+      if (centres_ref(mode)) {
         double c[3];
         orc_center(R, n_atom, mass, c);
         for (int a = 0; a < n_atom; ++a) {
           R[3 * a] -= c[0]; R[3 * a + 1] -= c[1]; R[3 * a + 2] -= c[2];
         }
       }
-      double r;
-      if (mode == ORC_FIT) r = orc_rmsd_centered_ref(R, T, n_atom, mass);
-      else if (mode == ORC_QCP) r = orc_rmsd_qcp(R, T, n_atom, mass);
-      else r = orc_rmsd_nofit(R, T, n_atom, mass);
+      const double r = pair_value(mode, R, T, n_atom, mass);
       if (r < 0.0) err |= 2;
       out[k] = r;
     }

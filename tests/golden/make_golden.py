@@ -10,11 +10,12 @@ Run in a container where the reference tree is mounted (default
      unit 2    `2drms crd1 :3-7 mass`     -> rmsd.mass.dat.save
      unit 5    `2drms :2 :11`             -> trp.dat.save    (tgt :2, ref :11, FULL)
      unit 6    `rms first :2-12@CA` then `2drms crd1 :2 nofit` -> nofit.dat.save
+     unit 4    `2drms crd1 :3-7 rmsout dme.dat dme` -> dme.dat.save (same frames as unit 1)
    Coordinates are stored as float32 because the implicit COORDS set of those
    runs holds single precision (src/CompactFrameArray.h:75-76).
 2. ref_pairs.npz -- FP64 RMSDs produced by cpptraj's own Frame code (built by
    `make -C oracle ref`) on seeded synthetic frames, for fit/nofit/qrmsd with
-   and without mass weighting.  This pins the restatement where the reference
+   and without mass weighting, and for dme (Frame::DISTRMSD).  This pins the restatement where the reference
    tree is absent.
 3. tz2_cluster_cmatrix.npz -- the pairwise cache of test/Test_Cluster's first
    unit (`cluster C1 :2-10 ... nofit savepairdist ... pairdist Cmatrix.cmatrix`
@@ -147,6 +148,7 @@ def make_tz2():
         rmsd_mass_save=read_square2d(os.path.join(d, "rmsd.mass.dat.save")),
         trp_save=read_square2d(os.path.join(d, "trp.dat.save")),
         nofit_save=read_square2d(os.path.join(d, "nofit.dat.save")),
+        dme_save=read_square2d(os.path.join(d, "dme.dat.save")),
     )
     print("tz2_rms2d.npz: atoms", len(m37), len(m2), len(m11), "CA", len(ca))
 
@@ -168,8 +170,9 @@ def make_ref_pairs():
         for wt, mm in (("w", m), ("u", None)):
             res[f"{tag}_{wt}"] = oracle.pairs_f64(X, pi, pj, mass=mm, mode=mode, use_reference_code=True)
     # rms2d TRI float32 output of the reference for fit / qrmsd / nofit, weighted.
-    for mode, tag in ((oracle.FIT, "fit"), (oracle.QCP, "qcp"), (oracle.NOFIT, "nofit")):
+    for mode, tag in ((oracle.FIT, "fit"), (oracle.QCP, "qcp"), (oracle.NOFIT, "nofit"), (oracle.DME, "dme")):
         res[f"tri_{tag}"] = oracle.allpairs(X, tgt_mass=m, mode=mode, use_reference_code=True)
+    res["dme_u"] = oracle.pairs_f64(X, pi, pj, mode=oracle.DME, use_reference_code=True)
     np.savez_compressed(os.path.join(HERE, "ref_pairs.npz"), **res)
     print("ref_pairs.npz:", len(pi), "pairs")
 

@@ -37,6 +37,7 @@ def tz2():
     ("rmsd_mass_save", "fit_xyz", "fit_mass", oracle.FIT),  # unit 2
     ("nofit_save", "nofit_xyz", None, oracle.NOFIT),      # unit 6
     ("rmsd_save", "fit_xyz", None, oracle.QCP),           # unit 8 (qrmsd)
+    ("dme_save", "fit_xyz", None, oracle.DME),            # unit 4 (dme)
 ])
 def test_tz2_triangle(tz2, save, xyz, mass, mode):
     out = oracle.allpairs(tz2[xyz], tgt_mass=tz2[mass] if mass else None, mode=mode)
@@ -65,7 +66,13 @@ def test_pairs_match_reference_code(refp, mode, tag, wt):
     np.testing.assert_allclose(got, refp[f"{tag}_{wt}"], rtol=0, atol=1e-9)
 
 
-@pytest.mark.parametrize("mode,tag", [(oracle.FIT, "fit"), (oracle.QCP, "qcp"), (oracle.NOFIT, "nofit")])
+def test_dme_pairs_match_reference_code(refp):
+    got = oracle.pairs_f64(refp["xyz"], refp["pi"], refp["pj"], mode=oracle.DME)
+    np.testing.assert_allclose(got, refp["dme_u"], rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("mode,tag", [(oracle.FIT, "fit"), (oracle.QCP, "qcp"), (oracle.NOFIT, "nofit"),
+                                      (oracle.DME, "dme")])
 def test_tri_bitwise_vs_reference_code(refp, mode, tag):
     got = oracle.allpairs(refp["xyz"], tgt_mass=refp["mass"], mode=mode)
     assert np.array_equal(got, refp[f"tri_{tag}"])

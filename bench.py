@@ -46,8 +46,8 @@ def parse():
                     help="tensor-core kernel shape (GBR_OPT_TC_PIPELINE); default: the library's")
     ap.add_argument("--profile", action="store_true",
                     help="warm up, then run exactly one all-pairs call (for ncu); prints stats only")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4"],
-                    help="c1 = the headline metric; c2/c3/c4 print secondary lines for the other configs")
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4", "dme"],
+                    help="c1 = the headline metric; c2/c3/c4/dme print secondary lines for the other configs")
     return ap.parse_args()
 
 
@@ -151,6 +151,52 @@ def main_c3(args):
                      "pairs_fixed": st["pairs_fixed"], "max_abs_err_A_first3": max(errs)}
     print(json.dumps({"workload": f"c3 batch of {n} trajectories, {pairs} pairs, {flops / 1e12:.2f} TFLOP "
                                   f"algorithmic", "results": res}), flush=True)
+
+
+def main_dme(args):
+    """rms2d `dme` (distance RMSD): 4,096 frames x 700 atoms, FP32, TRI in HBM;
+    the plain-GPU form of this mode (CUDA-core kernels), with the FP64 oracle
+    timed on a bounded row sample beside it."""
+    import torch
+
+    import oracle
+    from cpptraj_gb300 import gbrmsd, synth
+
+    F, N = 4096, 700
+    X, _ = synth.trajectory(5, F, N, 0.3, 2.5, np.float32, False)
+    pairs = F * (F - 1) // 2
+    nd = N * (N - 1) // 2
+    h = gbrmsd.Handle(0)
+    h.set_stream(torch.cuda.current_stream().cuda_stream)
+    h.set_option(gbrmsd.OPT_TIMING, 1)
+    dX = torch.from_numpy(X).cuda()
+    out = torch.empty(pairs, dtype=torch.float32, device="cuda")
+    ms = _gpu_time(lambda: h.allpairs(dX, mode="dme", out=out), max(2, args.steps), 1)
+    st = h.stats()
+    rng = np.random.default_rng(0)
+    pi = rng.integers(0, F - 1, 200)
+    pj = np.array([rng.integers(i + 1, F) for i in pi])
+    ref = oracle.pairs_f64(X, pi, pj, mode=oracle.DME)
+    idx = F * pi - ((pi + 1) * pi) // 2 + pj - pi - 1
+    got = out[torch.from_numpy(idx).cuda()].cpu().numpy().astype(np.float64)
+    # algorithmic work: a subtraction, a multiply and an add per atom pair and frame pair
+    flops = 3.0 * nd * pairs
+    peak = 152 * 128 * 2 * 2.07e9 / 1e12
+    cpairs = 8192
+    ci = rng.integers(0, F - 1, cpairs)
+    cj = np.array([rng.integers(i + 1, F) for i in ci])
+    t0 = time.perf_counter()
+    oracle.pairs_f64(X, ci, cj, mode=oracle.DME, nthreads=os.cpu_count() or 1)
+    cpu_s = time.perf_counter() - t0
+    print(json.dumps({"workload": f"rms2d dme, {F} frames x {N} atoms ({nd} atom pairs), FP32, TRI {pairs} pairs",
+                      "pairs_per_s": pairs / (ms / 1e3), "ms_per_call": ms, "kernel_launches": st["kernel_launches"],
+                      "algorithmic_tflops": flops / (ms / 1e3) / 1e12,
+                      "roofline_frac_of_nominal_fp32": flops / (ms / 1e3) / 1e12 / peak,
+                      "max_abs_err_A": float(np.abs(got - ref).max()),
+                      "cpu_baseline": {"value": cpairs / cpu_s, "unit": "pairs/s", "cores": os.cpu_count(),
+                                       "kind": "port", "sample": f"{cpairs} random pairs, FP64 oracle "
+                                                                 f"(Frame::DISTRMSD restatement), OpenMP, {cpu_s:.2f} s"}}),
+          flush=True)
 
 
 def main_c4(args):
@@ -446,7 +492,7 @@ def main():
     if args.profile:
         return main_profile(args)
     if args.workload != "c1":
-        return {"c2": main_c2, "c3": main_c3, "c4": main_c4}[args.workload](args)
+        return {"c2": main_c2, "c3": main_c3, "c4": main_c4, "dme": main_dme}[args.workload](args)
     import torch
     import torch.distributed as dist
 

@@ -122,7 +122,8 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
   if (!ref_xyz) return h->fail(GBR_ERR_ARG, "ref_xyz is NULL");
   if (!out) return h->fail(GBR_ERR_ARG, "out is NULL");
   if (dtype != GBR_F32 && dtype != GBR_F64) return h->fail(GBR_ERR_ARG, "dtype must be GBR_F32 or GBR_F64");
-  if (mode != GBR_FIT && mode != GBR_NOFIT) return h->fail(GBR_ERR_ARG, "mode must be GBR_FIT or GBR_NOFIT");
+  if (mode != GBR_FIT && mode != GBR_NOFIT && mode != GBR_DME)
+    return h->fail(GBR_ERR_ARG, "mode must be GBR_FIT, GBR_NOFIT or GBR_DME");
   if (out_kind != GBR_TRI && out_kind != GBR_FULL) return h->fail(GBR_ERR_ARG, "out_kind must be TRI or FULL");
   if (precision < GBR_PREC_FP32 || precision > GBR_PREC_FP64) return h->fail(GBR_ERR_ARG, "bad precision");
   if (n_atom < 1) return h->fail(GBR_ERR_ARG, "n_atom must be >= 1 (no atoms selected)");
@@ -138,9 +139,21 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
   if (row_end < 0 || row_end > n_rows) row_end = n_rows;
   if (row_begin < 0 || row_begin > row_end) return h->fail(GBR_ERR_ARG, "bad row range [%lld, %lld)",
                                                          (long long)row_begin, (long long)row_end);
+  const int64_t n_out = gbr_output_count(n_ref, n_tgt, out_kind, row_begin, row_end);
+  if (mode == GBR_DME) {  // no masses, no fit: its own kernels (gbr_dme.cu)
+    if (cudaSetDevice(h->device) != cudaSuccess) return h->cuda_fail(cudaGetLastError(), "cudaSetDevice");
+    int rc = GBR_OK;
+    if (n_out > 0)
+      rc = allpairs_dme(h, ref_xyz, tgt_xyz, dtype, n_ref, n_tgt, n_atom, out_kind, precision, out, row_begin,
+                        row_end, n_out);
+    else
+      h->stats.precision = (precision == GBR_PREC_FP64) ? GBR_PREC_FP64 : GBR_PREC_FP32;
+    h->stats.ms_total =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    return rc;
+  }
   if (precision == GBR_PREC_TC && !h->tc_ok)
     return h->fail(GBR_ERR_UNSUPPORTED, "tensor-core precision needs an sm_103 (GB300) device");
-  const int64_t n_out = gbr_output_count(n_ref, n_tgt, out_kind, row_begin, row_end);
   if (cudaSetDevice(h->device) != cudaSuccess) return h->cuda_fail(cudaGetLastError(), "cudaSetDevice");
   cudaStream_t st = h->stream;
 

@@ -105,6 +105,13 @@ struct PrepOut {
 
 cudaError_t run_prep(const PrepArgs& A, PrepOut& o, cudaStream_t st);
 
+}  // namespace gbr
+struct gbr_handle;
+namespace gbr {
+// rms2d `dme` mode (gbr_dme.cu): arguments already validated by gbr_allpairs.
+int allpairs_dme(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dtype, int64_t n_ref, int64_t n_tgt,
+                 int N, int out_kind, int precision, float* out, int64_t row_begin, int64_t row_end, int64_t n_out);
+
 
 // Tiles of the pair space: rows = reference frames, cols = target frames.
 struct TileSpace {

@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(HERE, "libgbrmsd.so")
 
 GBR_OK = 0
 GBR_F32, GBR_F64 = 0, 1
-FIT, NOFIT = 0, 1
+FIT, NOFIT, DME = 0, 1, 2
 TRI, FULL = 0, 1
 PREC_FP32, PREC_TC, PREC_FP64 = 0, 1, 2
 OPT_TAU, OPT_MAX_REFS, OPT_TOL, OPT_TIMING, OPT_TC_PIPELINE = 0, 1, 2, 3, 4
@@ -26,7 +26,7 @@ OPT_TAU, OPT_MAX_REFS, OPT_TOL, OPT_TIMING, OPT_TC_PIPELINE = 0, 1, 2, 3, 4
 TC_PIPELINE_DEFAULT = 2
 
 PRECISIONS = {"fp32": PREC_FP32, "tc": PREC_TC, "fp64": PREC_FP64}
-MODES = {"fit": FIT, "nofit": NOFIT}
+MODES = {"fit": FIT, "nofit": NOFIT, "dme": DME}
 
 #: Every symbol include/gbrmsd.h declares.
 EXPORTED = ("gbr_create", "gbr_destroy", "gbr_last_error", "gbr_allpairs", "gbr_output_count",

@@ -4,14 +4,15 @@
  * This is the drop-in boundary for cpptraj's all-pairs RMSD path.  Each entry
  * point replaces one loop of the reference:
  *
- *   gbr_allpairs      <- Analysis_Rms2d::Calculate_2D pair loop for RMS_FIT and
- *                        RMS_NOFIT (src/Analysis_Rms2d.cpp:247-290), and the
+ *   gbr_allpairs      <- Analysis_Rms2d::Calculate_2D pair loop for RMS_FIT,
+ *                        RMS_NOFIT and DME (src/Analysis_Rms2d.cpp:247-290), and the
  *                        Metric_RMS branch of MetricArray::calcFrameDistances
  *                        (src/Cluster/MetricArray.cpp:770-800).  The per-pair
  *                        arithmetic it reproduces is Frame::RMSD_CenteredRef
  *                        (src/Frame.cpp:1137-1273), Frame::RMSD
- *                        (src/Frame.cpp:1102-1109) and Frame::RMSD_NoFit
- *                        (src/Frame.cpp:1279-1307).
+ *                        (src/Frame.cpp:1102-1109), Frame::RMSD_NoFit
+ *                        (src/Frame.cpp:1279-1307) and Frame::DISTRMSD
+ *                        (src/Frame.cpp:1313-1344).
  *   gbr_allpairs_batched <- the same loop run over many independent COORDS
  *                        sets, one rms2d per set.
  *   gbr_write_cmatrix <- the pairwise-cache fill plus Cmatrix_Binary::WriteCmatrix
@@ -72,7 +73,11 @@ enum gbr_status {
 };
 
 enum gbr_dtype { GBR_F32 = 0, GBR_F64 = 1 };
-enum gbr_mode { GBR_FIT = 0, GBR_NOFIT = 1 };
+/* GBR_DME: distance RMSD (rms2d `dme`, Frame::DISTRMSD, src/Frame.cpp:1313-1344):
+ * masses are ignored and the reference is not centred, as in the reference;
+ * GBR_PREC_FP32 and GBR_PREC_TC both run the CUDA-core DME kernels (DME has no
+ * tensor-core form here; gbr_stats.precision reports GBR_PREC_FP32). */
+enum gbr_mode { GBR_FIT = 0, GBR_NOFIT = 1, GBR_DME = 2 };
 enum gbr_out_kind { GBR_TRI = 0, GBR_FULL = 1 };
 enum gbr_precision {
   GBR_PREC_FP32 = 0, /* CUDA-core FP32 contraction of pre-aligned residuals    */

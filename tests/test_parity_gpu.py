@@ -280,3 +280,14 @@ def test_pinned_host_overlap(h, precision):
     h.allpairs(torch.from_numpy(R).pin_memory(), torch.from_numpy(T).pin_memory(), tgt_mass=m,
                precision=precision, out=houtf)
     np.testing.assert_array_equal(houtf.numpy(), devf)
+
+
+@pytest.mark.parametrize("precision", _precisions())
+def test_qrmsd_maps_to_fit(h, precision):
+    """rms2d `qrmsd` (QuaternionRMSD_CenteredRef) is passed to the library as
+    GBR_FIT: same best-fit RMSD, QCP instead of Jacobi.  Check against
+    cpptraj's own qrmsd triangle (ref_pairs.npz, its Frame/QCP code)."""
+    refp = np.load(os.path.join(GOLD, "ref_pairs.npz"))
+    out = run(h, refp["xyz"], tgt_mass=refp["mass"], mode="fit", precision=precision)
+    tol = 2e-6 if precision == "fp64" else TOL
+    assert np.abs(out.astype(np.float64) - refp["tri_qcp"]).max() <= tol

@@ -572,6 +572,16 @@ def main():
         h.allpairs(hX, tgt_mass=hm, precision=precision, out=hout)
     torch.cuda.synchronize()
     e2e_ms = 1e3 * (time.perf_counter() - t0) / args.steps
+    # the same with the result staged in HBM and copied back in row bands
+    h.set_option(gbrmsd.OPT_HOST_OUT, 0)
+    h.allpairs(hX, tgt_mass=hm, precision=precision, out=hout)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        h.allpairs(hX, tgt_mass=hm, precision=precision, out=hout)
+    torch.cuda.synchronize()
+    e2e_banded_ms = 1e3 * (time.perf_counter() - t0) / args.steps
+    h.set_option(gbrmsd.OPT_HOST_OUT, 1)
 
     value = ws * pairs / (ms / 1e3)
     peaks = {}
@@ -608,7 +618,9 @@ def main():
                      "kernel_ms": kern_ms, "flops_per_launch": flops, "peak_kind": peak_desc},
         "e2e": {"value": ws * pairs / (e2e_ms / 1e3), "unit": "pairs/s",
                 "h2d_bytes_per_step": int(hX.numel() * 4 + hm.numel() * 8),
-                "d2h_bytes_per_step": int(hout.numel() * 4), "ms_per_step": e2e_ms},
+                "d2h_bytes_per_step": int(hout.numel() * 4), "ms_per_step": e2e_ms,
+                "result_path": "kernels store into the pinned host triangle over the host link",
+                "ms_per_step_banded_copy": e2e_banded_ms},
         "gpu_launches": launches,
         "clocks": clk,
         "stats": st,

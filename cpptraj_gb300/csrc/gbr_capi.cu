@@ -94,6 +94,10 @@ int gbr_set_option(gbr_handle* h, int key, double value) {
       if (value != 0.0 && value != 1.0 && value != 2.0) return h->fail(GBR_ERR_ARG, "tc pipeline must be 0, 1 or 2");
       h->tc_variant = (int)value;
       return GBR_OK;
+    case GBR_OPT_HOST_OUT:
+      if (value != 0.0 && value != 1.0) return h->fail(GBR_ERR_ARG, "host output mode must be 0 or 1");
+      h->host_out_direct = value != 0.0;
+      return GBR_OK;
   }
   return h->fail(GBR_ERR_ARG, "unknown option %d", key);
 }
@@ -185,7 +189,23 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
 
   const bool ref_dev = is_device_ptr(ref_xyz);
   const bool tgt_dev = tgt_xyz ? is_device_ptr(tgt_xyz) : ref_dev;
-  const bool out_dev = is_device_ptr(out);
+  // Pinned host output: by default the kernels store straight into it through
+  // its device alias (Grace-Blackwell's coherent host link carries the
+  // contraction's ~60 GB/s of results while it runs), instead of staging the
+  // triangle in HBM and copying it back in row bands afterwards.
+  const bool out_on_dev = is_device_ptr(out);
+  float* out_k = out;
+  bool out_direct = false;
+  if (!out_on_dev && h->host_out_direct) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, out) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer) {
+      out_k = (float*)at.devicePointer;
+      out_direct = true;
+    } else {
+      cudaGetLastError();
+    }
+  }
+  const bool out_dev = out_on_dev || out_direct;  // kernels can write `out_k` in place
   const size_t esz = (dtype == GBR_F64) ? 8 : 4;
   const int64_t F = (tgt_xyz ? n_ref + n_tgt : n_ref);
   const int64_t tgt0 = tgt_xyz ? n_ref : 0;
@@ -295,7 +315,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
   cudaMemsetAsync(P[21], 0, sizeof(unsigned long long) * kMaxBands, st);
   cudaMemsetAsync(P[25], 0, sizeof(int), st);
 
-  map.out = out_dev ? out : (float*)P[22];
+  map.out = out_dev ? out_k : (float*)P[22];
 
   PrepArgs pa{};
   pa.dtype_f64 = (dtype == GBR_F64);

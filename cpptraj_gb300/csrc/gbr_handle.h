@@ -67,6 +67,7 @@ struct gbr_handle {
   int num_sms = 0;
   int tc_ok = 0;
   int tc_variant = 2;  // pairs of SMs (cta_group::2)
+  bool host_out_direct = true;  // kernels store into pinned host output in place
   // batched path: auxiliary streams, fork/join events, pinned staging,
   // the captured graph of the last batch signature, the autotuner table
   static constexpr int kAux = 8;

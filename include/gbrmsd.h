@@ -182,9 +182,12 @@ int gbr_get_stats(const gbr_handle *h, gbr_stats *out);
  *   GBR_OPT_TC_PIPELINE  tensor-core kernel shape: 0 = one SM, 64-atom stages x 2,
  *                        1 = one SM, 32-atom stages x 4, 2 = pairs of SMs
  *                        sharing one 256-row MMA, 32-atom stages x 5 (default 2)
+ *   GBR_OPT_HOST_OUT     pinned host `out` of gbr_allpairs: 1 = the kernels
+ *                        store into it directly (default), 0 = results staged
+ *                        in device memory and copied back in row bands
  */
 enum gbr_option { GBR_OPT_TAU = 0, GBR_OPT_MAX_REFS = 1, GBR_OPT_TOL = 2, GBR_OPT_TIMING = 3,
-                  GBR_OPT_TC_PIPELINE = 4 };
+                  GBR_OPT_TC_PIPELINE = 4, GBR_OPT_HOST_OUT = 5 };
 int gbr_set_option(gbr_handle *h, int key, double value);
 
 #ifdef __cplusplus

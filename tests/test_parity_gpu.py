@@ -253,12 +253,15 @@ def test_tc_pipeline_full_and_rows(h, pipeline):
         h.set_option(gbrmsd.OPT_TC_PIPELINE, gbrmsd.TC_PIPELINE_DEFAULT)
 
 
+@pytest.mark.parametrize("host_out", [1, 0])
 @pytest.mark.parametrize("precision", ["tc", "fp32"])
-def test_pinned_host_overlap(h, precision):
+def test_pinned_host_overlap(h, precision, host_out):
     # pinned host inputs (chunked copies overlapping the first prep pass) and a
-    # pinned host result (row bands copied while later bands compute) must give
+    # pinned host result -- stored in place by the kernels (host_out 1) or in
+    # row bands copied while later bands compute (host_out 0) -- must give
     # exactly what the device-resident call gives
     torch = pytest.importorskip("torch")
+    h.set_option(gbrmsd.OPT_HOST_OUT, host_out)
     X, m = synth.trajectory(91, 4200, 800, 0.1, 3.0, np.float32, True)
     dev = run(h, torch.from_numpy(X).cuda(), tgt_mass=m, precision=precision).cpu().numpy()
     hX = torch.from_numpy(X).pin_memory()
@@ -280,6 +283,7 @@ def test_pinned_host_overlap(h, precision):
     h.allpairs(torch.from_numpy(R).pin_memory(), torch.from_numpy(T).pin_memory(), tgt_mass=m,
                precision=precision, out=houtf)
     np.testing.assert_array_equal(houtf.numpy(), devf)
+    h.set_option(gbrmsd.OPT_HOST_OUT, 1)
 
 
 @pytest.mark.parametrize("precision", _precisions())

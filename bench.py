@@ -46,7 +46,7 @@ def parse():
                     help="tensor-core kernel shape (GBR_OPT_TC_PIPELINE); default: the library's")
     ap.add_argument("--profile", action="store_true",
                     help="warm up, then run exactly one all-pairs call (for ncu); prints stats only")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4", "dme"],
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4", "dme", "rms", "accuracy"],
                     help="c1 = the headline metric; c2/c3/c4/dme print secondary lines for the other configs")
     return ap.parse_args()
 
@@ -197,6 +197,90 @@ def main_dme(args):
                                        "kind": "port", "sample": f"{cpairs} random pairs, FP64 oracle "
                                                                  f"(Frame::DISTRMSD restatement), OpenMP, {cpu_s:.2f} s"}}),
           flush=True)
+
+
+def main_rms(args):
+    """rms / align over a whole trajectory: 10,000 frames x 2,000 atoms, FP32,
+    mass-weighted, every frame fitted onto frame 0 and moved in place
+    (gbr_superpose, FP64 arithmetic), with the FP64 oracle on a frame sample."""
+    import torch
+
+    import oracle
+    from cpptraj_gb300 import gbrmsd, synth
+
+    F, N = 10000, 2000
+    X, m = synth.trajectory(8, F, N, 0.1, 3.0, np.float32, True)
+    h = gbrmsd.Handle(0)
+    h.set_stream(torch.cuda.current_stream().cuda_stream)
+    dX = torch.from_numpy(X).cuda()
+    dm = torch.from_numpy(m).cuda()
+    ref = dX[0].clone()
+    move = dX.clone()
+    ms_fit = _gpu_time(lambda: h.superpose(ref, dX, mass=dm), max(3, args.steps), 2)
+    ms_align = _gpu_time(lambda: (move.copy_(dX), h.superpose(ref, dX, mass=dm, move=move)), max(3, args.steps), 2)
+    ms_copy = _gpu_time(lambda: move.copy_(dX), max(3, args.steps), 2)
+    ms_align -= ms_copy  # the refresh of the moved frames is not part of the action
+    got = h.superpose(ref, dX, mass=dm)
+    sample = np.arange(0, F, 50)
+    want = oracle.superpose_f64(X[0], X[sample], mass=m)
+    err = float(np.abs(got[0].cpu().numpy()[sample] - want[0]).max())
+    rot_err = float(np.abs(got[1].cpu().numpy()[sample] - want[1]).max())
+    t0 = time.perf_counter()
+    oracle.superpose_f64(X[0], X[:2000], mass=m, move=X[:2000].astype(np.float64), nthreads=os.cpu_count() or 1)
+    cpu_s = time.perf_counter() - t0
+    # FP64 operations per atom: centre 3 FMA; covariance, E0: 3 sub + 3 mul + 9 FMA + 7 (E0) ;
+    # move: 3 sub + 9 FMA + 3 add -- counted as flops (FMA = 2)
+    fit_flops = N * F * (3 * 2 + 3 + 3 + 9 * 2 + 8 * 2)
+    move_flops = N * F * (3 + 9 * 2 + 3)
+    print(json.dumps({"workload": f"rms/align, {F} frames x {N} atoms, FP32 coords, mass-weighted, fit to frame 0",
+                      "frames_per_s_fit": F / (ms_fit / 1e3), "ms_fit": ms_fit,
+                      "frames_per_s_align": F / (ms_align / 1e3), "ms_align": ms_align,
+                      "fp64_tflops_fit": fit_flops / (ms_fit / 1e3) / 1e12,
+                      "fp64_tflops_align": (fit_flops + move_flops) / (ms_align / 1e3) / 1e12,
+                      "dram_bytes_align_min": 3 * X.nbytes,
+                      "max_abs_err_rmsd_A": err, "max_abs_err_rot": rot_err, "sample_frames": len(sample),
+                      "cpu_baseline": {"value": 2000 / cpu_s, "unit": "frames/s (fit + move)",
+                                       "cores": os.cpu_count(), "kind": "port",
+                                       "sample": f"frames 0-1999, FP64 oracle (Jacobi, as Frame::RMSD_CenteredRef), "
+                                                 f"OpenMP, {cpu_s:.2f} s"}}), flush=True)
+
+
+def main_accuracy(args):
+    """Error of the FP32 and tensor-core paths against the FP64 oracle on 3,000
+    sampled pairs, raw (the per-pair bound's FP64 re-check switched off by a
+    huge tolerance) and as shipped (tolerance 5e-5 Angstrom), on three kinds
+    of frames: config-1-like noise, clustered frames, and an MD-like
+    time-correlated trajectory."""
+    import torch
+
+    import oracle
+    from cpptraj_gb300 import gbrmsd, synth
+
+    cases = [("c1 shape 1000 x 2000, mass-weighted", *synth.trajectory(1, 1000, 2000, 0.1, 3.0, np.float32, True)),
+             ("clustered 3000 x 500, 20 centroids", synth.clustered(2, 3000, 500)[0], None),
+             ("MD-like correlated 1500 x 2000, mass-weighted", *synth.md_like(6, 1500, 2000, weighted=True))]
+    h = gbrmsd.Handle(0)
+    rows = []
+    for name, X, m in cases:
+        F = X.shape[0]
+        rng = np.random.default_rng(7)
+        pi = rng.integers(0, F - 1, 3000)
+        pj = np.array([rng.integers(i + 1, F) for i in pi])
+        ref = oracle.pairs_f64(X, pi, pj, mass=m)
+        idx = F * pi - ((pi + 1) * pi) // 2 + pj - pi - 1
+        dX = torch.from_numpy(X).cuda()
+        r = {"data": name}
+        for prec in ("fp32", "tc"):
+            for tag, tol in (("raw", 1e9), ("shipped", 5e-5)):
+                h.set_option(gbrmsd.OPT_TOL, tol)
+                out = h.allpairs(dX, tgt_mass=m, precision=prec).cpu().numpy()
+                st = h.stats()
+                r[f"{prec}_{tag}_max_err_A"] = float(np.abs(out[idx].astype(np.float64) - ref).max())
+                r[f"{prec}_{tag}_fixed_frac"] = st["pairs_fixed"] / st["pairs"]
+                r["n_refs"] = st["n_refs"]
+        rows.append(r)
+    h.set_option(gbrmsd.OPT_TOL, 5e-5)
+    print(json.dumps({"workload": "accuracy calibration, 3,000 sampled pairs per case", "rows": rows}), flush=True)
 
 
 def main_c4(args):
@@ -492,7 +576,8 @@ def main():
     if args.profile:
         return main_profile(args)
     if args.workload != "c1":
-        return {"c2": main_c2, "c3": main_c3, "c4": main_c4, "dme": main_dme}[args.workload](args)
+        return {"c2": main_c2, "c3": main_c3, "c4": main_c4, "dme": main_dme, "rms": main_rms,
+                "accuracy": main_accuracy}[args.workload](args)
     import torch
     import torch.distributed as dist
 

@@ -31,7 +31,7 @@ MODES = {"fit": FIT, "nofit": NOFIT, "dme": DME}
 #: Every symbol include/gbrmsd.h declares.
 EXPORTED = ("gbr_create", "gbr_destroy", "gbr_last_error", "gbr_allpairs", "gbr_output_count",
             "gbr_allpairs_batched", "gbr_rmsd_backward", "gbr_get_stats", "gbr_set_option", "gbr_set_stream",
-            "gbr_write_cmatrix",
+            "gbr_write_cmatrix", "gbr_superpose",
             "gbr_allpairs_fp64_static")
 
 
@@ -87,6 +87,8 @@ def load():
         L.gbr_set_stream.argtypes = [vp, vp]
         L.gbr_write_cmatrix.restype = ci
         L.gbr_write_cmatrix.argtypes = [vp, ctypes.c_char_p, vp, ci, i64, i32, vp, ci, ci, vp, i64, i64]
+        L.gbr_superpose.restype = ci
+        L.gbr_superpose.argtypes = [vp, vp, vp, ci, i64, i32, vp, vp, ci, vp, vp, vp, vp, vp, i32]
         L.gbr_allpairs_fp64_static.restype = ci
         L.gbr_allpairs_fp64_static.argtypes = [vp, ci, i64, i32, vp, ci, vp, vp]
         _lib = L
@@ -198,6 +200,36 @@ class Handle:
         self.allpairs_raw(ref, tgt, n_ref, n_tgt, n_atom, _dtype_code(ref), ref_mass, tgt_mass, m, out_kind, p,
                           out, row_begin, row_end)
         return out
+
+    def superpose(self, ref, xyz, mass=None, ref_mass=None, mode="fit", move=None):
+        """Per-frame best fit onto one reference frame (the rms / align actions).
+
+        ref: [atoms, 3]; xyz: [frames, atoms, 3] (numpy or torch, same dtype);
+        move: optional [frames, n_move, 3] array of that dtype, moved in place.
+        Returns (rmsd [F], rot [F, 3, 3], tgt_trans [F, 3], ref_trans [3]) as
+        float64 arrays of the same kind and device as ``xyz``."""
+        F, N = int(xyz.shape[0]), int(xyz.shape[1])
+        m = MODES[mode] if isinstance(mode, str) else mode
+        if isinstance(xyz, np.ndarray):
+            def mk(*shape):
+                return np.zeros(shape, np.float64)
+            if mass is not None:
+                mass = np.ascontiguousarray(mass, dtype=np.float64)
+            if ref_mass is not None:
+                ref_mass = np.ascontiguousarray(ref_mass, dtype=np.float64)
+        else:
+            import torch
+
+            def mk(*shape):
+                return torch.zeros(shape, dtype=torch.float64, device=xyz.device)
+        rmsd, rot, tt, rt = mk(F), mk(F, 3, 3), mk(F, 3), mk(3)
+        n_move = 0 if move is None else int(move.shape[1])
+        if move is not None and _dtype_code(move) != _dtype_code(xyz):
+            raise TypeError("move must have the dtype of xyz")
+        self._check(self.lib.gbr_superpose(self.h, _ptr(ref), _ptr(xyz), _dtype_code(xyz), F, N, _ptr(ref_mass),
+                                           _ptr(mass), m, _ptr(rmsd), _ptr(rot), _ptr(tt), _ptr(rt), _ptr(move),
+                                           n_move))
+        return rmsd, rot, tt, rt
 
     def allpairs_batched(self, trajs, masses=None, mode="fit", precision="fp32"):
         """trajs: list of float32 [F_t, N_t, 3] arrays; returns list of TRI outputs."""

@@ -17,6 +17,8 @@
  *                        sets, one rms2d per set.
  *   gbr_write_cmatrix <- the pairwise-cache fill plus Cmatrix_Binary::WriteCmatrix
  *                        (savepairdist) in one call.
+ *   gbr_superpose     <- the per-frame fit of the rms / align actions
+ *                        (Action_Rmsd::DoAction, Action_Align::DoAction).
  *   gbr_rmsd_backward <- no reference counterpart (cpptraj has no gradient of
  *                        RMSD); dL/dx for L = sum_{i<j} g_ij RMSD_ij.
  *
@@ -138,6 +140,33 @@ int gbr_write_cmatrix(gbr_handle *h, const char *path, const void *xyz, int dtyp
  * Pairs with RMSD == 0 contribute no gradient. */
 int gbr_rmsd_backward(gbr_handle *h, const float *xyz, int64_t n_frame, int32_t n_atom,
                       const double *mass, const float *g, float *grad_xyz, float *rmsd_out);
+
+/* Per-frame best fit of n_frame frames onto ONE reference frame: the `rms`
+ * action (Action_Rmsd::DoAction, src/Action_Rmsd.cpp:372-395) and `align`
+ * (Action_Align::DoAction, src/Action_Align.cpp:85-99) over a whole frame set.
+ *   ref_xyz   the reference frame (n_atom atoms, dtype), as selected by the
+ *             reference mask.  GBR_FIT centres it, as ReferenceAction does
+ *             with Frame::CenterOnOrigin: mass-weighted by ref_mass (NULL =>
+ *             mass) when mass is given, geometrically when mass is NULL (the
+ *             action's one `mass` keyword); GBR_NOFIT uses it as given.
+ *   xyz       n_frame frames of n_atom atoms (the target mask), dtype.
+ *   mass      target masses weighting every sum (NULL => unweighted), as
+ *             Frame::RMSD_CenteredRef / RMSD_NoFit use the target's masses.
+ *   rmsd      [n_frame] RMSD_CenteredRef (fit) or RMSD_NoFit (nofit), FP64.
+ *   rot       [n_frame][9] the best rotation U, row-major (U y ~ r for the
+ *             centred frame y); identity for nofit.
+ *   tgt_trans [n_frame][3] the frame's Trans of RMSD_CenteredRef, i.e. minus
+ *             its centre (mass-weighted when mass is given); 0 for nofit.
+ *   ref_trans [3] the reference's centre (ReferenceAction::RefTrans); 0 for nofit.
+ *   move_xyz  [n_frame][n_move][3] of dtype, or NULL: frame f's atoms to move
+ *             (align's move mask, rms's whole frame), transformed in place by
+ *             Frame::Trans_Rot_Trans(tgt_trans[f], U[f], ref_trans)
+ *             (src/Frame.h:572-581); untouched for nofit.
+ * Any output may be NULL.  Pointers may be host or device memory.  All
+ * arithmetic is FP64. */
+int gbr_superpose(gbr_handle *h, const void *ref_xyz, const void *xyz, int dtype, int64_t n_frame,
+                  int32_t n_atom, const double *ref_mass, const double *mass, int mode, double *rmsd,
+                  double *rot, double *tgt_trans, double *ref_trans, void *move_xyz, int32_t n_move);
 
 /* All-pairs RMSD that allocates nothing.  No counterpart in the reference:
  * cpptraj's loops allocate host frames per thread; this entry point exists for

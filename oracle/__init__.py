@@ -55,6 +55,11 @@ def lib():
         L.orc_pairs_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                     ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                     ctypes.c_void_p, ctypes.c_int]
+        L.orc_superpose_f64.restype = ctypes.c_int
+        L.orc_superpose_f64.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int64,
+                                        ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         L.orc_max_threads.restype = ctypes.c_int
         L.orc_grad_f64.restype = ctypes.c_int
         L.orc_grad_f64.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p,
@@ -86,6 +91,10 @@ def ref_lib():
         L.ref_pairs_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                     ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                     ctypes.c_void_p]
+        L.ref_superpose.restype = ctypes.c_int
+        L.ref_superpose.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int,
+                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         _ref = L
     return _ref
 
@@ -216,3 +225,29 @@ def ref_write_cmatrix(path, tri, frame_to_idx, sieve):
     rc = ref_lib().ref_write_cmatrix(path.encode(), _p(tri), _p(f2i), len(f2i), nrows, int(sieve))
     if rc != 0:
         raise RuntimeError("reference cmatrix writer failed")
+
+
+def superpose_f64(ref, xyz, ref_mass=None, mass=None, mode=FIT, move=None, nthreads=0, use_reference_code=False):
+    """Per-frame fit onto one reference frame (rms / align actions).  Returns
+    (rmsd [F], rot [F,3,3], tgt_trans [F,3], ref_trans [3], moved [F,M,3] or
+    None), all FP64.  ``move`` (FP64 [F, M, 3]) is copied, then moved."""
+    ref = np.ascontiguousarray(ref)
+    xyz = np.ascontiguousarray(xyz, dtype=ref.dtype)
+    F, N = xyz.shape[0], xyz.shape[1]
+    if mass is not None:
+        mass = np.ascontiguousarray(mass, dtype=np.float64)
+    if ref_mass is not None:
+        ref_mass = np.ascontiguousarray(ref_mass, dtype=np.float64)
+    rmsd = np.zeros(F)
+    rot = np.zeros((F, 3, 3))
+    tt = np.zeros((F, 3))
+    rt = np.zeros(3)
+    mv = None if move is None else np.array(move, dtype=np.float64, order="C", copy=True)
+    nm = 0 if mv is None else mv.shape[1]
+    if use_reference_code:
+        ref_lib().ref_superpose(_p(ref), _p(xyz), _dtype_code(ref), F, N, _p(ref_mass), _p(mass), _p(rmsd), _p(rot),
+                                _p(tt), _p(rt), _p(mv), nm)
+    else:
+        lib().orc_superpose_f64(_p(ref), _p(xyz), _dtype_code(ref), F, N, _p(ref_mass), _p(mass), mode, _p(rmsd),
+                                _p(rot), _p(tt), _p(rt), _p(mv), nm, nthreads)
+    return rmsd, rot, tt, rt, mv

@@ -101,3 +101,39 @@ extern "C" int ref_write_cmatrix(const char* path, const float* tri, const int* 
   Cpptraj::Cluster::Cmatrix_Binary w;
   return w.WriteCmatrix(FileName(path), tri, f2i, (size_t)nrows, sieve);
 }
+
+// Per-frame fit with cpptraj's own code, as the rms/align actions run it
+// (Action_Rmsd::DoAction src/Action_Rmsd.cpp:372-395, Action_Align::DoAction
+// src/Action_Align.cpp:85-99): the reference centred once with CenterOnOrigin
+// (ReferenceAction::SelectRefAtoms), RMSD_CenteredRef(ref, U, Trans) per frame
+// and Trans_Rot_Trans(Trans, U, refTrans) of the frame's n_move atoms.  Same
+// argument meaning as orc_superpose_f64 (fit only).
+extern "C" int ref_superpose(const void* ref_xyz, const void* xyz, int dtype, int64_t n_frame, int n_atom,
+                             const double* ref_mass, const double* mass, double* rmsd, double* rot,
+                             double* tgt_trans, double* ref_trans, double* move, int n_move) {
+  bool use_mass = (mass != nullptr);
+  Frame R = make(n_atom, ref_mass ? ref_mass : mass);
+  fill(R, ref_xyz, dtype, 0, n_atom);
+  Vec3 rt = R.CenterOnOrigin(use_mass);
+  for (int k = 0; k < 3; ++k) ref_trans[k] = rt[k];
+  Frame T = make(n_atom, mass);
+  std::vector<double> mv(3 * (size_t)n_move, 0.0), mm(n_move, 1.0);
+  Frame M;
+  M.SetupFrameXM(mv, mm);
+  for (int64_t f = 0; f < n_frame; ++f) {
+    fill(T, xyz, dtype, f, n_atom);
+    Matrix_3x3 U;
+    Vec3 tr;
+    rmsd[f] = T.RMSD_CenteredRef(R, U, tr, use_mass);
+    for (int k = 0; k < 9; ++k) rot[9 * f + k] = U[k];
+    for (int k = 0; k < 3; ++k) tgt_trans[3 * f + k] = tr[k];
+    if (move) {
+      double* x = M.xAddress();
+      double* src = move + (size_t)f * 3 * n_move;
+      for (int k = 0; k < 3 * n_move; ++k) x[k] = src[k];
+      M.Trans_Rot_Trans(tr, U, rt);
+      for (int k = 0; k < 3 * n_move; ++k) src[k] = x[k];
+    }
+  }
+  return 0;
+}

@@ -11,6 +11,8 @@
  *   - Matrix_3x3::Diagonalize_Sort   src/Matrix_3x3.cpp:219-280
  *   - Frame::RMSD_NoFit              src/Frame.cpp:1279-1307
  *   - Frame::DISTRMSD                src/Frame.cpp:1313-1344 (rms2d `dme`)
+ *   - Action_Rmsd / Action_Align per-frame fit, Frame::Trans_Rot_Trans
+ *                                    (orc_superpose_f64)
  *   - Frame::CenterOnOrigin          src/Frame.cpp:1043-1055, Frame.h:373-391
  *   - QCPRot::FastCalcRMSDAndRotation src/qcprot.cpp:167-246 (RMSD part) and
  *     do_quaternion_rmsd              src/QuaternionRMSD.cpp:25-120
@@ -176,8 +178,10 @@ static double target_moments(const double *ref, const double *tgt, int n, const 
   return W;
 }
 
-/* Kabsch RMSD of target to a centred ref (Frame::RMSD_CenteredRef). */
-double orc_rmsd_centered_ref(const double *ref, const double *tgt, int n, const double *mass) {
+/* Kabsch RMSD of target to a centred ref (Frame::RMSD_CenteredRef); with U
+ * non-NULL also the best rotation U (row-major, U y ~ r for the centred
+ * target y), built as at src/Frame.cpp:1239-1250. */
+static double fit_centered_ref(const double *ref, const double *tgt, int n, const double *mass, double *U) {
   double R[9], E0;
   double W = target_moments(ref, tgt, n, mass, R, &E0);
   if (W < 0.0) return -1.0;
@@ -187,7 +191,10 @@ double orc_rmsd_centered_ref(const double *ref, const double *tgt, int n, const 
     for (int j = 0; j < 3; ++j)
       RRt[3 * i + j] = R[3 * i] * R[3 * j] + R[3 * i + 1] * R[3 * j + 1] + R[3 * i + 2] * R[3 * j + 2];
   double v[9], d[3], e[9], mu[3];
-  if (jacobi3(RRt, v, d)) return 0.0; /* non-convergence returns 0, as the reference does */
+  if (jacobi3(RRt, v, d)) { /* non-convergence returns 0, as the reference does */
+    if (U) for (int k = 0; k < 9; ++k) U[k] = (k % 4 == 0) ? 1.0 : 0.0;
+    return 0.0;
+  }
   sort_eigen(v, d, e, mu);
   /* Third axis is the cross product of the first two. */
   e[6] = e[1] * e[5] - e[2] * e[4];
@@ -201,9 +208,18 @@ double orc_rmsd_centered_ref(const double *ref, const double *tgt, int n, const 
   }
   double cp[3] = {b[1] * b[5] - b[2] * b[4], b[2] * b[3] - b[0] * b[5], b[0] * b[4] - b[1] * b[3]};
   double sig3 = (cp[0] * b[6] + cp[1] * b[7] + cp[2] * b[8] < 0.0) ? -1.0 : 1.0;
+  if (U) {
+    b[6] = cp[0]; b[7] = cp[1]; b[8] = cp[2];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) U[3 * i + j] = e[j] * b[i] + e[3 + j] * b[3 + i] + e[6 + j] * b[6 + i];
+  }
   double r = E0 - sqrt(fabs(mu[0])) - sqrt(fabs(mu[1])) - sig3 * sqrt(fabs(mu[2]));
   if (r < 0.0) return 0.0;
   return sqrt(2.0 * r / W);
+}
+
+double orc_rmsd_centered_ref(const double *ref, const double *tgt, int n, const double *mass) {
+  return fit_centered_ref(ref, tgt, n, mass, NULL);
 }
 
 /* Quaternion (QCP) RMSD of target to a centred ref: Newton iteration from   */
@@ -428,6 +444,69 @@ int orc_pairs_f64(const void *xyz, int dtype, int n_atom, const double *mass, in
     free(R);
     free(T);
   }
+  return err;
+}
+
+/* Per-frame fit of n_frame target frames onto one reference frame: the rms
+ * action (Action_Rmsd::DoAction, src/Action_Rmsd.cpp:372-395) and align
+ * (Action_Align::DoAction, src/Action_Align.cpp:85-99).  Fit: the reference
+ * is centred (ReferenceAction::SelectRefAtoms, CenterOnOrigin; ref_trans =
+ * its centre) with ref_mass (NULL => mass) when mass is given, geometrically
+ * when it is not (one `mass` flag covers both frames); each frame gets RMSD_CenteredRef(ref, U, Trans)
+ * with Trans = -(its centre) and, when move is given, Trans_Rot_Trans(Trans,
+ * U, ref_trans) of its n_move atoms (Frame.h:572-581).  No-fit: RMSD_NoFit
+ * against the uncentred reference, U = I, translations 0, nothing moved.
+ * Outputs may be NULL.  move is FP64 [n_frame][n_move][3].  */
+int orc_superpose_f64(const void *ref_xyz, const void *xyz, int dtype, int64_t n_frame, int n_atom,
+                      const double *ref_mass, const double *mass, int mode, double *rmsd, double *rot,
+                      double *tgt_trans, double *ref_trans, double *move, int n_move, int nthreads) {
+  if (n_atom < 1) return 1;
+  double *R = (double *)malloc(sizeof(double) * 3 * (size_t)n_atom);
+  load_frame(ref_xyz, dtype, 0, n_atom, R);
+  double rc[3] = {0.0, 0.0, 0.0};
+  if (mode == ORC_FIT) {
+    orc_center(R, n_atom, mass ? (ref_mass ? ref_mass : mass) : NULL, rc);
+    for (int a = 0; a < n_atom; ++a) {
+      R[3 * a] -= rc[0]; R[3 * a + 1] -= rc[1]; R[3 * a + 2] -= rc[2];
+    }
+  }
+  if (ref_trans) { ref_trans[0] = rc[0]; ref_trans[1] = rc[1]; ref_trans[2] = rc[2]; }
+  int err = 0;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel reduction(| : err)
+#endif
+  {
+    double *T = (double *)malloc(sizeof(double) * 3 * (size_t)n_atom);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic)
+#endif
+    for (int64_t f = 0; f < n_frame; ++f) {
+      load_frame(xyz, dtype, f, n_atom, T);
+      double U[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}, c[3] = {0.0, 0.0, 0.0}, r;
+      if (mode == ORC_FIT) {
+        orc_center(T, n_atom, mass, c);
+        r = fit_centered_ref(R, T, n_atom, mass, U);
+      } else {
+        r = orc_rmsd_nofit(R, T, n_atom, mass);
+      }
+      if (r < 0.0) err |= 2;
+      if (rmsd) rmsd[f] = r;
+      if (rot) memcpy(rot + 9 * f, U, sizeof U);
+      if (tgt_trans) { tgt_trans[3 * f] = -c[0]; tgt_trans[3 * f + 1] = -c[1]; tgt_trans[3 * f + 2] = -c[2]; }
+      if (move && mode == ORC_FIT) {
+        double *m = move + (size_t)f * 3 * n_move;
+        for (int a = 0; a < n_move; ++a) {
+          const double x = m[3 * a] - c[0], y = m[3 * a + 1] - c[1], z = m[3 * a + 2] - c[2];
+          m[3 * a] = x * U[0] + y * U[1] + z * U[2] + rc[0];
+          m[3 * a + 1] = x * U[3] + y * U[4] + z * U[5] + rc[1];
+          m[3 * a + 2] = x * U[6] + y * U[7] + z * U[8] + rc[2];
+        }
+      }
+    }
+    free(T);
+  }
+  free(R);
   return err;
 }
 

@@ -23,6 +23,10 @@ Run in a container where the reference tree is mounted (default
    (frame f1 as target, RMSD_NoFit against f2) and the file bytes from its own
    Cmatrix_Binary::WriteCmatrix, for the full cache and for a regular sieve of
    3 (frames 0, 3, 6, ... kept).
+4. ref_superpose.npz -- the per-frame fit of the rms / align actions run by
+   cpptraj's own code (RMSD_CenteredRef with rotation and translation, then
+   Trans_Rot_Trans of a larger "move" atom set), mass-weighted and not, on
+   seeded synthetic frames.
 """
 from __future__ import annotations
 
@@ -215,7 +219,25 @@ def make_cluster_cmatrix():
     print("tz2_cluster_cmatrix.npz:", X.shape, {k: v.shape for k, v in out.items() if k.startswith("ctm")})
 
 
+def make_ref_superpose():
+    sys.path.insert(0, ROOT)
+    import oracle
+    from cpptraj_gb300 import synth
+
+    oracle.build(with_ref=True)
+    X, m = synth.trajectory(21, 30, 157, 0.05, 3.0, np.float32, True)
+    move, _ = synth.trajectory(22, 30, 301, 0.5, 1.0, np.float64, False)
+    res = {"xyz": X, "mass": m, "move": move}
+    for tag, mm in (("w", m), ("u", None)):
+        r, rot, tt, rt, mv = oracle.superpose_f64(X[5], X, mass=mm, move=move, use_reference_code=True)
+        res.update({f"rmsd_{tag}": r, f"rot_{tag}": rot, f"tgt_trans_{tag}": tt, f"ref_trans_{tag}": rt,
+                    f"moved_{tag}": mv})
+    np.savez_compressed(os.path.join(HERE, "ref_superpose.npz"), **res)
+    print("ref_superpose.npz:", X.shape, move.shape)
+
+
 if __name__ == "__main__":
     make_tz2()
     make_ref_pairs()
     make_cluster_cmatrix()
+    make_ref_superpose()

@@ -127,3 +127,18 @@ def test_cluster_cmatrix_fixture_matches_oracle():
         if sieve != 1:
             flags = raw[28 + 4 * n:]
             assert flags == b"".join(b"T" if v < 0 else b"F" for v in f2i)
+
+
+@pytest.mark.parametrize("wt", ["w", "u"])
+def test_superpose_matches_reference_code(wt):
+    """rms / align per-frame fit: the restatement against cpptraj's own
+    RMSD_CenteredRef(ref, U, Trans) + Trans_Rot_Trans output (ref_superpose.npz)."""
+    g = np.load(os.path.join(GOLD, "ref_superpose.npz"))
+    m = g["mass"] if wt == "w" else None
+    r, rot, tt, rt, mv = oracle.superpose_f64(g["xyz"][5], g["xyz"], mass=m, move=g["move"])
+    np.testing.assert_array_equal(r, g[f"rmsd_{wt}"])
+    np.testing.assert_array_equal(rot, g[f"rot_{wt}"])
+    np.testing.assert_array_equal(tt, g[f"tgt_trans_{wt}"])
+    np.testing.assert_array_equal(rt, g[f"ref_trans_{wt}"])
+    np.testing.assert_array_equal(mv, g[f"moved_{wt}"])
+    assert r[5] < 1e-6  # the reference frame itself

@@ -35,7 +35,7 @@ K2_TRAFFIC_BYTES = {(N_FRAME, N_ATOM): 2.244835e9 + 0.198118e9}
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="auto", choices=["auto", "tc", "fp32"])

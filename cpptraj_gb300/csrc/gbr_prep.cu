@@ -28,6 +28,7 @@
 //                  exact operand values the contraction reads.
 //   k_ref_terms    per reference pair: exact rotation U_ab, U_ab S_ba, and
 //                  sum w |r_a - U_ab r_b|^2 (O(N) per pair of references).
+#include <cooperative_groups.h>
 #include <cuda_fp16.h>
 
 #include <vector>
@@ -54,6 +55,68 @@ constexpr int kWarps = kPrepThreads / 32;
 // atoms with FP64 sums; their time is the serial FP64 tail of one thread (a
 // larger block measured slower).
 constexpr int kOneBlockThreads = 256;
+// Those kernels run as one cluster of kRefCluster CTAs (on as many SMs): each
+// CTA walks every kRefCluster-th block of atoms and the sums are combined
+// across the cluster in distributed shared memory (cluster_sum_f64).
+constexpr int kRefCluster = 8;
+
+namespace cg = cooperative_groups;
+
+// Sums of NV doubles over all threads of all CTAs of this cluster, returned
+// to every thread.  Each CTA's total goes to CTA 0's `slots`; after a cluster
+// barrier every CTA adds the slots in rank order, so all CTAs see the same
+// (deterministic) totals.  red: >= 32*NV doubles, slots: >= kRefCluster*NV,
+// bc: >= NV doubles of this CTA's shared memory.  Every thread of every CTA of
+// the cluster must call it (it contains block and cluster barriers).
+template <int NV>
+__device__ __forceinline__ void cluster_sum_f64(double (&v)[NV], double* red, double* slots, double* bc) {
+  block_sum_f64<NV>(v, red);
+  cg::cluster_group cl = cg::this_cluster();
+  const unsigned rank = cl.block_rank(), n = cl.num_blocks();
+  if (threadIdx.x == 0) {
+    double* dst = cl.map_shared_rank(slots, 0);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) dst[rank * NV + k] = v[k];
+  }
+  cl.sync();
+  if (threadIdx.x == 0) {
+    const double* src = cl.map_shared_rank(slots, 0);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double t = 0.0;
+      for (unsigned r = 0; r < n; ++r) t += src[r * NV + k];
+      bc[k] = t;
+    }
+  }
+  cl.sync();  // CTA 0's slots are free again; bc is visible in this CTA
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = bc[k];
+}
+
+// Maximum of a non-negative value over the cluster (same scheme, one slot per CTA).
+__device__ __forceinline__ double cluster_max_f64(double m, double* red, double* slots, double* bc) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  cg::cluster_group cl = cg::this_cluster();
+  const unsigned rank = cl.block_rank(), n = cl.num_blocks();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t = fmax(t, red[k]);
+    cl.map_shared_rank(slots, 0)[rank] = t;
+  }
+  cl.sync();
+  if (threadIdx.x == 0) {
+    const double* src = cl.map_shared_rank(slots, 0);
+    double t = 0.0;
+    for (unsigned r = 0; r < n; ++r) t = fmax(t, src[r]);
+    bc[0] = t;
+  }
+  cl.sync();
+  return bc[0];
+}
 constexpr int kSample = 2048;      // frames per reference that set its refined mean
 constexpr int kMeanChunks = 64;    // fixed partition of those frames
 constexpr int kFtab = 24;          // floats per frame in the rotation table
@@ -285,14 +348,15 @@ __device__ __forceinline__ float dot2_row(const float* Rh, const float* Rl, floa
 }
 
 // Weights in the forms the passes read; scal = {max sqrt(w), sum w, sum of
-// the reference centring masses}.  One block.
-__global__ void __launch_bounds__(kOneBlockThreads) k_weights(const double* w, const double* cmass_ref, int N,
-                                                          double* sqw, float* sqwf, float* wf, float* wfl,
-                                                          float* cmf_ref, float* cmfl_ref, double* scal) {
-  __shared__ double red[32 * 3];
-  double v[3] = {0.0, 0.0, 0.0};
+// the reference centring masses}.  One cluster of kRefCluster CTAs.
+__global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockThreads)
+    k_weights(const double* w, const double* cmass_ref, int N, double* sqw, float* sqwf, float* wf, float* wfl,
+              float* cmf_ref, float* cmfl_ref, double* scal) {
+  __shared__ double red[32 * 2], slots[kRefCluster * 2], bc[2];
+  const int stride = kRefCluster * blockDim.x;
+  double v[2] = {0.0, 0.0};
   double mx = 0.0;
-  for (int a = threadIdx.x; a < N; a += blockDim.x) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < N; a += stride) {
     const double wa = w ? w[a] : 1.0;
     const double ca = cmass_ref ? cmass_ref[a] : 1.0;
     const double s = sqrt(wa);
@@ -310,16 +374,10 @@ __global__ void __launch_bounds__(kOneBlockThreads) k_weights(const double* w, c
     v[0] += wa;
     v[1] += ca;
   }
-  // max via the sum helper's layout: reduce max separately in shared memory
-  __shared__ double smx[32];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if ((threadIdx.x & 31) == 0) smx[threadIdx.x >> 5] = mx;
-  block_sum_f64<3>(v, red);
-  if (threadIdx.x == 0) {
-    double m = 0.0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) m = fmax(m, smx[k]);
-    scal[0] = m;
+  cluster_sum_f64<2>(v, red, slots, bc);
+  mx = cluster_max_f64(mx, red, slots, bc);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    scal[0] = mx;
     scal[1] = v[0];
     scal[2] = v[1];
     scal[3] = 0.0;
@@ -362,54 +420,55 @@ __global__ void __launch_bounds__(kPrepThreads) k_centroid(FrameSrc<T> src, int6
 
 // Reference k := frame *fsel centred (and superposed onto reference `parent`
 // when fitting and use_parent).  Reference 0 is built before any centre is
-// known and centres its frame itself (FP64, one block).  Writes the FP64
-// reference, sqrt(w) r (FP32), r as hi + lo floats, sum w |r|^2, sum w r and
-// max |r|.
+// known and centres its frame itself.  Writes the FP64 reference, sqrt(w) r
+// (FP32), r as hi + lo floats, sum w |r|^2, sum w r and max |r|.  FP64 per
+// atom: one cluster of kRefCluster CTAs shares the atoms.
 template <typename T>
-__global__ void __launch_bounds__(kOneBlockThreads) k_make_ref(FrameSrc<T> src, const int64_t* fsel,
-                                                           const double* cen, const double* cmass_ref,
-                                                           const double* cmass_tgt, const double* w,
-                                                           const int* assign, int k, int use_parent, int nofit,
-                                                           double* refs, float* swr, float2* refhl,
-                                                           double* Eref, double* sr, float* rmax) {
-  __shared__ double red[32 * 10];
+__global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockThreads)
+    k_make_ref(FrameSrc<T> src, const int64_t* fsel, const double* cen, const double* cmass_ref,
+               const double* cmass_tgt, const double* w, const double* sqw, const int* assign, int k, int use_parent,
+               int nofit, double* refs, float* swr, float2* refhl, double* Eref, double* sr, float* rmax) {
+  __shared__ double red[32 * 10], slots[kRefCluster * 10], bc[10];
   __shared__ double Rs[9];
-  __shared__ double cs[3];
-  __shared__ float smx[32];
   const int N = src.N;
+  const int a_first = blockIdx.x * blockDim.x + threadIdx.x, stride = kRefCluster * blockDim.x;
   const int64_t f = *fsel;
   const T* x = src.frame(f);
   if (threadIdx.x < 9) Rs[threadIdx.x] = (threadIdx.x % 4 == 0) ? 1.0 : 0.0;
+  double c0 = 0.0, c1 = 0.0, c2 = 0.0;
   if (nofit || use_parent) {
-    if (threadIdx.x < 3) cs[threadIdx.x] = nofit ? 0.0 : cen[3 * f + threadIdx.x];
+    if (!nofit) {
+      c0 = cen[3 * f];
+      c1 = cen[3 * f + 1];
+      c2 = cen[3 * f + 2];
+    }
   } else {
     const double* m = (f < src.n_ref) ? cmass_ref : cmass_tgt;
     double v[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int a = threadIdx.x; a < N; a += blockDim.x) {
+    for (int a = a_first; a < N; a += stride) {
       const double wm = m ? m[a] : 1.0;
       v[0] += wm * (double)x[3 * a];
       v[1] += wm * (double)x[3 * a + 1];
       v[2] += wm * (double)x[3 * a + 2];
       v[3] += wm;
     }
-    block_sum_f64<4>(v, red);
-    if (threadIdx.x == 0) {
-      double wt = m ? v[3] : (double)N;
-      if (m && wt == 0.0) {
-        wt = 1.0;
-        v[0] = v[1] = v[2] = 0.0;
-      }
-      for (int q = 0; q < 3; ++q) cs[q] = v[q] / wt;
+    cluster_sum_f64<4>(v, red, slots, bc);
+    double wt = m ? v[3] : (double)N;
+    if (m && wt == 0.0) {
+      wt = 1.0;
+      v[0] = v[1] = v[2] = 0.0;
     }
+    c0 = v[0] / wt;
+    c1 = v[1] / wt;
+    c2 = v[2] / wt;
   }
   __syncthreads();
-  const double c0 = cs[0], c1 = cs[1], c2 = cs[2];
   double* rk = refs + (size_t)k * 3 * N;
   const int parent = use_parent ? assign[f] : -1;
   if (!nofit && parent >= 0) {
     const double* rp = refs + (size_t)parent * 3 * N;
     double v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int a = threadIdx.x; a < N; a += blockDim.x) {
+    for (int a = a_first; a < N; a += stride) {
       const double wa = w ? w[a] : 1.0;
       const double y0 = (double)x[3 * a] - c0, y1 = (double)x[3 * a + 1] - c1, y2 = (double)x[3 * a + 2] - c2;
       const double r0 = rp[3 * a], r1 = rp[3 * a + 1], r2 = rp[3 * a + 2];
@@ -418,8 +477,8 @@ __global__ void __launch_bounds__(kOneBlockThreads) k_make_ref(FrameSrc<T> src, 
       v[6] += wa * y2 * r0; v[7] += wa * y2 * r1; v[8] += wa * y2 * r2;
       v[9] += wa * (y0 * y0 + y1 * y1 + y2 * y2 + r0 * r0 + r1 * r1 + r2 * r2);
     }
-    block_sum_f64<10>(v, red);
-    if (threadIdx.x == 0) {
+    cluster_sum_f64<10>(v, red, slots, bc);
+    if (threadIdx.x == 0) {  // the same totals in every CTA give the same rotation
       double R[9];
       qcp_lambda_rot(v, 0.5 * v[9], R);
       for (int q = 0; q < 9; ++q) Rs[q] = R[q];
@@ -427,15 +486,15 @@ __global__ void __launch_bounds__(kOneBlockThreads) k_make_ref(FrameSrc<T> src, 
     __syncthreads();
   }
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
-  float mx = 0.0f;
-  for (int a = threadIdx.x; a < N; a += blockDim.x) {
+  double mx = 0.0;
+  for (int a = a_first; a < N; a += stride) {
     const double wa = w ? w[a] : 1.0;
     const double y0 = (double)x[3 * a] - c0, y1 = (double)x[3 * a + 1] - c1, y2 = (double)x[3 * a + 2] - c2;
     double r[3];
     r[0] = Rs[0] * y0 + Rs[1] * y1 + Rs[2] * y2;
     r[1] = Rs[3] * y0 + Rs[4] * y1 + Rs[5] * y2;
     r[2] = Rs[6] * y0 + Rs[7] * y1 + Rs[8] * y2;
-    const double sw = sqrt(wa);
+    const double sw = w ? sqw[a] : 1.0;
     for (int p = 0; p < 3; ++p) {
       rk[3 * a + p] = r[p];
       swr[((size_t)k * N + a) * 3 + p] = (float)(sw * r[p]);
@@ -445,20 +504,16 @@ __global__ void __launch_bounds__(kOneBlockThreads) k_make_ref(FrameSrc<T> src, 
     }
     const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
     acc[0] += wa * r2;
-    mx = fmaxf(mx, (float)sqrt(r2));
+    mx = fmax(mx, r2);
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if ((threadIdx.x & 31) == 0) smx[threadIdx.x >> 5] = mx;
-  block_sum_f64<4>(acc, red);
-  if (threadIdx.x == 0) {
-    float m = 0.0f;
-    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) m = fmaxf(m, smx[q]);
+  cluster_sum_f64<4>(acc, red, slots, bc);
+  mx = cluster_max_f64(mx, red, slots, bc);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
     Eref[k] = acc[0];
     sr[3 * k] = acc[1];
     sr[3 * k + 1] = acc[2];
     sr[3 * k + 2] = acc[3];
-    rmax[k] = m;
+    rmax[k] = (float)sqrt(mx);
   }
 }
 
@@ -753,18 +808,18 @@ __global__ void __launch_bounds__(128) k_sample_sum(FrameSrc<T> src, int64_t F, 
 // rmax[k] only grows (atomicMax on the non-negative float bits), so it stays
 // an upper bound of |r_k|.  Eref and sr describe the unrefined references
 // and are not read after this point.
-__global__ void __launch_bounds__(128) k_ref_update(double* refs, float* swr, float2* refhl, float* rmax,
-                                                    const float* partial, const int* offsets, int64_t F,
-                                                    const double* w, int N, int Np) {
-  __shared__ float smx[4];
+__global__ void __launch_bounds__(32) k_ref_update(double* refs, float* swr, float2* refhl, float* rmax,
+                                                   const float* partial, const int* offsets, int64_t F,
+                                                   const double* sqw, int N, int Np) {
+  // one warp per block: the FP64 sums of the kMeanChunks partial means are
+  // spread over as many SMs as there are 32-atom groups
   const int k = blockIdx.y;
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t cnt = std::min<int64_t>((offsets ? (int64_t)(offsets[k + 1] - offsets[k]) : F), (int64_t)kSample);
   float mx = 0.0f;
   if (a < N) {
     double* r = refs + (size_t)k * 3 * N;
-    const double wa = w ? w[a] : 1.0;
-    const double sw = sqrt(wa);
+    const double sw = sqw ? sqw[a] : 1.0;
     double rr[3];
     for (int p = 0; p < 3; ++p) {
       double sum = 0.0;
@@ -780,12 +835,7 @@ __global__ void __launch_bounds__(128) k_ref_update(double* refs, float* swr, fl
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if ((threadIdx.x & 31) == 0) smx[threadIdx.x >> 5] = mx;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const float m = fmaxf(fmaxf(smx[0], smx[1]), fmaxf(smx[2], smx[3]));
-    atomicMax(reinterpret_cast<int*>(rmax + k), __float_as_int(m));
-  }
+  if (threadIdx.x == 0) atomicMax(reinterpret_cast<int*>(rmax + k), __float_as_int(mx));
 }
 
 struct BuildArgs {
@@ -928,15 +978,17 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
 // Reference-pair table (kRefPairStride floats per b*K + a): the exact FP64
 // rotation U_ab taking r_b onto r_a, SU_ab = U_ab S_ba, its antisymmetric
 // combos and sum w |r_a - U_ab r_b|^2.  No-fit mode keeps U = I.
-__global__ void __launch_bounds__(kOneBlockThreads) k_ref_terms(const double* refs, int N, int K, const double* w,
-                                                            int nofit, float* RP) {
-  __shared__ double red[32 * 10];
+__global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockThreads)
+    k_ref_terms(const double* refs, int N, int K, const double* w, int nofit, float* RP) {
+  __shared__ double red[32 * 10], slots[kRefCluster * 10], bc[10];
   __shared__ double Us[9];
-  const int b = blockIdx.x / K, a = blockIdx.x % K;
+  const int pair = blockIdx.x / kRefCluster;  // one cluster per reference pair
+  const int b = pair / K, a = pair % K;
+  const int i_first = (blockIdx.x % kRefCluster) * blockDim.x + threadIdx.x, stride = kRefCluster * blockDim.x;
   const double* rb = refs + (size_t)b * 3 * N;
   const double* ra = refs + (size_t)a * 3 * N;
   double v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+  for (int i = i_first; i < N; i += stride) {
     const double wa = w ? w[i] : 1.0;
     const double b0 = rb[3 * i], b1 = rb[3 * i + 1], b2 = rb[3 * i + 2];
     const double a0 = ra[3 * i], a1 = ra[3 * i + 1], a2 = ra[3 * i + 2];
@@ -945,8 +997,8 @@ __global__ void __launch_bounds__(kOneBlockThreads) k_ref_terms(const double* re
     v[6] += wa * b2 * a0; v[7] += wa * b2 * a1; v[8] += wa * b2 * a2;
     v[9] += wa * (b0 * b0 + b1 * b1 + b2 * b2 + a0 * a0 + a1 * a1 + a2 * a2);
   }
-  block_sum_f64<10>(v, red);
-  if (threadIdx.x == 0) {
+  cluster_sum_f64<10>(v, red, slots, bc);
+  if (threadIdx.x == 0) {  // the same totals in every CTA give the same rotation
     double U[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     if (a != b && !nofit) qcp_lambda_rot(v, 0.5 * v[9], U);
     for (int k = 0; k < 9; ++k) Us[k] = U[k];
@@ -954,7 +1006,7 @@ __global__ void __launch_bounds__(kOneBlockThreads) k_ref_terms(const double* re
   __syncthreads();
   // SS_ab = sum w |r_a - U r_b|^2, accumulated directly (no cancellation).
   double e[1] = {0.0};
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+  for (int i = i_first; i < N; i += stride) {
     const double wa = w ? w[i] : 1.0;
     const double b0 = rb[3 * i], b1 = rb[3 * i + 1], b2 = rb[3 * i + 2];
     const double d0 = ra[3 * i] - (Us[0] * b0 + Us[1] * b1 + Us[2] * b2);
@@ -962,13 +1014,13 @@ __global__ void __launch_bounds__(kOneBlockThreads) k_ref_terms(const double* re
     const double d2 = ra[3 * i + 2] - (Us[6] * b0 + Us[7] * b1 + Us[8] * b2);
     e[0] += wa * (d0 * d0 + d1 * d1 + d2 * d2);
   }
-  block_sum_f64<1>(e, red);
-  if (threadIdx.x == 0) {
+  cluster_sum_f64<1>(e, red, slots, bc);
+  if (blockIdx.x % kRefCluster == 0 && threadIdx.x == 0) {
     double SU[9];
     for (int p = 0; p < 3; ++p)
       for (int q = 0; q < 3; ++q)
         SU[p * 3 + q] = Us[p * 3] * v[q] + Us[p * 3 + 1] * v[3 + q] + Us[p * 3 + 2] * v[6 + q];
-    float* o = RP + (size_t)blockIdx.x * kRefPairStride;
+    float* o = RP + (size_t)pair * kRefPairStride;
     for (int k = 0; k < 9; ++k) o[k] = (float)Us[k];
     for (int k = 0; k < 9; ++k) o[9 + k] = (float)SU[k];
     o[18] = (float)(SU[5] - SU[7]);
@@ -1013,8 +1065,8 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
   }
   const PrepScratch S = prep_carve(A.scratch, F, N, A.max_refs);
   const bool ref_distinct = A.cmass_ref != nullptr && A.cmass_ref != A.w;
-  k_weights<<<1, kOneBlockThreads, 0, st>>>(A.w, ref_distinct ? A.cmass_ref : nullptr, N, A.sqw, A.sqwf, S.wf,
-                                        S.wfl, S.cmf_ref, S.cmfl_ref, S.scal);
+  k_weights<<<kRefCluster, kOneBlockThreads, 0, st>>>(A.w, ref_distinct ? A.cmass_ref : nullptr, N, A.sqw, A.sqwf,
+                                                      S.wf, S.wfl, S.cmf_ref, S.cmfl_ref, S.scal);
   ++launches;
   ScanArgs sa{};
   sa.cm_tgt = A.w ? S.wf : nullptr;
@@ -1036,8 +1088,9 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
   // chunk when the frames are still arriving).
   cudaMemsetAsync(A.fsel, 0, sizeof(int64_t), st);
   if (A.n_chunks > 0) cudaStreamWaitEvent(st, A.chunk_ev[0], 0);
-  k_make_ref<T><<<1, kOneBlockThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w, A.assign, 0, 0,
-                                            A.nofit, A.refs, A.swr, S.refhl, A.Eref, S.sr, S.rmax);
+  k_make_ref<T><<<kRefCluster, kOneBlockThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w, A.sqw,
+                                                          A.assign, 0, 0, A.nofit, A.refs, A.swr, S.refhl, A.Eref,
+                                                          S.sr, S.rmax);
   sa.k = 0;
   sa.swr = A.swr;
   sa.sr = S.sr;
@@ -1069,8 +1122,9 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return e;
     if (!(dmax > A.tau)) break;
-    k_make_ref<T><<<1, kOneBlockThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w, A.assign, K, 1,
-                                              A.nofit, A.refs, A.swr, S.refhl, A.Eref, S.sr, S.rmax);
+    k_make_ref<T><<<kRefCluster, kOneBlockThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w,
+                                                            A.sqw, A.assign, K, 1, A.nofit, A.refs, A.swr, S.refhl,
+                                                            A.Eref, S.sr, S.rmax);
     sa.k = K;
     sa.swr = A.swr + (size_t)K * 3 * N;
     sa.sr = S.sr + 3 * K;
@@ -1111,8 +1165,8 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
   }
   dim3 gs((unsigned)((A.Np + 127) / 128), (unsigned)kMeanChunks, (unsigned)K);
   k_sample_sum<T><<<gs, 128, 0, st>>>(src, F, A.Np, S.ftab, order, offsets, S.refhl, A.partial);
-  k_ref_update<<<dim3((unsigned)((N + 127) / 128), (unsigned)K), 128, 0, st>>>(A.refs, A.swr, S.refhl, S.rmax,
-                                                                             A.partial, offsets, F, A.w, N, A.Np);
+  k_ref_update<<<dim3((unsigned)((N + 31) / 32), (unsigned)K), 32, 0, st>>>(
+      A.refs, A.swr, S.refhl, S.rmax, A.partial, offsets, F, A.w ? A.sqw : nullptr, N, A.Np);
   launches += 2;
   o.launches = launches;
   return cudaGetLastError();
@@ -1150,7 +1204,7 @@ static cudaError_t finish_impl(const FinishArgs& fa, cudaStream_t st) {
   b.pos = fa.sorted ? S.pos : nullptr;
   b.assign_pos = S.assign_pos;
   k_build<T><<<prep_grid(A.F, kBuildBlocksPerSM), kPrepThreads, 0, st>>>(src, A.F, b);
-  k_ref_terms<<<fa.K * fa.K, kOneBlockThreads, 0, st>>>(A.refs, A.N, fa.K, A.w, A.nofit, fa.RP);
+  k_ref_terms<<<fa.K * fa.K * kRefCluster, kOneBlockThreads, 0, st>>>(A.refs, A.N, fa.K, A.w, A.nofit, fa.RP);
   return cudaGetLastError();
 }
 

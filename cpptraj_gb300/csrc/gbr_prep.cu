@@ -126,7 +126,7 @@ static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 size_t prep_scratch_bytes(int64_t F, int N, int Kmax) {
   size_t b = 0;
   b += align256(sizeof(float) * N) * 4;
-  b += align256(sizeof(double) * 4);
+  b += align256(sizeof(double) * 8);
   b += align256(sizeof(float2) * (size_t)Kmax * 3 * N);
   b += align256(sizeof(double) * 3 * Kmax);
   b += align256(sizeof(float) * Kmax);
@@ -149,7 +149,7 @@ PrepScratch prep_carve(void* base, int64_t F, int N, int Kmax) {
   s.wfl = (float*)take(sizeof(float) * N);
   s.cmf_ref = (float*)take(sizeof(float) * N);
   s.cmfl_ref = (float*)take(sizeof(float) * N);
-  s.scal = (double*)take(sizeof(double) * 4);
+  s.scal = (double*)take(sizeof(double) * 8);
   s.refhl = (float2*)take(sizeof(float2) * (size_t)Kmax * 3 * N);
   s.sr = (double*)take(sizeof(double) * 3 * Kmax);
   s.rmax = (float*)take(sizeof(float) * Kmax);
@@ -348,7 +348,9 @@ __device__ __forceinline__ float dot2_row(const float* Rh, const float* Rl, floa
 }
 
 // Weights in the forms the passes read; scal = {max sqrt(w), sum w, sum of
-// the reference centring masses}.  One cluster of kRefCluster CTAs.
+// the reference centring masses, 0, 1 / sum w, 1 / sum of the reference
+// centring masses} (a reciprocal is 0 when its sum is 0).  One cluster of
+// kRefCluster CTAs.
 __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockThreads)
     k_weights(const double* w, const double* cmass_ref, int N, double* sqw, float* sqwf, float* wf, float* wfl,
               float* cmf_ref, float* cmfl_ref, double* scal) {
@@ -381,6 +383,8 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
     scal[1] = v[0];
     scal[2] = v[1];
     scal[3] = 0.0;
+    scal[4] = (v[0] != 0.0) ? 1.0 / v[0] : 0.0;
+    scal[5] = (v[1] != 0.0) ? 1.0 / v[1] : 0.0;
   }
 }
 
@@ -524,7 +528,7 @@ struct ScanArgs {
   const float* cml_tgt;
   const float* wf;      // fit weights (FP32) or nullptr; read only when they differ from cm_ref
   int cm_ref_is_w;      // reference frames centre with the fit weights
-  const double* scal;   // [1] sum w (or N), [2] sum of reference centring masses
+  const double* scal;   // k_weights' scal: [1] sum w, [2] sum of reference centring masses, [4], [5] reciprocals
   const float* sqwf;    // sqrt(w) or nullptr
   const float* swr;     // sqrt(w) r_k, [N][3]
   const double* sr;     // sum w r_k, [3]
@@ -645,42 +649,50 @@ __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) umax = fmaxf(umax, __shfl_xor_sync(0xffffffffu, umax, o));
     if (lane == 0) {
-      double d2 = 0.0;
+      // Per-frame tail, one lane.  Only the centre needs FP64 (it feeds the
+      // exact superposition of the later passes); the distance to the
+      // reference, E0 and the QCP input only choose the nearest reference and
+      // start the FP32 QCP, so they stay in FP32 -- a warp-wide FP64
+      // instruction costs the whole warp's turn on GB300's narrow FP64 pipe.
+      float d2 = 0.0f;
       float q[4] = {1.0f, 0.0f, 0.0f, 0.0f};
+      const float Wf = (float)s.Wsum, iWf = (float)(1.0 / s.Wsum);
       if (!fit) {
-        d2 = (double)v[9] / s.Wsum;
+        d2 = v[9] * iWf;
         if (FIRST) {
           s.cen[3 * f] = s.cen[3 * f + 1] = s.cen[3 * f + 2] = 0.0;
-          s.ymax[f] = sqrtf(umax) * (1.0f + 1e-6f);
+          s.ymax[f] = sqrtf(umax) * (1.0f + 2e-6f);
         }
       } else {
-        double del[3] = {0.0, 0.0, 0.0};
+        float del[3] = {0.0f, 0.0f, 0.0f};
         if (FIRST) {
-          const double Wc = (in_ref && !s.cm_ref_is_w) ? s.scal[2] : s.scal[1];
+          const double iWc = (in_ref && !s.cm_ref_is_w) ? s.scal[5] : s.scal[4];
           for (int p = 0; p < 3; ++p) {
             const double xo = (p == 0) ? o0 : (p == 1) ? o1 : o2;
-            const double sum = (double)v[10 + p] + (double)ce[p];
-            del[p] = (Wc != 0.0) ? sum / Wc : -xo;  // zero mass: centre at the origin
-            s.cen[3 * f + p] = xo + del[p];
+            const double dd = (iWc != 0.0) ? ((double)v[10 + p] + (double)ce[p]) * iWc : -xo;  // zero mass: origin
+            s.cen[3 * f + p] = xo + dd;
+            del[p] = (float)dd;
           }
-          s.ymax[f] = (float)((sqrt((double)umax) + sqrt(del[0] * del[0] + del[1] * del[1] + del[2] * del[2])) *
-                              (1.0 + 1e-6));
+          s.ymax[f] = (sqrtf(umax) + sqrtf(del[0] * del[0] + del[1] * del[1] + del[2] * del[2])) * (1.0f + 2e-6f);
         }
-        double su[3];
-        for (int p = 0; p < 3; ++p) su[p] = same_w ? (double)v[10 + p] + (double)ce[p] : (double)v[13 + p];
+        float su[3], sr[3];
+        for (int p = 0; p < 3; ++p) {
+          su[p] = same_w ? v[10 + p] + ce[p] : v[13 + p];
+          sr[p] = (float)s.sr[p];
+        }
         float M[9];
         for (int i = 0; i < 3; ++i)
-          for (int j = 0; j < 3; ++j) M[3 * i + j] = (float)((double)v[3 * i + j] - del[i] * s.sr[j]);
-        const double Ey = (double)v[9] - 2.0 * (del[0] * su[0] + del[1] * su[1] + del[2] * su[2]) +
-                          s.Wsum * (del[0] * del[0] + del[1] * del[1] + del[2] * del[2]);
-        const double E0 = 0.5 * (Ey + *s.Eref);
-        if (E0 > 0.0) {
+          for (int j = 0; j < 3; ++j) M[3 * i + j] = fmaf(-del[i], sr[j], v[3 * i + j]);
+        const float Ey = v[9] - 2.0f * (del[0] * su[0] + del[1] * su[1] + del[2] * su[2]) +
+                         Wf * (del[0] * del[0] + del[1] * del[1] + del[2] * del[2]);
+        const float E0 = 0.5f * (Ey + (float)*s.Eref);
+        if (E0 > 0.0f) {
           float lr = 1.0f;
-          qcp_vec_f32(M, (float)E0, q, &lr);
-          d2 = 2.0 * E0 * (1.0 - (double)lr) / s.Wsum;
+          qcp_vec_f32(M, E0, q, &lr);
+          d2 = 2.0f * E0 * (1.0f - lr) * iWf;
         }
       }
-      const float d = (float)sqrt(fmax(d2, 0.0));
+      const float d = sqrtf(fmaxf(d2, 0.0f));
       if (s.k == 0 || d < s.dist[f]) {
         s.dist[f] = d;
         s.assign[f] = s.k;

@@ -198,6 +198,7 @@ cudaError_t enqueue_prob(gbr_handle* h, Prob& p, int mode, bool host_in, bool ho
     terms.RP = p.RP;
     terms.K = 1;
     terms.W = (float)p.W;
+    terms.two_over_w = (float)(2.0 / (double)p.W);
     terms.tol = (float)h->tol;
     terms.gem_s = tc ? 6.0e-7f : 1.2e-7f;
     terms.gem_c = tc ? 1.2e-8f * (float)p.N : 1.2e-7f * std::sqrt((float)p.N);

@@ -405,6 +405,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     terms.RP = (float*)P[17];
     terms.K = K;
     terms.W = (float)Wsum;
+    terms.two_over_w = (float)(2.0 / (double)Wsum);
     terms.tol = (float)h->tol;
     // FP32 FMA accumulation: 3-sigma random walk of half-ulp roundings (x2
     // margin), ~1.2e-7 sqrt(N) |tr D|.  Tensor memory: the FP16 hi+lo split
@@ -729,6 +730,7 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   terms.RP = (float*)P[19];
   terms.K = 1;
   terms.W = (float)Wsum;
+  terms.two_over_w = (float)(2.0 / (double)Wsum);
   terms.tol = (float)h->tol;
   terms.gem_s = 1.2e-7f;
   terms.gem_c = 1.2e-7f * std::sqrt((float)N);

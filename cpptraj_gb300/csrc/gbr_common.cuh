@@ -189,6 +189,7 @@ struct FrameTerms {
   const float* RP;    // [K][K][kRefPairStride]
   int K;
   float W;            // total weight
+  float two_over_w;   // 2 / W
   float tol;          // per-pair tolerance (Angstrom)
   // A-priori bound of the contraction error in tr D (see pair_epilogue):
   //   gem_s * sqrt(n_i n_j) + gem_c * |tr D|
@@ -211,7 +212,9 @@ __device__ __forceinline__ float solve_sym3(float a00, float a01, float a02, flo
   const float c12 = a01 * a02 - a00 * a12;
   const float c22 = a00 * a11 - a01 * a01;
   const float det = a00 * c00 + a01 * c01 + a02 * c02;
-  const float id = 1.0f / det;
+  // Approximate reciprocal (2 ulp): the solve only produces the trial vector
+  // of a Rayleigh quotient, whose value is second order in the vector's error.
+  const float id = __fdividef(1.0f, det);
   x0 = (c00 * b0 + c01 * b1 + c02 * b2) * id;
   x1 = (c01 * b0 + c11 * b1 + c12 * b2) * id;
   x2 = (c02 * b0 + c12 * b1 + c22 * b2) * id;
@@ -371,7 +374,7 @@ static __device__ __noinline__ float pair_solve(const F9 Dv, float ni, float nj,
   const float gem = t.gem_s * sqrtf(fmaxf(ni, 0.0f) * fmaxf(nj, 0.0f)) + t.gem_c * fabsf(D[0] + D[4] + D[8]);
   if (t.nofit) {
     // RMSD_NoFit: sum w |x_i - x_j|^2 / W = 2*G00/W (references are not rotated).
-    const float r = sqrtf(fmaxf(2.0f * G00 / W, 0.0f));
+    const float r = sqrtf(fmaxf(G00 * t.two_over_w, 0.0f));
     const float err = 2.0f * gem + t.epi_coef * g00mag;
     *flag = !(err <= t.tol * W * fmaxf(r, 1e-3f));
     return r;
@@ -414,11 +417,12 @@ static __device__ __noinline__ float pair_solve(const F9 Dv, float ni, float nj,
   const float t00 = q0 * q0 * G00, t01 = 2.f * q0 * (q1 * g1 + q2 * g2 + q3 * g3);
   const float t11 = q1 * q1 * G11 + q2 * q2 * G22 + q3 * q3 * G33;
   const float t12 = 2.f * (q1 * q2 * G12 + q1 * q3 * G13 + q2 * q3 * G23);
-  const float rq = (t00 + t01 + t11 + t12) / qq;
+  const float iqq = __fdividef(1.0f, qq);  // qq in [1, 2) on the fast path
+  const float rq = (t00 + t01 + t11 + t12) * iqq;
   const float mag = (q0 * q0 * g00mag + 2.f * fabsf(q0) * (fabsf(q1 * g1) + fabsf(q2 * g2) + fabsf(q3 * g3)) +
-                     fabsf(t11) + 2.f * (fabsf(q1 * q2 * G12) + fabsf(q1 * q3 * G13) + fabsf(q2 * q3 * G23))) /
-                    qq;
-  const float r = sqrtf(fmaxf(2.0f * rq / W, 0.0f));
+                     fabsf(t11) + 2.f * (fabsf(q1 * q2 * G12) + fabsf(q1 * q3 * G13) + fabsf(q2 * q3 * G23))) *
+                    iqq;
+  const float r = sqrtf(fmaxf(rq * t.two_over_w, 0.0f));
   const float err = t.epi_coef * mag + 2.0f * gem;
   *flag = !(err <= t.tol * W * fmaxf(r, 1e-3f));
   if (qout) {

@@ -21,8 +21,9 @@ namespace gbr {
 
 namespace {
 
-// B := B + B^T for a square n x n matrix (in place), 32 x 32 tile pairs.
-__global__ void k_symmetrize(float* B, int64_t n) {
+// B := B + B^T for a square n x n matrix with row stride ld (in place), 32 x
+// 32 tile pairs.
+__global__ void k_symmetrize(float* B, int64_t n, int64_t ld) {
   __shared__ float t1[32][33], t2[32][33];
   const int64_t tiles = (n + 31) / 32;
   // blockIdx.x enumerates tile pairs (ti <= tj)
@@ -37,30 +38,34 @@ __global__ void k_symmetrize(float* B, int64_t n) {
   for (int y = y0; y < 32; y += 8) {
     const int64_t r1 = ti * 32 + y, c1 = tj * 32 + x;
     const int64_t r2 = tj * 32 + y, c2 = ti * 32 + x;
-    t1[y][x] = (r1 < n && c1 < n) ? B[r1 * n + c1] : 0.f;
-    t2[y][x] = (r2 < n && c2 < n) ? B[r2 * n + c2] : 0.f;
+    t1[y][x] = (r1 < n && c1 < n) ? B[r1 * ld + c1] : 0.f;
+    t2[y][x] = (r2 < n && c2 < n) ? B[r2 * ld + c2] : 0.f;
   }
   __syncthreads();
   for (int y = y0; y < 32; y += 8) {
     const int64_t r1 = ti * 32 + y, c1 = tj * 32 + x;
     const int64_t r2 = tj * 32 + y, c2 = ti * 32 + x;
     if (ti == tj) {
-      if (r1 < n && c1 < n) B[r1 * n + c1] = t1[y][x] + t1[x][y];
+      if (r1 < n && c1 < n) B[r1 * ld + c1] = t1[y][x] + t1[x][y];
     } else {
-      if (r1 < n && c1 < n) B[r1 * n + c1] = t1[y][x] + t2[x][y];
-      if (r2 < n && c2 < n) B[r2 * n + c2] = t2[y][x] + t1[x][y];
+      if (r1 < n && c1 < n) B[r1 * ld + c1] = t1[y][x] + t2[x][y];
+      if (r2 < n && c2 < n) B[r2 * ld + c2] = t2[y][x] + t1[x][y];
     }
   }
 }
 
-// C[M x N] = A[M x K] * Bm[K x N], FP32, row-major.  128 x 128 tiles, 8-deep
-// K slabs, 256 threads with 8 x 8 outputs each.
-constexpr int GM = 128, GN = 128, GK = 8;
+// C[M x N] = A[M x K] * Bm[K x N], FP32, row-major, on the CUDA cores.
+// 128 x 128 output tiles, 256 threads with 8 x 8 outputs each, 16-deep K
+// slabs in shared memory, double-buffered: the next slab's 16-byte global
+// loads are in flight in registers while the current slab is multiplied.
+// Requires lda, ldb, ldc multiples of 4 (16-byte rows) and columns K..lda of
+// A zero, so a 4-wide load that starts below K stays in its row.
+constexpr int GM = 128, GN = 128, GK = 16;
 __global__ void __launch_bounds__(256) k_sgemm(int64_t M, int64_t N, int64_t K, const float* __restrict__ A,
                                                int64_t lda, const float* __restrict__ Bm, int64_t ldb,
                                                float* __restrict__ C, int64_t ldc) {
-  __shared__ __align__(16) float As[GK][GM + 4];
-  __shared__ __align__(16) float Bs[GK][GN + 4];
+  __shared__ __align__(16) float As[2][GK][GM + 4];
+  __shared__ __align__(16) float Bs[2][GK][GN + 4];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int64_t m0 = (int64_t)blockIdx.y * GM, n0 = (int64_t)blockIdx.x * GN;
   float acc[8][8];
@@ -68,28 +73,44 @@ __global__ void __launch_bounds__(256) k_sgemm(int64_t M, int64_t N, int64_t K, 
   for (int i = 0; i < 8; ++i)
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-  const int ar = tid >> 1, ac = (tid & 1) * 4;   // A tile: 128 rows x 8 cols
-  const int br = tid >> 5, bc = (tid & 31) * 4;  // B tile: 8 rows x 128 cols
-  for (int64_t k0 = 0; k0 < K; k0 += GK) {
-    float av[4], bv[4];
+  // A slab: 128 rows x 16 k = 512 float4, two per thread (rows ar, ar + 64; k columns ak..ak+3)
+  const int ar = tid >> 2, ak = (tid & 3) * 4;
+  // B slab: 16 rows x 128 columns = 512 float4, two per thread (rows br, br + 8; columns bc..bc+3)
+  const int br = tid >> 5, bc = (tid & 31) * 4;
+  float4 ra[2], rb[2];
+  auto fetch = [&](int64_t k0) {
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int64_t r = m0 + ar, c = k0 + ac + u;
-      av[u] = (r < M && c < K) ? A[r * lda + c] : 0.f;
-      const int64_t rb = k0 + br, cb = n0 + bc + u;
-      bv[u] = (rb < K && cb < N) ? Bm[rb * ldb + cb] : 0.f;
+    for (int h = 0; h < 2; ++h) {
+      const int64_t r = m0 + ar + 64 * h, c = k0 + ak;
+      ra[h] = (r < M && c < K) ? *reinterpret_cast<const float4*>(A + r * lda + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+      const int64_t kb = k0 + br + 8 * h, cb = n0 + bc;
+      rb[h] = (kb < K && cb < N) ? *reinterpret_cast<const float4*>(Bm + kb * ldb + cb) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    __syncthreads();
+  };
+  auto stash = [&](int buf) {
 #pragma unroll
-    for (int u = 0; u < 4; ++u) As[ac + u][ar] = av[u];
-    *reinterpret_cast<float4*>(&Bs[br][bc]) = make_float4(bv[0], bv[1], bv[2], bv[3]);
-    __syncthreads();
+    for (int h = 0; h < 2; ++h) {
+      const int m = ar + 64 * h;
+      As[buf][ak][m] = ra[h].x;
+      As[buf][ak + 1][m] = ra[h].y;
+      As[buf][ak + 2][m] = ra[h].z;
+      As[buf][ak + 3][m] = ra[h].w;
+      *reinterpret_cast<float4*>(&Bs[buf][br + 8 * h][bc]) = rb[h];
+    }
+  };
+  fetch(0);
+  stash(0);
+  __syncthreads();
+  int buf = 0;
+  for (int64_t k0 = 0; k0 < K; k0 += GK) {
+    const bool more = k0 + GK < K;
+    if (more) fetch(k0 + GK);
 #pragma unroll
     for (int k = 0; k < GK; ++k) {
-      const float4 a0 = *reinterpret_cast<const float4*>(&As[k][ty * 4]);
-      const float4 a1 = *reinterpret_cast<const float4*>(&As[k][64 + ty * 4]);
-      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[k][tx * 4]);
-      const float4 b1 = *reinterpret_cast<const float4*>(&Bs[k][64 + tx * 4]);
+      const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][k][ty * 4]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&As[buf][k][64 + ty * 4]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[buf][k][tx * 4]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&Bs[buf][k][64 + tx * 4]);
       const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
       const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
@@ -97,15 +118,22 @@ __global__ void __launch_bounds__(256) k_sgemm(int64_t M, int64_t N, int64_t K, 
 #pragma unroll
         for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
     }
+    if (more) {
+      stash(buf ^ 1);  // the other buffer was last read before the previous barrier
+      __syncthreads();
+      buf ^= 1;
+    }
   }
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const int64_t r = m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
     if (r >= M) continue;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int64_t c = n0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
-      if (c < N) C[r * ldc + c] = acc[i][j];
+    for (int h = 0; h < 2; ++h) {
+      const int64_t c = n0 + h * 64 + tx * 4;
+      if (c < N)
+        *reinterpret_cast<float4*>(C + r * ldc + c) =
+            make_float4(acc[i][4 * h], acc[i][4 * h + 1], acc[i][4 * h + 2], acc[i][4 * h + 3]);
     }
   }
 }
@@ -118,8 +146,9 @@ __global__ void __launch_bounds__(256) k_sgemm(int64_t M, int64_t N, int64_t K, 
 // RMSD.  One warp per frame: the first pass stores the unprojected values
 // and their sum, the second projects and rotates them.
 __global__ void __launch_bounds__(256) k_grad_final(int64_t F, int N, int Np, const float* E, const float* Cs,
-                                                    const double* rot, const double* r, const double* w, double W,
-                                                    const float* plane, const float* Z, float* grad) {
+                                                    const double* rot, const double* r, const double* w,
+                                                    const double* sqw, double iW, const float* plane, const float* Z,
+                                                    float* grad) {
   const int lane = threadIdx.x & 31;
   for (int64_t f = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; f < F;
        f += ((int64_t)gridDim.x * blockDim.x) >> 5) {
@@ -128,13 +157,13 @@ __global__ void __launch_bounds__(256) k_grad_final(int64_t F, int N, int Np, co
     double S[3] = {0.0, 0.0, 0.0};
     for (int a = lane; a < N; a += 32) {
       const double wa = w ? w[a] : 1.0;
-      const double sw = sqrt(wa);
+      const double sw = w ? sqw[a] : 1.0;
       const double r0 = r[3 * a], r1 = r[3 * a + 1], r2 = r[3 * a + 2];
 #pragma unroll
       for (int p = 0; p < 3; ++p) {
         const double er = (double)Ef[p * 3] * r0 + (double)Ef[p * 3 + 1] * r1 + (double)Ef[p * 3 + 2] * r2;
         const size_t row = (size_t)(3 * f + p);
-        const double gp = (wa * er + sw * (cf * (double)plane[row * Np + a] - (double)Z[row * Np + a])) / W;
+        const double gp = (wa * er + sw * (cf * (double)plane[row * Np + a] - (double)Z[row * Np + a])) * iW;
         S[p] += gp;
         grad[((size_t)f * N + a) * 3 + p] = (float)gp;
       }
@@ -150,7 +179,7 @@ __global__ void __launch_bounds__(256) k_grad_final(int64_t F, int N, int Np, co
       float* g = grad + ((size_t)f * N + a) * 3;
       double gp[3];
 #pragma unroll
-      for (int p = 0; p < 3; ++p) gp[p] = (double)g[p] - wa * S[p] / W;
+      for (int p = 0; p < 3; ++p) gp[p] = (double)g[p] - wa * S[p] * iW;
 #pragma unroll
       for (int q = 0; q < 3; ++q) g[q] = (float)(R[q] * gp[0] + R[3 + q] * gp[1] + R[6 + q] * gp[2]);
     }
@@ -161,11 +190,12 @@ __global__ void __launch_bounds__(256) k_grad_final(int64_t F, int N, int Np, co
 cudaError_t run_backward_tail(const BackwardTail& T, cudaStream_t st) {
   const int64_t n = 3 * T.F;
   const int64_t tiles = (n + 31) / 32;
-  k_symmetrize<<<(unsigned)(tiles * (tiles + 1) / 2), dim3(32, 8), 0, st>>>(T.B, n);
+  k_symmetrize<<<(unsigned)(tiles * (tiles + 1) / 2), dim3(32, 8), 0, st>>>(T.B, n, T.ldB);
   dim3 grid((unsigned)((T.Np + GN - 1) / GN), (unsigned)((n + GM - 1) / GM));
-  k_sgemm<<<grid, 256, 0, st>>>(n, T.Np, n, T.B, n, T.plane, T.Np, T.Z, T.Np);
+  k_sgemm<<<grid, 256, 0, st>>>(n, T.Np, n, T.B, T.ldB, T.plane, T.Np, T.Z, T.Np);
   const int g = (int)std::min<int64_t>((T.F + 7) / 8, 152 * 16);
-  k_grad_final<<<g, 256, 0, st>>>(T.F, T.N, T.Np, T.E, T.C, T.rot, T.ref0, T.w, T.W, T.plane, T.Z, T.grad);
+  k_grad_final<<<g, 256, 0, st>>>(T.F, T.N, T.Np, T.E, T.C, T.rot, T.ref0, T.w, T.sqw, 1.0 / T.W, T.plane, T.Z,
+                                  T.grad);
   return cudaGetLastError();
 }
 

@@ -632,6 +632,7 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   const bool g_dev = g ? is_device_ptr(g) : false;
   const bool r_dev = rmsd_out ? is_device_ptr(rmsd_out) : false;
   const int64_t npairs = F * (F - 1) / 2;
+  const int64_t ldB = (3 * F + 3) / 4 * 4;  // 16-byte rows for the GEMM's vector loads
   if (F < 2) {
     if (grad_dev) cudaMemsetAsync(grad_xyz, 0, sizeof(float) * 3 * N * F, st);
     else std::memset(grad_xyz, 0, sizeof(float) * 3 * N * F);
@@ -660,7 +661,7 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
     p[17] = A.take<float>(9 * (size_t)F);           // P
     p[18] = A.take<float>(F);                       // trP
     p[19] = A.take<float>(kRefPairStride);          // reference-pair table
-    p[20] = A.take<float>((size_t)9 * F * F);       // B
+    p[20] = A.take<float>((size_t)3 * F * ldB);     // B [3F][ldB]
     p[21] = A.take<float>(9 * (size_t)F);           // E
     p[22] = A.take<float>(F);                       // C
     p[23] = A.take<float>((size_t)3 * F * Np);      // Z
@@ -759,13 +760,13 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   if ((e = run_finish(fa, st)) != cudaSuccess) return h->cuda_fail(e, "finish");
   launches += 2;
   float* B = (float*)P[20];
-  cudaMemsetAsync(B, 0, sizeof(float) * 9 * F * F, st);
+  cudaMemsetAsync(B, 0, sizeof(float) * 3 * F * ldB, st);
   cudaMemsetAsync(P[21], 0, sizeof(float) * 9 * F, st);
   cudaMemsetAsync(P[22], 0, sizeof(float) * F, st);
   if (h->timing) cudaEventRecord(h->ev[1], st);
   PairLaunch L{};
   L.bwd.B = B;
-  L.bwd.ldB = 3 * F;
+  L.bwd.ldB = ldB;
   L.bwd.E = (float*)P[21];
   L.bwd.C = (float*)P[22];
   L.bwd.g = d_g;
@@ -791,6 +792,7 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   T.N = N;
   T.Np = Np;
   T.B = B;
+  T.ldB = ldB;
   T.plane = pa.plane;
   T.Z = (float*)P[23];
   T.E = (float*)P[21];
@@ -798,6 +800,7 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   T.rot = pa.rot;
   T.ref0 = pa.refs;
   T.w = d_w;
+  T.sqw = pa.sqw;
   T.W = Wsum;
   T.grad = d_grad;
   if ((e = run_backward_tail(T, st)) != cudaSuccess) return h->cuda_fail(e, "backward tail");

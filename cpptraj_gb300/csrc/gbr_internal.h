@@ -127,7 +127,7 @@ TileSpace make_tiles(const OutMap& m, int bm, int bn);
 // Backward-mode outputs of the FP32 pair kernel (nullptr B = forward mode).
 struct BwdArgs {
   float* B;          // [3F][3F], upper pair blocks c*T (row 3i+p, column 3j+q, i < j)
-  int64_t ldB;       // 3F
+  int64_t ldB;       // row stride of B: 3F rounded up to a multiple of 4
   float* E;          // [F][9] sum_h c_fh (I - T_fh)
   float* C;          // [F]    sum_h c_fh
   const float* g;    // TRI upstream weights (nullptr = 1)
@@ -180,7 +180,8 @@ int64_t tc_max_tiles(const OutMap& m);
 struct BackwardTail {
   int64_t F;
   int N, Np;
-  float* B;            // [3F][3F]
+  float* B;            // [3F][ldB], columns 3F..ldB zero
+  int64_t ldB;         // 3F rounded up to a multiple of 4
   const float* plane;  // [F][3][Np]  (= [3F][Np])
   float* Z;            // [3F][Np]
   const float* E;      // [F][9]
@@ -188,6 +189,7 @@ struct BackwardTail {
   const double* rot;   // [F][9] pre-alignment rotations
   const double* ref0;  // [N][3] the (single) pre-alignment reference
   const double* w;     // masses or nullptr
+  const double* sqw;   // sqrt of the masses (when w is given)
   double W;
   float* grad;         // [F][N][3]
 };

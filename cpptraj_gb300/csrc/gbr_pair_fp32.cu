@@ -179,43 +179,59 @@ __global__ void __launch_bounds__(THREADS, 1) k_pairs_fp32(PairLaunch L) {
     for (int k = tid; k < BN * 10; k += THREADS) (&Ecol[0][0])[k] = 0.f;
     __syncthreads();
     const BwdArgs& bw = L.bwd;
+    // The 32 lanes of a warp share the reference row il (64 consecutive
+    // threads per row): its E/C terms are summed across the warp before one
+    // shared-memory atomic per value; each lane's column jl is its own.
 #pragma unroll 1
     for (int r = 0; r < (BM * BN) / THREADS; ++r) {
       const int jl = tid & 63, il = (tid >> 6) + 4 * r;
       const int64_t i = i0 + il, j = jt0 + jl;
-      if (i >= i_end || j >= jt_end || !(j > i)) continue;
-      const int slot = il * BN + jl;
-      float D[9];
+      float er[10];
 #pragma unroll
-      for (int c = 0; c < 9; ++c) D[c] = Ds[slot * 9 + c];
-      bool flag = false;
-      float q[4];
-      const float rm = pair_epilogue(D, i, j, L.terms, &flag, q);
-      const int64_t t = tri_index(L.map.n_ref, i, j);
-      if (bw.rmsd) bw.rmsd[t] = rm;
-      const float gij = bw.g ? bw.g[t] : 1.0f;
-      const float c = (rm > 1e-6f) ? gij / rm : 0.0f;
-      const float a = q[0], x = q[1], y = q[2], z = q[3];
-      // QCP rotation R(q) (row-major); T = R^T.
-      const float R0 = a * a + x * x - y * y - z * z, R1 = 2.f * (x * y + a * z), R2 = 2.f * (z * x - a * y);
-      const float R3 = 2.f * (x * y - a * z), R4 = a * a - x * x + y * y - z * z, R5 = 2.f * (y * z + a * x);
-      const float R6 = 2.f * (z * x + a * y), R7 = 2.f * (y * z - a * x), R8 = a * a - x * x - y * y + z * z;
-      float* Bi = bw.B + (size_t)(3 * i) * bw.ldB + 3 * j;
-      Bi[0] = c * R0; Bi[1] = c * R3; Bi[2] = c * R6;
-      Bi += bw.ldB;
-      Bi[0] = c * R1; Bi[1] = c * R4; Bi[2] = c * R7;
-      Bi += bw.ldB;
-      Bi[0] = c * R2; Bi[1] = c * R5; Bi[2] = c * R8;
-      const float d00 = 2.f * (y * y + z * z), d11 = 2.f * (x * x + z * z), d22 = 2.f * (x * x + y * y);
-      // E_i += c (I - R^T);  E_j += c (I - R)
-      atomicAdd(&Erow[il][0], c * d00); atomicAdd(&Erow[il][1], -c * R3); atomicAdd(&Erow[il][2], -c * R6);
-      atomicAdd(&Erow[il][3], -c * R1); atomicAdd(&Erow[il][4], c * d11); atomicAdd(&Erow[il][5], -c * R7);
-      atomicAdd(&Erow[il][6], -c * R2); atomicAdd(&Erow[il][7], -c * R5); atomicAdd(&Erow[il][8], c * d22);
-      atomicAdd(&Erow[il][9], c);
-      atomicAdd(&Ecol[jl][0], c * d00); atomicAdd(&Ecol[jl][1], -c * R1); atomicAdd(&Ecol[jl][2], -c * R2);
-      atomicAdd(&Ecol[jl][3], -c * R3); atomicAdd(&Ecol[jl][4], c * d11); atomicAdd(&Ecol[jl][5], -c * R5);
-      atomicAdd(&Ecol[jl][6], -c * R6); atomicAdd(&Ecol[jl][7], -c * R7); atomicAdd(&Ecol[jl][8], c * d22);
-      atomicAdd(&Ecol[jl][9], c);
+      for (int k = 0; k < 10; ++k) er[k] = 0.f;
+      const bool live = i < i_end && j < jt_end && j > i;
+      if (live) {
+        const int slot = il * BN + jl;
+        float D[9];
+#pragma unroll
+        for (int c = 0; c < 9; ++c) D[c] = Ds[slot * 9 + c];
+        bool flag = false;
+        float q[4];
+        const float rm = pair_epilogue(D, i, j, L.terms, &flag, q);
+        const int64_t t = tri_index(L.map.n_ref, i, j);
+        if (bw.rmsd) bw.rmsd[t] = rm;
+        const float gij = bw.g ? bw.g[t] : 1.0f;
+        const float c = (rm > 1e-6f) ? gij / rm : 0.0f;
+        const float a = q[0], x = q[1], y = q[2], z = q[3];
+        // QCP rotation R(q) (row-major); T = R^T.
+        const float R0 = a * a + x * x - y * y - z * z, R1 = 2.f * (x * y + a * z), R2 = 2.f * (z * x - a * y);
+        const float R3 = 2.f * (x * y - a * z), R4 = a * a - x * x + y * y - z * z, R5 = 2.f * (y * z + a * x);
+        const float R6 = 2.f * (z * x + a * y), R7 = 2.f * (y * z - a * x), R8 = a * a - x * x - y * y + z * z;
+        float* Bi = bw.B + (size_t)(3 * i) * bw.ldB + 3 * j;
+        Bi[0] = c * R0; Bi[1] = c * R3; Bi[2] = c * R6;
+        Bi += bw.ldB;
+        Bi[0] = c * R1; Bi[1] = c * R4; Bi[2] = c * R7;
+        Bi += bw.ldB;
+        Bi[0] = c * R2; Bi[1] = c * R5; Bi[2] = c * R8;
+        const float d00 = 2.f * (y * y + z * z), d11 = 2.f * (x * x + z * z), d22 = 2.f * (x * x + y * y);
+        // E_i += c (I - R^T);  E_j += c (I - R)
+        er[0] = c * d00; er[1] = -c * R3; er[2] = -c * R6;
+        er[3] = -c * R1; er[4] = c * d11; er[5] = -c * R7;
+        er[6] = -c * R2; er[7] = -c * R5; er[8] = c * d22;
+        er[9] = c;
+        atomicAdd(&Ecol[jl][0], c * d00); atomicAdd(&Ecol[jl][1], -c * R1); atomicAdd(&Ecol[jl][2], -c * R2);
+        atomicAdd(&Ecol[jl][3], -c * R3); atomicAdd(&Ecol[jl][4], c * d11); atomicAdd(&Ecol[jl][5], -c * R5);
+        atomicAdd(&Ecol[jl][6], -c * R6); atomicAdd(&Ecol[jl][7], -c * R7); atomicAdd(&Ecol[jl][8], c * d22);
+        atomicAdd(&Ecol[jl][9], c);
+      }
+#pragma unroll
+      for (int k = 0; k < 10; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) er[k] += __shfl_xor_sync(0xffffffffu, er[k], o);
+      if ((tid & 31) == 0)
+#pragma unroll
+        for (int k = 0; k < 10; ++k)
+          if (er[k] != 0.f) atomicAdd(&Erow[il][k], er[k]);
     }
     __syncthreads();
     for (int k = tid; k < BM * 10; k += THREADS) {

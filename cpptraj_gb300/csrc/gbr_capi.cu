@@ -388,6 +388,31 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     if ((e = run_exact(ex, st)) != cudaSuccess) return h->cuda_fail(e, "exact kernel");
     ++launches;
   } else {
+    // The operand build, as run_finish does it; while chunked host input
+    // lands, prep runs it speculatively for one reference (K = 1, unsorted).
+    FinishArgs fa{};
+    fa.prep = &pa;
+    fa.plane = pa.plane;
+    fa.F = F;
+    fa.N = N;
+    fa.Np = Np;
+    fa.K = 1;
+    fa.mean = pa.mean;
+    fa.assign = pa.assign;
+    fa.swr = pa.swr;
+    fa.tc = tc;
+    fa.hi = P[23];
+    fa.lo = P[24];
+    fa.inv_scale = (float*)P[13];
+    fa.write_plane = !tc;
+    fa.nrm = (float*)P[14];
+    fa.P = (float*)P[15];
+    fa.trP = (float*)P[16];
+    fa.refs = pa.refs;
+    fa.w = d_w;
+    fa.nofit = nofit;
+    fa.RP = (float*)P[17];
+    if (n_chunks > 0) pa.spec_build = &fa;
     PrepOut po;
     if ((e = run_prep(pa, po, st)) != cudaSuccess) return h->cuda_fail(e, "prep");
     launches += po.launches;
@@ -416,31 +441,11 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     terms.gem_c = tc ? 1.2e-8f * (float)N : 1.2e-7f * std::sqrt((float)N);
     terms.epi_coef = 8e-7f;
     terms.nofit = nofit;
-    FinishArgs fa{};
-    fa.prep = &pa;
     fa.sorted = po.sorted;
-    fa.plane = pa.plane;
-    fa.F = F;
-    fa.N = N;
-    fa.Np = Np;
     fa.K = K;
-    fa.mean = pa.mean;
-    fa.assign = pa.assign;
-    fa.swr = pa.swr;
-    fa.tc = tc;
-    fa.hi = P[23];
-    fa.lo = P[24];
-    fa.inv_scale = (float*)P[13];
-    fa.write_plane = !tc;
-    fa.nrm = (float*)terms.nrm;
-    fa.P = (float*)terms.P;
-    fa.trP = (float*)terms.trP;
-    fa.refs = pa.refs;
-    fa.w = d_w;
-    fa.nofit = nofit;
-    fa.RP = (float*)terms.RP;
+    fa.built = po.built;
     if ((e = run_finish(fa, st)) != cudaSuccess) return h->cuda_fail(e, "finish");
-    launches += 2;
+    launches += po.built ? 1 : 2;
     // One launch of the pair kernel over the rows of map m.
     auto launch_pairs = [&](const OutMap& m, const FlagList& f) -> cudaError_t {
       if (tc) {

@@ -50,6 +50,9 @@ struct PrepArgs {
   int n_chunks;
   int64_t chunk_end[8];
   cudaEvent_t chunk_ev[8];
+  // With chunks: the operand build for one reference (K = 1, unsorted), run
+  // speculatively while the chunks land (PrepOut::built reports success).
+  const struct FinishArgs* spec_build;
 };
 
 // Further per-call prep buffers, carved from PrepArgs::scratch.
@@ -58,7 +61,7 @@ struct PrepScratch {
   float* wfl;      // [N] w - wf (the low part)
   float* cmf_ref;  // [N] centring masses of reference frames in FP32
   float* cmfl_ref; // [N] their low parts
-  double* scal;    // [4] max sqrt(w), sum w, sum of reference centring masses
+  double* scal;    // [8] max sqrt(w), sum w, sum of reference centring masses, 0, their reciprocals
   float2* refhl;   // [Kmax][N][3] references as hi + lo floats
   double* sr;      // [Kmax][3] sum_a w_a r_k,a
   float* rmax;     // [Kmax] max_a |r_k,a|
@@ -67,6 +70,7 @@ struct PrepScratch {
   float* ftab;     // [F][24] rotation hi/lo (9 + 9), R c hi/lo (3 + 3)
   int* pos;        // [F] frame -> position when frames are laid out sorted by reference
   int* assign_pos; // [F] reference of the frame at each position
+  float* swr0;     // [N][3] sqrt(w) r_0 before refinement (scans that run after a speculative refinement)
 };
 size_t prep_scratch_bytes(int64_t F, int N, int Kmax);
 PrepScratch prep_carve(void* base, int64_t F, int N, int Kmax);
@@ -94,6 +98,7 @@ struct FinishArgs {
   const double* w;
   int nofit;
   float* RP;
+  int built;          // the operands are built already (speculative prep): only the reference-pair terms
 };
 cudaError_t run_finish(const FinishArgs& A, cudaStream_t st);
 
@@ -101,6 +106,7 @@ struct PrepOut {
   int K = 1;
   int launches = 0;
   int sorted = 0;  // operands and per-frame terms are at sorted positions (PrepScratch::pos)
+  int built = 0;   // the operands were built during prep (one reference, chunked input)
 };
 
 cudaError_t run_prep(const PrepArgs& A, PrepOut& o, cudaStream_t st);

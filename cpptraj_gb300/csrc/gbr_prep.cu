@@ -134,6 +134,7 @@ size_t prep_scratch_bytes(int64_t F, int N, int Kmax) {
   b += align256(sizeof(float) * F);
   b += align256(sizeof(float) * kFtab * F);
   b += align256(sizeof(int) * F) * 2;
+  b += align256(sizeof(float) * 3 * N);
   return b;
 }
 
@@ -158,6 +159,7 @@ PrepScratch prep_carve(void* base, int64_t F, int N, int Kmax) {
   s.ftab = (float*)take(sizeof(float) * kFtab * F);
   s.pos = (int*)take(sizeof(int) * F);
   s.assign_pos = (int*)take(sizeof(int) * F);
+  s.swr0 = (float*)take(sizeof(float) * 3 * N);
   return s;
 }
 
@@ -735,8 +737,10 @@ __global__ void k_argmax(const float* dist, int64_t F, float* out_val, int64_t* 
 
 // One thread per frame: the exact (FP64-orthogonal) rotation of the frame's
 // quaternion, t = R c, and both split into FP32 hi + lo.  No-fit: R = I, t = 0.
-__global__ void k_rot(int64_t F, const float4* quat, const double* cen, int nofit, float* ftab, double* rot) {
-  for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < F; f += (int64_t)gridDim.x * blockDim.x) {
+__global__ void k_rot(int64_t f_begin, int64_t F, const float4* quat, const double* cen, int nofit, float* ftab,
+                      double* rot) {
+  for (int64_t f = f_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < F;
+       f += (int64_t)gridDim.x * blockDim.x) {
     double R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     if (!nofit) {
       const float4 q4 = quat[f];
@@ -880,11 +884,12 @@ struct BuildArgs {
 // below FP32 rounding), and continues with the value hi + lo represents.
 // n_f = sum |p|^2 and P_fc = sum p (sqrt(w) r_c)^T use those exact operands.
 template <typename T>
-__global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int64_t F, BuildArgs b) {
+__global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int64_t f_begin, int64_t F,
+                                                             BuildArgs b) {
   __shared__ __align__(16) float sbuf[kWarps][kPipe * kStage];
   const int N = src.N, Np = b.Np, lane = threadIdx.x & 31;
   const float sqwmax = (float)b.scal[0];
-  const int64_t f_first = blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5);
+  const int64_t f_first = f_begin + blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5);
   const int64_t f_stride = (int64_t)gridDim.x * kWarps;
   WarpPipe<T> pipe;
   pipe.init(src, f_first, F, f_stride, sbuf[threadIdx.x >> 5], lane);
@@ -1047,6 +1052,7 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
 // ---------------------------------------------------------------------------
 // Host driver for the prep passes.
 // ---------------------------------------------------------------------------
+static BuildArgs build_args(const FinishArgs& fa, const PrepArgs& A, const PrepScratch& S);
 // Blocks for a warp-per-frame pass over F frames: one wave of per_sm resident
 // blocks on each of GB300's 152 SMs at most.  The cp.async-pipelined passes
 // (k_scan, k_build) are persistent: each warp streams several frames, so the
@@ -1109,6 +1115,22 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
   sa.Eref = A.Eref;
   ++launches;
   if (A.n_chunks > 0) {
+    // Frames arriving in chunks.  With spec_build, the passes after the scan
+    // run speculatively for one reference as the chunks land: once the first
+    // kSample frames are scanned, reference 0 is refined to their mean and
+    // the operands of every scanned chunk are built.  If all frames turn out
+    // within tau of reference 0, that is the final state; otherwise the
+    // unrefined reference 0 is restored and the general path below runs.
+    const int64_t nsample = std::min<int64_t>(F, (int64_t)kSample);
+    BuildArgs bspec{};
+    if (A.spec_build) {
+      bspec = build_args(*A.spec_build, A, S);
+      // every frame is scanned against the unrefined reference 0, as in the
+      // general path: the refinement rewrites swr in place
+      cudaMemcpyAsync(S.swr0, A.swr, sizeof(float) * 3 * N, cudaMemcpyDeviceToDevice, st);
+      sa.swr = S.swr0;
+    }
+    bool refined = false;
     int64_t f0 = 0;
     for (int c = 0; c < A.n_chunks; ++c) {
       if (c > 0) cudaStreamWaitEvent(st, A.chunk_ev[c], 0);
@@ -1116,8 +1138,50 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
       if (f1 > f0) {
         k_scan<T, true><<<prep_grid(f1 - f0, kScanBlocksPerSM), kPrepThreads, 0, st>>>(src, f0, f1, sa);
         ++launches;
+        if (A.spec_build) {
+          const int64_t b0 = refined ? f0 : 0;
+          if (refined || f1 >= nsample) {
+            k_rot<<<(int)std::min<int64_t>((f1 - b0 + 255) / 256, 1024), 256, 0, st>>>(b0, f1, S.quat, A.cen,
+                                                                                       A.nofit, S.ftab, A.rot);
+            ++launches;
+          }
+          if (!refined && f1 >= nsample) {
+            dim3 gs((unsigned)((A.Np + 127) / 128), (unsigned)kMeanChunks, 1u);
+            k_sample_sum<T><<<gs, 128, 0, st>>>(src, F, A.Np, S.ftab, nullptr, nullptr, S.refhl, A.partial);
+            k_ref_update<<<dim3((unsigned)((N + 31) / 32), 1u), 32, 0, st>>>(
+                A.refs, A.swr, S.refhl, S.rmax, A.partial, nullptr, F, A.w ? A.sqw : nullptr, N, A.Np);
+            launches += 2;
+            refined = true;
+          }
+          if (refined) {
+            k_build<T><<<prep_grid(f1 - b0, kBuildBlocksPerSM), kPrepThreads, 0, st>>>(src, b0, f1, bspec);
+            ++launches;
+          }
+        }
       }
       f0 = f1;
+    }
+    sa.swr = A.swr;
+    if (A.spec_build && refined) {
+      k_argmax<<<1, 1024, 0, st>>>(A.dist, F, A.dmax, A.fsel);
+      ++launches;
+      float dmax = 0.0f;
+      cudaMemcpyAsync(&dmax, A.dmax, sizeof(float), cudaMemcpyDeviceToHost, st);
+      cudaError_t e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) return e;
+      if (!(dmax > A.tau) || A.max_refs == 1 || F <= 1) {
+        o.K = 1;
+        o.built = 1;
+        o.launches = launches;
+        return cudaGetLastError();
+      }
+      // More references are needed: rebuild the unrefined reference 0 the
+      // k-centre choice below starts from (the scan results stand).
+      cudaMemsetAsync(A.fsel, 0, sizeof(int64_t), st);
+      k_make_ref<T><<<kRefCluster, kOneBlockThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w,
+                                                              A.sqw, A.assign, 0, 0, A.nofit, A.refs, A.swr,
+                                                              S.refhl, A.Eref, S.sr, S.rmax);
+      ++launches;
     }
   } else {
     k_scan<T, true><<<prep_grid(F, kScanBlocksPerSM), kPrepThreads, 0, st>>>(src, 0, F, sa);
@@ -1146,7 +1210,8 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
     ++K;
   }
   o.K = K;
-  k_rot<<<(int)std::min<int64_t>((F + 255) / 256, 1024), 256, 0, st>>>(F, S.quat, A.cen, A.nofit, S.ftab, A.rot);
+  k_rot<<<(int)std::min<int64_t>((F + 255) / 256, 1024), 256, 0, st>>>(0, F, S.quat, A.cen, A.nofit, S.ftab,
+                                                                        A.rot);
   ++launches;
   // Frames grouped by reference (host counting sort) when there are several.
   const int* order = nullptr;
@@ -1188,11 +1253,7 @@ cudaError_t run_prep(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
   return A.dtype_f64 ? prep_impl<double>(A, o, st) : prep_impl<float>(A, o, st);
 }
 
-template <typename T>
-static cudaError_t finish_impl(const FinishArgs& fa, cudaStream_t st) {
-  const PrepArgs& A = *fa.prep;
-  FrameSrc<T> src{(const T*)A.ref, (const T*)(A.tgt ? A.tgt : A.ref), A.n_ref, A.N};
-  const PrepScratch S = prep_carve(A.scratch, A.F, A.N, A.max_refs);
+static BuildArgs build_args(const FinishArgs& fa, const PrepArgs& A, const PrepScratch& S) {
   BuildArgs b{};
   b.ftab = S.ftab;
   b.assign = A.assign;
@@ -1215,7 +1276,18 @@ static cudaError_t finish_impl(const FinishArgs& fa, cudaStream_t st) {
   b.trP = fa.trP;
   b.pos = fa.sorted ? S.pos : nullptr;
   b.assign_pos = S.assign_pos;
-  k_build<T><<<prep_grid(A.F, kBuildBlocksPerSM), kPrepThreads, 0, st>>>(src, A.F, b);
+  return b;
+}
+
+template <typename T>
+static cudaError_t finish_impl(const FinishArgs& fa, cudaStream_t st) {
+  const PrepArgs& A = *fa.prep;
+  FrameSrc<T> src{(const T*)A.ref, (const T*)(A.tgt ? A.tgt : A.ref), A.n_ref, A.N};
+  const PrepScratch S = prep_carve(A.scratch, A.F, A.N, A.max_refs);
+  if (!fa.built) {
+    const BuildArgs b = build_args(fa, A, S);
+    k_build<T><<<prep_grid(A.F, kBuildBlocksPerSM), kPrepThreads, 0, st>>>(src, 0, A.F, b);
+  }
   k_ref_terms<<<fa.K * fa.K * kRefCluster, kOneBlockThreads, 0, st>>>(A.refs, A.N, fa.K, A.w, A.nofit, fa.RP);
   return cudaGetLastError();
 }

@@ -295,3 +295,24 @@ def test_qrmsd_maps_to_fit(h, precision):
     out = run(h, refp["xyz"], tgt_mass=refp["mass"], mode="fit", precision=precision)
     tol = 2e-6 if precision == "fp64" else TOL
     assert np.abs(out.astype(np.float64) - refp["tri_qcp"]).max() <= tol
+
+
+@pytest.mark.parametrize("sig_hi,expect_refs", [(1.0, 1), (6.0, None)])
+def test_pinned_input_speculative_prep(h, sig_hi, expect_refs):
+    # Chunked pinned host input: the operands are built for one reference as
+    # the chunks land.  Tight frames keep that build (one reference); spread
+    # frames need more references, and the call falls back to the general
+    # path.  Either way the result equals the device-resident call bit for bit.
+    torch = pytest.importorskip("torch")
+    X, m = synth.trajectory(93, 3000, 1000, 0.1, sig_hi, np.float32, True)
+    dev = run(h, torch.from_numpy(X).cuda(), tgt_mass=m, precision="tc").cpu().numpy()
+    refs_dev = h.stats()["n_refs"]
+    hX = torch.from_numpy(X).pin_memory()
+    hout = torch.empty(dev.size, dtype=torch.float32).pin_memory()
+    run(h, hX, tgt_mass=m, precision="tc", out=hout)
+    assert h.stats()["n_refs"] == refs_dev
+    if expect_refs is not None:
+        assert refs_dev == expect_refs
+    else:
+        assert refs_dev > 1
+    np.testing.assert_array_equal(hout.numpy(), dev)

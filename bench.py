@@ -42,7 +42,7 @@ def parse():
     ap.add_argument("--frames", type=int, default=N_FRAME)
     ap.add_argument("--atoms", type=int, default=N_ATOM)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--tc-pipeline", type=int, default=None, choices=[0, 1, 2],
+    ap.add_argument("--tc-pipeline", type=int, default=None, choices=[-1, 0, 1, 2, 3],
                     help="tensor-core kernel shape (GBR_OPT_TC_PIPELINE); default: the library's")
     ap.add_argument("--profile", action="store_true",
                     help="warm up, then run exactly one all-pairs call (for ncu); prints stats only")

@@ -24,6 +24,14 @@ using namespace gbr;
 
 namespace {
 constexpr int kMaxBands = 8;  // output row bands whose copies overlap the contraction
+// Atom count from which the pair-of-SMs kernel uses its deep operand pipeline
+// (64-atom stages x 3, measured 6-7 % faster at 1,500-3,000 atoms): below it
+// the per-pair epilogue, not the operand feed, bounds the kernel, and the
+// wider epilogue chunks of the shallow shape win (9 % at 1,024 atoms, 20 % at
+// 500).  The deep shape's 4-frame chunks store 16-byte row segments, which
+// HBM's L2 merges but the host link does not: results written straight into
+// pinned host memory keep the shallow shape.
+constexpr int kDeepStageAtoms = 1280;
 }
 
 extern "C" {
@@ -91,7 +99,8 @@ int gbr_set_option(gbr_handle* h, int key, double value) {
       h->timing = value != 0.0;
       return GBR_OK;
     case GBR_OPT_TC_PIPELINE:
-      if (value != 0.0 && value != 1.0 && value != 2.0) return h->fail(GBR_ERR_ARG, "tc pipeline must be 0, 1 or 2");
+      if (!(value == -1.0 || value == 0.0 || value == 1.0 || value == 2.0 || value == 3.0))
+        return h->fail(GBR_ERR_ARG, "tc pipeline must be -1 (automatic), 0, 1, 2 or 3");
       h->tc_variant = (int)value;
       return GBR_OK;
     case GBR_OPT_HOST_OUT:
@@ -464,7 +473,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
         L.flags = f;
         L.dev_error = (int*)P[25];
         L.num_sms = h->num_sms;
-        L.variant = h->tc_variant;
+        L.variant = (h->tc_variant >= 0) ? h->tc_variant : ((N >= kDeepStageAtoms && !out_direct) ? 3 : 2);
         return run_pairs_tc(L, st);
       }
       PairLaunch L{};

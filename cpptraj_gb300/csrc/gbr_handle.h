@@ -66,7 +66,7 @@ struct gbr_handle {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   int num_sms = 0;
   int tc_ok = 0;
-  int tc_variant = 2;  // pairs of SMs (cta_group::2)
+  int tc_variant = -1;  // -1: pairs of SMs, stage shape chosen by atom count (see gbr_set_option)
   bool host_out_direct = true;  // kernels store into pinned host output in place
   // batched path: auxiliary streams, fork/join events, pinned staging,
   // the captured graph of the last batch signature, the autotuner table

@@ -170,7 +170,8 @@ struct TcLaunch {
   int* dev_error;    // set non-zero when a bounded wait gives up
   int num_sms;
   int variant;       // 0: 64-atom stages (128B swizzle, 2 stages); 1: 32-atom stages (64B swizzle, 4 stages);
-                     // 2: pairs of SMs (cta_group::2, 32-atom stages, 6 stages)
+                     // 2: pairs of SMs (cta_group::2), 32-atom stages x 5, 8-frame epilogue chunks;
+                     // 3: pairs of SMs, 64-atom stages x 3, 4-frame epilogue chunks
   int64_t ready_tiles;  // > 0: tile_buf already holds this many tiles (no host build or copy)
 };
 // Tile list of the tensor-core kernel for this map (host side).

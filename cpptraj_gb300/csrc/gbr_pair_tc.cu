@@ -62,10 +62,20 @@ struct Pipe {
 constexpr int EPI_WARPS = 16;          // four groups of four warps (one per TMEM lane quadrant)
 constexpr int EPI_GROUPS = EPI_WARPS / 4;
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
-constexpr int CH_TGT = 8;              // target frames per epilogue chunk
-constexpr int CH_COLS = 3 * CH_TGT;    // 24 accumulator columns
-constexpr int ST_STRIDE = CH_COLS + 1;
-constexpr int STAGING_BYTES = 128 * ST_STRIDE * 4;
+// Epilogue shape: CH target frames (3 CH accumulator columns) per chunk read
+// from tensor memory and staged in shared memory, one staging buffer per
+// group.  Wider chunks give each group more pairs per barrier (the epilogue-
+// bound small-N case); narrower ones leave shared memory for deeper operand
+// pipelines (large N).
+template <int CH>
+struct Epi {
+  static constexpr int CH_TGT = CH;
+  static constexpr int CH_COLS = 3 * CH;
+  static constexpr int ST_STRIDE = CH_COLS + 1;
+  static constexpr int STAGING_BYTES = 128 * ST_STRIDE * 4;
+};
+using Epi1 = Epi<8>;  // the one-SM kernels: 24 accumulator columns per chunk
+constexpr int STAGING_BYTES = Epi1::STAGING_BYTES;
 // Per-tile frame terms staged in shared memory, two buffers.  With A the
 // reference (pre-alignment) of the tile's first reference frame and B that of
 // its first target frame, each frame slot holds n, 1/scale, its reference,
@@ -73,7 +83,11 @@ constexpr int STAGING_BYTES = 128 * ST_STRIDE * 4;
 // (target frames): everything a pair with references (A, B) reads.
 constexpr int TERM_STRIDE = 13;
 constexpr int TERM_FLOATS = ((TI + TJ) * TERM_STRIDE + 3) & ~3;
-constexpr int EPI_BYTES = EPI_GROUPS * STAGING_BYTES + 2 * TERM_FLOATS * 4;
+template <class E>
+constexpr int epi_bytes() {
+  return EPI_GROUPS * E::STAGING_BYTES + 2 * TERM_FLOATS * 4;
+}
+constexpr int EPI_BYTES = epi_bytes<Epi1>();
 constexpr int BAR_BYTES = 128;
 constexpr int SMEM_BYTES = 1024 + 2 * (2 * UM * 128 + 2 * UN * 128) + EPI_BYTES + BAR_BYTES;
 static_assert(SMEM_BYTES <= 232448, "one-SM kernel shared memory");
@@ -203,6 +217,14 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
 #pragma unroll
   for (int k = 0; k < 8; ++k) v[k] = __uint_as_float(r[k]);
 }
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v) {
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
+#pragma unroll
+  for (int k = 0; k < 4; ++k) v[k] = __uint_as_float(r[k]);
+}
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 __device__ __forceinline__ void named_sync(int id, int n) {
@@ -219,6 +241,7 @@ __device__ __forceinline__ void mbar_arrive_remote(uint32_t caddr) {
 // chunks g, g + 4, ...), and run the per-pair solve.  The reference frames of
 // a tile start at i_base + ti * ti_frames + i_off.  acce_bar is the address
 // the warps arrive on when the buffer is free (remote: CTA 0 of a pair).
+template <class E>
 __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_base, float* staging, float* terms,
                                                volatile int* okf, uint32_t accf0, uint32_t acce_bar, bool remote,
                                                int64_t t0, int64_t tstep, int ti_frames, int i_off, int warp,
@@ -229,6 +252,7 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
   const int row = 32 * q + lane;        // accumulator row = (reference frame, component)
   const int tid = (e & 3) * 32 + lane;  // 0..127 within the group
   const int etid = e * 32 + lane;       // 0..511
+  constexpr int CH_TGT = E::CH_TGT, CH_COLS = E::CH_COLS, ST_STRIDE = E::ST_STRIDE;
   float* st = staging + g * (128 * ST_STRIDE);
   const bool tri = P.map.tri;
   const int K = P.terms.K;
@@ -284,8 +308,15 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
       for (int c = g; c < TJ / CH_TGT; c += EPI_GROUPS) {
         float v[CH_COLS];
         const uint32_t taddr = tmem_base + ((uint32_t)(32 * q) << 16) + b * ACC_STRIDE + c * CH_COLS;
-        tmem_ld16(taddr, v);
-        tmem_ld8(taddr + 16, v + 16);
+        if constexpr (CH_COLS == 24) {
+          tmem_ld16(taddr, v);
+          tmem_ld8(taddr + 16, v + 16);
+        } else {
+          static_assert(CH_COLS == 12, "chunks of 8 or 4 target frames");
+          tmem_ld4(taddr, v);
+          tmem_ld4(taddr + 4, v + 4);
+          tmem_ld4(taddr + 8, v + 8);
+        }
         tmem_wait_ld();
 #pragma unroll
         for (int k = 0; k < CH_COLS; ++k) st[row * ST_STRIDE + k] = v[k];
@@ -457,7 +488,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
   } else {
     // ---------------- epilogue ----------------
-    epilogue_tiles(P, tmem_base, staging, terms, okf, accf0, acce0, false, blockIdx.x, gridDim.x, TI, 0, warp, lane);
+    epilogue_tiles<Epi1>(P, tmem_base, staging, terms, okf, accf0, acce0, false, blockIdx.x, gridDim.x, TI, 0, warp,
+                         lane);
   }
 
   tc_fence_before();
@@ -488,18 +520,33 @@ constexpr int TI2 = 2 * TI;            // reference frames per cluster tile (84)
 constexpr int TJH = TJ / 2;            // target frames per CTA half of B (32)
 constexpr int UM2 = 256;
 constexpr int UNH = 3 * TJH;           // 96 B rows per CTA
-constexpr int KA2 = 32;                // atoms per stage (64-byte rows, 64B swizzle)
-constexpr int ROW2 = 2 * KA2;
-constexpr int STAGES2 = 5;
-constexpr int A2_BYTES = UM * ROW2;    // 8 KB (per CTA: 128 rows)
-constexpr int BH_BYTES = UNH * ROW2;   // 6 KB
-constexpr int A2_TX = 3 * TI * ROW2;
-constexpr int BH_TX = UNH * ROW2;
-constexpr int STAGE2_BYTES = 2 * A2_BYTES + 2 * BH_BYTES;
 constexpr int BAR2_BYTES = 256;
-constexpr int SMEM2_BYTES = 1024 + STAGES2 * STAGE2_BYTES + EPI_BYTES + BAR2_BYTES;
-static_assert(SMEM2_BYTES <= 232448, "pair kernel shared memory");
-static_assert(STAGE2_BYTES % 1024 == 0 && A2_BYTES % 1024 == 0 && BH_BYTES % 1024 == 0, "swizzle alignment");
+// Pipeline and epilogue shape of the pair kernel: KA atoms per stage (rows of
+// 2 KA bytes, 64- or 128-byte swizzle), STAGES stages, epilogue chunks of CH
+// target frames.
+template <int KA_, int STAGES_, int CH_>
+struct PairCfg {
+  static constexpr int KA2 = KA_;
+  static constexpr int ROW2 = 2 * KA_;
+  static constexpr int STAGES2 = STAGES_;
+  using E = Epi<CH_>;
+  static constexpr int A2_BYTES = UM * ROW2;  // per CTA: 128 rows, TMA writes 126
+  static constexpr int BH_BYTES = UNH * ROW2;
+  static constexpr int A2_TX = 3 * TI * ROW2;
+  static constexpr int BH_TX = UNH * ROW2;
+  static constexpr int STAGE2_BYTES = 2 * A2_BYTES + 2 * BH_BYTES;
+  static constexpr int EPI2_BYTES = epi_bytes<E>();
+  static constexpr int SMEM2_BYTES = 1024 + STAGES2 * STAGE2_BYTES + EPI2_BYTES + BAR2_BYTES;
+  static constexpr uint32_t SBO = 8 * ROW2;                     // 8-row core-matrix groups
+  static constexpr uint64_t LAYOUT = (KA_ == 64) ? 2ull : 4ull;  // SWIZZLE_128B : SWIZZLE_64B
+  static_assert(SMEM2_BYTES <= 232448, "pair kernel shared memory");
+  static_assert(STAGE2_BYTES % 1024 == 0 && A2_BYTES % 1024 == 0 && BH_BYTES % 1024 == 0, "swizzle alignment");
+  static_assert(KA_ == 32 || KA_ == 64, "32- or 64-atom stages");
+};
+// Small N (epilogue-bound): 32-atom stages x 5, 8-frame epilogue chunks.
+using PairShallow = PairCfg<32, 5, 8>;
+// Large N (operand-feed bound): 64-atom stages (128-byte rows) x 3, 4-frame chunks.
+using PairDeep = PairCfg<64, 3, 4>;
 constexpr uint32_t IDESC2 = (1u << 4) | ((uint32_t)(UN >> 3) << 17) | ((uint32_t)(UM2 >> 4) << 24);
 
 __device__ __forceinline__ uint32_t cluster_rank() {
@@ -548,19 +595,24 @@ __device__ __forceinline__ void umma_commit_pair(uint32_t bar) {
 __device__ __forceinline__ void umma_commit_pair_local(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
-__device__ __forceinline__ uint64_t smem_desc64(uint32_t addr) {
+template <class PC>
+__device__ __forceinline__ uint64_t smem_desc_pair(uint32_t addr) {
   uint64_t d = 0;
   d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)((8 * ROW2) >> 4) << 32;
+  d |= (uint64_t)(PC::SBO >> 4) << 32;
   d |= 1ull << 46;
-  d |= 4ull << 61;  // SWIZZLE_64B
+  d |= PC::LAYOUT << 61;
   return d;
 }
 
+template <class PC>
 __global__ void __launch_bounds__(THREADS, 1)
     k_pairs_tc2(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                 const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
                 const TcParams P) {
+  constexpr int KA2 = PC::KA2, STAGES2 = PC::STAGES2, A2_BYTES = PC::A2_BYTES, BH_BYTES = PC::BH_BYTES,
+                A2_TX = PC::A2_TX, BH_TX = PC::BH_TX, STAGE2_BYTES = PC::STAGE2_BYTES,
+                STAGING_BYTES = PC::E::STAGING_BYTES, EPI_BYTES = PC::EPI2_BYTES;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* stage_base = smem;
@@ -656,9 +708,9 @@ __global__ void __launch_bounds__(THREADS, 1)
           const uint32_t sb = smem_u32(stage_base + s * STAGE2_BYTES);
 #pragma unroll
           for (int kk = 0; kk < KA2 / 16; ++kk) {
-            const uint64_t ah = smem_desc64(sb + kk * 32), al = smem_desc64(sb + A2_BYTES + kk * 32);
-            const uint64_t bh = smem_desc64(sb + 2 * A2_BYTES + kk * 32);
-            const uint64_t bl = smem_desc64(sb + 2 * A2_BYTES + BH_BYTES + kk * 32);
+            const uint64_t ah = smem_desc_pair<PC>(sb + kk * 32), al = smem_desc_pair<PC>(sb + A2_BYTES + kk * 32);
+            const uint64_t bh = smem_desc_pair<PC>(sb + 2 * A2_BYTES + kk * 32);
+            const uint64_t bl = smem_desc_pair<PC>(sb + 2 * A2_BYTES + BH_BYTES + kk * 32);
             umma_f16_pair(d, ah, bh, (kc | kk) != 0);
             umma_f16_pair(d, al, bh, 1u);
             umma_f16_pair(d, ah, bl, 1u);
@@ -674,7 +726,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
   } else {
     // ---------------- epilogue (both CTAs) ----------------
-    epilogue_tiles(P, tmem_base, staging, terms, okf, accf0, mapa_rank(acce0, 0), true, cluster, n_clusters, TI2,
+    epilogue_tiles<typename PC::E>(P, tmem_base, staging, terms, okf, accf0, mapa_rank(acce0, 0), true, cluster,
+                                   n_clusters, TI2,
                    (int)rank * TI, warp, lane);
   }
 
@@ -760,14 +813,16 @@ int64_t tc_build_tiles(const OutMap& m, std::vector<int2>& tiles, int64_t& i_bas
 }
 
 int64_t tc_build_tile_list(const OutMap& m, std::vector<int2>& tiles, TcTileInfo& info, int variant) {
-  return tc_build_tiles(m, tiles, info.i_base, info.jt_base, info.i_end, info.jt_end, variant == 2 ? TI2 : TI);
+  return tc_build_tiles(m, tiles, info.i_base, info.jt_base, info.i_end, info.jt_end, variant >= 2 ? TI2 : TI);
 }
 
 // Launch of the pair-of-SMs kernel: clusters of two CTAs, as many clusters
 // as can be resident at once (one CTA per SM), at most one per tile.
+template <class PC>
 static cudaError_t launch_pair_kernel(const CUtensorMap& mAh, const CUtensorMap& mAl, const CUtensorMap& mBh,
                                       const CUtensorMap& mBl, const TcParams& P, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(k_pairs_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_BYTES);
+  cudaError_t e =
+      cudaFuncSetAttribute(k_pairs_tc2<PC>, cudaFuncAttributeMaxDynamicSharedMemorySize, PC::SMEM2_BYTES);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
@@ -776,7 +831,7 @@ static cudaError_t launch_pair_kernel(const CUtensorMap& mAh, const CUtensorMap&
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.blockDim = dim3(THREADS, 1, 1);
-  cfg.dynamicSmemBytes = SMEM2_BYTES;
+  cfg.dynamicSmemBytes = PC::SMEM2_BYTES;
   cfg.stream = st;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
@@ -784,14 +839,14 @@ static cudaError_t launch_pair_kernel(const CUtensorMap& mAh, const CUtensorMap&
   if (max_clusters == 0) {
     cfg.gridDim = dim3(2 * 76, 1, 1);
     int n = 0;
-    e = cudaOccupancyMaxActiveClusters(&n, k_pairs_tc2, &cfg);
+    e = cudaOccupancyMaxActiveClusters(&n, k_pairs_tc2<PC>, &cfg);
     if (e != cudaSuccess) return e;
     if (n < 1) return cudaErrorInvalidConfiguration;
     max_clusters = n;
   }
   const int64_t nc = std::min<int64_t>(P.n_tiles, (int64_t)max_clusters);
   cfg.gridDim = dim3((unsigned)(2 * nc), 1, 1);
-  return cudaLaunchKernelEx(&cfg, k_pairs_tc2, mAh, mAl, mBh, mBl, P);
+  return cudaLaunchKernelEx(&cfg, k_pairs_tc2<PC>, mAh, mAl, mBh, mBl, P);
 }
 
 cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
@@ -799,7 +854,7 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
   int64_t i_base, jt_base, i_end, jt_end;
   int64_t n;
   cudaError_t e = cudaSuccess;
-  const bool pair = (L.variant == 2);
+  const bool pair = (L.variant >= 2);
   const int ti_frames = pair ? TI2 : TI;
   if (L.ready_tiles > 0) {
     // The caller uploaded the list already (batched / graph-captured path).
@@ -817,7 +872,10 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
     // The copy reads `tiles` asynchronously from pageable memory; cudaMemcpyAsync
     // from pageable memory returns after the source has been consumed.
   }
-  const int ka = (L.variant == 0) ? 64 : 32;
+  const int ka = (L.variant == 0)   ? 64
+                 : (L.variant == 1) ? 32
+                 : (L.variant == 3) ? PairDeep::KA2
+                                    : PairShallow::KA2;
   const int bj = pair ? TJH : TJ;
   CUtensorMap mAh, mAl, mBh, mBl;
   if (!make_map(&mAh, L.hi, L.F, L.Np, TI, ka) || !make_map(&mAl, L.lo, L.F, L.Np, TI, ka) ||
@@ -838,7 +896,8 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
   P.flags = L.flags;
   P.err = L.dev_error;
   if (pair) {
-    e = launch_pair_kernel(mAh, mAl, mBh, mBl, P, st);
+    e = (L.variant == 3) ? launch_pair_kernel<PairDeep>(mAh, mAl, mBh, mBl, P, st)
+                         : launch_pair_kernel<PairShallow>(mAh, mAl, mBh, mBl, P, st);
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
   }

@@ -23,7 +23,7 @@ TRI, FULL = 0, 1
 PREC_FP32, PREC_TC, PREC_FP64 = 0, 1, 2
 OPT_TAU, OPT_MAX_REFS, OPT_TOL, OPT_TIMING, OPT_TC_PIPELINE, OPT_HOST_OUT = 0, 1, 2, 3, 4, 5
 #: The library's default tensor-core kernel shape (pairs of SMs).
-TC_PIPELINE_DEFAULT = 2
+TC_PIPELINE_DEFAULT = -1  # automatic: deep stages from 1,280 atoms (device results), shallow otherwise
 
 PRECISIONS = {"fp32": PREC_FP32, "tc": PREC_TC, "fp64": PREC_FP64}
 MODES = {"fit": FIT, "nofit": NOFIT, "dme": DME}

@@ -27,9 +27,10 @@ sys.path.insert(0, ROOT)
 METRIC = "RMSD pairs/s, 10k frames x 2k atoms: tensor-core vs plain GPU at 1e-4 Angstrom"
 N_FRAME, N_ATOM = 10000, 2000
 FLOPS_PER_PAIR = 18 * N_ATOM  # 9 products x N atoms x 2 (SURVEY 18*N; split extras not counted)
-# DRAM bytes (read + write) of one k_pairs_tc2 launch on this workload, from an
-# ncu capture of `python bench.py --profile --warmup 2` (profiles/k_pairs_tc2_10000x2000_full.md).
-K2_TRAFFIC_BYTES = {(N_FRAME, N_ATOM): 2.244835e9 + 0.198118e9}
+# DRAM bytes (read + write) of one k_pairs_tc2 launch on this workload (the
+# deep 64-atom-stage shape the library picks at 2,000 atoms), from an ncu
+# capture of `python bench.py --profile --warmup 2` (profiles/k_pairs_tc2_10000x2000_full.md).
+K2_TRAFFIC_BYTES = {(N_FRAME, N_ATOM): 1.873646e9 + 0.193895e9}
 
 
 def parse():

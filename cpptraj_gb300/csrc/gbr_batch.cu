@@ -31,7 +31,12 @@ using namespace gbr;
 
 namespace {
 
-enum Choice { kTC64 = 0, kTC32 = 1, kFP32 = 2, kFP64 = 3 };
+// Kernel per trajectory: the one-SM tensor-core kernel (64- or 32-atom stages),
+// the pair-of-SMs tensor-core kernel (shallow or deep stages), the FP32
+// CUDA-core kernel, or FP64 for every pair.
+enum Choice { kTC64 = 0, kTC32 = 1, kFP32 = 2, kFP64 = 3, kTCPairS = 4, kTCPairD = 5 };
+bool is_tc(int c) { return c == kTC64 || c == kTC32 || c == kTCPairS || c == kTCPairD; }
+int tc_variant_of(int c) { return c == kTC64 ? 0 : c == kTC32 ? 1 : c == kTCPairS ? 2 : 3; }
 
 struct Prob {
   int64_t F = 0;
@@ -78,7 +83,7 @@ struct Prob {
 
 void layout_prob(Arena& A, Prob& p, bool host_in, bool host_out) {
   const size_t F = (size_t)p.F, N = (size_t)p.N, Np = (size_t)p.Np;
-  const bool tc = (p.choice == kTC64 || p.choice == kTC32);
+  const bool tc = is_tc(p.choice);
   const bool planes = (p.choice != kFP64);
   p.d_xyz = host_in ? A.take<float>(F * 3 * N) : nullptr;
   p.d_w = A.take<double>(N);
@@ -247,7 +252,7 @@ cudaError_t enqueue_prob(gbr_handle* h, Prob& p, int mode, bool host_in, bool ho
       L.flags = fl;
       L.dev_error = derr;
       L.num_sms = h->num_sms;
-      L.variant = (p.choice == kTC32) ? 1 : 0;
+      L.variant = tc_variant_of(p.choice);
       if (p.n_tiles > 0 && (e = run_pairs_tc(L, st)) != cudaSuccess) return e;
     } else {
       PairLaunch L{};
@@ -341,7 +346,12 @@ extern "C" int gbr_allpairs_batched(gbr_handle* h, int32_t n_traj, const float* 
     if (precision == GBR_PREC_FP64) return std::vector<int>{kFP64};
     if (precision == GBR_PREC_FP32) return std::vector<int>{kFP32};
     c = {kTC32, kTC64, kFP32};
-    (void)p;
+    // the pair kernel's tile holds 84 reference frames: worth timing when a
+    // trajectory fills at least one such tile row
+    if (p.F >= 84) {
+      c.push_back(kTCPairS);
+      c.push_back(kTCPairD);
+    }
     return c;
   };
   std::vector<int> to_tune;
@@ -367,10 +377,10 @@ extern "C" int gbr_allpairs_batched(gbr_handle* h, int32_t n_traj, const float* 
     all.clear();
     for (auto& p : probs) {
       p.n_tiles = 0;
-      if (p.choice == kTC64 || p.choice == kTC32) {
+      if (is_tc(p.choice)) {
         std::vector<int2> tl;
         TcTileInfo info;
-        p.n_tiles = tc_build_tile_list(tri_map(p, nullptr), tl, info);
+        p.n_tiles = tc_build_tile_list(tri_map(p, nullptr), tl, info, tc_variant_of(p.choice));
         p.tile_off = all.size();
         all.insert(all.end(), tl.begin(), tl.end());
       }

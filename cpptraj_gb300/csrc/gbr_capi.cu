@@ -473,7 +473,8 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
         L.flags = f;
         L.dev_error = (int*)P[25];
         L.num_sms = h->num_sms;
-        L.variant = (h->tc_variant >= 0) ? h->tc_variant : ((N >= kDeepStageAtoms && !out_direct) ? 3 : 2);
+        L.variant = (h->tc_variant >= 0) ? h->tc_variant : (N >= kDeepStageAtoms ? 3 : 2);
+        L.row_stores = 1;
         return run_pairs_tc(L, st);
       }
       PairLaunch L{};

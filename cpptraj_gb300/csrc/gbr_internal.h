@@ -173,6 +173,7 @@ struct TcLaunch {
                      // 2: pairs of SMs (cta_group::2), 32-atom stages x 5, 8-frame epilogue chunks;
                      // 3: pairs of SMs, 64-atom stages x 3, 4-frame epilogue chunks
   int64_t ready_tiles;  // > 0: tile_buf already holds this many tiles (no host build or copy)
+  int row_stores;       // pair kernels, triangle output: gather each tile's results and store whole rows
 };
 // Tile list of the tensor-core kernel for this map (host side).
 struct TcTileInfo {

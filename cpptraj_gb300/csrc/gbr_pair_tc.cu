@@ -73,6 +73,10 @@ struct Epi {
   static constexpr int CH_COLS = 3 * CH;
   static constexpr int ST_STRIDE = CH_COLS + 1;
   static constexpr int STAGING_BYTES = 128 * ST_STRIDE * 4;
+  // Result rows of one tile (pair kernels, triangle output): TI rows of TJ
+  // values, padded by one chunk so the chunk writes hit 32 distinct banks.
+  static constexpr int RB_STRIDE = TJ + CH;
+  static constexpr int ROWBUF_BYTES = TI * RB_STRIDE * 4;
 };
 using Epi1 = Epi<8>;  // the one-SM kernels: 24 accumulator columns per chunk
 constexpr int STAGING_BYTES = Epi1::STAGING_BYTES;
@@ -113,6 +117,7 @@ struct TcParams {
   OutMap map;
   FlagList flags;
   int* err;
+  int row_stores;  // triangle results gathered into whole tile rows before the store (pair kernels)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -243,9 +248,9 @@ __device__ __forceinline__ void mbar_arrive_remote(uint32_t caddr) {
 // the warps arrive on when the buffer is free (remote: CTA 0 of a pair).
 template <class E>
 __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_base, float* staging, float* terms,
-                                               volatile int* okf, uint32_t accf0, uint32_t acce_bar, bool remote,
-                                               int64_t t0, int64_t tstep, int ti_frames, int i_off, int warp,
-                                               int lane) {
+                                               float* rowbuf, volatile int* okf, uint32_t accf0, uint32_t acce_bar,
+                                               bool remote, int64_t t0, int64_t tstep, int ti_frames, int i_off,
+                                               int warp, int lane) {
   const int e = warp - 2;
   const int g = e >> 2;
   const int q = warp & 3;               // TMEM lane quadrant this warp may access
@@ -255,6 +260,11 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
   constexpr int CH_TGT = E::CH_TGT, CH_COLS = E::CH_COLS, ST_STRIDE = E::ST_STRIDE;
   float* st = staging + g * (128 * ST_STRIDE);
   const bool tri = P.map.tri;
+  // Row stores: the pairs of a tile gather in shared memory and leave as
+  // whole rows of the triangle (TJ contiguous values) instead of CH_TGT-value
+  // pieces, which matters when the output is host memory across the link.
+  const bool rows = rowbuf != nullptr && tri && P.row_stores != 0;
+  constexpr int RB_STRIDE = E::RB_STRIDE;
   const int K = P.terms.K;
   uint32_t it = 0;
   for (int64_t t = t0; t < P.n_tiles; t += tstep, ++it) {
@@ -358,11 +368,16 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
             r = pair_epilogue(D, i, P.tgt0 + jt, P.terms, &flag);
           }
           if (flag) flag_pair(P.flags, P.map, i, jt);
-          P.map.out[idx] = r;
+          if (rows)
+            rowbuf[il * RB_STRIDE + c * CH_TGT + jl] = r;
+          else
+            P.map.out[idx] = r;
         }
         named_sync(1 + g, 128);
       }
     }
+    // Every tensor-memory read of this tile has completed (tmem_wait_ld per
+    // chunk): the accumulator buffer is released before the row stores.
     tc_fence_before();
     __syncwarp();
     if (lane == 0) {
@@ -372,6 +387,19 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
         mbar_arrive(acce_bar + 8 * b);
     }
     if (!ok) break;
+    if (rows) {
+      // The next tile writes rowbuf only after its own all-group barrier,
+      // which every thread reaches after these stores.
+      named_sync(1 + EPI_GROUPS, EPI_WARPS * 32);
+#pragma unroll 1
+      for (int x = etid; x < TI * TJ; x += EPI_WARPS * 32) {
+        const int il = x / TJ, jl = x % TJ;
+        const int64_t i = i0 + il, jt = jt0 + jl;
+        if (i >= P.i_end || jt >= P.jt_end) continue;
+        const int64_t idx = out_index(P.map, i, jt);
+        if (idx >= 0) P.map.out[idx] = rowbuf[il * RB_STRIDE + jl];
+      }
+    }
   }
 }
 
@@ -488,7 +516,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
   } else {
     // ---------------- epilogue ----------------
-    epilogue_tiles<Epi1>(P, tmem_base, staging, terms, okf, accf0, acce0, false, blockIdx.x, gridDim.x, TI, 0, warp,
+    epilogue_tiles<Epi1>(P, tmem_base, staging, terms, nullptr, okf, accf0, acce0, false, blockIdx.x, gridDim.x, TI, 0, warp,
                          lane);
   }
 
@@ -535,7 +563,7 @@ struct PairCfg {
   static constexpr int A2_TX = 3 * TI * ROW2;
   static constexpr int BH_TX = UNH * ROW2;
   static constexpr int STAGE2_BYTES = 2 * A2_BYTES + 2 * BH_BYTES;
-  static constexpr int EPI2_BYTES = epi_bytes<E>();
+  static constexpr int EPI2_BYTES = epi_bytes<E>() + E::ROWBUF_BYTES;
   static constexpr int SMEM2_BYTES = 1024 + STAGES2 * STAGE2_BYTES + EPI2_BYTES + BAR2_BYTES;
   static constexpr uint32_t SBO = 8 * ROW2;                     // 8-row core-matrix groups
   static constexpr uint64_t LAYOUT = (KA_ == 64) ? 2ull : 4ull;  // SWIZZLE_128B : SWIZZLE_64B
@@ -618,6 +646,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint8_t* stage_base = smem;
   float* staging = (float*)(smem + STAGES2 * STAGE2_BYTES);
   float* terms = (float*)(smem + STAGES2 * STAGE2_BYTES + EPI_GROUPS * STAGING_BYTES);
+  float* rowbuf = terms + 2 * TERM_FLOATS;
   uint64_t* bars = (uint64_t*)(smem + STAGES2 * STAGE2_BYTES + EPI_BYTES);
   // bars: full[STAGES2] empty[STAGES2] accf[2] acce[2] done; TMEM address; verdicts.
   constexpr int kFull = 0, kEmpty = STAGES2, kAccf = 2 * STAGES2, kAcce = 2 * STAGES2 + 2, kDone = 2 * STAGES2 + 4;
@@ -726,9 +755,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
   } else {
     // ---------------- epilogue (both CTAs) ----------------
-    epilogue_tiles<typename PC::E>(P, tmem_base, staging, terms, okf, accf0, mapa_rank(acce0, 0), true, cluster,
-                                   n_clusters, TI2,
-                   (int)rank * TI, warp, lane);
+    epilogue_tiles<typename PC::E>(P, tmem_base, staging, terms, rowbuf, okf, accf0, mapa_rank(acce0, 0), true,
+                                   cluster, n_clusters, TI2, (int)rank * TI, warp, lane);
   }
 
   tc_fence_before();
@@ -895,6 +923,7 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
   P.map = L.map;
   P.flags = L.flags;
   P.err = L.dev_error;
+  P.row_stores = L.row_stores;
   if (pair) {
     e = (L.variant == 3) ? launch_pair_kernel<PairDeep>(mAh, mAl, mBh, mBl, P, st)
                          : launch_pair_kernel<PairShallow>(mAh, mAl, mBh, mBl, P, st);

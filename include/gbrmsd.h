@@ -213,8 +213,7 @@ int gbr_get_stats(const gbr_handle *h, gbr_stats *out);
  *                        sharing one 256-row MMA, 32-atom stages x 5,
  *                        3 = pairs of SMs, 64-atom stages x 3 with narrower
  *                        epilogue chunks; -1 (default) = 3 from 1,280 atoms
- *                        on (unless results go straight to pinned host
- *                        memory), 2 otherwise
+ *                        on, 2 otherwise
  *   GBR_OPT_HOST_OUT     pinned host `out` of gbr_allpairs: 1 = the kernels
  *                        store into it directly (default), 0 = results staged
  *                        in device memory and copied back in row bands

@@ -47,7 +47,7 @@ def parse():
                     help="tensor-core kernel shape (GBR_OPT_TC_PIPELINE); default: the library's")
     ap.add_argument("--profile", action="store_true",
                     help="warm up, then run exactly one all-pairs call (for ncu); prints stats only")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4", "dme", "rms", "accuracy"],
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4", "dme", "rms", "centroids", "accuracy"],
                     help="c1 = the headline metric; c2/c3/c4/dme print secondary lines for the other configs")
     return ap.parse_args()
 
@@ -244,6 +244,41 @@ def main_rms(args):
                                        "cores": os.cpu_count(), "kind": "port",
                                        "sample": f"frames 0-1999, FP64 oracle (Jacobi, as Frame::RMSD_CenteredRef), "
                                                  f"OpenMP, {cpu_s:.2f} s"}}), flush=True)
+
+
+def main_centroids(args):
+    """Cluster centroids (Metric_RMS::CalculateCentroid) of the clustering
+    workload: 50,000 frames x 500 atoms around 20 centroids, FP32, unweighted,
+    fit, members in frame order per label (gbr_cluster_centroids), with the
+    FP64 oracle on all host cores (one cluster per thread)."""
+    import torch
+
+    import oracle
+    from cpptraj_gb300 import gbrmsd, synth
+
+    F, N, K = 50000, 500, 20
+    X, labels = synth.clustered(3, F, N, K, 0.8)
+    members, offsets = oracle.members_offsets(labels, K)
+    h = gbrmsd.Handle(0)
+    h.set_stream(torch.cuda.current_stream().cuda_stream)
+    dX = torch.from_numpy(X).cuda()
+    dmem, doff = torch.from_numpy(members).cuda(), torch.from_numpy(offsets).cuda()
+    ms = _gpu_time(lambda: h.cluster_centroids(dX, dmem, doff), max(3, args.steps), 3)
+    ms_nofit = _gpu_time(lambda: h.cluster_centroids(dX, dmem, doff, mode="nofit"), max(3, args.steps), 3)
+    got = h.cluster_centroids(dX, dmem, doff).cpu().numpy()
+    t0 = time.perf_counter()
+    want = oracle.cluster_centroids_f64(X, members, offsets, nthreads=os.cpu_count() or 1)
+    cpu_s = time.perf_counter() - t0
+    steps = int(np.diff(offsets).max())
+    print(json.dumps({"workload": f"cluster centroids, {F} frames x {N} atoms in {K} clusters, FP32, fit",
+                      "ms": ms, "members_per_s": F / (ms / 1e3), "ms_nofit": ms_nofit,
+                      "longest_chain": steps, "us_per_chain_step": ms * 1e3 / steps,
+                      "max_abs_err_A": float(np.abs(got - want).max()), "against": "FP64 oracle, all centroids",
+                      "cpu_baseline": {"value": F / cpu_s, "unit": "members/s", "cores": os.cpu_count(),
+                                       "kind": "port",
+                                       "sample": f"all {K} clusters, FP64 oracle (restatement of "
+                                                 f"Metric_RMS::CalculateCentroid), OpenMP over clusters, "
+                                                 f"{cpu_s:.2f} s"}}), flush=True)
 
 
 def main_accuracy(args):
@@ -577,7 +612,7 @@ def main():
     if args.profile:
         return main_profile(args)
     if args.workload != "c1":
-        return {"c2": main_c2, "c3": main_c3, "c4": main_c4, "dme": main_dme, "rms": main_rms,
+        return {"c2": main_c2, "c3": main_c3, "c4": main_c4, "dme": main_dme, "rms": main_rms, "centroids": main_centroids,
                 "accuracy": main_accuracy}[args.workload](args)
     import torch
     import torch.distributed as dist

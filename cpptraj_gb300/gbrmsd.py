@@ -31,7 +31,7 @@ MODES = {"fit": FIT, "nofit": NOFIT, "dme": DME}
 #: Every symbol include/gbrmsd.h declares.
 EXPORTED = ("gbr_create", "gbr_destroy", "gbr_last_error", "gbr_allpairs", "gbr_output_count",
             "gbr_allpairs_batched", "gbr_rmsd_backward", "gbr_get_stats", "gbr_set_option", "gbr_set_stream",
-            "gbr_write_cmatrix", "gbr_superpose",
+            "gbr_write_cmatrix", "gbr_superpose", "gbr_cluster_centroids",
             "gbr_allpairs_fp64_static")
 
 
@@ -89,6 +89,8 @@ def load():
         L.gbr_write_cmatrix.argtypes = [vp, ctypes.c_char_p, vp, ci, i64, i32, vp, ci, ci, vp, i64, i64]
         L.gbr_superpose.restype = ci
         L.gbr_superpose.argtypes = [vp, vp, vp, ci, i64, i32, vp, vp, ci, vp, vp, vp, vp, vp, i32]
+        L.gbr_cluster_centroids.restype = ci
+        L.gbr_cluster_centroids.argtypes = [vp, vp, ci, i64, i32, vp, ci, vp, vp, i64, vp]
         L.gbr_allpairs_fp64_static.restype = ci
         L.gbr_allpairs_fp64_static.argtypes = [vp, ci, i64, i32, vp, ci, vp, vp]
         _lib = L
@@ -230,6 +232,30 @@ class Handle:
                                            _ptr(mass), m, _ptr(rmsd), _ptr(rot), _ptr(tt), _ptr(rt), _ptr(move),
                                            n_move))
         return rmsd, rot, tt, rt
+
+    def cluster_centroids(self, xyz, members, offsets, mass=None, mode="fit"):
+        """Cluster centroids (Metric_RMS::CalculateCentroid).
+
+        xyz: [frames, atoms, 3] (numpy or torch); members (int32) and
+        offsets (int64, [n_cluster + 1]): cluster c is members[offsets[c]:
+        offsets[c + 1]] in visiting order.  Returns [n_cluster, atoms, 3]
+        float64 of the same kind and device as ``xyz``."""
+        F, N = int(xyz.shape[0]), int(xyz.shape[1])
+        nc = int(offsets.shape[0]) - 1
+        m = MODES[mode] if isinstance(mode, str) else mode
+        if isinstance(xyz, np.ndarray):
+            members = np.ascontiguousarray(members, dtype=np.int32)
+            offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+            if mass is not None:
+                mass = np.ascontiguousarray(mass, dtype=np.float64)
+            out = np.zeros((max(nc, 0), N, 3), np.float64)
+        else:
+            import torch
+
+            out = torch.zeros((max(nc, 0), N, 3), dtype=torch.float64, device=xyz.device)
+        self._check(self.lib.gbr_cluster_centroids(self.h, _ptr(xyz), _dtype_code(xyz), F, N, _ptr(mass), m,
+                                                   _ptr(members), _ptr(offsets), nc, _ptr(out)))
+        return out
 
     def allpairs_batched(self, trajs, masses=None, mode="fit", precision="fp32"):
         """trajs: list of float32 [F_t, N_t, 3] arrays; returns list of TRI outputs."""

@@ -18,6 +18,7 @@
  *   gbr_write_cmatrix <- the pairwise-cache fill plus Cmatrix_Binary::WriteCmatrix
  *                        (savepairdist) in one call.
  *   gbr_superpose     <- the per-frame fit of the rms / align actions
+ *   gbr_cluster_centroids <- Metric_RMS::CalculateCentroid (cluster centroids)
  *                        (Action_Rmsd::DoAction, Action_Align::DoAction).
  *   gbr_rmsd_backward <- no reference counterpart (cpptraj has no gradient of
  *                        RMSD); dL/dx for L = sum_{i<j} g_ij RMSD_ij.
@@ -167,6 +168,31 @@ int gbr_rmsd_backward(gbr_handle *h, const float *xyz, int64_t n_frame, int32_t 
 int gbr_superpose(gbr_handle *h, const void *ref_xyz, const void *xyz, int dtype, int64_t n_frame,
                   int32_t n_atom, const double *ref_mass, const double *mass, int mode, double *rmsd,
                   double *rot, double *tgt_trans, double *ref_trans, void *move_xyz, int32_t n_move);
+
+/* Cluster centroids as Metric_RMS::CalculateCentroid builds them
+ * (src/Cluster/Metric_RMS.cpp:86-108), every cluster in one call.
+ *   xyz        n_frame frames of n_atom atoms (the metric's mask), dtype.
+ *   mass       masses (NULL => unweighted, the metric's useMass_ off).
+ *   mode       GBR_FIT: in member order, the first member centred starts a
+ *              running sum; each later member is centred, fitted onto the sum
+ *              (Frame::RMSD_CenteredRef), rotated and added.  GBR_NOFIT: the
+ *              plain sum of the members as given.
+ *   members    frame indices (0 <= index < n_frame) of all clusters back to
+ *              back, each cluster in the order the reference visits it
+ *              (its Cframes list);
+ *   offsets    [n_cluster + 1]: cluster c is members[offsets[c] ..
+ *              offsets[c + 1]).
+ *   centroids  [n_cluster][n_atom][3] FP64: the sum divided by the member
+ *              count.  An empty cluster's centroid is NaN (the reference's
+ *              has no atoms).
+ * Pointers may be host or device memory.  Per-atom sums are FP32 with the
+ * running sum kept as an FP32 hi + lo pair, the fit itself FP64: centroid
+ * coordinates agree with the reference's FP64 chain to ~1e-6 Angstrom.
+ * Frame indices out of range return GBR_ERR_ARG; a zero total mass with
+ * GBR_FIT returns GBR_ERR_ZERO_MASS. */
+int gbr_cluster_centroids(gbr_handle *h, const void *xyz, int dtype, int64_t n_frame, int32_t n_atom,
+                          const double *mass, int mode, const int32_t *members, const int64_t *offsets,
+                          int64_t n_cluster, double *centroids);
 
 /* All-pairs RMSD that allocates nothing.  No counterpart in the reference:
  * cpptraj's loops allocate host frames per thread; this entry point exists for

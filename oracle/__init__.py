@@ -60,6 +60,10 @@ def lib():
                                         ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.orc_cluster_centroids_f64.restype = ctypes.c_int
+        L.orc_cluster_centroids_f64.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int,
+                                                ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                                ctypes.c_int64, ctypes.c_void_p, ctypes.c_int]
         L.orc_max_threads.restype = ctypes.c_int
         L.orc_grad_f64.restype = ctypes.c_int
         L.orc_grad_f64.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p,
@@ -95,6 +99,10 @@ def ref_lib():
         L.ref_superpose.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int,
                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        L.ref_cluster_centroids.restype = ctypes.c_int
+        L.ref_cluster_centroids.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int,
+                                            ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_int64, ctypes.c_void_p]
         _ref = L
     return _ref
 
@@ -251,3 +259,39 @@ def superpose_f64(ref, xyz, ref_mass=None, mass=None, mode=FIT, move=None, nthre
         lib().orc_superpose_f64(_p(ref), _p(xyz), _dtype_code(ref), F, N, _p(ref_mass), _p(mass), mode, _p(rmsd),
                                 _p(rot), _p(tt), _p(rt), _p(mv), nm, nthreads)
     return rmsd, rot, tt, rt, mv
+
+
+def members_offsets(labels, n_cluster=None):
+    """Cluster member lists in the reference's visiting order (increasing frame
+    index within a cluster) from per-frame labels (-1 = noise, no cluster):
+    (members int32, offsets int64 [n_cluster + 1])."""
+    labels = np.asarray(labels)
+    if n_cluster is None:
+        n_cluster = int(labels.max()) + 1 if labels.size else 0
+    members = [np.flatnonzero(labels == c) for c in range(n_cluster)]
+    offsets = np.zeros(n_cluster + 1, np.int64)
+    offsets[1:] = np.cumsum([len(m) for m in members])
+    flat = np.concatenate(members) if members else np.zeros(0)
+    return flat.astype(np.int32), offsets
+
+
+def cluster_centroids_f64(xyz, members, offsets, mass=None, mode=FIT, nthreads=0, use_reference_code=False):
+    """Cluster centroids (Metric_RMS::CalculateCentroid): [n_cluster, N, 3]
+    FP64.  members / offsets as returned by members_offsets."""
+    xyz = np.ascontiguousarray(xyz)
+    F, N = xyz.shape[0], xyz.shape[1]
+    members = np.ascontiguousarray(members, dtype=np.int32)
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    nc = len(offsets) - 1
+    if mass is not None:
+        mass = np.ascontiguousarray(mass, dtype=np.float64)
+    out = np.zeros((nc, N, 3))
+    if use_reference_code:
+        rc = ref_lib().ref_cluster_centroids(_p(xyz), _dtype_code(xyz), F, N, _p(mass), mode, _p(members),
+                                             _p(offsets), nc, _p(out))
+    else:
+        rc = lib().orc_cluster_centroids_f64(_p(xyz), _dtype_code(xyz), F, N, _p(mass), mode, _p(members),
+                                             _p(offsets), nc, _p(out), nthreads)
+    if rc != 0:
+        raise ValueError("cluster centroids: error %d" % rc)
+    return out

@@ -137,3 +137,42 @@ extern "C" int ref_superpose(const void* ref_xyz, const void* xyz, int dtype, in
   }
   return 0;
 }
+
+// Cluster centroids with cpptraj's own Frame code, in the steps of
+// Metric_RMS::CalculateCentroid (src/Cluster/Metric_RMS.cpp:86-108): the first
+// member copied (and centred with CenterOnOrigin when fitting), each later
+// member fitted onto the running sum by RMSD_CenteredRef(sum, Rot, Trans),
+// rotated with Frame::Rotate and added with +=, the sum divided by the member
+// count.  Same argument meaning as orc_cluster_centroids_f64 (fit = mode 0,
+// nofit = mode 1); empty clusters are skipped.
+extern "C" int ref_cluster_centroids(const void* xyz, int dtype, int64_t n_frame, int n_atom, const double* mass,
+                                     int mode, const int32_t* members, const int64_t* offsets, int64_t n_cluster,
+                                     double* out) {
+  (void)n_frame;
+  const bool use_mass = (mass != nullptr), nofit = (mode == 1);
+  Frame frm = make(n_atom, mass);
+  for (int64_t c = 0; c < n_cluster; ++c) {
+    Frame cent;
+    for (int64_t k = offsets[c]; k < offsets[c + 1]; ++k) {
+      fill(frm, xyz, dtype, members[k], n_atom);
+      if (cent.empty()) {
+        cent = frm;
+        if (!nofit) cent.CenterOnOrigin(use_mass);
+      } else {
+        if (!nofit) {
+          Matrix_3x3 Rot;
+          Vec3 Trans;
+          frm.RMSD_CenteredRef(cent, Rot, Trans, use_mass);
+          frm.Rotate(Rot);
+        }
+        cent += frm;
+      }
+    }
+    const int64_t n = offsets[c + 1] - offsets[c];
+    if (n <= 0) continue;
+    cent.Divide((double)n);
+    const double* x = cent.xAddress();
+    for (int k = 0; k < 3 * n_atom; ++k) out[(size_t)c * 3 * n_atom + k] = x[k];
+  }
+  return 0;
+}

@@ -13,6 +13,8 @@
  *   - Frame::DISTRMSD                src/Frame.cpp:1313-1344 (rms2d `dme`)
  *   - Action_Rmsd / Action_Align per-frame fit, Frame::Trans_Rot_Trans
  *                                    (orc_superpose_f64)
+ *   - Metric_RMS::CalculateCentroid  src/Cluster/Metric_RMS.cpp:86-108
+ *                                    (orc_cluster_centroids_f64)
  *   - Frame::CenterOnOrigin          src/Frame.cpp:1043-1055, Frame.h:373-391
  *   - QCPRot::FastCalcRMSDAndRotation src/qcprot.cpp:167-246 (RMSD part) and
  *     do_quaternion_rmsd              src/QuaternionRMSD.cpp:25-120
@@ -507,6 +509,69 @@ int orc_superpose_f64(const void *ref_xyz, const void *xyz, int dtype, int64_t n
     free(T);
   }
   free(R);
+  return err;
+}
+
+/* Cluster centroids as Metric_RMS::CalculateCentroid builds them
+ * (src/Cluster/Metric_RMS.cpp:86-108), one cluster per thread.  Fit: in
+ * member order, the first frame centred (CenterOnOrigin) starts the running
+ * sum S; every later frame is centred and fitted onto S by
+ * RMSD_CenteredRef(S, U, Trans) -- S is not divided first, the rotation does
+ * not depend on its scale -- rotated about the origin (Frame::Rotate,
+ * src/Frame.h:508-517) and added (Frame::operator+=, src/Frame.cpp:901-910).
+ * No-fit: the plain sum of the frames as given.  The centroid is S / n
+ * (Frame::Divide, src/Frame.cpp:968-976).  members holds the frame indices of
+ * all clusters back to back, cluster c being members[offsets[c] ..
+ * offsets[c + 1]).  out: [n_cluster][n_atom][3]; an empty cluster's rows are
+ * NaN (the reference leaves a frame with no atoms).  Returns 1 for a bad
+ * argument (frame index out of range), 2 when a fit met a zero total mass. */
+int orc_cluster_centroids_f64(const void *xyz, int dtype, int64_t n_frame, int n_atom, const double *mass,
+                              int mode, const int32_t *members, const int64_t *offsets, int64_t n_cluster,
+                              double *out, int nthreads) {
+  if (n_atom < 1) return 1;
+  for (int64_t c = 0; c < n_cluster; ++c)
+    for (int64_t k = offsets[c]; k < offsets[c + 1]; ++k)
+      if (members[k] < 0 || members[k] >= n_frame) return 1;
+  int err = 0;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel reduction(| : err)
+#endif
+  {
+    double *T = (double *)malloc(sizeof(double) * 3 * (size_t)n_atom);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic)
+#endif
+    for (int64_t c = 0; c < n_cluster; ++c) {
+      double *S = out + (size_t)c * 3 * n_atom;
+      const int64_t n = offsets[c + 1] - offsets[c];
+      if (n <= 0) {
+        for (int k = 0; k < 3 * n_atom; ++k) S[k] = NAN;
+        continue;
+      }
+      for (int64_t k = 0; k < n; ++k) {
+        load_frame(xyz, dtype, members[offsets[c] + k], n_atom, T);
+        double tc[3] = {0.0, 0.0, 0.0}, U[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+        if (mode == ORC_FIT) {
+          if (k > 0 && fit_centered_ref(S, T, n_atom, mass, U) < 0.0) err |= 2;
+          orc_center(T, n_atom, mass, tc);
+        }
+        for (int a = 0; a < n_atom; ++a) {
+          const double x = T[3 * a] - tc[0], y = T[3 * a + 1] - tc[1], z = T[3 * a + 2] - tc[2];
+          const double r0 = x * U[0] + y * U[1] + z * U[2];
+          const double r1 = x * U[3] + y * U[4] + z * U[5];
+          const double r2 = x * U[6] + y * U[7] + z * U[8];
+          if (k == 0) {
+            S[3 * a] = r0; S[3 * a + 1] = r1; S[3 * a + 2] = r2;
+          } else {
+            S[3 * a] += r0; S[3 * a + 1] += r1; S[3 * a + 2] += r2;
+          }
+        }
+      }
+      for (int k = 0; k < 3 * n_atom; ++k) S[k] /= (double)n;
+    }
+    free(T);
+  }
   return err;
 }
 

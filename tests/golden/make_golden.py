@@ -27,6 +27,11 @@ Run in a container where the reference tree is mounted (default
    cpptraj's own code (RMSD_CenteredRef with rotation and translation, then
    Trans_Rot_Trans of a larger "move" atom set), mass-weighted and not, on
    seeded synthetic frames.
+5. ref_centroids.npz -- cluster centroids built by cpptraj's own Frame code in
+   the steps of Metric_RMS::CalculateCentroid (fit: RMSD_CenteredRef onto the
+   running sum, Rotate, +=, Divide; nofit: the plain sum), mass-weighted and
+   not, for seeded synthetic frames split into 5 clusters (one of them empty)
+   by seeded labels.
 """
 from __future__ import annotations
 
@@ -236,8 +241,25 @@ def make_ref_superpose():
     print("ref_superpose.npz:", X.shape, move.shape)
 
 
+def make_ref_centroids():
+    sys.path.insert(0, ROOT)
+    import oracle
+    from cpptraj_gb300 import synth
+
+    oracle.build(with_ref=True)
+    X, m = synth.trajectory(31, 90, 67, 0.3, 2.5, np.float32, True)
+    labels = np.random.default_rng(32).integers(-1, 4, 90)  # -1: noise; cluster 4 stays empty
+    members, offsets = oracle.members_offsets(labels, 5)
+    res = {"xyz": X, "mass": m, "members": members, "offsets": offsets}
+    for tag, mm, mode in (("fit_w", m, oracle.FIT), ("fit_u", None, oracle.FIT), ("nofit", None, oracle.NOFIT)):
+        res[tag] = oracle.cluster_centroids_f64(X, members, offsets, mass=mm, mode=mode, use_reference_code=True)
+    np.savez_compressed(os.path.join(HERE, "ref_centroids.npz"), **res)
+    print("ref_centroids.npz:", X.shape, offsets)
+
+
 if __name__ == "__main__":
     make_tz2()
     make_ref_pairs()
     make_cluster_cmatrix()
     make_ref_superpose()
+    make_ref_centroids()

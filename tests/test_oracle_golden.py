@@ -142,3 +142,23 @@ def test_superpose_matches_reference_code(wt):
     np.testing.assert_array_equal(rt, g[f"ref_trans_{wt}"])
     np.testing.assert_array_equal(mv, g[f"moved_{wt}"])
     assert r[5] < 1e-6  # the reference frame itself
+
+
+@pytest.mark.parametrize("tag", ["fit_w", "fit_u", "nofit"])
+def test_cluster_centroids_match_reference_code(tag):
+    """Cluster centroids: the restatement against cpptraj's own Frame code run
+    in the steps of Metric_RMS::CalculateCentroid (ref_centroids.npz)."""
+    g = np.load(os.path.join(GOLD, "ref_centroids.npz"))
+    m = g["mass"] if tag == "fit_w" else None
+    mode = oracle.NOFIT if tag == "nofit" else oracle.FIT
+    got = oracle.cluster_centroids_f64(g["xyz"], g["members"], g["offsets"], mass=m, mode=mode)
+    sizes = np.diff(g["offsets"])
+    np.testing.assert_allclose(got[sizes > 0], g[tag][sizes > 0], rtol=0, atol=1e-12)
+    assert np.all(np.isnan(got[sizes == 0]))
+    # a one-member cluster's centroid is that frame, centred when fitting
+    one = oracle.cluster_centroids_f64(g["xyz"], np.array([7], np.int32), np.array([0, 1]), mass=m, mode=mode)
+    want = g["xyz"][7].astype(np.float64)
+    if mode == oracle.FIT:
+        w = m if m is not None else np.ones(len(want))
+        want = want - (w[:, None] * want).sum(0) / w.sum()
+    np.testing.assert_allclose(one[0], want, rtol=0, atol=1e-12)

@@ -107,6 +107,10 @@ int gbr_set_option(gbr_handle* h, int key, double value) {
       if (value != 0.0 && value != 1.0) return h->fail(GBR_ERR_ARG, "host output mode must be 0 or 1");
       h->host_out_direct = value != 0.0;
       return GBR_OK;
+    case GBR_OPT_INPUT_OVERLAP:
+      if (value != 0.0 && value != 1.0) return h->fail(GBR_ERR_ARG, "input overlap must be 0 or 1");
+      h->input_overlap = value != 0.0;
+      return GBR_OK;
   }
   return h->fail(GBR_ERR_ARG, "unknown option %d", key);
 }
@@ -262,7 +266,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     p[22] = out_dev ? nullptr : A.take<float>(n_out);                   // out staging
     p[23] = tc ? A.take<__half_raw>((size_t)F * 3 * Np) : nullptr;      // hi
     p[24] = tc ? A.take<__half_raw>((size_t)F * 3 * Np) : nullptr;      // lo
-    p[25] = A.take<int>(1);                                             // device error flag
+    p[25] = A.take<int>(2);                                             // device error, speculation flags
     p[26] = tc ? A.take<int2>(tc_tiles) : nullptr;                      // tile list
     p[27] = need_planes ? A.take<float>((size_t)Kmax * 3 * Np) : nullptr;  // reference means
     p[28] = need_planes ? A.take<float>((size_t)Kmax * 64 * 3 * Np) : nullptr;  // chunk sums
@@ -292,26 +296,32 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
                         h->ensure_xfer();
   int n_chunks = 0;
   int64_t chunk_end[8];
+  struct ChunkCopy {
+    void* dst;
+    const void* src;
+    size_t bytes;
+  };
+  std::vector<ChunkCopy> chunk_copies;
   if (chunk_in) {
-    cudaEventRecord(h->xev[h->kXev - 1], st);  // the copies follow earlier work on the caller's stream
-    cudaStreamWaitEvent(h->xfer, h->xev[h->kXev - 1], 0);
-    auto add_chunks = [&](const void* src, void* dst, int64_t set0, int64_t nf, bool dev, int parts) {
+    auto plan_chunks = [&](const void* src, void* dst, int64_t set0, int64_t nf, bool dev, int parts) {
       for (int c = 0; c < parts; ++c) {
         const int64_t a = nf * c / parts, b = nf * (c + 1) / parts;
         if (b <= a) continue;
-        if (!dev)
-          cudaMemcpyAsync((char*)dst + esz * 3 * (size_t)N * a, (const char*)src + esz * 3 * (size_t)N * a,
-                          esz * 3 * (size_t)N * (b - a), cudaMemcpyHostToDevice, h->xfer);
-        cudaEventRecord(h->xev[n_chunks], h->xfer);
+        const size_t o = esz * 3 * (size_t)N * a;
+        chunk_copies.push_back({dev ? nullptr : (char*)dst + o, (const char*)src + o, esz * 3 * (size_t)N * (b - a)});
         chunk_end[n_chunks++] = set0 + b;
       }
     };
-    add_chunks(ref_xyz, P[0], 0, n_ref, ref_dev, tgt_xyz ? 4 : 8);
-    if (tgt_xyz) add_chunks(tgt_xyz, P[1], n_ref, n_tgt, tgt_dev, 4);
+    plan_chunks(ref_xyz, P[0], 0, n_ref, ref_dev, tgt_xyz ? 4 : 8);
+    if (tgt_xyz) plan_chunks(tgt_xyz, P[1], n_ref, n_tgt, tgt_dev, 4);
   } else {
     if (!ref_dev) cudaMemcpyAsync(P[0], ref_xyz, esz * 3 * (size_t)N * n_ref, cudaMemcpyDefault, st);
     if (tgt_xyz && !tgt_dev) cudaMemcpyAsync(P[1], tgt_xyz, esz * 3 * (size_t)N * n_tgt, cudaMemcpyDefault, st);
   }
+  // Copies from pageable memory (weights, tile list) go before the chunk
+  // copies are queued: a pageable copy returns only once it has been done,
+  // and behind the queued chunks that would hold the host until the whole
+  // input has landed.
   double* d_w = tgt_mass ? (double*)P[2] : nullptr;
   double* d_wref = nullptr;
   if (tgt_mass) {
@@ -321,8 +331,49 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
       cudaMemcpyAsync(d_wref, wref_h.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st);
     }
   }
+  // Chunked input of one frame set, triangle into device (or mapped host)
+  // memory: the contraction also runs speculatively, stage by stage.  The
+  // tiles are grouped by the first chunk that completes the frames they read
+  // (grouped order kept within a stage); when prep has built the operands
+  // through a chunk, the tiles ready by then are launched behind it.
+  const int tc_variant = (h->tc_variant >= 0) ? h->tc_variant : (N >= kDeepStageAtoms ? 3 : 2);
+  bool overlap = h->input_overlap && n_chunks > 0 && tc && map.tri && !tgt_xyz && out_dev;
+  std::vector<int64_t> stage_off;
+  std::vector<int2> stage_tiles;
+  if (overlap) {
+    TcTileInfo info;
+    std::vector<int2> tiles;
+    const int64_t nt = tc_build_tile_list(map, tiles, info, tc_variant);
+    if (nt > tc_tiles) {
+      overlap = false;
+    } else {
+      std::vector<int> stage(nt);
+      stage_off.assign(n_chunks + 1, 0);
+      for (int64_t t = 0; t < nt; ++t) {
+        const int64_t fe = std::min(tc_tile_frame_end(info, tiles[t], tc_variant), F);
+        int c = 0;
+        while (c < n_chunks - 1 && chunk_end[c] < fe) ++c;
+        stage[t] = c;
+        stage_off[c + 1]++;
+      }
+      for (int c = 0; c < n_chunks; ++c) stage_off[c + 1] += stage_off[c];
+      stage_tiles.resize(nt);
+      std::vector<int64_t> fill(stage_off.begin(), stage_off.end() - 1);
+      for (int64_t t = 0; t < nt; ++t) stage_tiles[fill[stage[t]]++] = tiles[t];
+      if (nt > 0) cudaMemcpyAsync(P[26], stage_tiles.data(), sizeof(int2) * nt, cudaMemcpyHostToDevice, st);
+    }
+  }
+  if (chunk_in) {
+    cudaEventRecord(h->xev[h->kXev - 1], st);  // the copies follow earlier work on the caller's stream
+    cudaStreamWaitEvent(h->xfer, h->xev[h->kXev - 1], 0);
+    for (int c = 0; c < n_chunks; ++c) {
+      const ChunkCopy& cc = chunk_copies[c];
+      if (cc.dst) cudaMemcpyAsync(cc.dst, cc.src, cc.bytes, cudaMemcpyHostToDevice, h->xfer);
+      cudaEventRecord(h->xev[c], h->xfer);
+    }
+  }
   cudaMemsetAsync(P[21], 0, sizeof(unsigned long long) * kMaxBands, st);
-  cudaMemsetAsync(P[25], 0, sizeof(int), st);
+  cudaMemsetAsync(P[25], 0, 2 * sizeof(int), st);
 
   map.out = out_dev ? out_k : (float*)P[22];
 
@@ -421,62 +472,112 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     fa.w = d_w;
     fa.nofit = nofit;
     fa.RP = (float*)P[17];
+    // Per-frame terms as the pair kernels read them, for K references (sorted:
+    // reference-grouped operand positions).
+    auto make_terms = [&](int Kt, bool sorted) {
+      FrameTerms t{};
+      t.assign = sorted ? prep_carve(pa.scratch, F, N, Kmax).assign_pos : pa.assign;
+      t.nrm = (float*)P[14];
+      t.P = (float*)P[15];
+      t.trP = (float*)P[16];
+      t.RP = (float*)P[17];
+      t.K = Kt;
+      t.W = (float)Wsum;
+      t.two_over_w = (float)(2.0 / (double)Wsum);
+      t.tol = (float)h->tol;
+      // FP32 FMA accumulation: 3-sigma random walk of half-ulp roundings (x2
+      // margin), ~1.2e-7 sqrt(N) |tr D|.  Tensor memory: the FP16 hi+lo split
+      // represents each product to ~2^-22 (taken coherent), and accumulation
+      // measured on correlated frames behaves like truncation, about
+      // eps/2 per add over 3N/16 adds: ~5.6e-9 N |tr D|, bounded with x2 margin.
+      t.gem_s = tc ? 6.0e-7f : 1.2e-7f;
+      t.gem_c = tc ? 1.2e-8f * (float)N : 1.2e-7f * std::sqrt((float)N);
+      t.epi_coef = 8e-7f;
+      t.nofit = nofit;
+      return t;
+    };
+    // One tensor-core launch: over the tiles of map m, or (n_ready > 0) over
+    // n_ready tiles already in the tile buffer from tile0 on.
+    auto launch_tc = [&](const OutMap& m, const FlagList& f, const FrameTerms& t, int64_t tile0, int64_t n_ready,
+                         const int* skip) -> cudaError_t {
+      TcLaunch L{};
+      L.hi = P[23];
+      L.lo = P[24];
+      L.tile_buf = (int2*)P[26] + tile0;
+      L.tile_cap = tc_tiles - tile0;
+      L.ready_tiles = n_ready;
+      L.F = F;
+      L.Np = Np;
+      L.N = N;
+      L.tgt0 = tgt0;
+      L.inv_scale = (const float*)P[13];
+      L.terms = t;
+      L.map = m;
+      L.flags = f;
+      L.dev_error = (int*)P[25];
+      L.num_sms = h->num_sms;
+      L.variant = tc_variant;
+      L.row_stores = 1;
+      L.skip = skip;
+      return run_pairs_tc(L, st);
+    };
+    // Speculative stages (see above): launched from prep through on_built.
+    // Each launch exits at once if a chunk check has already seen a frame
+    // farther than tau from reference 0; if the final reference count is not
+    // one, everything is recomputed below.
+    const FrameTerms terms1 = make_terms(1, false);
+    int next_stage = 0;
+    bool spec_terms = false;
+    std::function<cudaError_t(int64_t)> on_built = [&](int64_t built_end) -> cudaError_t {
+      int c1 = next_stage;
+      while (c1 < n_chunks && chunk_end[c1] <= built_end) ++c1;
+      if (c1 == next_stage) return cudaSuccess;
+      const int64_t t0 = stage_off[next_stage], t1 = stage_off[c1];
+      next_stage = c1;
+      if (t1 == t0) return cudaSuccess;
+      cudaError_t e2;
+      if (!spec_terms) {  // reference-pair terms of reference 0, as run_finish computes them
+        FinishArgs f1 = fa;
+        f1.K = 1;
+        f1.built = 1;
+        f1.sorted = 0;
+        if ((e2 = run_finish(f1, st)) != cudaSuccess) return e2;
+        spec_terms = true;
+        ++launches;
+        if (h->timing) cudaEventRecord(h->ev[1], st);
+      }
+      FlagList fl{(int2*)P[20], (unsigned long long*)P[21], flag_cap};
+      e2 = launch_tc(map, fl, terms1, t0, t1 - t0, (const int*)P[25] + 1);
+      ++launches;
+      return e2;
+    };
+    if (overlap) {
+      pa.on_built = &on_built;
+      pa.spec_fail = (int*)P[25] + 1;
+    }
     if (n_chunks > 0) pa.spec_build = &fa;
     PrepOut po;
     if ((e = run_prep(pa, po, st)) != cudaSuccess) return h->cuda_fail(e, "prep");
     launches += po.launches;
     K = po.K;
+    // Every stage was launched by the time the last chunk was built; the
+    // speculation stands when prep kept its one-reference build.
+    const bool spec_done = overlap && po.built && spec_terms;
+    if (overlap && !spec_done)
+      cudaMemsetAsync(P[21], 0, sizeof(unsigned long long) * kMaxBands, st);  // discard speculative flags
     OutMap pmap = map;  // the pair kernels' view: sorted positions when po.sorted
-    FrameTerms terms{};
-    terms.assign = pa.assign;
-    if (po.sorted) {
-      pmap.perm = pa.order;
-      terms.assign = prep_carve(pa.scratch, F, N, Kmax).assign_pos;
-    }
-    terms.nrm = (float*)P[14];
-    terms.P = (float*)P[15];
-    terms.trP = (float*)P[16];
-    terms.RP = (float*)P[17];
-    terms.K = K;
-    terms.W = (float)Wsum;
-    terms.two_over_w = (float)(2.0 / (double)Wsum);
-    terms.tol = (float)h->tol;
-    // FP32 FMA accumulation: 3-sigma random walk of half-ulp roundings (x2
-    // margin), ~1.2e-7 sqrt(N) |tr D|.  Tensor memory: the FP16 hi+lo split
-    // represents each product to ~2^-22 (taken coherent), and accumulation
-    // measured on correlated frames behaves like truncation, about
-    // eps/2 per add over 3N/16 adds: ~5.6e-9 N |tr D|, bounded with x2 margin.
-    terms.gem_s = tc ? 6.0e-7f : 1.2e-7f;
-    terms.gem_c = tc ? 1.2e-8f * (float)N : 1.2e-7f * std::sqrt((float)N);
-    terms.epi_coef = 8e-7f;
-    terms.nofit = nofit;
+    if (po.sorted) pmap.perm = pa.order;
+    const FrameTerms terms = make_terms(K, po.sorted != 0);
     fa.sorted = po.sorted;
     fa.K = K;
     fa.built = po.built;
-    if ((e = run_finish(fa, st)) != cudaSuccess) return h->cuda_fail(e, "finish");
-    launches += po.built ? 1 : 2;
+    if (!spec_done) {
+      if ((e = run_finish(fa, st)) != cudaSuccess) return h->cuda_fail(e, "finish");
+      launches += po.built ? 1 : 2;
+    }
     // One launch of the pair kernel over the rows of map m.
     auto launch_pairs = [&](const OutMap& m, const FlagList& f) -> cudaError_t {
-      if (tc) {
-        TcLaunch L{};
-        L.hi = P[23];
-        L.lo = P[24];
-        L.tile_buf = P[26];
-        L.tile_cap = tc_tiles;
-        L.F = F;
-        L.Np = Np;
-        L.N = N;
-        L.tgt0 = tgt0;
-        L.inv_scale = (const float*)P[13];
-        L.terms = terms;
-        L.map = m;
-        L.flags = f;
-        L.dev_error = (int*)P[25];
-        L.num_sms = h->num_sms;
-        L.variant = (h->tc_variant >= 0) ? h->tc_variant : (N >= kDeepStageAtoms ? 3 : 2);
-        L.row_stores = 1;
-        return run_pairs_tc(L, st);
-      }
+      if (tc) return launch_tc(m, f, terms, 0, 0, nullptr);
       PairLaunch L{};
       L.plane = pa.plane;
       L.Np = Np;
@@ -488,7 +589,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
       L.tiles = make_tiles(m, 64, 64);
       return run_pairs_fp32(L, st);
     };
-    if (h->timing) cudaEventRecord(h->ev[1], st);
+    if (h->timing && !spec_done) cudaEventRecord(h->ev[1], st);
     // A large result bound for pinned host memory leaves in row bands: each
     // band's pairs are computed and checked (FP64 re-check of its flagged
     // pairs, list length read on the device), then copied on the copy stream
@@ -498,8 +599,10 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     int derr = 0;
     if (!band_out) {
       FlagList fl{(int2*)P[20], (unsigned long long*)P[21], flag_cap};
-      if ((e = launch_pairs(pmap, fl)) != cudaSuccess) return h->cuda_fail(e, "pair kernel launch");
-      ++launches;
+      if (!spec_done) {
+        if ((e = launch_pairs(pmap, fl)) != cudaSuccess) return h->cuda_fail(e, "pair kernel launch");
+        ++launches;
+      }
       if (h->timing) cudaEventRecord(h->ev[2], st);
       cudaMemcpyAsync(&nflag, P[21], sizeof nflag, cudaMemcpyDeviceToHost, st);
       cudaMemcpyAsync(&derr, P[25], sizeof derr, cudaMemcpyDeviceToHost, st);

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <functional>
 #include <vector>
 
 #include "gbr_common.cuh"
@@ -53,6 +54,14 @@ struct PrepArgs {
   // With chunks: the operand build for one reference (K = 1, unsorted), run
   // speculatively while the chunks land (PrepOut::built reports success).
   const struct FinishArgs* spec_build;
+  // With spec_build: called on the host after each chunk's operands are
+  // enqueued, with the end of the frame range [0, end) built so far (work the
+  // caller enqueues there runs between the chunks' prep passes).
+  const std::function<cudaError_t(int64_t)>* on_built;
+  // With spec_build: an int on the device, set to 1 by the chunk checks once
+  // a scanned frame is farther than tau from reference 0 (the speculation
+  // will fail); work enqueued through on_built may test it.
+  int* spec_fail;
 };
 
 // Further per-call prep buffers, carved from PrepArgs::scratch.
@@ -174,12 +183,16 @@ struct TcLaunch {
                      // 3: pairs of SMs, 64-atom stages x 3, 4-frame epilogue chunks
   int64_t ready_tiles;  // > 0: tile_buf already holds this many tiles (no host build or copy)
   int row_stores;       // pair kernels, triangle output: gather each tile's results and store whole rows
+  const int* skip;      // device int or nullptr: when it reads non-zero at launch, the kernel does nothing
 };
 // Tile list of the tensor-core kernel for this map (host side).
 struct TcTileInfo {
   int64_t i_base, jt_base, i_end, jt_end;
 };
 int64_t tc_build_tile_list(const OutMap& m, std::vector<int2>& tiles, TcTileInfo& info, int variant = 1);
+// Frame range [0, end) a tile of this list reads (reference and target rows),
+// for launching tiles as their frames become ready; unclamped.
+int64_t tc_tile_frame_end(const TcTileInfo& info, int2 tile, int variant);
 cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st);
 int tc_supported(int device);
 int64_t tc_max_tiles(const OutMap& m);

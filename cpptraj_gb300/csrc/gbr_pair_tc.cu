@@ -118,6 +118,7 @@ struct TcParams {
   FlagList flags;
   int* err;
   int row_stores;  // triangle results gathered into whole tile rows before the store (pair kernels)
+  const int* skip;  // non-null and non-zero at launch: the kernel returns at once
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -410,6 +411,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                const TcParams P) {
   constexpr int STAGES = PP::STAGES, KA = PP::KA, STAGE_BYTES = PP::STAGE_BYTES, A_BYTES = PP::A_BYTES,
                 B_BYTES = PP::B_BYTES, A_TX = PP::A_TX, B_TX = PP::B_TX;
+  if (P.skip && *P.skip != 0) return;  // a speculative launch whose speculation failed
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* stage_base = smem;
@@ -641,6 +643,9 @@ __global__ void __launch_bounds__(THREADS, 1)
   constexpr int KA2 = PC::KA2, STAGES2 = PC::STAGES2, A2_BYTES = PC::A2_BYTES, BH_BYTES = PC::BH_BYTES,
                 A2_TX = PC::A2_TX, BH_TX = PC::BH_TX, STAGE2_BYTES = PC::STAGE2_BYTES,
                 STAGING_BYTES = PC::E::STAGING_BYTES, EPI_BYTES = PC::EPI2_BYTES;
+  // Speculative launches: every CTA reads the same flag, written by kernels
+  // earlier in the stream, so both CTAs of a pair leave before any barrier.
+  if (P.skip && *P.skip != 0) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* stage_base = smem;
@@ -844,6 +849,12 @@ int64_t tc_build_tile_list(const OutMap& m, std::vector<int2>& tiles, TcTileInfo
   return tc_build_tiles(m, tiles, info.i_base, info.jt_base, info.i_end, info.jt_end, variant >= 2 ? TI2 : TI);
 }
 
+int64_t tc_tile_frame_end(const TcTileInfo& info, int2 tile, int variant) {
+  const int64_t i1 = info.i_base + (int64_t)(tile.x + 1) * (variant >= 2 ? TI2 : TI);
+  const int64_t j1 = info.jt_base + (int64_t)(tile.y + 1) * TJ;
+  return std::max(i1, j1);
+}
+
 // Launch of the pair-of-SMs kernel: clusters of two CTAs, as many clusters
 // as can be resident at once (one CTA per SM), at most one per tile.
 template <class PC>
@@ -924,6 +935,7 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
   P.flags = L.flags;
   P.err = L.dev_error;
   P.row_stores = L.row_stores;
+  P.skip = L.skip;
   if (pair) {
     e = (L.variant == 3) ? launch_pair_kernel<PairDeep>(mAh, mAl, mBh, mBl, P, st)
                          : launch_pair_kernel<PairShallow>(mAh, mAl, mBh, mBl, P, st);

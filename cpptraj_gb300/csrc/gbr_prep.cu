@@ -248,6 +248,17 @@ __device__ __forceinline__ int chunk_head(const float* src, int n) {
   return head > n ? n : head;
 }
 
+// Warms this SM's L1 with a per-atom table every warp of the block reads:
+// the block's warps start on atom 0 together, and without this each of them
+// would miss on the same lines at once.  Fire and forget -- the lines land
+// while the warps wait for their first staged coordinates.
+__device__ __forceinline__ void prefetch_l1(const void* p, size_t bytes) {
+  if (!p) return;
+  const char* c = (const char*)p;
+  for (size_t o = (size_t)threadIdx.x * 128; o < bytes; o += (size_t)blockDim.x * 128)
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(c + o));
+}
+
 template <typename T>
 struct WarpPipe {
   FrameSrc<T> src;
@@ -560,6 +571,19 @@ __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64
   const int64_t f_stride = (int64_t)gridDim.x * kWarps;
   WarpPipe<T> pipe;
   pipe.init(src, f_first, F, f_stride, sbuf[threadIdx.x >> 5], lane);
+  {
+    const size_t n4 = (size_t)N * 4;
+    prefetch_l1(s.sqwf, n4);
+    prefetch_l1(s.swr, 3 * n4);
+    if (FIRST) {
+      prefetch_l1(s.cm_ref, n4);
+      prefetch_l1(s.cml_ref, n4);
+      if (s.cm_tgt != s.cm_ref && f_begin + (int64_t)gridDim.x * kWarps > src.n_ref) {
+        prefetch_l1(s.cm_tgt, n4);
+        prefetch_l1(s.cml_tgt, n4);
+      }
+    }
+  }
   for (int64_t f = f_first; f < F; f += f_stride) {
     const T* x = src.frame(f);
     const bool in_ref = f < src.n_ref;
@@ -583,7 +607,7 @@ __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64
     for (int q = 0; q < 16; ++q) v[q] = 0.0f;
     float umax = 0.0f;
     pipe.for_each_atom(f, lane, [&](int a, int a0, const float* xs) {
-      const float sw = s.sqwf ? s.sqwf[a] : 1.0f;
+      const float sw = s.sqwf ? __ldg(s.sqwf + a) : 1.0f;
       float xh[3], xl[3], u[3], ue[3];
       fetch_atom(x, xs, a, a0, xh, xl);
       two_sum(xh[0], -o0, u[0], ue[0]);
@@ -591,7 +615,7 @@ __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64
       two_sum(xh[2], -o2, u[2], ue[2]);
       ue[0] += xl[0]; ue[1] += xl[1]; ue[2] += xl[2];
       const float u0 = u[0], u1 = u[1], u2 = u[2];
-      const float r0 = s.swr[3 * a], r1 = s.swr[3 * a + 1], r2 = s.swr[3 * a + 2];
+      const float r0 = __ldg(s.swr + 3 * a), r1 = __ldg(s.swr + 3 * a + 1), r2 = __ldg(s.swr + 3 * a + 2);
       const float y0 = sw * u0, y1 = sw * u1, y2 = sw * u2;
       if (fit) {
         v[0] += y0 * r0; v[1] += y0 * r1; v[2] += y0 * r2;
@@ -604,8 +628,8 @@ __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64
       }
       if (FIRST) {
         if (fit) {
-          const float c = cm ? cm[a] : 1.0f;
-          const float cl = cm ? cml[a] : 0.0f;
+          const float c = cm ? __ldg(cm + a) : 1.0f;
+          const float cl = cm ? __ldg(cml + a) : 0.0f;
 #pragma unroll
           for (int p = 0; p < 3; ++p) {
             float pt, pe, q;
@@ -614,7 +638,7 @@ __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64
             ce[p] += q + fmaf(c, ue[p], fmaf(cl, u[p], pe));
           }
           if (!same_w) {
-            const float wa = s.wf ? s.wf[a] : 1.0f;
+            const float wa = s.wf ? __ldg(s.wf + a) : 1.0f;
             v[13] += wa * u0; v[14] += wa * u1; v[15] += wa * u2;
           }
         }
@@ -703,6 +727,16 @@ __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64
     }
   }
   pipe.drain();
+}
+
+// Speculation check of one chunk: fail = 1 once a frame of [f0, f1) is
+// farther than tau from reference 0 (the test the reference-count decision
+// applies to the maximum over all frames).
+__global__ void __launch_bounds__(256) k_spec_check(const float* dist, int64_t f0, int64_t f1, float tau,
+                                                    int* fail) {
+  bool far = false;
+  for (int64_t f = f0 + threadIdx.x; f < f1; f += 256) far |= (dist[f] > tau);
+  if (__syncthreads_or(far) && threadIdx.x == 0) *fail = 1;
 }
 
 // Single-block argmax of dist[0..F): out_val, out_idx (lowest index on ties).
@@ -893,6 +927,9 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
   const int64_t f_stride = (int64_t)gridDim.x * kWarps;
   WarpPipe<T> pipe;
   pipe.init(src, f_first, F, f_stride, sbuf[threadIdx.x >> 5], lane);
+  prefetch_l1(b.sqwf, (size_t)N * 4);
+  prefetch_l1(b.refhl, (size_t)N * 24);  // reference 0 (the only one when K = 1)
+  prefetch_l1(b.swr, (size_t)N * 12);
   for (int64_t f = f_first; f < F; f += f_stride) {
     const T* x = src.frame(f);
     const int ra = b.assign[f];
@@ -919,10 +956,10 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
     pipe.for_each_atom(f, lane, [&](int a, int a0, const float* xs) {
         float xh[3], xl[3], v[3];
         fetch_atom(x, xs, a, a0, xh, xl);
-        const float sw = b.sqwf ? b.sqwf[a] : 1.0f;
+        const float sw = b.sqwf ? __ldg(b.sqwf + a) : 1.0f;
 #pragma unroll
         for (int p = 0; p < 3; ++p) {
-          const float2 r = rr[3 * a + p];
+          const float2 r = __ldg(rr + 3 * a + p);
           v[p] = sw * dot2_row(Tb.Rh + 3 * p, Tb.Rl + 3 * p, Tb.th[p], Tb.tl[p], xh, xl, r.x, r.y);
         }
 #pragma unroll
@@ -938,7 +975,7 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
           if (b.write_plane) b.plane[base + (size_t)p * Np + a] = v[p];
           acc[9] += v[p] * v[p];
         }
-        const float c0 = r0[3 * a], c1 = r0[3 * a + 1], c2 = r0[3 * a + 2];
+        const float c0 = __ldg(r0 + 3 * a), c1 = __ldg(r0 + 3 * a + 1), c2 = __ldg(r0 + 3 * a + 2);
         acc[0] += v[0] * c0; acc[1] += v[0] * c1; acc[2] += v[0] * c2;
         acc[3] += v[1] * c0; acc[4] += v[1] * c1; acc[5] += v[1] * c2;
         acc[6] += v[2] * c0; acc[7] += v[2] * c1; acc[8] += v[2] * c2;
@@ -1138,6 +1175,10 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
       if (f1 > f0) {
         k_scan<T, true><<<prep_grid(f1 - f0, kScanBlocksPerSM), kPrepThreads, 0, st>>>(src, f0, f1, sa);
         ++launches;
+        if (A.spec_build && A.spec_fail && A.max_refs > 1 && F > 1) {
+          k_spec_check<<<1, 256, 0, st>>>(A.dist, f0, f1, (float)A.tau, A.spec_fail);
+          ++launches;
+        }
         if (A.spec_build) {
           const int64_t b0 = refined ? f0 : 0;
           if (refined || f1 >= nsample) {
@@ -1156,6 +1197,10 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
           if (refined) {
             k_build<T><<<prep_grid(f1 - b0, kBuildBlocksPerSM), kPrepThreads, 0, st>>>(src, b0, f1, bspec);
             ++launches;
+            if (A.on_built) {
+              const cudaError_t e = (*A.on_built)(f1);
+              if (e != cudaSuccess) return e;
+            }
           }
         }
       }

@@ -21,7 +21,7 @@ GBR_F32, GBR_F64 = 0, 1
 FIT, NOFIT, DME = 0, 1, 2
 TRI, FULL = 0, 1
 PREC_FP32, PREC_TC, PREC_FP64 = 0, 1, 2
-OPT_TAU, OPT_MAX_REFS, OPT_TOL, OPT_TIMING, OPT_TC_PIPELINE, OPT_HOST_OUT = 0, 1, 2, 3, 4, 5
+OPT_TAU, OPT_MAX_REFS, OPT_TOL, OPT_TIMING, OPT_TC_PIPELINE, OPT_HOST_OUT, OPT_INPUT_OVERLAP = 0, 1, 2, 3, 4, 5, 6
 #: The library's default tensor-core kernel shape (pairs of SMs).
 TC_PIPELINE_DEFAULT = -1  # automatic: deep stages from 1,280 atoms (device results), shallow otherwise
 

@@ -297,8 +297,9 @@ def test_qrmsd_maps_to_fit(h, precision):
     assert np.abs(out.astype(np.float64) - refp["tri_qcp"]).max() <= tol
 
 
+@pytest.mark.parametrize("overlap", [0, 1])
 @pytest.mark.parametrize("sig_hi,expect_refs", [(1.0, 1), (6.0, None)])
-def test_pinned_input_speculative_prep(h, sig_hi, expect_refs):
+def test_pinned_input_speculative_prep(h, sig_hi, expect_refs, overlap):
     # Chunked pinned host input: the operands are built for one reference as
     # the chunks land.  Tight frames keep that build (one reference); spread
     # frames need more references, and the call falls back to the general
@@ -309,10 +310,43 @@ def test_pinned_input_speculative_prep(h, sig_hi, expect_refs):
     refs_dev = h.stats()["n_refs"]
     hX = torch.from_numpy(X).pin_memory()
     hout = torch.empty(dev.size, dtype=torch.float32).pin_memory()
-    run(h, hX, tgt_mass=m, precision="tc", out=hout)
+    h.set_option(gbrmsd.OPT_INPUT_OVERLAP, overlap)
+    try:
+        run(h, hX, tgt_mass=m, precision="tc", out=hout)
+    finally:
+        h.set_option(gbrmsd.OPT_INPUT_OVERLAP, 0)
     assert h.stats()["n_refs"] == refs_dev
     if expect_refs is not None:
         assert refs_dev == expect_refs
     else:
         assert refs_dev > 1
     np.testing.assert_array_equal(hout.numpy(), dev)
+
+
+def test_pinned_input_late_speculation_failure(h):
+    # With GBR_OPT_INPUT_OVERLAP the contraction starts on the chunks that
+    # have landed; a far frame in the last chunk ends the speculation after
+    # several stages already ran.  Their results are discarded and the general
+    # path recomputes the whole triangle: bit-identical to the device-resident
+    # call.
+    torch = pytest.importorskip("torch")
+    X, m = synth.trajectory(93, 3000, 1000, 0.1, 0.5, np.float32, True)
+    Y, _ = synth.trajectory(94, 40, 1000, 0.1, 0.5, np.float32, True)
+    X[2960:] = Y  # another chain: far more than tau from frame 0
+    dev = run(h, torch.from_numpy(X).cuda(), tgt_mass=m, precision="tc").cpu().numpy()
+    assert h.stats()["n_refs"] > 1
+    hX = torch.from_numpy(X).pin_memory()
+    hout = torch.empty(dev.size, dtype=torch.float32).pin_memory()
+    h.set_option(gbrmsd.OPT_INPUT_OVERLAP, 1)
+    try:
+        run(h, hX, tgt_mass=m, precision="tc", out=hout)
+        np.testing.assert_array_equal(hout.numpy(), dev)
+        # one reference allowed: the speculation always stands
+        h.set_option(gbrmsd.OPT_MAX_REFS, 1)
+        dev1 = run(h, torch.from_numpy(X).cuda(), tgt_mass=m, precision="tc").cpu().numpy()
+        run(h, hX, tgt_mass=m, precision="tc", out=hout)
+        assert h.stats()["n_refs"] == 1
+        np.testing.assert_array_equal(hout.numpy(), dev1)
+    finally:
+        h.set_option(gbrmsd.OPT_MAX_REFS, 32)
+        h.set_option(gbrmsd.OPT_INPUT_OVERLAP, 0)

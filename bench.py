@@ -47,6 +47,8 @@ def parse():
                     help="tensor-core kernel shape (GBR_OPT_TC_PIPELINE); default: the library's")
     ap.add_argument("--profile", action="store_true",
                     help="warm up, then run exactly one all-pairs call (for ncu); prints stats only")
+    ap.add_argument("--host-io", action="store_true",
+                    help="with --profile: pinned host input and output (the e2e path) instead of HBM")
     ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4", "dme", "rms", "centroids", "accuracy"],
                     help="c1 = the headline metric; c2/c3/c4/dme print secondary lines for the other configs")
     return ap.parse_args()
@@ -361,15 +363,20 @@ def main_profile(args):
     h = gbrmsd.Handle(0)
     _apply_pipeline(h, args)
     prec = "tc" if args.precision == "auto" else args.precision
-    dX = torch.from_numpy(X).cuda()
-    out = torch.empty(pairs, dtype=torch.float32, device="cuda")
+    if args.host_io:
+        dX = torch.from_numpy(X).pin_memory()
+        out = torch.empty(pairs, dtype=torch.float32).pin_memory()
+    else:
+        dX = torch.from_numpy(X).cuda()
+        out = torch.empty(pairs, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
         h.allpairs(dX, tgt_mass=m, precision=prec, out=out)
     torch.cuda.synchronize()
     h.set_option(gbrmsd.OPT_TIMING, 1)
     h.allpairs(dX, tgt_mass=m, precision=prec, out=out)
     torch.cuda.synchronize()
-    print(json.dumps({"profile_call": h.stats(), "frames": X.shape[0], "atoms": X.shape[1], "precision": prec}))
+    print(json.dumps({"profile_call": h.stats(), "frames": X.shape[0], "atoms": X.shape[1], "precision": prec,
+                      "io": "pinned host" if args.host_io else "HBM"}))
 
 
 def dist_env():

@@ -26,7 +26,8 @@
 //             made an FP64 solve ~8 us);
 //   sweep 2   per atom: S += U y.
 // FP32 frames come through a shared-memory ring (cp.async, three members
-// ahead), so the chain does not wait on DRAM.
+// ahead), so the chain does not wait on DRAM.  Sweep 2 of step k runs fused
+// with sweep 1 of step k + 1 (one pass over the atoms per step).
 // Per-atom arithmetic is FP32 (GB300's FP64 rate would make the two sweeps
 // FP64-pipe bound); S is kept as an unevaluated FP32 sum hi + lo (TwoSum), so
 // adding thousands of members loses nothing to rounding; the solve and the
@@ -44,10 +45,10 @@
 namespace gbr {
 namespace {
 
-constexpr int kCenThreads = 256;
-constexpr int kCenWarps = kCenThreads / 32;
-constexpr int kCenNV = 14;  // covariance 9, sum w|y|^2, sum w|S|^2, next centre 3
-constexpr int kRing = 4;           // staged members: k, k + 1 in use, k + 2, k + 3 in flight
+constexpr int kChainWarps = 7;   // fitted chain: 6 sweeping warps + the solving warp
+constexpr int kSolverWarp = 3;
+constexpr int kRing = 8;           // staged members: k - 1, k, k + 1 in use, k + 2 .. k + 4 in flight
+constexpr int kAhead = 3;          // members in flight beyond the ones in use
 constexpr int kExactSteps = 32;    // chain steps solved in FP64
 constexpr size_t kStageMaxBytes = 200 * 1024;
 constexpr int kSumThreads = 256;   // no-fit: one thread per centroid coordinate
@@ -58,6 +59,7 @@ struct CenArgs {
   const int64_t* offsets;  // [n_cluster + 1]
   const float* w;          // [N] masses, nullptr = unweighted
   double inv_W;            // 1 / sum of w (or 1 / N)
+  float inv_Wf;            // the same in FP32 (per-step centres: FP32 sums, no FP64 on the chain)
   int N;
   float2* S;               // [n_cluster][3N] running sums, hi + lo (when not in shared memory)
   double* out;             // [n_cluster][N][3]
@@ -80,48 +82,6 @@ __device__ __forceinline__ void load3(const T* x, int i, float (&v)[3]) {
 }
 
 __device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000LL); }
-
-// Sum of kCenNV floats over the block; the totals land in tot[] (visible to
-// every thread after the call).  red: [kCenWarps][16].
-__device__ __forceinline__ void block_sum_nv(float (&v)[kCenNV], float (*red)[16], float* tot) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < kCenNV; ++k)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-  if (lane == 0) {
-#pragma unroll
-    for (int k = 0; k < kCenNV; ++k) red[warp][k] = v[k];
-  }
-  __syncthreads();
-  if (warp == 0 && lane < kCenNV) {
-    float s = 0.0f;
-#pragma unroll
-    for (int q = 0; q < kCenWarps; ++q) s += red[q][lane];
-    tot[lane] = s;
-  }
-  __syncthreads();
-}
-
-// Warp sums of 16 values in 16 shuffles (each round keeps half of the values
-// and trades the other half with the partner lane).  On return v[0] of lane
-// l holds the warp's total of value index
-//   8 * bit4(l) + 4 * bit3(l) + 2 * bit2(l) + bit1(l).
-__device__ __forceinline__ void warp_sum16(float (&v)[16], int lane) {
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const int h = 8 >> r;         // values kept after this round
-    const int o = 16 >> r;        // partner lane distance
-    const bool up = (lane & o) != 0;
-#pragma unroll
-    for (int j = 0; j < h; ++j) {
-      const float send = up ? v[j] : v[j + h];
-      const float keep = up ? v[j + h] : v[j];
-      v[j] = keep + __shfl_xor_sync(0xffffffffu, send, o);
-    }
-  }
-  v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
-}
 
 // Stages each thread's own atoms of a frame into shared memory (4-byte
 // cp.async: a thread later reads exactly what it copied, so completion needs
@@ -227,24 +187,71 @@ __device__ __forceinline__ void qcp_rot_f32(const float M[9], float E0, float U[
   rotation_from_quat_f32(q, U);
 }
 
-// Fitted centroids, one CTA per cluster.  STAGE (FP32 frames, the running
-// sum and kRing frames fitting kStageMaxBytes of shared memory): S lives in
-// shared memory (the sweeps re-read it every step; global stores do not stay
-// in L1) and frames come through a ring of kRing shared-memory buffers,
-// member k + 3 issued while member k is fitted, so the chain never waits on
-// DRAM.  Otherwise S is in global memory and frames are read from there.
+// Warp sums of 32 values in 31 shuffles (each round keeps half of the values
+// and trades the other half with the partner lane).  On return v[0] of lane
+// l holds the warp's total of value index
+//   16 * bit4(l) + 8 * bit3(l) + 4 * bit2(l) + 2 * bit1(l) + bit0(l).
+__device__ __forceinline__ void warp_sum32(float (&v)[32], int lane) {
+#pragma unroll
+  for (int r = 0; r < 5; ++r) {
+    const int h = 16 >> r;  // values kept after this round
+    const int o = 16 >> r;  // partner lane distance
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int j = 0; j < h; ++j) {
+      const float send = up ? v[j] : v[j + h];
+      const float keep = up ? v[j + h] : v[j];
+      v[j] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+  }
+}
+__device__ __forceinline__ int warp_sum32_index(int lane) {
+  return ((lane >> 4) & 1) * 16 + ((lane >> 3) & 1) * 8 + ((lane >> 2) & 1) * 4 + ((lane >> 1) & 1) * 2 + (lane & 1);
+}
+
+// Per-step sums of the pipelined chain (slots of red[][][32]).
+constexpr int kP = 0;    // 9: sum w y_{j+1} S_j^T
+constexpr int kQ = 9;    // 9: sum w y_{j+1} y_j^T
+constexpr int kGy = 18;  // sum w |y_{j+1}|^2
+constexpr int kGs = 19;  // sum w |S_j|^2
+constexpr int kC = 20;   // 3: centre sums of member j + 2
+constexpr int kNV = 23;
+
+// Fitted centroids, one CTA per cluster: kChainWarps - 1 sweeping warps and
+// one solving warp, pipelined.  With S_j the sum of members 0..j-1 (each rotated)
+// and y_j member j centred, member j's rotation U_j solves the covariance
+//   A_j = sum w y_j S_j^T = P_j + Q_j U_{j-1}^T,
+//   P_j = sum w y_j S_{j-1}^T,  Q_j = sum w y_j y_{j-1}^T,
+// because S_j = S_{j-1} + U_{j-1} y_{j-1}.  P_j and Q_j need no U_{j-1}, so
+// step j's sweep (S_{j-1} += U_{j-2} y_{j-2}, then P, Q for member j + 1)
+// runs while the solving warp turns A_j into U_j; then one barrier.  The
+// solver keeps A_j, U_j and sum w|y_j|^2 for the next step's
+//   sum w |S_{j+1}|^2 = sum w |S_j|^2 + 2 tr(U_j A_j) + sum w |y_j|^2.
+// Reduction partials and the broadcast U are double-buffered by step parity.
+// STAGE (FP32 frames, S and kRing frames fitting kStageMaxBytes of shared
+// memory): S lives in shared memory (it is re-read every step; global stores
+// do not stay in L1) and frames come through a ring of kRing shared-memory
+// buffers, kAhead members issued ahead of the four in use.  Otherwise S is in
+// global memory and frames are read from there.
 template <typename T, bool STAGE>
-__global__ void __launch_bounds__(kCenThreads) k_centroid_chain(const T* __restrict__ xyz, CenArgs a) {
+__global__ void __launch_bounds__(32 * kChainWarps) k_centroid_chain(const T* __restrict__ xyz, CenArgs a) {
   extern __shared__ float4 dyn[];
-  __shared__ float red[kCenWarps][16];
-  __shared__ float tot[kCenNV];
-  __shared__ float bc[21];  // U as FP32 hi (9) and lo (9) parts, row-major; centre of the next member
+  __shared__ float red[2][kChainWarps - 1][32];
+  __shared__ float bc[2][18];  // U_j as FP32 hi (9) and lo (9), row-major, by step parity
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, N = a.N;
+  // kChainWarps warps: the solving warp is warp kSolverWarp, alone on its
+  // scheduler (warps of an SM sub-partition share warp index mod 4), so its
+  // latency-bound chain does not wait for issue slots behind the sweeps; the
+  // other nsw warps sweep, as sweeping warp sw.
+  constexpr int nsw = kChainWarps - 1, nst = 32 * nsw;
+  const bool solver = (warp == kSolverWarp);
+  const int sw = warp < kSolverWarp ? warp : warp - 1;
+  const int sid = 32 * sw + lane;  // sweeping thread index
   const int64_t cl = blockIdx.x;
   const int64_t o0 = a.offsets[cl], n = a.offsets[cl + 1] - o0;
   double* out = a.out + (size_t)cl * 3 * N;
   if (n <= 0) {  // the reference's centroid has no atoms
-    for (int i = tid; i < 3 * N; i += kCenThreads) out[i] = qnan();
+    for (int i = tid; i < 3 * N; i += blockDim.x) out[i] = qnan();
     return;
   }
   float2* S = STAGE ? (float2*)dyn : a.S + (size_t)cl * 3 * N;
@@ -259,7 +266,7 @@ __global__ void __launch_bounds__(kCenThreads) k_centroid_chain(const T* __restr
       if (k < n) {
         const float* src = (const float*)frame_at(f);
         float* dst = ring + (size_t)(k & (kRing - 1)) * 3 * N;
-        for (int i = tid; i < N; i += kCenThreads) {
+        for (int i = sid; i < N; i += nst) {
           cp_async4(dst + 3 * i, src + 3 * i);
           cp_async4(dst + 3 * i + 1, src + 3 * i + 1);
           cp_async4(dst + 3 * i + 2, src + 3 * i + 2);
@@ -277,142 +284,249 @@ __global__ void __launch_bounds__(kCenThreads) k_centroid_chain(const T* __restr
     }
   };
   static_assert((kRing & (kRing - 1)) == 0, "ring size is a power of two");
+  static_assert(kRing >= kAhead + 4, "the ring holds members j - 1 .. j + 2 and kAhead in flight");
 
-  int32_t f_ahead = 0;  // frame of member k + kRing, loaded one step before its copy is issued
-  if constexpr (STAGE) {
+  // ---- prologue (sweeping warps; the solver takes part in the barriers) ----
+  // Members 0 .. kAhead + 1 issued; step j issues member j + kAhead + 2, whose
+  // frame index was loaded one step earlier.
+  int32_t f_ahead = 0;
+  if (!solver && STAGE) {
 #pragma unroll
-    for (int k = 0; k < kRing; ++k) stage(k, k < n ? mem[k] : 0);
-    f_ahead = (kRing < n) ? mem[kRing] : 0;
-    cp_async_wait<kRing - 2>();  // members 0 and 1 are in
+    for (int k = 0; k < kAhead + 2; ++k) stage(k, k < n ? mem[k] : 0);
+    f_ahead = (kAhead + 2 < n) ? mem[kAhead + 2] : 0;
+    cp_async_wait<kAhead>();  // members 0 and 1 are in
   }
-  // Centres of members 0 and 1 (one reduction), then S = member 0 centred.
-  float v[16];
-#pragma unroll
-  for (int q = 0; q < 16; ++q) v[q] = 0.0f;
-  for (int i = tid; i < N; i += kCenThreads) {
-    float p[3], r[3];
-    get(0, i, p);
-    get(n > 1 ? 1 : 0, i, r);
-    const float wi = wt(i);
-    v[0] += wi * p[0]; v[1] += wi * p[1]; v[2] += wi * p[2];
-    v[11] += wi * r[0]; v[12] += wi * r[1]; v[13] += wi * r[2];
-  }
+  // Centres of members 0 and 1.
   {
-    float v14[kCenNV];
+    float v[32];
 #pragma unroll
-    for (int q = 0; q < kCenNV; ++q) v14[q] = v[q];
-    block_sum_nv(v14, red, tot);
-  }
-  float c[3] = {(float)((double)tot[0] * a.inv_W), (float)((double)tot[1] * a.inv_W),
-                (float)((double)tot[2] * a.inv_W)};
-  float cn[3] = {(float)((double)tot[11] * a.inv_W), (float)((double)tot[12] * a.inv_W),
-                 (float)((double)tot[13] * a.inv_W)};
-  for (int i = tid; i < N; i += kCenThreads) {
-    float p[3];
-    get(0, i, p);
-#pragma unroll
-    for (int q = 0; q < 3; ++q) S[3 * i + q] = make_float2(p[q] - c[q], 0.0f);
-  }
-  for (int64_t k = 1; k < n; ++k) {
-    c[0] = cn[0]; c[1] = cn[1]; c[2] = cn[2];
-    if constexpr (STAGE) {
-      // Buffer (k + kRing - 1) % kRing held member k - 1, which this thread
-      // last read in the previous step.
-      const int32_t f = f_ahead;
-      f_ahead = (k + kRing < n) ? mem[k + kRing] : 0;
-      stage(k + kRing - 1, f);
-      cp_async_wait<kRing - 2>();  // members k and k + 1 are in
+    for (int q = 0; q < 32; ++q) v[q] = 0.0f;
+    if (!solver) {
+      for (int i = sid; i < N; i += nst) {
+        float p[3], r[3];
+        get(0, i, p);
+        get(n > 1 ? 1 : 0, i, r);
+        const float wi = wt(i);
+        v[0] += wi * p[0]; v[1] += wi * p[1]; v[2] += wi * p[2];
+        v[3] += wi * r[0]; v[4] += wi * r[1]; v[5] += wi * r[2];
+      }
+      warp_sum32(v, lane);
+      red[1][sw][warp_sum32_index(lane)] = v[0];
     }
-    const bool has_next = (k + 1 < n);
-#pragma unroll
-    for (int q = 0; q < 16; ++q) v[q] = 0.0f;
-    for (int i = tid; i < N; i += kCenThreads) {
-      float y[3], s[3];
-      get(k, i, y);
-      const float wi = wt(i);
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        y[q] -= c[q];
-        s[q] = S[3 * i + q].x;
-      }
-#pragma unroll
-      for (int p = 0; p < 3; ++p) {
-        const float wy = wi * y[p];
-        v[3 * p] += wy * s[0];
-        v[3 * p + 1] += wy * s[1];
-        v[3 * p + 2] += wy * s[2];
-      }
-      v[9] += wi * (y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
-      v[10] += wi * (s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
-      if (has_next) {
-        float r[3];
-        get(k + 1, i, r);
-        v[11] += wi * r[0]; v[12] += wi * r[1]; v[13] += wi * r[2];
-      }
-    }
-    // Block totals for the solving thread only: warp sums, one barrier, and
-    // warp 0 adds the warps' partials.
-    warp_sum16(v, lane);
-    if ((lane & 1) == 0) red[warp][((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 +
-                                   ((lane >> 1) & 1)] = v[0];
     __syncthreads();
-    if (warp == 0) {
-      float t = 0.0f;
-      if (lane < kCenNV) {
+  }
+  // Sweeping threads keep the centres of members j - 1, j, j + 1.
+  float cm1[3] = {0.0f, 0.0f, 0.0f}, c0[3], c1[3];
 #pragma unroll
-        for (int q = 0; q < kCenWarps; ++q) t += red[q][lane];
-      }
-      float ts[kCenNV];
+  for (int q = 0; q < 3; ++q) {
+    float s0 = 0.0f, s1 = 0.0f;
+    for (int w = 0; w < nsw; ++w) {
+      s0 += red[1][w][q];
+      s1 += red[1][w][3 + q];
+    }
+    c0[q] = s0 * a.inv_Wf;
+    c1[q] = s1 * a.inv_Wf;
+  }
+  // S_1 = member 0 centred.
+  if (!solver)
+    for (int i = sid; i < N; i += nst) {
+      float p[3];
+      get(0, i, p);
 #pragma unroll
-      for (int q = 0; q < kCenNV; ++q) ts[q] = __shfl_sync(0xffffffffu, t, q);
-      if (lane == 0) {
-        if (k <= kExactSteps) {
-          // FP64 solve, U out as hi + lo: the first members' turns set the
-          // orientation of the whole centroid, and an FP32-rounded U would
-          // turn each of them by ~1e-7 rad.
-          const double ik = 1.0 / (double)k;
-          double A[9], U[9];
+      for (int q = 0; q < 3; ++q) S[3 * i + q] = make_float2(p[q] - c0[q], 0.0f);
+    }
+  // From here, at step j: cm1 = c_{j-1}, c0 = c_j, c1 = c_{j+1}.
+
+  // Solver state (lane 0 of the solving warp): A_j, U_j, sum w|y_j|^2.
+  float A_prev[9], Uh_prev[9], Ul_prev[9], gy_prev = 0.0f;
+
+  // Step j = 0 .. n-1.  Sweep j: S_j from S_{j-1} (j >= 2), then the sums of
+  // member j + 1.  Solve j (j >= 1): U_j from the sums of sweep j - 1.
+  for (int64_t j = 0; j < n; ++j) {
+    const int par = (int)(j & 1), prv = par ^ 1;
+    if (solver) {
+      if (j >= 1 && lane == 0) {
+        // The totals of sweep j - 1: independent shared-memory loads, so
+        // their latencies overlap (a shuffle gather serialises them).
+        float ts[kNV];
 #pragma unroll
-          for (int q = 0; q < 9; ++q) A[q] = (double)ts[q] * ik;
-          const double E0 = 0.5 * ((double)ts[9] + (double)ts[10] * ik * ik);
-          qcp_lambda_rot(A, E0, U);
+        for (int q = 0; q < kNV; ++q) ts[q] = red[prv][0][q];
 #pragma unroll
-          for (int q = 0; q < 9; ++q) {
-            const float hi = (float)U[q];
-            bc[q] = hi;
-            bc[9 + q] = (float)(U[q] - (double)hi);
+        for (int w = 1; w < nsw; ++w)
+#pragma unroll
+          for (int q = 0; q < kNV; ++q) ts[q] += red[prv][w][q];
+        {
+          float A[9];
+          const float gy = ts[kGy];
+          if (j <= kExactSteps) {
+            // FP64 steps: A_j, sum w|S_j|^2 and the solve in FP64, U out as
+            // hi + lo.  The first members' turns set the orientation of the
+            // whole centroid: an FP32-rounded U (or A formed from it) would
+            // turn each of them by ~1e-7 rad.
+            double Ad[9], Gs;
+            if (j == 1) {
+#pragma unroll
+              for (int q = 0; q < 9; ++q) Ad[q] = (double)ts[kP + q];  // swept against S_1 itself
+              Gs = (double)ts[kGs];
+            } else {
+              double trUA = 0.0;
+#pragma unroll
+              for (int p = 0; p < 3; ++p)
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                  double acc = (double)ts[kP + 3 * p + q];
+#pragma unroll
+                  for (int r = 0; r < 3; ++r)
+                    acc += (double)ts[kQ + 3 * p + r] * ((double)Uh_prev[3 * q + r] + (double)Ul_prev[3 * q + r]);
+                  Ad[3 * p + q] = acc;
+                  trUA += ((double)Uh_prev[3 * p + q] + (double)Ul_prev[3 * p + q]) * (double)A_prev[3 * q + p];
+                }
+              Gs = (double)ts[kGs] + 2.0 * trUA + (double)gy_prev;  // sum w |S_j|^2
+            }
+#pragma unroll
+            for (int q = 0; q < 9; ++q) A[q] = (float)Ad[q];
+            const double ik = 1.0 / (double)j;
+            double U[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) Ad[q] *= ik;
+            qcp_lambda_rot(Ad, 0.5 * ((double)gy + Gs * ik * ik), U);
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+              const float hi = (float)U[q];
+              Uh_prev[q] = hi;
+              Ul_prev[q] = (float)(U[q] - (double)hi);
+            }
+          } else {
+            float trUA = 0.0f;
+#pragma unroll
+            for (int p = 0; p < 3; ++p)
+#pragma unroll
+              for (int q = 0; q < 3; ++q) {
+                float acc = ts[kP + 3 * p + q];
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+                  acc = fmaf(ts[kQ + 3 * p + r], Uh_prev[3 * q + r] + Ul_prev[3 * q + r], acc);
+                A[3 * p + q] = acc;
+                trUA = fmaf(Uh_prev[3 * p + q] + Ul_prev[3 * p + q], A_prev[3 * q + p], trUA);
+              }
+            const float Gs = ts[kGs] + 2.0f * trUA + gy_prev;  // sum w |S_j|^2
+            // FP32 solve: a later member moves the sum by 1/j of its own
+            // weight, so its rotation error averages out.
+            const float ik = __fdividef(1.0f, (float)j);
+            float M[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) M[q] = A[q] * ik;
+            qcp_rot_f32(M, 0.5f * (gy + Gs * ik * ik), Uh_prev);
+#pragma unroll
+            for (int q = 0; q < 9; ++q) Ul_prev[q] = 0.0f;
           }
-        } else {
-          // FP32 solve: a later member moves the sum by 1/k of its own
-          // weight, so its rotation error averages out.
-          const float ik = __fdividef(1.0f, (float)k);
-          float M[9], U[9];
-#pragma unroll
-          for (int q = 0; q < 9; ++q) M[q] = ts[q] * ik;
-          qcp_rot_f32(M, 0.5f * (ts[9] + ts[10] * ik * ik), U);
 #pragma unroll
           for (int q = 0; q < 9; ++q) {
-            bc[q] = U[q];
-            bc[9 + q] = 0.0f;
+            bc[par][q] = Uh_prev[q];
+            bc[par][9 + q] = Ul_prev[q];
+            A_prev[q] = A[q];
+          }
+          gy_prev = gy;
+        }
+      }
+    } else {
+      if constexpr (STAGE) {
+        // Buffer (j + kAhead + 2) % kRing last held member j + kAhead + 2 -
+        // kRing <= j - 2, which no later step reads.
+        const int32_t f = f_ahead;
+        f_ahead = (j + kAhead + 3 < n) ? mem[j + kAhead + 3] : 0;
+        stage(j + kAhead + 2, f);
+        cp_async_wait<kAhead>();  // members up to j + 2 are in
+      }
+      if (j >= 1) {  // c_{j+1} from sweep j - 1's centre sums
+        cm1[0] = c0[0]; cm1[1] = c0[1]; cm1[2] = c0[2];
+        c0[0] = c1[0]; c0[1] = c1[1]; c0[2] = c1[2];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          float sq = 0.0f;
+          for (int w = 0; w < nsw; ++w) sq += red[prv][w][kC + q];
+          c1[q] = sq * a.inv_Wf;
+        }
+      }
+      const bool upd = (j >= 2), next = (j + 1 < n);
+      float Uh[9], Ul[9];
+      if (upd) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+          Uh[q] = bc[prv][q];
+          Ul[q] = bc[prv][9 + q];
+        }
+      }
+      float v[32];
+#pragma unroll
+      for (int q = 0; q < 32; ++q) v[q] = 0.0f;
+      if (upd || next) {
+        for (int i = sid; i < N; i += nst) {
+          float2 sv[3];
+#pragma unroll
+          for (int q = 0; q < 3; ++q) sv[q] = S[3 * i + q];
+          if (upd) {  // S_j = S_{j-1} + U_{j-1} y_{j-1}
+            float y[3];
+            get(j - 1, i, y);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) y[q] -= cm1[q];
+#pragma unroll
+            for (int p = 0; p < 3; ++p) {
+              const float lo = Ul[3 * p] * y[0] + Ul[3 * p + 1] * y[1] + Ul[3 * p + 2] * y[2];
+              const float r = fmaf(Uh[3 * p], y[0], fmaf(Uh[3 * p + 1], y[1], fmaf(Uh[3 * p + 2], y[2], lo)));
+              sv[p] = add_hl(sv[p], r);
+              S[3 * i + p] = sv[p];
+            }
+          }
+          if (next) {
+            const float wi = wt(i);
+            float y1[3], y0[3], x2[3];
+            get(j + 1, i, y1);
+            get(j, i, y0);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              y1[q] -= c1[q];
+              y0[q] -= c0[q];
+            }
+#pragma unroll
+            for (int p = 0; p < 3; ++p) {
+              const float wy = wi * y1[p];
+#pragma unroll
+              for (int q = 0; q < 3; ++q) {
+                v[kP + 3 * p + q] += wy * sv[q].x;
+                v[kQ + 3 * p + q] += wy * y0[q];
+              }
+            }
+            v[kGy] += wi * (y1[0] * y1[0] + y1[1] * y1[1] + y1[2] * y1[2]);
+            v[kGs] += wi * (sv[0].x * sv[0].x + sv[1].x * sv[1].x + sv[2].x * sv[2].x);
+            if (j + 2 < n) {
+              get(j + 2, i, x2);
+              v[kC] += wi * x2[0]; v[kC + 1] += wi * x2[1]; v[kC + 2] += wi * x2[2];
+            }
           }
         }
-#pragma unroll
-        for (int q = 0; q < 3; ++q) bc[18 + q] = (float)((double)ts[11 + q] * a.inv_W);
       }
+      warp_sum32(v, lane);
+      red[par][sw][warp_sum32_index(lane)] = v[0];
     }
+    // U_j and sweep j's sums published; red[prv] and bc[prv] were read.
     __syncthreads();
+  }
+  // The last member: S_n = S_{n-1} + U_{n-1} y_{n-1}.
+  if (!solver && n >= 2) {
+    const int lp = (int)((n - 1) & 1);
     float Uh[9], Ul[9];
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
-      Uh[q] = bc[q];
-      Ul[q] = bc[9 + q];
+      Uh[q] = bc[lp][q];
+      Ul[q] = bc[lp][9 + q];
     }
-    cn[0] = bc[18]; cn[1] = bc[19]; cn[2] = bc[20];
-    for (int i = tid; i < N; i += kCenThreads) {
+    // c0 holds c_{n-1} after the last step's rotation of the centres
+    for (int i = sid; i < N; i += nst) {
       float y[3];
-      get(k, i, y);
+      get(n - 1, i, y);
 #pragma unroll
-      for (int q = 0; q < 3; ++q) y[q] -= c[q];
+      for (int q = 0; q < 3; ++q) y[q] -= c0[q];
 #pragma unroll
       for (int p = 0; p < 3; ++p) {
         const float lo = Ul[3 * p] * y[0] + Ul[3 * p + 1] * y[1] + Ul[3 * p + 2] * y[2];
@@ -420,15 +534,13 @@ __global__ void __launch_bounds__(kCenThreads) k_centroid_chain(const T* __restr
         S[3 * i + p] = add_hl(S[3 * i + p], r);
       }
     }
-    // bc and red are rewritten only after the next step's first barrier,
-    // which every thread reaches after reading them here.
   }
   if constexpr (STAGE) cp_async_wait<0>();
   // The sums were written per atom (thread t: elements 3t..3t+2); they are
   // read per element below.
   __syncthreads();
   const double inv_n = 1.0 / (double)n;
-  for (int i = tid; i < 3 * N; i += kCenThreads) {
+  for (int i = tid; i < 3 * N; i += blockDim.x) {
     const float2 sv = S[i];
     out[i] = ((double)sv.x + (double)sv.y) * inv_n;
   }
@@ -554,11 +666,13 @@ extern "C" int gbr_cluster_centroids(gbr_handle* h, const void* xyz, int dtype, 
   a.offsets = (const int64_t*)P[1];
   a.w = mass ? (const float*)P[3] : nullptr;
   a.inv_W = 1.0 / W;
+  a.inv_Wf = (float)(1.0 / W);
   a.N = N;
   a.S = (float2*)P[4];
   a.out = o_dev ? centroids : (double*)P[5];
   const void* x = x_dev ? xyz : P[0];
   const unsigned grid = (unsigned)n_cluster;
+  const int chain_threads = 32 * kChainWarps;
   const size_t stage_bytes = (size_t)3 * N * (sizeof(float2) + kRing * sizeof(float));
   cudaError_t e = cudaSuccess;
   if (mode == GBR_NOFIT) {
@@ -571,11 +685,11 @@ extern "C" int gbr_cluster_centroids(gbr_handle* h, const void* xyz, int dtype, 
     e = cudaFuncSetAttribute(k_centroid_chain<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)stage_bytes);
     if (e != cudaSuccess) return h->cuda_fail(e, "centroid kernel attribute");
-    k_centroid_chain<float, true><<<grid, kCenThreads, stage_bytes, st>>>((const float*)x, a);
+    k_centroid_chain<float, true><<<grid, chain_threads, stage_bytes, st>>>((const float*)x, a);
   } else if (dtype == GBR_F32) {
-    k_centroid_chain<float, false><<<grid, kCenThreads, 0, st>>>((const float*)x, a);
+    k_centroid_chain<float, false><<<grid, chain_threads, 0, st>>>((const float*)x, a);
   } else {
-    k_centroid_chain<double, false><<<grid, kCenThreads, 0, st>>>((const double*)x, a);
+    k_centroid_chain<double, false><<<grid, chain_threads, 0, st>>>((const double*)x, a);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return h->cuda_fail(e, "centroid kernel launch");

@@ -316,12 +316,13 @@ struct F9 {
   float v[9];
 };
 
-// Solver part of the epilogue with every per-frame term given (by value, so
-// nothing goes through local memory at the call): P_ja, P_ib, trPia / trPjb
-// (read only when a != b), rp the reference-pair entry of (a, b).
-static __device__ __noinline__ float pair_solve(const F9 Dv, float ni, float nj, const F9 Pjav, const F9 Pibv,
-                                                float trPia, float trPjb, const float* rp, bool same,
-                                                const FrameTerms& t, bool* flag, float* qout = nullptr) {
+// Solver part of the epilogue with every per-frame term given (by value):
+// P_ja, P_ib, trPia / trPjb (read only when a != b), rp the reference-pair
+// entry of (a, b).
+static __device__ __forceinline__ float pair_solve_inl(const F9 Dv, float ni, float nj, const F9 Pjav,
+                                                      const F9 Pibv, float trPia, float trPjb, const float* rp,
+                                                      bool same, const FrameTerms& t, bool* flag,
+                                                      float* qout = nullptr) {
   const float* D = Dv.v;
   const float* Pja = Pjav.v;
   const float* Pib = Pibv.v;
@@ -433,29 +434,54 @@ static __device__ __noinline__ float pair_solve(const F9 Dv, float ni, float nj,
   return r;
 }
 
+// The same as a call: the CUDA-core kernels, whose per-thread state already
+// fills the register file, keep the solver out of line.
+static __device__ __noinline__ float pair_solve(const F9 Dv, float ni, float nj, const F9 Pjav, const F9 Pibv,
+                                                float trPia, float trPjb, const float* rp, bool same,
+                                                const FrameTerms& t, bool* flag, float* qout = nullptr) {
+  return pair_solve_inl(Dv, ni, nj, Pjav, Pibv, trPia, trPjb, rp, same, t, flag, qout);
+}
+
 // The pair epilogue with its per-frame terms read from global memory.
-static __device__ __forceinline__ float pair_epilogue(const float D[9], int64_t i, int64_t j, const FrameTerms& t,
-                                                      bool* flag, float* qout = nullptr) {
+// The solver's inputs for pair (i, j): every per-frame term read from
+// global memory.
+struct PairIn {
+  F9 pja, pib;
+  float ni, nj, trPia, trPjb;
+  const float* rp;
+  bool same;
+};
+static __device__ __forceinline__ void pair_terms(int64_t i, int64_t j, const FrameTerms& t, PairIn& in) {
   const int K = t.K;
   const int a = (K > 1) ? __ldg(t.assign + i) : 0;
   const int b = (K > 1) ? __ldg(t.assign + j) : 0;
-  const float ni = __ldg(t.nrm + i), nj = __ldg(t.nrm + j);
+  in.ni = __ldg(t.nrm + i);
+  in.nj = __ldg(t.nrm + j);
   const float* Pja = t.P + ((size_t)j * K + a) * 9;
   const float* Pib = t.P + ((size_t)i * K + b) * 9;
-  const float* rp = t.RP + (size_t)(b * K + a) * kRefPairStride;
-  F9 dv, pja, pib;
+  in.rp = t.RP + (size_t)(b * K + a) * kRefPairStride;
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
-    dv.v[k] = D[k];
-    pja.v[k] = __ldg(Pja + k);
-    pib.v[k] = __ldg(Pib + k);
+    in.pja.v[k] = __ldg(Pja + k);
+    in.pib.v[k] = __ldg(Pib + k);
   }
-  float trPia = 0.0f, trPjb = 0.0f;
+  in.trPia = 0.0f;
+  in.trPjb = 0.0f;
   if (a != b) {
-    trPia = __ldg(t.trP + i * K + a);
-    trPjb = __ldg(t.trP + j * K + b);
+    in.trPia = __ldg(t.trP + i * K + a);
+    in.trPjb = __ldg(t.trP + j * K + b);
   }
-  return pair_solve(dv, ni, nj, pja, pib, trPia, trPjb, rp, a == b, t, flag, qout);
+  in.same = (a == b);
+}
+
+static __device__ __forceinline__ float pair_epilogue(const float D[9], int64_t i, int64_t j, const FrameTerms& t,
+                                                      bool* flag, float* qout = nullptr) {
+  PairIn in;
+  pair_terms(i, j, t, in);
+  F9 dv;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) dv.v[k] = D[k];
+  return pair_solve(dv, in.ni, in.nj, in.pja, in.pib, in.trPia, in.trPjb, in.rp, in.same, t, flag, qout);
 }
 
 __host__ __device__ inline int64_t tri_index(int64_t n, int64_t i, int64_t j) {

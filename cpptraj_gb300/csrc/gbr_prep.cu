@@ -51,6 +51,16 @@ struct FrameSrc {
 
 constexpr int kPrepThreads = 256;
 constexpr int kWarps = kPrepThreads / 32;
+// k_scan and k_build split each frame's atom chunks over kWPF warps: a chunk
+// of input (1,250 frames) then keeps twice the warps busy.  The parts' sums
+// meet in shared memory in a fixed order, so every launch shape gives the
+// same bits.
+constexpr int kWPF = 2;
+constexpr int kFPB = kWarps / kWPF;  // frames per block per round
+
+__device__ __forceinline__ void group_sync(int grp) {
+  asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(32 * kWPF) : "memory");
+}
 // Single-block kernels (weights, one reference, reference-pair terms) walk N
 // atoms with FP64 sums; their time is the serial FP64 tail of one thread (a
 // larger block measured slower).
@@ -263,17 +273,20 @@ template <typename T>
 struct WarpPipe {
   FrameSrc<T> src;
   int64_t f_next, F, stride;  // next frame to issue, end, this warp's frame stride
-  int c_next, nch, issued;    // next chunk of f_next, chunks per frame, chunks issued
+  int c_next, c_lo, c_hi, issued;  // next chunk of f_next, this warp's chunks [c_lo, c_hi), chunks issued
   float* ring;                // kPipe * kStage floats, 16-byte aligned
 
+  // The warp streams chunks [c_lo, c_hi) of each of its frames (its part of
+  // a frame shared by kWPF warps).
   __device__ __forceinline__ void init(const FrameSrc<T>& s, int64_t f0, int64_t f_end, int64_t str, float* buf,
-                                       int lane) {
+                                       int lane, int lo, int hi) {
     src = s;
     f_next = f0;
     F = f_end;
     stride = str;
-    c_next = 0;
-    nch = (s.N + kChunkAtoms - 1) / kChunkAtoms;
+    c_lo = lo;
+    c_hi = hi;
+    c_next = lo;
     issued = 0;
     ring = buf;
     if constexpr (sizeof(T) == 4) {
@@ -283,7 +296,7 @@ struct WarpPipe {
   }
   __device__ __forceinline__ void issue(int lane) {
     if constexpr (sizeof(T) == 4) {
-      if (f_next < F && nch > 0) {
+      if (f_next < F && c_hi > c_lo) {
         const int N = src.N, a0 = c_next * kChunkAtoms;
         const float* x = (const float*)src.frame(f_next) + 3 * (size_t)a0;
         const int n = 3 * (min(a0 + kChunkAtoms, N) - a0);
@@ -297,8 +310,8 @@ struct WarpPipe {
         }
         if (lane < head) cp_async4(dst + lane, x + lane);
         if (lane < n - tail0) cp_async4(dst + tail0 + lane, x + tail0 + lane);
-        if (++c_next == nch) {
-          c_next = 0;
+        if (++c_next == c_hi) {
+          c_next = c_lo;
           f_next += stride;
         }
       }
@@ -313,7 +326,7 @@ struct WarpPipe {
     const int N = src.N;
     if constexpr (sizeof(T) == 4) {
       const float* x = (const float*)src.frame(f);
-      for (int c = 0; c < nch; ++c) {
+      for (int c = c_lo; c < c_hi; ++c) {
         const int a0 = c * kChunkAtoms;
         const int consumed = issued - (kPipe - 1);
         cp_async_wait<kPipe - 2>();
@@ -330,7 +343,8 @@ struct WarpPipe {
         __syncwarp();
       }
     } else {
-      for (int a = lane; a < N; a += 32) body(a, 0, ring);
+      const int a_hi = min(c_hi * kChunkAtoms, N);
+      for (int a = c_lo * kChunkAtoms + lane; a < a_hi; a += 32) body(a, 0, ring);
     }
   }
   __device__ __forceinline__ void drain() {
@@ -565,12 +579,15 @@ struct ScanArgs {
 template <typename T, bool FIRST>
 __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64_t f_begin, int64_t F, ScanArgs s) {
   __shared__ __align__(16) float sbuf[kWarps][kPipe * kStage];
-  const int N = src.N, lane = threadIdx.x & 31;
+  __shared__ float xpart[2][kFPB][kWPF - 1][20];  // the other parts' sums, by frame parity
+  const int N = src.N, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int grp = warp / kWPF, part = warp % kWPF;
   const bool fit = !s.nofit;
-  const int64_t f_first = f_begin + blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5);
-  const int64_t f_stride = (int64_t)gridDim.x * kWarps;
+  const int64_t f_first = f_begin + blockIdx.x * (int64_t)kFPB + grp;
+  const int64_t f_stride = (int64_t)gridDim.x * kFPB;
+  const int nch = (N + kChunkAtoms - 1) / kChunkAtoms;
   WarpPipe<T> pipe;
-  pipe.init(src, f_first, F, f_stride, sbuf[threadIdx.x >> 5], lane);
+  pipe.init(src, f_first, F, f_stride, sbuf[warp], lane, part * nch / kWPF, (part + 1) * nch / kWPF);
   {
     const size_t n4 = (size_t)N * 4;
     prefetch_l1(s.sqwf, n4);
@@ -578,13 +595,14 @@ __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64
     if (FIRST) {
       prefetch_l1(s.cm_ref, n4);
       prefetch_l1(s.cml_ref, n4);
-      if (s.cm_tgt != s.cm_ref && f_begin + (int64_t)gridDim.x * kWarps > src.n_ref) {
+      if (s.cm_tgt != s.cm_ref && f_begin + (int64_t)gridDim.x * kFPB > src.n_ref) {
         prefetch_l1(s.cm_tgt, n4);
         prefetch_l1(s.cml_tgt, n4);
       }
     }
   }
-  for (int64_t f = f_first; f < F; f += f_stride) {
+  int it = 0;
+  for (int64_t f = f_first; f < F; f += f_stride, ++it) {
     const T* x = src.frame(f);
     const bool in_ref = f < src.n_ref;
     const float* cm = in_ref ? s.cm_ref : s.cm_tgt;
@@ -674,7 +692,33 @@ __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) umax = fmaxf(umax, __shfl_xor_sync(0xffffffffu, umax, o));
-    if (lane == 0) {
+    // The frame's other parts hand their sums to part 0 (the centre terms
+    // stay compensated: TwoSum, parts in order).
+    if (part != 0 && lane == 0) {
+      float* o = xpart[it & 1][grp][part - 1];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) o[q] = v[q];
+      o[16] = ce[0]; o[17] = ce[1]; o[18] = ce[2]; o[19] = umax;
+    }
+    group_sync(grp);
+    if (part == 0 && lane == 0) {
+#pragma unroll
+      for (int pp = 0; pp < kWPF - 1; ++pp) {
+        const float* o = xpart[it & 1][grp][pp];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          if (q >= 10 && q < 13) {
+            float e;
+            two_sum(v[q], o[q], v[q], e);
+            ce[q - 10] += o[16 + q - 10] + e;
+          } else {
+            v[q] += o[q];
+          }
+        }
+        umax = fmaxf(umax, o[19]);
+      }
+    }
+    if (part == 0 && lane == 0) {
       // Per-frame tail, one lane.  Only the centre needs FP64 (it feeds the
       // exact superposition of the later passes); the distance to the
       // reference, E0 and the QCP input only choose the nearest reference and
@@ -921,12 +965,29 @@ template <typename T>
 __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int64_t f_begin, int64_t F,
                                                              BuildArgs b) {
   __shared__ __align__(16) float sbuf[kWarps][kPipe * kStage];
-  const int N = src.N, Np = b.Np, lane = threadIdx.x & 31;
+  __shared__ float xpart[2][kFPB][kWPF - 1][10];  // the other parts' sums, by round parity
+  const int N = src.N, Np = b.Np, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int grp = warp / kWPF, part = warp % kWPF;
   const float sqwmax = (float)b.scal[0];
-  const int64_t f_first = f_begin + blockIdx.x * (int64_t)kWarps + (threadIdx.x >> 5);
-  const int64_t f_stride = (int64_t)gridDim.x * kWarps;
+  const int64_t f_first = f_begin + blockIdx.x * (int64_t)kFPB + grp;
+  const int64_t f_stride = (int64_t)gridDim.x * kFPB;
+  const int nch = (N + kChunkAtoms - 1) / kChunkAtoms;
+  const int c_lo = part * nch / kWPF, c_hi = (part + 1) * nch / kWPF;
+  const int a_lo = c_lo * kChunkAtoms, a_hi = min(c_hi * kChunkAtoms, N);  // this part's atoms
   WarpPipe<T> pipe;
-  pipe.init(src, f_first, F, f_stride, sbuf[threadIdx.x >> 5], lane);
+  pipe.init(src, f_first, F, f_stride, sbuf[warp], lane, c_lo, c_hi);
+  // Sums of NV values over the frame's parts: part 0's lane 0 ends with the
+  // total (parts added in order).
+  int rnd = 0;
+  auto combine = [&](float* acc, int nv) {
+    if (part != 0 && lane == 0)
+      for (int q = 0; q < nv; ++q) xpart[rnd & 1][grp][part - 1][q] = acc[q];
+    group_sync(grp);
+    if (part == 0 && lane == 0)
+      for (int pp = 0; pp < kWPF - 1; ++pp)
+        for (int q = 0; q < nv; ++q) acc[q] += xpart[rnd & 1][grp][pp][q];
+    ++rnd;
+  };
   prefetch_l1(b.sqwf, (size_t)N * 4);
   prefetch_l1(b.refhl, (size_t)N * 24);  // reference 0 (the only one when K = 1)
   prefetch_l1(b.swr, (size_t)N * 12);
@@ -934,7 +995,7 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
     const T* x = src.frame(f);
     const int ra = b.assign[f];
     const int64_t pf = b.pos ? (int64_t)b.pos[f] : f;  // where this frame's operands go
-    if (b.pos && lane == 0) b.assign_pos[pf] = ra;
+    if (b.pos && part == 0 && lane == 0) b.assign_pos[pf] = ra;
     FrameTable Tb;
     load_table(b.ftab, f, lane, Tb);
     float scale = 1.0f, inv = 1.0f;
@@ -945,7 +1006,7 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
       e = max(-100, min(100, e));
       scale = ldexpf(1.0f, 14 - e);
       inv = ldexpf(1.0f, e - 14);
-      if (lane == 0) b.inv_scale[pf] = inv;
+      if (part == 0 && lane == 0) b.inv_scale[pf] = inv;
     }
     const float2* rr = b.refhl + (size_t)ra * 3 * N;
     const float* r0 = b.swr;  // reference 0 for the fused P term
@@ -980,8 +1041,8 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
         acc[3] += v[1] * c0; acc[4] += v[1] * c1; acc[5] += v[1] * c2;
         acc[6] += v[2] * c0; acc[7] += v[2] * c1; acc[8] += v[2] * c2;
     });
-    // zero padding [N, Np)
-    for (int a = N + lane; a < Np; a += 32) {
+    // zero padding [N, Np), by the last part
+    for (int a = N + lane; a < Np && part == kWPF - 1; a += 32) {
 #pragma unroll
       for (int p = 0; p < 3; ++p) {
         if (b.tc) {
@@ -992,21 +1053,22 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
       }
     }
     warp_sum_f32<10>(acc);
-    if (lane == 0) {
+    combine(acc, 10);
+    if (part == 0 && lane == 0) {
       b.nrm[pf] = acc[9];
       float* Pf = b.P + (size_t)pf * b.K * 9;
       for (int q = 0; q < 9; ++q) Pf[q] = acc[q];
       b.trP[(size_t)pf * b.K] = acc[0] + acc[4] + acc[8];
     }
     // P against the other references: read the operands back (this lane's own
-    // writes, same atom mapping).
+    // writes, same atom mapping, this part's atoms).
     __syncwarp();
     for (int c = 1; c < b.K; ++c) {
       const float* rc = b.swr + (size_t)c * N * 3;
       float h9[9];
 #pragma unroll
       for (int q = 0; q < 9; ++q) h9[q] = 0.0f;
-      for (int a = lane; a < N; a += 32) {
+      for (int a = a_lo + lane; a < a_hi; a += 32) {
         float v[3];
 #pragma unroll
         for (int p = 0; p < 3; ++p) {
@@ -1019,7 +1081,8 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
         h9[6] += v[2] * c0; h9[7] += v[2] * c1; h9[8] += v[2] * c2;
       }
       warp_sum_f32<9>(h9);
-      if (lane == 0) {
+      combine(h9, 9);
+      if (part == 0 && lane == 0) {
         float* Pf = b.P + ((size_t)pf * b.K + c) * 9;
         for (int q = 0; q < 9; ++q) Pf[q] = h9[q];
         b.trP[(size_t)pf * b.K + c] = h9[0] + h9[4] + h9[8];
@@ -1090,12 +1153,13 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
 // Host driver for the prep passes.
 // ---------------------------------------------------------------------------
 static BuildArgs build_args(const FinishArgs& fa, const PrepArgs& A, const PrepScratch& S);
-// Blocks for a warp-per-frame pass over F frames: one wave of per_sm resident
-// blocks on each of GB300's 152 SMs at most.  The cp.async-pipelined passes
-// (k_scan, k_build) are persistent: each warp streams several frames, so the
+// Blocks for a pass over F frames, fpb frames per block at a time: one wave
+// of per_sm resident blocks on each of GB300's 152 SMs at most.  The
+// cp.async-pipelined passes (k_scan, k_build; kFPB frames per block, each on
+// kWPF warps) are persistent: each warp streams several frames, so the
 // pipeline fills once per warp rather than once per frame.
-static int prep_grid(int64_t F, int per_sm = 16) {
-  return (int)std::min<int64_t>((F + kWarps - 1) / kWarps, 152 * per_sm);
+static int prep_grid(int64_t F, int per_sm = 16, int fpb = kWarps) {
+  return (int)std::min<int64_t>((F + fpb - 1) / fpb, 152 * per_sm);
 }
 constexpr int kScanBlocksPerSM = 4;   // k_scan: __launch_bounds__(kPrepThreads, 4)
 constexpr int kBuildBlocksPerSM = 3;  // k_build: __launch_bounds__(kPrepThreads, 3)
@@ -1173,7 +1237,7 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
       if (c > 0) cudaStreamWaitEvent(st, A.chunk_ev[c], 0);
       const int64_t f1 = A.chunk_end[c];
       if (f1 > f0) {
-        k_scan<T, true><<<prep_grid(f1 - f0, kScanBlocksPerSM), kPrepThreads, 0, st>>>(src, f0, f1, sa);
+        k_scan<T, true><<<prep_grid(f1 - f0, kScanBlocksPerSM, kFPB), kPrepThreads, 0, st>>>(src, f0, f1, sa);
         ++launches;
         if (A.spec_build && A.spec_fail && A.max_refs > 1 && F > 1) {
           k_spec_check<<<1, 256, 0, st>>>(A.dist, f0, f1, (float)A.tau, A.spec_fail);
@@ -1195,7 +1259,7 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
             refined = true;
           }
           if (refined) {
-            k_build<T><<<prep_grid(f1 - b0, kBuildBlocksPerSM), kPrepThreads, 0, st>>>(src, b0, f1, bspec);
+            k_build<T><<<prep_grid(f1 - b0, kBuildBlocksPerSM, kFPB), kPrepThreads, 0, st>>>(src, b0, f1, bspec);
             ++launches;
             if (A.on_built) {
               const cudaError_t e = (*A.on_built)(f1);
@@ -1229,7 +1293,7 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
       ++launches;
     }
   } else {
-    k_scan<T, true><<<prep_grid(F, kScanBlocksPerSM), kPrepThreads, 0, st>>>(src, 0, F, sa);
+    k_scan<T, true><<<prep_grid(F, kScanBlocksPerSM, kFPB), kPrepThreads, 0, st>>>(src, 0, F, sa);
     ++launches;
   }
   // Greedy k-centre: add the farthest frame as a reference while it is
@@ -1250,7 +1314,7 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
     sa.swr = A.swr + (size_t)K * 3 * N;
     sa.sr = S.sr + 3 * K;
     sa.Eref = A.Eref + K;
-    k_scan<T, false><<<prep_grid(F, kScanBlocksPerSM), kPrepThreads, 0, st>>>(src, 0, F, sa);
+    k_scan<T, false><<<prep_grid(F, kScanBlocksPerSM, kFPB), kPrepThreads, 0, st>>>(src, 0, F, sa);
     launches += 2;
     ++K;
   }
@@ -1331,7 +1395,7 @@ static cudaError_t finish_impl(const FinishArgs& fa, cudaStream_t st) {
   const PrepScratch S = prep_carve(A.scratch, A.F, A.N, A.max_refs);
   if (!fa.built) {
     const BuildArgs b = build_args(fa, A, S);
-    k_build<T><<<prep_grid(A.F, kBuildBlocksPerSM), kPrepThreads, 0, st>>>(src, 0, A.F, b);
+    k_build<T><<<prep_grid(A.F, kBuildBlocksPerSM, kFPB), kPrepThreads, 0, st>>>(src, 0, A.F, b);
   }
   k_ref_terms<<<fa.K * fa.K * kRefCluster, kOneBlockThreads, 0, st>>>(A.refs, A.N, fa.K, A.w, A.nofit, fa.RP);
   return cudaGetLastError();

@@ -61,6 +61,7 @@ void gbr_destroy(gbr_handle* h) {
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   if (h->ws) cudaFree(h->ws);
+  blas_destroy(h->blas);
   h->release_batch();
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
@@ -921,6 +922,8 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   T.sqw = pa.sqw;
   T.W = Wsum;
   T.grad = d_grad;
+  if (!h->blas && !(h->blas = blas_create())) return h->fail(GBR_ERR_NOMEM, "cannot create the cuBLAS handle");
+  T.blas = h->blas;
   if ((e = run_backward_tail(T, st)) != cudaSuccess) return h->cuda_fail(e, "backward tail");
   launches += 4;
   if (h->timing) cudaEventRecord(h->ev[3], st);

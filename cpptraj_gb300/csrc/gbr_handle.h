@@ -69,6 +69,7 @@ struct gbr_handle {
   int tc_variant = -1;  // -1: pairs of SMs, stage shape chosen by atom count (see gbr_set_option)
   bool host_out_direct = true;  // kernels store into pinned host output in place
   bool input_overlap = false;   // the contraction starts on input chunks that have landed
+  void* blas = nullptr;         // cuBLAS handle of the backward pass, created on first use
   // batched path: auxiliary streams, fork/join events, pinned staging,
   // the captured graph of the last batch signature, the autotuner table
   static constexpr int kAux = 8;

@@ -213,8 +213,12 @@ struct BackwardTail {
   const double* sqw;   // sqrt of the masses (when w is given)
   double W;
   float* grad;         // [F][N][3]
+  void* blas;          // cuBLAS handle (blas_create)
 };
 cudaError_t run_backward_tail(const BackwardTail& T, cudaStream_t st);
+// cuBLAS handle for the backward pass's plain GEMM (strict FP32), or nullptr.
+void* blas_create();
+void blas_destroy(void* hb);
 
 // Direct FP64 recomputation (flagged pairs or every pair).
 struct ExactLaunch {

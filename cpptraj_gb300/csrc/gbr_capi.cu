@@ -759,6 +759,16 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
     return GBR_OK;
   }
   const int Np = (N + 63) / 64 * 64;
+  // The pair pass on the tensor cores (pair-of-SMs kernel, backward
+  // instantiation) where they are usable, else on the FP32 CUDA-core kernel.
+  const bool tc = h->tc_ok != 0;
+  OutMap map{};
+  map.n_ref = F;
+  map.n_tgt = F;
+  map.tri = 1;
+  map.row_begin = 0;
+  map.row_end = F;
+  const int64_t tc_tiles = tc ? tc_max_tiles(map) : 0;
   auto layout = [&](Arena& A, void** p) {
     p[0] = xyz_dev ? nullptr : A.take<float>((size_t)F * 3 * N);
     p[1] = A.take<double>(N);                       // w
@@ -792,8 +802,12 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
     p[29] = A.take<double>(N);                      // sqrt(w)
     p[30] = A.take<float>(N);                       // sqrt(w), FP32
     p[31] = A.take<char>(prep_scratch_bytes(F, N, 1));  // prep tables
+    p[32] = tc ? A.take<__half_raw>((size_t)F * 3 * Np) : nullptr;  // FP16 hi
+    p[33] = tc ? A.take<__half_raw>((size_t)F * 3 * Np) : nullptr;  // FP16 lo
+    p[34] = tc ? A.take<int2>(tc_tiles) : nullptr;                   // tile list
+    p[35] = A.take<int>(1);                                          // device error flag
   };
-  void* P[32];
+  void* P[36];
   Arena sizing;
   layout(sizing, P);
   if (!h->reserve(sizing.off + 256))
@@ -852,8 +866,8 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   terms.W = (float)Wsum;
   terms.two_over_w = (float)(2.0 / (double)Wsum);
   terms.tol = (float)h->tol;
-  terms.gem_s = 1.2e-7f;
-  terms.gem_c = 1.2e-7f * std::sqrt((float)N);
+  terms.gem_s = tc ? 6.0e-7f : 1.2e-7f;
+  terms.gem_c = tc ? 1.2e-8f * (float)N : 1.2e-7f * std::sqrt((float)N);
   terms.epi_coef = 8e-7f;
   terms.nofit = 0;
   FinishArgs fa{};
@@ -866,8 +880,10 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   fa.mean = pa.mean;
   fa.assign = pa.assign;
   fa.swr = pa.swr;
-  fa.tc = 0;
-  fa.write_plane = 1;
+  fa.tc = tc;
+  fa.hi = P[32];
+  fa.lo = P[33];
+  fa.write_plane = 1;  // the GEMM reads the plane (with tc: the values hi + lo represent)
   fa.inv_scale = (float*)P[12];
   fa.nrm = (float*)terms.nrm;
   fa.P = (float*)terms.P;
@@ -882,6 +898,7 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   cudaMemsetAsync(B, 0, sizeof(float) * 3 * F * ldB, st);
   cudaMemsetAsync(P[21], 0, sizeof(float) * 9 * F, st);
   cudaMemsetAsync(P[22], 0, sizeof(float) * F, st);
+  cudaMemsetAsync(P[35], 0, sizeof(int), st);
   if (h->timing) cudaEventRecord(h->ev[1], st);
   PairLaunch L{};
   L.bwd.B = B;
@@ -895,16 +912,31 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   L.N = N;
   L.tgt0 = 0;
   L.terms = terms;
-  OutMap map{};
-  map.n_ref = F;
-  map.n_tgt = F;
-  map.tri = 1;
-  map.row_begin = 0;
-  map.row_end = F;
   L.map = map;
   L.flags = FlagList{nullptr, (unsigned long long*)P[27], 0};
-  L.tiles = make_tiles(map, 64, 64);
-  if ((e = run_pairs_fp32(L, st)) != cudaSuccess) return h->cuda_fail(e, "backward pair kernel");
+  if (tc) {
+    TcLaunch T2{};
+    T2.hi = P[32];
+    T2.lo = P[33];
+    T2.tile_buf = P[34];
+    T2.tile_cap = tc_tiles;
+    T2.F = F;
+    T2.Np = Np;
+    T2.N = N;
+    T2.tgt0 = 0;
+    T2.inv_scale = (const float*)P[12];
+    T2.terms = terms;
+    T2.map = map;
+    T2.flags = L.flags;
+    T2.dev_error = (int*)P[35];
+    T2.num_sms = h->num_sms;
+    T2.variant = (h->tc_variant >= 2) ? h->tc_variant : (N >= kDeepStageAtoms ? 3 : 2);
+    T2.bwd = &L.bwd;
+    if ((e = run_pairs_tc(T2, st)) != cudaSuccess) return h->cuda_fail(e, "backward pair kernel");
+  } else {
+    L.tiles = make_tiles(map, 64, 64);
+    if ((e = run_pairs_fp32(L, st)) != cudaSuccess) return h->cuda_fail(e, "backward pair kernel");
+  }
   if (h->timing) cudaEventRecord(h->ev[2], st);
   BackwardTail T{};
   T.F = F;
@@ -929,10 +961,13 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   if (h->timing) cudaEventRecord(h->ev[3], st);
   if (!grad_dev) cudaMemcpyAsync(grad_xyz, d_grad, sizeof(float) * 3 * N * F, cudaMemcpyDefault, st);
   if (rmsd_out && !r_dev) cudaMemcpyAsync(rmsd_out, d_rmsd, sizeof(float) * npairs, cudaMemcpyDefault, st);
+  int derr = 0;
+  cudaMemcpyAsync(&derr, P[35], sizeof derr, cudaMemcpyDeviceToHost, st);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return h->cuda_fail(e, "backward");
+  if (derr != 0) return h->fail(GBR_ERR_DEVICE, "pair kernel reported device error %d (bounded wait expired)", derr);
   h->stats.pairs = npairs;
   h->stats.n_refs = 1;
-  h->stats.precision = GBR_PREC_FP32;
+  h->stats.precision = tc ? GBR_PREC_TC : GBR_PREC_FP32;
   h->stats.kernel_launches = launches;
   if (h->timing) {
     float a = 0, b = 0, c = 0;

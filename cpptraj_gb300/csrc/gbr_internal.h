@@ -184,6 +184,7 @@ struct TcLaunch {
   int64_t ready_tiles;  // > 0: tile_buf already holds this many tiles (no host build or copy)
   int row_stores;       // pair kernels, triangle output: gather each tile's results and store whole rows
   const int* skip;      // device int or nullptr: when it reads non-zero at launch, the kernel does nothing
+  const BwdArgs* bwd;   // non-null: the backward pass (variants 2 and 3, one set, TRI, one reference)
 };
 // Tile list of the tensor-core kernel for this map (host side).
 struct TcTileInfo {

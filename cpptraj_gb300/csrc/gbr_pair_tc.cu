@@ -119,6 +119,7 @@ struct TcParams {
   int* err;
   int row_stores;  // triangle results gathered into whole tile rows before the store (pair kernels)
   const int* skip;  // non-null and non-zero at launch: the kernel returns at once
+  BwdArgs bwd;      // backward instantiation: c*T blocks, row terms, forward values
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -247,7 +248,13 @@ __device__ __forceinline__ void mbar_arrive_remote(uint32_t caddr) {
 // chunks g, g + 4, ...), and run the per-pair solve.  The reference frames of
 // a tile start at i_base + ti * ti_frames + i_off.  acce_bar is the address
 // the warps arrive on when the buffer is free (remote: CTA 0 of a pair).
-template <class E>
+// BWD (one frame set, TRI, one reference): for each pair i < j, with
+// c = g_ij / RMSD_ij and T the rotation taking x'_j onto x'_i, the block
+// B[3i..3i+2][3j..3j+2] = c T and the row terms E_i += c (I - T),
+// E_j += c (I - T^T), C_i += c, C_j += c.  The row terms are summed across
+// the warp's lanes that share a frame, then in shared memory per tile
+// (rowbuf), and added to E / C once per tile.
+template <class E, bool BWD = false>
 __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_base, float* staging, float* terms,
                                                float* rowbuf, volatile int* okf, uint32_t accf0, uint32_t acce_bar,
                                                bool remote, int64_t t0, int64_t tstep, int ti_frames, int i_off,
@@ -264,9 +271,18 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
   // Row stores: the pairs of a tile gather in shared memory and leave as
   // whole rows of the triangle (TJ contiguous values) instead of CH_TGT-value
   // pieces, which matters when the output is host memory across the link.
-  const bool rows = rowbuf != nullptr && tri && P.row_stores != 0;
+  const bool rows = !BWD && rowbuf != nullptr && tri && P.row_stores != 0;
   constexpr int RB_STRIDE = E::RB_STRIDE;
   const int K = P.terms.K;
+  // BWD: this CTA's row terms, [TI][10] for its reference frames then
+  // [TJ][10] for the tile's target frames, zero between tiles.
+  float* Erow = rowbuf;
+  float* Ecol = rowbuf + TI * 10;
+  constexpr int kEterms = (TI + TJ) * 10;
+  if constexpr (BWD) {
+    static_assert(kEterms <= TI * E::RB_STRIDE, "row terms fit the row buffer");
+    for (int x = etid; x < kEterms; x += EPI_WARPS * 32) rowbuf[x] = 0.0f;  // ordered by the first tile's barrier
+  }
   uint32_t it = 0;
   for (int64_t t = t0; t < P.n_tiles; t += tstep, ++it) {
     const uint32_t b = it & 1u, aph = (it >> 1) & 1u;
@@ -333,6 +349,89 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
         for (int k = 0; k < CH_COLS; ++k) st[row * ST_STRIDE + k] = v[k];
         named_sync(1 + g, 128);
         const int64_t jc0 = jt0 + (int64_t)c * CH_TGT;
+        if constexpr (BWD) {
+          // Warp-uniform trip count (the lanes meet in shuffles); pairs
+          // outside the triangle contribute zero.
+#pragma unroll 1
+          for (int pb = 0; pb < TI * CH_TGT; pb += 128) {
+            const int p = pb + tid;
+            const int il = p / CH_TGT, jl = p % CH_TGT;
+            const int64_t i = i0 + il, j = jc0 + jl;
+            float er[10], ec[10];
+#pragma unroll
+            for (int k = 0; k < 10; ++k) er[k] = ec[k] = 0.0f;
+            if (p < TI * CH_TGT && i < P.i_end && j < P.jt_end && j > i) {
+              const float* Ti = T + il * TERM_STRIDE;
+              const float* Tj = T + (TI + c * CH_TGT + jl) * TERM_STRIDE;
+              PairIn in;
+              F9 D;
+              const float sc = Ti[1] * Tj[1];
+              in.ni = Ti[0];
+              in.nj = Tj[0];
+#pragma unroll
+              for (int k = 0; k < 9; ++k) {
+                in.pja.v[k] = Tj[4 + k];
+                in.pib.v[k] = Ti[4 + k];
+              }
+              in.trPia = Ti[3];
+              in.trPjb = Tj[3];
+              in.rp = P.terms.RP;
+              in.same = true;
+#pragma unroll
+              for (int pj = 0; pj < 3; ++pj)
+#pragma unroll
+                for (int pi = 0; pi < 3; ++pi) D.v[pj * 3 + pi] = st[(3 * il + pi) * ST_STRIDE + 3 * jl + pj] * sc;
+              bool flag = false;
+              float qv[4];
+              const float rm = pair_solve_inl(D, in.ni, in.nj, in.pja, in.pib, in.trPia, in.trPjb, in.rp, in.same,
+                                              P.terms, &flag, qv);
+              const int64_t t = tri_index(P.map.n_ref, i, j);
+              if (P.bwd.rmsd) P.bwd.rmsd[t] = rm;
+              const float gij = P.bwd.g ? P.bwd.g[t] : 1.0f;
+              const float cw = (rm > 1e-6f) ? gij / rm : 0.0f;
+              const float a = qv[0], x = qv[1], y = qv[2], z = qv[3];
+              // QCP rotation R(q) (row-major); T = R^T.  I - T comes straight
+              // from the quaternion, so it is accurate when T ~ I.
+              const float R0 = a * a + x * x - y * y - z * z, R1 = 2.f * (x * y + a * z), R2 = 2.f * (z * x - a * y);
+              const float R3 = 2.f * (x * y - a * z), R4 = a * a - x * x + y * y - z * z, R5 = 2.f * (y * z + a * x);
+              const float R6 = 2.f * (z * x + a * y), R7 = 2.f * (y * z - a * x), R8 = a * a - x * x - y * y + z * z;
+              float* Bi = P.bwd.B + (size_t)(3 * i) * P.bwd.ldB + 3 * j;
+              Bi[0] = cw * R0; Bi[1] = cw * R3; Bi[2] = cw * R6;
+              Bi += P.bwd.ldB;
+              Bi[0] = cw * R1; Bi[1] = cw * R4; Bi[2] = cw * R7;
+              Bi += P.bwd.ldB;
+              Bi[0] = cw * R2; Bi[1] = cw * R5; Bi[2] = cw * R8;
+              const float d00 = 2.f * (y * y + z * z), d11 = 2.f * (x * x + z * z), d22 = 2.f * (x * x + y * y);
+              er[0] = cw * d00; er[1] = -cw * R3; er[2] = -cw * R6;
+              er[3] = -cw * R1; er[4] = cw * d11; er[5] = -cw * R7;
+              er[6] = -cw * R2; er[7] = -cw * R5; er[8] = cw * d22;
+              er[9] = cw;
+              ec[0] = cw * d00; ec[1] = -cw * R1; ec[2] = -cw * R2;
+              ec[3] = -cw * R3; ec[4] = cw * d11; ec[5] = -cw * R5;
+              ec[6] = -cw * R6; ec[7] = -cw * R7; ec[8] = cw * d22;
+              ec[9] = cw;
+            }
+            // lanes of one reference frame: CH_TGT consecutive lanes; of one
+            // target frame: every CH_TGT-th lane
+#pragma unroll
+            for (int k = 0; k < 10; ++k) {
+#pragma unroll
+              for (int o = 1; o < CH_TGT; o <<= 1) er[k] += __shfl_xor_sync(0xffffffffu, er[k], o);
+#pragma unroll
+              for (int o = CH_TGT; o < 32; o <<= 1) ec[k] += __shfl_xor_sync(0xffffffffu, ec[k], o);
+            }
+            if ((lane & (CH_TGT - 1)) == 0 && p < TI * CH_TGT)
+#pragma unroll
+              for (int k = 0; k < 10; ++k)
+                if (er[k] != 0.0f) atomicAdd(&Erow[il * 10 + k], er[k]);
+            if (lane < CH_TGT)
+#pragma unroll
+              for (int k = 0; k < 10; ++k)
+                if (ec[k] != 0.0f) atomicAdd(&Ecol[(c * CH_TGT + jl) * 10 + k], ec[k]);
+          }
+          named_sync(1 + g, 128);
+          continue;
+        }
 #pragma unroll 1
         for (int p = tid; p < TI * CH_TGT; p += 128) {
           const int il = tri ? p / CH_TGT : p % TI;
@@ -394,6 +493,24 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
         mbar_arrive(acce_bar + 8 * b);
     }
     if (!ok) break;
+    if constexpr (BWD) {
+      // Every group's shared-memory adds for this tile are done; the next
+      // tile adds only after its own all-group barrier, past this flush.
+      named_sync(1 + EPI_GROUPS, EPI_WARPS * 32);
+      for (int x = etid; x < kEterms; x += EPI_WARPS * 32) {
+        const float v = rowbuf[x];
+        if (v == 0.0f) continue;
+        rowbuf[x] = 0.0f;
+        const int fl = x / 10, k = x % 10;
+        const int64_t f = (fl < TI) ? i0 + fl : jt0 + (fl - TI);
+        if (f < P.map.n_ref) {
+          if (k < 9)
+            atomicAdd(P.bwd.E + f * 9 + k, v);
+          else
+            atomicAdd(P.bwd.C + f, v);
+        }
+      }
+    }
     if (rows) {
       // The next tile writes rowbuf only after its own all-group barrier,
       // which every thread reaches after these stores.
@@ -641,7 +758,7 @@ __device__ __forceinline__ uint64_t smem_desc_pair(uint32_t addr) {
   return d;
 }
 
-template <class PC>
+template <class PC, bool BWD = false>
 __global__ void __launch_bounds__(THREADS, 1)
     k_pairs_tc2(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                 const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
@@ -766,7 +883,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
   } else {
     // ---------------- epilogue (both CTAs) ----------------
-    epilogue_tiles<typename PC::E>(P, tmem_base, staging, terms, rowbuf, okf, accf0, mapa_rank(acce0, 0), true,
+    epilogue_tiles<typename PC::E, BWD>(P, tmem_base, staging, terms, rowbuf, okf, accf0, mapa_rank(acce0, 0), true,
                                    cluster, n_clusters, TI2, (int)rank * TI, warp, lane);
   }
 
@@ -863,11 +980,11 @@ int64_t tc_tile_frame_end(const TcTileInfo& info, int2 tile, int variant) {
 
 // Launch of the pair-of-SMs kernel: clusters of two CTAs, as many clusters
 // as can be resident at once (one CTA per SM), at most one per tile.
-template <class PC>
+template <class PC, bool BWD = false>
 static cudaError_t launch_pair_kernel(const CUtensorMap& mAh, const CUtensorMap& mAl, const CUtensorMap& mBh,
                                       const CUtensorMap& mBl, const TcParams& P, cudaStream_t st) {
   cudaError_t e =
-      cudaFuncSetAttribute(k_pairs_tc2<PC>, cudaFuncAttributeMaxDynamicSharedMemorySize, PC::SMEM2_BYTES);
+      cudaFuncSetAttribute(k_pairs_tc2<PC, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, PC::SMEM2_BYTES);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
@@ -884,14 +1001,14 @@ static cudaError_t launch_pair_kernel(const CUtensorMap& mAh, const CUtensorMap&
   if (max_clusters == 0) {
     cfg.gridDim = dim3(2 * 76, 1, 1);
     int n = 0;
-    e = cudaOccupancyMaxActiveClusters(&n, k_pairs_tc2<PC>, &cfg);
+    e = cudaOccupancyMaxActiveClusters(&n, k_pairs_tc2<PC, BWD>, &cfg);
     if (e != cudaSuccess) return e;
     if (n < 1) return cudaErrorInvalidConfiguration;
     max_clusters = n;
   }
   const int64_t nc = std::min<int64_t>(P.n_tiles, (int64_t)max_clusters);
   cfg.gridDim = dim3((unsigned)(2 * nc), 1, 1);
-  return cudaLaunchKernelEx(&cfg, k_pairs_tc2<PC>, mAh, mAl, mBh, mBl, P);
+  return cudaLaunchKernelEx(&cfg, k_pairs_tc2<PC, BWD>, mAh, mAl, mBh, mBl, P);
 }
 
 cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
@@ -942,6 +1059,15 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
   P.err = L.dev_error;
   P.row_stores = L.row_stores;
   P.skip = L.skip;
+  if (L.bwd) {  // the backward instantiation exists for the pair-of-SMs kernels only
+    if (!pair) return cudaErrorInvalidValue;
+    P.bwd = *L.bwd;
+    P.row_stores = 0;
+    e = (L.variant == 3) ? launch_pair_kernel<PairDeep, true>(mAh, mAl, mBh, mBl, P, st)
+                         : launch_pair_kernel<PairShallow, true>(mAh, mAl, mBh, mBl, P, st);
+    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+  }
   if (pair) {
     e = (L.variant == 3) ? launch_pair_kernel<PairDeep>(mAh, mAl, mBh, mBl, P, st)
                          : launch_pair_kernel<PairShallow>(mAh, mAl, mBh, mBl, P, st);

@@ -32,6 +32,19 @@ def test_gradient_matches_fp64(h, weighted):
     assert err <= 1e-5, err
 
 
+def test_gradient_deep_stage_shape(h):
+    # from 1,280 atoms the pair pass runs the deep-stage shape of the kernel
+    X, m = synth.trajectory(5, 90, 1400, 0.5, 1.5, np.float32, True)
+    rng = np.random.default_rng(3)
+    g = rng.uniform(0.5, 1.5, 90 * 89 // 2).astype(np.float32)
+    r = np.zeros(90 * 89 // 2, np.float32)
+    grad = h.backward(X, mass=m, g=g, rmsd_out=r)
+    ref = oracle.grad_f64(X, mass=m, g=g)
+    err = np.abs(grad - ref).max() / np.abs(ref).max()
+    assert err <= 1e-5, err
+    assert np.abs(r - oracle.allpairs_f64(X, tgt_mass=m)).max() <= 1e-4
+
+
 def test_gradient_matches_finite_differences(h):
     X, m = synth.trajectory(40, 128, 300, 1.0, 1.0, np.float32, False)
     grad = h.backward(X)

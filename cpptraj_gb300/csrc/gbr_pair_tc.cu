@@ -536,7 +536,10 @@ __global__ void __launch_bounds__(THREADS, 1)
                 B_BYTES = PP::B_BYTES, A_TX = PP::A_TX, B_TX = PP::B_TX;
   if (P.skip && *P.skip != 0) return;  // a speculative launch whose speculation failed
   extern __shared__ uint8_t smem_raw[];
-  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  // 1024-byte aligned by pointer arithmetic on the shared array itself (not
+  // through an integer), so every access through it stays a shared-memory
+  // access (LDS/STS), not a generic one.
+  uint8_t* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   uint8_t* stage_base = smem;
   float* staging = (float*)(smem + STAGES * STAGE_BYTES);
   float* terms = (float*)(smem + STAGES * STAGE_BYTES + EPI_GROUPS * STAGING_BYTES);
@@ -770,7 +773,10 @@ __global__ void __launch_bounds__(THREADS, 1)
   // earlier in the stream, so both CTAs of a pair leave before any barrier.
   if (P.skip && *P.skip != 0) return;
   extern __shared__ uint8_t smem_raw[];
-  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  // 1024-byte aligned by pointer arithmetic on the shared array itself (not
+  // through an integer), so every access through it stays a shared-memory
+  // access (LDS/STS), not a generic one.
+  uint8_t* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   uint8_t* stage_base = smem;
   float* staging = (float*)(smem + STAGES2 * STAGE2_BYTES);
   float* terms = (float*)(smem + STAGES2 * STAGE2_BYTES + EPI_GROUPS * STAGING_BYTES);

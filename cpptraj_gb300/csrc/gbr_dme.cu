@@ -16,8 +16,9 @@
 // which cancels for similar frames.  Two kernels per chunk of atom pairs:
 //   k_dme_dist   distance planes D[k][f] (frames contiguous per atom pair k,
 //                FP32; the target set's frames in their own 64-aligned block)
-//   k_dme_pairs  64 x 64 frame tiles on the CUDA cores, 4 x 4 pairs per
-//                thread; slabs of 32 atom pairs staged in shared memory;
+//   k_dme_pairs  128 x 64 frame tiles on the CUDA cores, 8 x 4 pairs per
+//                thread (64 x 64 and 4 x 4 for FP64 planes); slabs of 32
+//                atom pairs staged in shared memory;
 //                each slab's 32-term FP32 sum folded into a TwoSum-compensated
 //                (hi, lo) accumulator, so the result is as accurate as FP64
 //                accumulation of FP32-rounded distances.
@@ -37,9 +38,15 @@
 namespace gbr {
 namespace {
 
-constexpr int kDT = 64;         // frames per tile side
+constexpr int kDT = 64;         // target frames per tile (tile columns)
 constexpr int kDKS = 32;        // atom pairs per shared-memory slab
-constexpr int kDThreads = 256;  // 16 x 16 threads, 4 x 4 pairs each
+constexpr int kDThreads = 256;  // 16 x 16 threads, MR x 4 pairs each
+// Reference frames per tile (tile rows): 16 MR, MR = 8 for FP32 planes (32
+// pair terms per three 16-byte shared-memory loads), 4 for FP64 planes.
+template <typename P>
+constexpr int dme_rows() {
+  return sizeof(P) == 4 ? 128 : 64;
+}
 constexpr int kDistFrames = 128;
 constexpr size_t kPlaneBudget = size_t(2) << 30;
 
@@ -139,55 +146,69 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& c, float v) {
   s = t;
 }
 
-// Tiles (ti, tj): reference frames i0 = ti*64 .. +64, target frames
-// j0 = tj*64 .. +64.  grid (n_tiles, splits).  part[(split * n_out + idx)]
-// accumulates this chunk's sum for output element idx: (hi, lo) for FP32,
-// (sum, unused) for FP64.
+// Tiles (ti, tj): reference frames i0 = ti*TR .. +TR (TR = dme_rows<P>()),
+// target frames j0 = tj*64 .. +64.  grid (n_tiles, splits).
+// part[(split * n_out + idx)] accumulates this chunk's sum for output element
+// idx: (hi, lo) for FP32, (sum, unused) for FP64.
 template <typename P>
 __global__ void __launch_bounds__(kDThreads, 2)
     k_dme_pairs(const P* __restrict__ D, int64_t Dstride, int64_t nk, int64_t tgt_col0, const int2* __restrict__ tiles,
                 OutMap map, int64_t n_out, P* __restrict__ part, int first_chunk) {
-  __shared__ __align__(16) P As[kDKS][kDT];
+  // Thread (ty, tx) owns rows g * 64 + ty * 4 + (0..3) for each 64-row group
+  // g of the tile (MR / 4 groups) and columns tx * 4 + (0..3).
+  constexpr int TR = dme_rows<P>(), MR = TR / 16;
+  __shared__ __align__(16) P As[kDKS][TR];
   __shared__ __align__(16) P Bs[kDKS][kDT];
   const int2 tl = tiles[blockIdx.x];
-  const int64_t i0 = (int64_t)tl.x * kDT, j0 = (int64_t)tl.y * kDT;
+  const int64_t i0 = (int64_t)tl.x * TR, j0 = (int64_t)tl.y * kDT;
   const int split = blockIdx.y, splits = gridDim.y;
   const int64_t nslab = (nk + kDKS - 1) / kDKS;
   const int64_t s_begin = nslab * split / splits, s_end = nslab * (split + 1) / splits;
   const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
-  P sh[4][4], sl[4][4];
+  P sh[MR][4], sl[MR][4];
 #pragma unroll
-  for (int m = 0; m < 4; ++m)
+  for (int m = 0; m < MR; ++m)
 #pragma unroll
     for (int n = 0; n < 4; ++n) sh[m][n] = sl[m][n] = P(0);
-  // staging: each thread moves 2 x 4 values of A and of B per slab
-  const int lr = tid >> 4, lc = (tid & 15) * 4;  // slab rows lr, lr + 16; columns lc..lc+3
+  // staging: A slab kDKS x TR (TR/4 float4 per row), B slab kDKS x 64
+  constexpr int AV = TR / 4;                    // 4-wide vectors per A row
+  constexpr int AH = kDKS * AV / kDThreads;     // A vectors per thread
+  const int lr = tid >> 4, lc = (tid & 15) * 4;  // B: slab rows lr, lr + 16; columns lc..lc+3
   for (int64_t sl_i = s_begin; sl_i < s_end; ++sl_i) {
     const int64_t kb = sl_i * kDKS;
 #pragma unroll
+    for (int h = 0; h < AH; ++h) {
+      const int v = tid + kDThreads * h, r = v / AV, cc = (v % AV) * 4;
+      P va[4] = {P(0), P(0), P(0), P(0)};
+      if (kb + r < nk) ld4(D + (size_t)(kb + r) * Dstride + i0 + cc, va);
+      st4(&As[r][cc], va);
+    }
+#pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int r = lr + 16 * h;
-      P va[4] = {P(0), P(0), P(0), P(0)}, vb[4] = {P(0), P(0), P(0), P(0)};
-      if (kb + r < nk) {
-        ld4(D + (size_t)(kb + r) * Dstride + i0 + lc, va);
-        ld4(D + (size_t)(kb + r) * Dstride + tgt_col0 + j0 + lc, vb);
-      }
-      st4(&As[r][lc], va);
+      P vb[4] = {P(0), P(0), P(0), P(0)};
+      if (kb + r < nk) ld4(D + (size_t)(kb + r) * Dstride + tgt_col0 + j0 + lc, vb);
       st4(&Bs[r][lc], vb);
     }
     __syncthreads();
-    P acc[4][4];
+    P acc[MR][4];
 #pragma unroll
-    for (int m = 0; m < 4; ++m)
+    for (int m = 0; m < MR; ++m)
 #pragma unroll
       for (int n = 0; n < 4; ++n) acc[m][n] = P(0);
 #pragma unroll 8
     for (int kk = 0; kk < kDKS; ++kk) {
-      P av[4], bv[4];
-      ld4(&As[kk][ty * 4], av);
+      P av[MR], bv[4];
+#pragma unroll
+      for (int hh = 0; hh < MR / 4; ++hh) {
+        P a4[4];
+        ld4(&As[kk][hh * 64 + ty * 4], a4);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) av[4 * hh + t] = a4[t];
+      }
       ld4(&Bs[kk][tx * 4], bv);
 #pragma unroll
-      for (int m = 0; m < 4; ++m)
+      for (int m = 0; m < MR; ++m)
 #pragma unroll
         for (int n = 0; n < 4; ++n) {
           const P d = av[m] - bv[n];
@@ -195,7 +216,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
         }
     }
 #pragma unroll
-    for (int m = 0; m < 4; ++m)
+    for (int m = 0; m < MR; ++m)
 #pragma unroll
       for (int n = 0; n < 4; ++n) {
         if constexpr (sizeof(P) == 4)
@@ -207,10 +228,10 @@ __global__ void __launch_bounds__(kDThreads, 2)
   }
   P* pbase = part + (size_t)split * n_out * 2;
 #pragma unroll
-  for (int m = 0; m < 4; ++m)
+  for (int m = 0; m < MR; ++m)
 #pragma unroll
     for (int n = 0; n < 4; ++n) {
-      const int64_t idx = out_index(map, i0 + ty * 4 + m, j0 + tx * 4 + n);
+      const int64_t idx = out_index(map, i0 + (m / 4) * 64 + ty * 4 + (m % 4), j0 + tx * 4 + n);
       if (idx < 0) continue;
       P* q = pbase + 2 * idx;
       if (first_chunk) {
@@ -292,18 +313,20 @@ int allpairs_dme(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
   map.base = (map.tri && row_begin < n_ref - 1) ? tri_index(n_ref, row_begin, row_begin + 1) : 0;
 
   // Plane columns: reference frames [0, ref_cols), target frames after them
-  // (FULL), each block padded to the tile size so every tile load is aligned.
-  DmeCols cols{n_ref, (n_ref + kDT - 1) / kDT * kDT};
+  // (FULL), each block padded to its tile size so every tile load is aligned.
+  const int64_t TR = f64 ? dme_rows<double>() : dme_rows<float>();
+  DmeCols cols{n_ref, (n_ref + TR - 1) / TR * TR};
   const int64_t tgt_cols = tgt_xyz ? (n_tgt + kDT - 1) / kDT * kDT : 0;
   const int64_t n_cols = cols.ref_cols + tgt_cols;
   const int64_t tgt_col0 = tgt_xyz ? cols.ref_cols : 0;
 
-  // Tiles of 64 reference x 64 target frames covering this call's rows.
+  // Tiles of TR reference x 64 target frames covering this call's rows.
   std::vector<int2> tiles;
-  const int64_t nti = (n_ref + kDT - 1) / kDT, ntj = (n_tgt + kDT - 1) / kDT;
+  const int64_t nti = (n_ref + TR - 1) / TR, ntj = (n_tgt + kDT - 1) / kDT;
   if (map.tri) {
-    for (int64_t ti = row_begin / kDT; ti < (row_end + kDT - 1) / kDT; ++ti)
-      for (int64_t tj = ti; tj < ntj; ++tj) tiles.push_back(make_int2((int)ti, (int)tj));
+    // a tile holds a pair of the upper triangle once its last column passes its first row
+    for (int64_t ti = row_begin / TR; ti < (row_end + TR - 1) / TR; ++ti)
+      for (int64_t tj = (ti * TR) / kDT; tj < ntj; ++tj) tiles.push_back(make_int2((int)ti, (int)tj));
   } else {
     for (int64_t tj = row_begin / kDT; tj < (row_end + kDT - 1) / kDT; ++tj)
       for (int64_t ti = 0; ti < nti; ++ti) tiles.push_back(make_int2((int)ti, (int)tj));

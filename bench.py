@@ -26,7 +26,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "RMSD pairs/s, 10k frames x 2k atoms: tensor-core vs plain GPU at 1e-4 Angstrom"
 N_FRAME, N_ATOM = 10000, 2000
-FLOPS_PER_PAIR = 18 * N_ATOM  # 9 products x N atoms x 2 (SURVEY 18*N; split extras not counted)
+FLOPS_PER_PAIR = 18 * N_ATOM  # algorithmic: 9 products x N atoms x 2 (the split's extra products not counted)
 # DRAM bytes (read + write) of one k_pairs_tc2 launch on this workload (the
 # deep 64-atom-stage shape the library picks at 2,000 atoms), from an ncu
 # capture of `python bench.py --profile --warmup 2` (profiles/k_pairs_tc2_10000x2000_full.md).
@@ -388,7 +388,7 @@ def dist_env():
 
 class _NvmlSampler:
     """Read-only NVML polling (SM clock, max SM clock, power, clock-event
-    reasons) in a background thread, through ctypes on the driver's
+    reasons) in a background thread, through ctypes on NVIDIA's
     libnvidia-ml; None when NVML cannot be opened."""
 
     REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",

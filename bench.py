@@ -16,6 +16,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -457,7 +458,7 @@ class Clocks:
         self.gpu = gpu_index
         self.proc = None
         self.nvml = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"gbr_clocks_{os.getpid()}.csv")
 
     def start(self):
         try:

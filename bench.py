@@ -50,8 +50,10 @@ def parse():
                     help="warm up, then run exactly one all-pairs call (for ncu); prints stats only")
     ap.add_argument("--host-io", action="store_true",
                     help="with --profile: pinned host input and output (the e2e path) instead of HBM")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3", "c4", "dme", "rms", "centroids", "accuracy"],
-                    help="c1 = the headline metric; c2/c3/c4/dme print secondary lines for the other configs")
+    ap.add_argument("--workload", default="c1",
+                    choices=["c1", "c2", "c3", "c4", "dme", "rms", "centroids", "accuracy", "hostlink"],
+                    help="c1 = the headline metric; c2/c3/c4/dme print secondary lines for the other configs; "
+                         "hostlink times plain pinned host<->device copies of the c1 input and output sizes")
     return ap.parse_args()
 
 
@@ -247,6 +249,44 @@ def main_rms(args):
                                        "cores": os.cpu_count(), "kind": "port",
                                        "sample": f"frames 0-1999, FP64 oracle (Jacobi, as Frame::RMSD_CenteredRef), "
                                                  f"OpenMP, {cpu_s:.2f} s"}}), flush=True)
+
+
+def main_hostlink(args):
+    """Plain copy-engine transfers between pinned host memory and HBM of the
+    c1 input (10,000 x 2,000 x 3 FP32) and output (the 49,995,000-float
+    triangle), in one copy and in 8 chunks spread over 1 and 4 streams: the
+    floor under the e2e numbers of the all-pairs call."""
+    import torch
+
+    sizes = {"h2d_input": 10000 * 2000 * 3 * 4, "d2h_output": 49995000 * 4}
+    rows = []
+    main_stream = torch.cuda.current_stream()
+    streams = [torch.cuda.Stream() for _ in range(4)]
+    for name, nbytes in sizes.items():
+        host = torch.empty(nbytes // 4, dtype=torch.float32, pin_memory=True)
+        host.fill_(1.0)
+        dev = torch.empty(nbytes // 4, dtype=torch.float32, device="cuda")
+        src, dst = (host, dev) if name.startswith("h2d") else (dev, host)
+        for n_chunks, n_streams in ((1, 1), (8, 1), (8, 4)):
+            bounds = np.linspace(0, src.numel(), n_chunks + 1).astype(np.int64) // 4 * 4
+            bounds[-1] = src.numel()
+
+            def run():
+                ev = torch.cuda.Event()
+                ev.record(main_stream)
+                for k in range(n_chunks):
+                    st = streams[k % n_streams] if n_streams > 1 else main_stream
+                    st.wait_event(ev)
+                    with torch.cuda.stream(st):
+                        dst[bounds[k]:bounds[k + 1]].copy_(src[bounds[k]:bounds[k + 1]], non_blocking=True)
+                for st in streams[:n_streams] if n_streams > 1 else []:
+                    main_stream.wait_stream(st)
+
+            ms = _gpu_time(run, max(5, args.steps), max(3, args.warmup))
+            rows.append({"copy": name, "bytes": nbytes, "chunks": n_chunks, "streams": n_streams, "ms": ms,
+                         "GB_per_s": nbytes / (ms * 1e6)})
+    print(json.dumps({"workload": "pinned host <-> HBM copies of the all-pairs input and output sizes",
+                      "rows": rows}), flush=True)
 
 
 def main_centroids(args):
@@ -621,7 +661,7 @@ def main():
         return main_profile(args)
     if args.workload != "c1":
         return {"c2": main_c2, "c3": main_c3, "c4": main_c4, "dme": main_dme, "rms": main_rms, "centroids": main_centroids,
-                "accuracy": main_accuracy}[args.workload](args)
+                "accuracy": main_accuracy, "hostlink": main_hostlink}[args.workload](args)
     import torch
     import torch.distributed as dist
 

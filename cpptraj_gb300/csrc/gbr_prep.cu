@@ -460,7 +460,7 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
                const double* cmass_tgt, const double* w, const double* sqw, const int* assign, int k, int use_parent,
                int nofit, double* refs, float* swr, float2* refhl, double* Eref, double* sr, float* rmax) {
   __shared__ double red[32 * 10], slots[kRefCluster * 10], bc[10];
-  __shared__ double Rs[9];
+  __shared__ double Rs[9], cs[3];
   const int N = src.N;
   const int a_first = blockIdx.x * blockDim.x + threadIdx.x, stride = kRefCluster * blockDim.x;
   const int64_t f = *fsel;
@@ -484,14 +484,21 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
       v[3] += wm;
     }
     cluster_sum_f64<4>(v, red, slots, bc);
-    double wt = m ? v[3] : (double)N;
-    if (m && wt == 0.0) {
-      wt = 1.0;
-      v[0] = v[1] = v[2] = 0.0;
+    // one thread divides (an FP64 division is a long sequence on the FP64 pipe)
+    if (threadIdx.x == 0) {
+      double wt = m ? v[3] : (double)N;
+      if (m && wt == 0.0) {
+        wt = 1.0;
+        v[0] = v[1] = v[2] = 0.0;
+      }
+      cs[0] = v[0] / wt;
+      cs[1] = v[1] / wt;
+      cs[2] = v[2] / wt;
     }
-    c0 = v[0] / wt;
-    c1 = v[1] / wt;
-    c2 = v[2] / wt;
+    __syncthreads();
+    c0 = cs[0];
+    c1 = cs[1];
+    c2 = cs[2];
   }
   __syncthreads();
   double* rk = refs + (size_t)k * 3 * N;
@@ -521,10 +528,12 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
   for (int a = a_first; a < N; a += stride) {
     const double wa = w ? w[a] : 1.0;
     const double y0 = (double)x[3 * a] - c0, y1 = (double)x[3 * a + 1] - c1, y2 = (double)x[3 * a + 2] - c2;
-    double r[3];
-    r[0] = Rs[0] * y0 + Rs[1] * y1 + Rs[2] * y2;
-    r[1] = Rs[3] * y0 + Rs[4] * y1 + Rs[5] * y2;
-    r[2] = Rs[6] * y0 + Rs[7] * y1 + Rs[8] * y2;
+    double r[3] = {y0, y1, y2};  // no parent fit: R = I
+    if (!nofit && parent >= 0) {
+      r[0] = Rs[0] * y0 + Rs[1] * y1 + Rs[2] * y2;
+      r[1] = Rs[3] * y0 + Rs[4] * y1 + Rs[5] * y2;
+      r[2] = Rs[6] * y0 + Rs[7] * y1 + Rs[8] * y2;
+    }
     const double sw = w ? sqw[a] : 1.0;
     for (int p = 0; p < 3; ++p) {
       rk[3 * a + p] = r[p];
@@ -877,21 +886,21 @@ __global__ void __launch_bounds__(128) k_sample_sum(FrameSrc<T> src, int64_t F, 
   const int64_t cnt = std::min<int64_t>((offsets ? (int64_t)offsets[k + 1] : F) - lo, (int64_t)kSample);
   const int64_t per = (cnt + kMeanChunks - 1) / kMeanChunks;
   const int64_t b0 = ch * per, b1 = std::min<int64_t>(cnt, b0 + per);
+  // Plain FP32 (the hi parts of R, t and r): the mean only has to put the
+  // reference near its frames, and every later pass takes the reference as
+  // stored, whatever its last bits.
   float s[3] = {0.0f, 0.0f, 0.0f};
   if (a < N) {
-    float rh[3], rl[3];
-    for (int p = 0; p < 3; ++p) {
-      const float2 r = refhl[((size_t)k * N + a) * 3 + p];
-      rh[p] = r.x;
-      rl[p] = r.y;
-    }
+    float rh[3];
+    for (int p = 0; p < 3; ++p) rh[p] = refhl[((size_t)k * N + a) * 3 + p].x;
     for (int64_t n = b0; n < b1; ++n) {
       const int64_t f = order ? order[lo + n] : lo + n;
       const float* tb = ftab + (size_t)kFtab * f;
       float xh[3], xl[3];
       load_atom(src.frame(f), a, xh, xl);
 #pragma unroll
-      for (int p = 0; p < 3; ++p) s[p] += dot2_row(tb + 3 * p, tb + 9 + 3 * p, tb[18 + p], tb[21 + p], xh, xl, rh[p], rl[p]);
+      for (int p = 0; p < 3; ++p)
+        s[p] += fmaf(tb[3 * p], xh[0], fmaf(tb[3 * p + 1], xh[1], fmaf(tb[3 * p + 2], xh[2], -tb[18 + p]))) - rh[p];
     }
   }
   for (int p = 0; p < 3; ++p) partial[(((size_t)k * kMeanChunks + ch) * 3 + p) * Np + a] = s[p];
@@ -1121,17 +1130,20 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
     for (int k = 0; k < 9; ++k) Us[k] = U[k];
   }
   __syncthreads();
-  // SS_ab = sum w |r_a - U r_b|^2, accumulated directly (no cancellation).
+  // SS_ab = sum w |r_a - U r_b|^2, accumulated directly (no cancellation);
+  // 0 for a reference with itself (a and b are the same in the whole cluster).
   double e[1] = {0.0};
-  for (int i = i_first; i < N; i += stride) {
-    const double wa = w ? w[i] : 1.0;
-    const double b0 = rb[3 * i], b1 = rb[3 * i + 1], b2 = rb[3 * i + 2];
-    const double d0 = ra[3 * i] - (Us[0] * b0 + Us[1] * b1 + Us[2] * b2);
-    const double d1 = ra[3 * i + 1] - (Us[3] * b0 + Us[4] * b1 + Us[5] * b2);
-    const double d2 = ra[3 * i + 2] - (Us[6] * b0 + Us[7] * b1 + Us[8] * b2);
-    e[0] += wa * (d0 * d0 + d1 * d1 + d2 * d2);
+  if (a != b) {
+    for (int i = i_first; i < N; i += stride) {
+      const double wa = w ? w[i] : 1.0;
+      const double b0 = rb[3 * i], b1 = rb[3 * i + 1], b2 = rb[3 * i + 2];
+      const double d0 = ra[3 * i] - (Us[0] * b0 + Us[1] * b1 + Us[2] * b2);
+      const double d1 = ra[3 * i + 1] - (Us[3] * b0 + Us[4] * b1 + Us[5] * b2);
+      const double d2 = ra[3 * i + 2] - (Us[6] * b0 + Us[7] * b1 + Us[8] * b2);
+      e[0] += wa * (d0 * d0 + d1 * d1 + d2 * d2);
+    }
+    cluster_sum_f64<1>(e, red, slots, bc);
   }
-  cluster_sum_f64<1>(e, red, slots, bc);
   if (blockIdx.x % kRefCluster == 0 && threadIdx.x == 0) {
     double SU[9];
     for (int p = 0; p < 3; ++p)

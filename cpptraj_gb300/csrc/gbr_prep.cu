@@ -923,12 +923,15 @@ __global__ void __launch_bounds__(32) k_ref_update(double* refs, float* swr, flo
   if (a < N) {
     double* r = refs + (size_t)k * 3 * N;
     const double sw = sqw ? sqw[a] : 1.0;
-    double rr[3];
+    double rr[3], sum[3] = {0.0, 0.0, 0.0};
+    // the chunk sums in chunk order, several chunks' loads in flight at once
+    const float* src = partial + (size_t)k * kMeanChunks * 3 * Np + a;
+#pragma unroll 8
+    for (int ch = 0; ch < kMeanChunks; ++ch)
+#pragma unroll
+      for (int p = 0; p < 3; ++p) sum[p] += (double)src[((size_t)ch * 3 + p) * Np];
     for (int p = 0; p < 3; ++p) {
-      double sum = 0.0;
-      for (int ch = 0; ch < kMeanChunks; ++ch)
-        sum += (double)partial[(((size_t)k * kMeanChunks + ch) * 3 + p) * Np + a];
-      rr[p] = r[3 * a + p] + ((cnt > 0) ? sum / (double)cnt : 0.0);
+      rr[p] = r[3 * a + p] + ((cnt > 0) ? sum[p] / (double)cnt : 0.0);
       r[3 * a + p] = rr[p];
       swr[((size_t)k * N + a) * 3 + p] = (float)(sw * rr[p]);
       const float h = (float)rr[p];
@@ -1175,6 +1178,10 @@ static int prep_grid(int64_t F, int per_sm = 16, int fpb = kWarps) {
 }
 constexpr int kScanBlocksPerSM = 4;   // k_scan: __launch_bounds__(kPrepThreads, 4)
 constexpr int kBuildBlocksPerSM = 3;  // k_build: __launch_bounds__(kPrepThreads, 3)
+// k_rot: one thread per frame, FP64 throughout; small blocks spread the
+// frames' FP64 work over more SMs.
+constexpr int kRotThreads = 64;
+static int rot_grid(int64_t frames) { return (int)std::min<int64_t>((frames + kRotThreads - 1) / kRotThreads, 4096); }
 
 template <typename T>
 static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
@@ -1258,8 +1265,7 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
         if (A.spec_build) {
           const int64_t b0 = refined ? f0 : 0;
           if (refined || f1 >= nsample) {
-            k_rot<<<(int)std::min<int64_t>((f1 - b0 + 255) / 256, 1024), 256, 0, st>>>(b0, f1, S.quat, A.cen,
-                                                                                       A.nofit, S.ftab, A.rot);
+            k_rot<<<rot_grid(f1 - b0), kRotThreads, 0, st>>>(b0, f1, S.quat, A.cen, A.nofit, S.ftab, A.rot);
             ++launches;
           }
           if (!refined && f1 >= nsample) {
@@ -1331,8 +1337,7 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
     ++K;
   }
   o.K = K;
-  k_rot<<<(int)std::min<int64_t>((F + 255) / 256, 1024), 256, 0, st>>>(0, F, S.quat, A.cen, A.nofit, S.ftab,
-                                                                        A.rot);
+  k_rot<<<rot_grid(F), kRotThreads, 0, st>>>(0, F, S.quat, A.cen, A.nofit, S.ftab, A.rot);
   ++launches;
   // Frames grouped by reference (host counting sort) when there are several.
   const int* order = nullptr;

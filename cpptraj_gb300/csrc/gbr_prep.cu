@@ -83,20 +83,20 @@ __device__ __forceinline__ void cluster_sum_f64(double (&v)[NV], double* red, do
   block_sum_f64<NV>(v, red);
   cg::cluster_group cl = cg::this_cluster();
   const unsigned rank = cl.block_rank(), n = cl.num_blocks();
-  if (threadIdx.x == 0) {
+  // Thread k handles value k (the slots of the NV values side by side, each
+  // summed in rank order).
+  if (threadIdx.x < NV) {
     double* dst = cl.map_shared_rank(slots, 0);
 #pragma unroll
-    for (int k = 0; k < NV; ++k) dst[rank * NV + k] = v[k];
+    for (int k = 0; k < NV; ++k)
+      if ((int)threadIdx.x == k) dst[rank * NV + k] = v[k];
   }
   cl.sync();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < NV) {
     const double* src = cl.map_shared_rank(slots, 0);
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      double t = 0.0;
-      for (unsigned r = 0; r < n; ++r) t += src[r * NV + k];
-      bc[k] = t;
-    }
+    double t = 0.0;
+    for (unsigned r = 0; r < n; ++r) t += src[r * NV + threadIdx.x];
+    bc[threadIdx.x] = t;
   }
   cl.sync();  // CTA 0's slots are free again; bc is visible in this CTA
 #pragma unroll

@@ -429,55 +429,54 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
               for (int k = 0; k < 10; ++k)
                 if (ec[k] != 0.0f) atomicAdd(&Ecol[(c * CH_TGT + jl) * 10 + k], ec[k]);
           }
-          named_sync(1 + g, 128);
-          continue;
-        }
+        } else {
 #pragma unroll 1
-        for (int p = tid; p < TI * CH_TGT; p += 128) {
-          const int il = tri ? p / CH_TGT : p % TI;
-          const int jl = tri ? p % CH_TGT : p / TI;
-          const int64_t i = i0 + il, jt = jc0 + jl;
-          if (i >= P.i_end || jt >= P.jt_end) continue;
-          const int64_t idx = out_index(P.map, i, jt);
-          if (idx < 0) continue;
-          bool flag = false;
-          const float* Ti = T + il * TERM_STRIDE;
-          const float* Tj = T + (TI + c * CH_TGT + jl) * TERM_STRIDE;
-          // The solver's inputs from the tile's staged terms when the pair's
-          // references are the tile's, else from global memory; one inlined
-          // solve for both, so a pair's result never depends on its tile.
-          PairIn in;
-          F9 D;
-          float sc;
-          if (__float_as_int(Ti[2]) == A && __float_as_int(Tj[2]) == B) {
-            sc = Ti[1] * Tj[1];
-            in.ni = Ti[0];
-            in.nj = Tj[0];
+          for (int p = tid; p < TI * CH_TGT; p += 128) {
+            const int il = tri ? p / CH_TGT : p % TI;
+            const int jl = tri ? p % CH_TGT : p / TI;
+            const int64_t i = i0 + il, jt = jc0 + jl;
+            if (i >= P.i_end || jt >= P.jt_end) continue;
+            const int64_t idx = out_index(P.map, i, jt);
+            if (idx < 0) continue;
+            bool flag = false;
+            const float* Ti = T + il * TERM_STRIDE;
+            const float* Tj = T + (TI + c * CH_TGT + jl) * TERM_STRIDE;
+            // The solver's inputs from the tile's staged terms when the pair's
+            // references are the tile's, else from global memory; one inlined
+            // solve for both, so a pair's result never depends on its tile.
+            PairIn in;
+            F9 D;
+            float sc;
+            if (__float_as_int(Ti[2]) == A && __float_as_int(Tj[2]) == B) {
+              sc = Ti[1] * Tj[1];
+              in.ni = Ti[0];
+              in.nj = Tj[0];
 #pragma unroll
-            for (int k = 0; k < 9; ++k) {
-              in.pja.v[k] = Tj[4 + k];
-              in.pib.v[k] = Ti[4 + k];
+              for (int k = 0; k < 9; ++k) {
+                in.pja.v[k] = Tj[4 + k];
+                in.pib.v[k] = Ti[4 + k];
+              }
+              in.trPia = Ti[3];
+              in.trPjb = Tj[3];
+              in.rp = P.terms.RP + (size_t)(B * K + A) * kRefPairStride;
+              in.same = (A == B);
+            } else {
+              sc = __ldg(P.inv_scale + i) * __ldg(P.inv_scale + P.tgt0 + jt);
+              pair_terms(i, P.tgt0 + jt, P.terms, in);
             }
-            in.trPia = Ti[3];
-            in.trPjb = Tj[3];
-            in.rp = P.terms.RP + (size_t)(B * K + A) * kRefPairStride;
-            in.same = (A == B);
-          } else {
-            sc = __ldg(P.inv_scale + i) * __ldg(P.inv_scale + P.tgt0 + jt);
-            pair_terms(i, P.tgt0 + jt, P.terms, in);
+#pragma unroll
+            for (int pj = 0; pj < 3; ++pj)
+#pragma unroll
+              for (int pi = 0; pi < 3; ++pi) D.v[pj * 3 + pi] = st[(3 * il + pi) * ST_STRIDE + 3 * jl + pj] * sc;
+            // inline: the tensor-core kernels have registers to spare (96 of 113)
+            const float r = pair_solve_inl(D, in.ni, in.nj, in.pja, in.pib, in.trPia, in.trPjb, in.rp, in.same,
+                                           P.terms, &flag);
+            if (flag) flag_pair(P.flags, P.map, i, jt);
+            if (rows)
+              rowbuf[il * RB_STRIDE + c * CH_TGT + jl] = r;
+            else
+              P.map.out[idx] = r;
           }
-#pragma unroll
-          for (int pj = 0; pj < 3; ++pj)
-#pragma unroll
-            for (int pi = 0; pi < 3; ++pi) D.v[pj * 3 + pi] = st[(3 * il + pi) * ST_STRIDE + 3 * jl + pj] * sc;
-          // inline: the tensor-core kernels have registers to spare (96 of 113)
-          const float r = pair_solve_inl(D, in.ni, in.nj, in.pja, in.pib, in.trPia, in.trPjb, in.rp, in.same,
-                                         P.terms, &flag);
-          if (flag) flag_pair(P.flags, P.map, i, jt);
-          if (rows)
-            rowbuf[il * RB_STRIDE + c * CH_TGT + jl] = r;
-          else
-            P.map.out[idx] = r;
         }
         named_sync(1 + g, 128);
       }

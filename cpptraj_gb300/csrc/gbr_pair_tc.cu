@@ -32,6 +32,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 
+#include <atomic>
 #include <vector>
 
 #include "gbr_common.cuh"
@@ -903,15 +904,20 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
 }
 
+// The driver's tensor-map encoder, looked up once (handles on several host
+// threads may race here: the pointer is published atomically).
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::atomic<PFN_cuTensorMapEncodeTiled_v12000> cached{nullptr};
+  PFN_cuTensorMapEncodeTiled_v12000 fn = cached.load(std::memory_order_acquire);
   if (!fn) {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
             cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
+        q == cudaDriverEntryPointSuccess) {
       fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+      cached.store(fn, std::memory_order_release);
+    }
   }
   return fn;
 }
@@ -1002,7 +1008,8 @@ static cudaError_t launch_pair_kernel(const CUtensorMap& mAh, const CUtensorMap&
   cfg.stream = st;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  static int max_clusters = 0;
+  static std::atomic<int> cached_clusters{0};  // per kernel instantiation; same value from every thread
+  int max_clusters = cached_clusters.load(std::memory_order_relaxed);
   if (max_clusters == 0) {
     cfg.gridDim = dim3(2 * 76, 1, 1);
     int n = 0;
@@ -1010,6 +1017,7 @@ static cudaError_t launch_pair_kernel(const CUtensorMap& mAh, const CUtensorMap&
     if (e != cudaSuccess) return e;
     if (n < 1) return cudaErrorInvalidConfiguration;
     max_clusters = n;
+    cached_clusters.store(n, std::memory_order_relaxed);
   }
   const int64_t nc = std::min<int64_t>(P.n_tiles, (int64_t)max_clusters);
   cfg.gridDim = dim3((unsigned)(2 * nc), 1, 1);

@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--frames", type=int, default=N_FRAME)
     ap.add_argument("--atoms", type=int, default=N_ATOM)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the secondary workloads (c0, c2, c3, c4) reported under `secondary`")
     ap.add_argument("--tc-pipeline", type=int, default=None, choices=[-1, 0, 1, 2, 3],
                     help="tensor-core kernel shape (GBR_OPT_TC_PIPELINE); default: the library's")
     ap.add_argument("--profile", action="store_true",
@@ -71,8 +73,71 @@ def _gpu_time(fn, steps, warmup):
     return ev0.elapsed_time(ev1) / steps
 
 
-def main_c2(args):
-    """Clustering pairwise cache: 50,000 frames x 500 atoms around 20 centroids, TRI in HBM."""
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def _tc_peak(peaks):
+    """(peak TFLOP/s, description) of the dense fp16/bf16 tensor pipe."""
+    if "bf16_tflops" in peaks:
+        return float(peaks["bf16_tflops"]), "dense bf16/fp16 tensor burst (measured)"
+    return 1900.0, "dense bf16/fp16 tensor burst (fallback)"
+
+
+def _sample_pairs(F, n, seed):
+    rng = np.random.default_rng(seed)
+    pi = rng.integers(0, F - 1, n)
+    pj = np.array([rng.integers(i + 1, F) for i in pi], dtype=np.int64)
+    return pi, pj, F * pi - ((pi + 1) * pi) // 2 + pj - pi - 1
+
+
+def _roof(flops, ms, peaks):
+    peak, kind = _tc_peak(peaks)
+    tf = flops / (ms / 1e3) / 1e12
+    return {"algorithmic_tflops": tf, "frac": tf / peak, "peak": peak, "peak_kind": kind,
+            "flops_per_call": flops}
+
+
+def sec_c0(args, peaks):
+    """rms2d, 500 frames x 304 atoms, FP64 coordinates, unweighted, fit; every
+    pair against the FP64 oracle; the whole triangle on the CPU beside it."""
+    import torch
+
+    import oracle
+    from cpptraj_gb300 import gbrmsd, synth
+
+    X, _ = synth.workload_c0()
+    F, N = X.shape[0], X.shape[1]
+    pairs = F * (F - 1) // 2
+    h = gbrmsd.Handle(0)
+    h.set_stream(torch.cuda.current_stream().cuda_stream)
+    h.set_option(gbrmsd.OPT_TIMING, 1)
+    dX = torch.from_numpy(X).cuda()
+    out = torch.empty(pairs, dtype=torch.float32, device="cuda")
+    ms = _gpu_time(lambda: h.allpairs(dX, precision="tc", out=out), max(5, args.steps), 3)
+    st = h.stats()
+    ref = oracle.allpairs_f64(X)
+    err = float(np.abs(out.cpu().numpy().astype(np.float64) - ref).max())
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    oracle.allpairs(X, nthreads=threads)
+    cpu_s = time.perf_counter() - t0
+    h.close()
+    return {"workload": f"rms2d fit, {F} frames x {N} atoms, FP64 coords, unweighted, TRI {pairs} pairs",
+            "precision": "tc", "pairs_per_s": pairs / (ms / 1e3), "ms_per_call": ms, "kernel_ms": st["ms_pairs"],
+            **_roof(pairs * 18.0 * N, ms, peaks), "bound": "launch/latency (parity case)",
+            "max_abs_err_A": err, "err_sample": "every pair vs FP64 oracle",
+            "cpu_baseline": {"value": pairs / cpu_s, "unit": "pairs/s", "cores": threads, "kind": "port",
+                             "sample": f"the whole {pairs}-pair triangle, FP64 oracle (restatement of "
+                                       f"Frame::RMSD_CenteredRef), OpenMP, {cpu_s:.3f} s"}}
+
+
+def sec_c2(args, peaks, precisions=("tc",)):
+    """Clustering pairwise cache: 50,000 frames x 500 atoms around 20
+    centroids, TRI (1.25e9 floats, 5 GB) in HBM."""
     import torch
 
     import oracle
@@ -87,28 +152,41 @@ def main_c2(args):
     h.set_option(gbrmsd.OPT_TIMING, 1)
     dX = torch.from_numpy(X).cuda()
     out = torch.empty(pairs, dtype=torch.float32, device="cuda")
+    pi, pj, idx = _sample_pairs(F, 2000, 0)
+    ref = oracle.pairs_f64(X, pi, pj)
     res = {}
-    for prec in ("tc", "fp32"):
-        ms = _gpu_time(lambda: h.allpairs(dX, precision=prec, out=out), max(1, args.steps // 2), 1)
+    for prec in precisions:
+        ms = _gpu_time(lambda: h.allpairs(dX, precision=prec, out=out), max(2, args.steps // 4), 1)
         st = h.stats()
-        rng = np.random.default_rng(0)
-        pi = rng.integers(0, F - 1, 2000)
-        pj = np.array([rng.integers(i + 1, F) for i in pi])
-        ref = oracle.pairs_f64(X, pi, pj)
-        idx = F * pi - ((pi + 1) * pi) // 2 + pj - pi - 1
         got = out[torch.from_numpy(idx).cuda()].cpu().numpy().astype(np.float64)
         same = labels[pi] == labels[pj]
         res[prec] = {"pairs_per_s": pairs / (ms / 1e3), "ms_per_call": ms, "kernel_ms": st["ms_pairs"],
                      "prep_ms": st["ms_prep"], "fixup_ms": st["ms_fixup"], "pairs_fixed": st["pairs_fixed"],
-                     "n_refs": st["n_refs"], "max_abs_err_A": float(np.abs(got - ref).max()),
+                     "n_refs": st["n_refs"], **_roof(pairs * 18.0 * N, ms, peaks),
+                     "kernel_tflops": pairs * 18.0 * N / (st["ms_pairs"] / 1e3) / 1e12 if st["ms_pairs"] else None,
+                     "max_abs_err_A": float(np.abs(got - ref).max()), "err_sample": "2000 random pairs vs FP64 oracle",
                      "mean_rmsd_same_centroid": float(got[same].mean()),
                      "mean_rmsd_other_centroid": float(got[~same].mean())}
-    print(json.dumps({"workload": f"c2 clustering cache, {F} frames x {N} atoms, 20 centroids, TRI {pairs} "
-                                  f"pairs ({pairs * 4 / 1e9:.2f} GB) in HBM", "results": res}), flush=True)
+    del out, dX
+    h.close()
+    torch.cuda.empty_cache()
+    threads = os.cpu_count() or 1
+    rows, cpairs = cpu_sample_rows(F, N, 2_000_000)
+    t0 = time.perf_counter()
+    oracle.allpairs(X, row_begin=0, row_end=rows, nthreads=threads)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": f"clustering pairwise cache, {F} frames x {N} atoms, 20 centroids, FP32, unweighted, "
+                        f"TRI {pairs} pairs ({pairs * 4 / 1e9:.2f} GB) in HBM",
+            "bound": "epilogue (N = 500 atoms)", **res,
+            "cpu_baseline": {"value": cpairs / cpu_s, "unit": "pairs/s", "cores": threads, "kind": "port",
+                             "sample": f"rows [0,{rows}) = {cpairs} pairs, FP64 oracle, OpenMP, {cpu_s:.2f} s"}}
 
 
-def main_c3(args):
-    """256 independent trajectories (frames U[100,4000], atoms U[50,3000]), mass-weighted, one batched call."""
+def sec_c3(args, peaks, precisions=("tc",)):
+    """256 independent trajectories (frames U[100,4000], atoms U[50,3000]),
+    mass-weighted, one batched call (autotuned, CUDA graph)."""
+    import ctypes
+
     import torch
 
     import oracle
@@ -118,7 +196,6 @@ def main_c3(args):
     h = gbrmsd.Handle(0)
     _apply_pipeline(h, args)
     h.set_stream(torch.cuda.current_stream().cuda_stream)
-    import ctypes
     n = len(batch)
     dX = [torch.from_numpy(X).cuda() for X, _ in batch]
     dm = [torch.from_numpy(m).cuda() for _, m in batch]
@@ -130,9 +207,15 @@ def main_c3(args):
     ms_ = P(*[m.data_ptr() for m in dm])
     op = P(*[o.data_ptr() for o in outs])
     pairs = sum(X.shape[0] * (X.shape[0] - 1) // 2 for X, _ in batch)
-    flops = sum(18 * X.shape[1] * X.shape[0] * (X.shape[0] - 1) // 2 for X, _ in batch)
+    flops = float(sum(18 * X.shape[1] * X.shape[0] * (X.shape[0] - 1) // 2 for X, _ in batch))
+    check = list(range(0, n, n // 8))
+    samples = {}
+    for t in check:
+        X, m = batch[t]
+        pi, pj, idx = _sample_pairs(X.shape[0], 500, t)
+        samples[t] = (idx, oracle.pairs_f64(X, pi, pj, mass=m))
     res = {}
-    for prec in ("tc", "fp32"):
+    for prec in precisions:
         p = gbrmsd.PRECISIONS[prec]
 
         def call():
@@ -140,23 +223,43 @@ def main_c3(args):
                                                 ctypes.cast(nf, ctypes.c_void_p), ctypes.cast(na, ctypes.c_void_p),
                                                 ctypes.cast(ms_, ctypes.c_void_p), gbrmsd.FIT, p,
                                                 ctypes.cast(op, ctypes.c_void_p)))
-        import time as _t
-        t0 = _t.perf_counter()
+        t0 = time.perf_counter()
         call()  # autotune unseen shape buckets + capture the graph
         torch.cuda.synchronize()
-        first_ms = 1e3 * (_t.perf_counter() - t0)
-        ms = _gpu_time(call, max(2, args.steps), 1)
+        first_ms = 1e3 * (time.perf_counter() - t0)
+        ms = _gpu_time(call, max(2, args.steps // 4), 1)
         st = h.stats()
-        errs = []
-        for t in (0, 1, 2):
-            X, m = batch[t]
-            ref = oracle.allpairs_f64(X, tgt_mass=m)
-            errs.append(float(np.abs(outs[t].cpu().numpy() - ref).max()))
+        err = 0.0
+        for t, (idx, ref) in samples.items():
+            got = outs[t][torch.from_numpy(idx).cuda()].cpu().numpy().astype(np.float64)
+            err = max(err, float(np.abs(got - ref).max()))
         res[prec] = {"pairs_per_s": pairs / (ms / 1e3), "ms_per_call": ms, "first_call_ms": first_ms,
-                     "algorithmic_tflops": flops / (ms / 1e3) / 1e12, "kernel_launches": st["kernel_launches"],
-                     "pairs_fixed": st["pairs_fixed"], "max_abs_err_A_first3": max(errs)}
-    print(json.dumps({"workload": f"c3 batch of {n} trajectories, {pairs} pairs, {flops / 1e12:.2f} TFLOP "
-                                  f"algorithmic", "results": res}), flush=True)
+                     **_roof(flops, ms, peaks), "kernel_launches": st["kernel_launches"],
+                     "pairs_fixed": st["pairs_fixed"], "max_abs_err_A": err,
+                     "err_sample": f"500 random pairs in each of trajectories {check} vs FP64 oracle"}
+    del outs, dX, dm
+    h.close()
+    torch.cuda.empty_cache()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    cpairs = 0
+    for X, m in batch:
+        oracle.allpairs(X, tgt_mass=m, row_begin=0, row_end=1, nthreads=threads)
+        cpairs += X.shape[0] - 1
+    cpu_s = time.perf_counter() - t0
+    return {"workload": f"batch of {n} trajectories (frames U[100,4000], atoms U[50,3000]), FP32, mass-weighted, "
+                        f"{pairs} pairs, {flops / 1e12:.2f} TFLOP algorithmic, one call", **res,
+            "cpu_baseline": {"value": cpairs / cpu_s, "unit": "pairs/s", "cores": threads, "kind": "port",
+                             "sample": f"row 0 of every trajectory = {cpairs} pairs, FP64 oracle, OpenMP, "
+                                       f"{cpu_s:.2f} s"}}
+
+
+def main_c2(args):
+    print(json.dumps(sec_c2(args, _peaks(), ("tc", "fp32"))), flush=True)
+
+
+def main_c3(args):
+    print(json.dumps(sec_c3(args, _peaks(), ("tc", "fp32"))), flush=True)
 
 
 def main_dme(args):
@@ -362,8 +465,10 @@ def main_accuracy(args):
     print(json.dumps({"workload": "accuracy calibration, 3,000 sampled pairs per case", "rows": rows}), flush=True)
 
 
-def main_c4(args):
-    """Gradient of sum_{i<j} RMSD_ij, 4,096 frames x 1,000 atoms, FP32 with FD check on 64 coordinates."""
+def sec_c4(args, peaks):
+    """Gradient of L = sum_{i<j} RMSD_ij, 4,096 frames x 1,000 atoms, FP32:
+    central finite differences (h = 1e-3 Angstrom) on 64 coordinates and the
+    analytic FP64 gradient of every coordinate (the oracle, OpenMP)."""
     import torch
 
     import oracle
@@ -371,26 +476,49 @@ def main_c4(args):
 
     X, _ = synth.workload_c4()
     F, N = X.shape[0], X.shape[1]
+    pairs = F * (F - 1) // 2
     h = gbrmsd.Handle(0)
     _apply_pipeline(h, args)
     h.set_stream(torch.cuda.current_stream().cuda_stream)
     h.set_option(gbrmsd.OPT_TIMING, 1)
     dX = torch.from_numpy(X).cuda()
     grad = torch.empty_like(dX)
-    out = torch.empty(F * (F - 1) // 2, device="cuda")
-    fwd_ms = _gpu_time(lambda: h.allpairs(dX, precision="tc", out=out), 3, 2)
-    bwd_ms = _gpu_time(lambda: h.backward(dX, grad=grad), max(2, args.steps // 2), 1)
+    out = torch.empty(pairs, device="cuda")
+    fwd_ms = _gpu_time(lambda: h.allpairs(dX, precision="tc", out=out), max(3, args.steps // 4), 2)
+    bwd_ms = _gpu_time(lambda: h.backward(dX, grad=grad), max(3, args.steps // 4), 2)
     st = h.stats()
-    g = grad.cpu().numpy()
+    g = grad.cpu().numpy().astype(np.float64)
+    h.close()
     rng = np.random.default_rng(4)
+    threads = os.cpu_count() or 1
     worst, gmax = 0.0, float(np.abs(g).max())
     for _ in range(64):
         f, a, p = int(rng.integers(0, F)), int(rng.integers(0, N)), int(rng.integers(0, 3))
-        fd = oracle.fd_f64(X, f, a, p, 1e-3)
-        worst = max(worst, float(abs(float(g[f, a, p]) - fd) / max(abs(fd), 1e-3 * gmax)))
-    print(json.dumps({"workload": f"c4 gradient of sum RMSD, {F} frames x {N} atoms",
-                      "forward_tc_ms": fwd_ms, "backward_ms": bwd_ms, "backward_stats": st,
-                      "fd_check": {"coordinates": 64, "h": 1e-3, "max_rel_err": worst}}), flush=True)
+        fd = oracle.fd_f64(X, f, a, p, 1e-3, nthreads=threads)
+        worst = max(worst, float(abs(g[f, a, p] - fd) / max(abs(fd), 1e-3 * gmax)))
+    t0 = time.perf_counter()
+    g64 = oracle.grad_f64(X, nthreads=threads)
+    cpu_s = time.perf_counter() - t0
+    d = np.abs(g - g64)
+    big = np.abs(g64) > 1e-3 * np.abs(g64).max()
+    # algorithmic flops of the backward: the pair pass (18 N per pair, as the
+    # forward) plus the per-pair block contraction (2 x 9 N per ordered pair)
+    flops = pairs * (18.0 + 36.0) * N
+    return {"workload": f"gradient of sum_(i<j) RMSD_ij, {F} frames x {N} atoms, FP32",
+            "forward_tc_ms": fwd_ms, "backward_ms": bwd_ms, "pairs_per_s": pairs / (bwd_ms / 1e3),
+            **_roof(flops, bwd_ms, peaks), "backward_stats": st,
+            "fd_check": {"coordinates": 64, "h": 1e-3, "max_rel_err": worst},
+            "fp64_gradient_check": {"coordinates": int(g.size), "max_abs_err": float(d.max()),
+                                    "max_abs_err_rel_to_max_grad": float(d.max() / np.abs(g64).max()),
+                                    "max_rel_err_where_large": float((d[big] / np.abs(g64[big])).max()),
+                                    "rel_l2_err": float(np.linalg.norm(g - g64) / np.linalg.norm(g64))},
+            "cpu_baseline": {"value": pairs / cpu_s, "unit": "pairs/s (gradient)", "cores": threads,
+                             "kind": "port", "sample": f"the full FP64 analytic gradient, oracle, OpenMP, "
+                                                       f"{cpu_s:.2f} s"}}
+
+
+def main_c4(args):
+    print(json.dumps(sec_c4(args, _peaks())), flush=True)
 
 
 def main_profile(args):
@@ -800,9 +928,24 @@ def main():
         except Exception as e:  # the baseline is reported, never required
             line["cpu_baseline"] = {"value": None, "unit": "pairs/s", "cores": os.cpu_count(), "kind": "port",
                                     "sample": f"failed: {e}"}
+    h.close()
+    if rank == 0 and ws == 1 and not args.no_secondary:
+        # the other configurations of this path, each with its own accuracy
+        # check and CPU baseline (steps scaled down; see each function)
+        del dX, dm, out, hX, hout
+        torch.cuda.empty_cache()
+        sec = {}
+        for name, fn in (("c0", sec_c0), ("c2", sec_c2), ("c3", sec_c3), ("c4", sec_c4)):
+            t0 = time.perf_counter()
+            try:
+                sec[name] = fn(args, peaks)
+            except Exception as e:  # reported, never fatal for the headline line
+                sec[name] = {"error": f"{type(e).__name__}: {e}"}
+            sec[name]["wall_s"] = time.perf_counter() - t0
+            torch.cuda.empty_cache()
+        line["secondary"] = sec
     if rank == 0:
         print(json.dumps(line), flush=True)
-    h.close()
     if ws > 1:
         dist.destroy_process_group()
 

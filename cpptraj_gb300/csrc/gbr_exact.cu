@@ -82,15 +82,16 @@ __global__ void __launch_bounds__(256) k_exact(ExactLaunch L) {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
     if (lane == 0) {
+      const double Wsum = L.dWsum ? *L.dWsum : L.Wsum;
       double rms;
       if (L.nofit) {
-        rms = (v[9] < 0.0) ? 0.0 : sqrt(v[9] / L.Wsum);
+        rms = (v[9] < 0.0) ? 0.0 : sqrt(v[9] / Wsum);
       } else {
         double R[9];
         const double E0 = 0.5 * v[9];
         const double lam = qcp_lambda_rot(v, E0, R);
         const double e = E0 - lam;
-        rms = (e < 0.0) ? 0.0 : sqrt(2.0 * e / L.Wsum);
+        rms = (e < 0.0) ? 0.0 : sqrt(2.0 * e / Wsum);
       }
       const int64_t idx = out_index(L.map, i, jt);
       if (idx >= 0) L.map.out[idx] = (float)rms;

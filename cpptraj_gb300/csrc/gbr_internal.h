@@ -231,6 +231,7 @@ struct ExactLaunch {
   const double* cen;  // [F][3] set-frame centres (zeros for no-fit)
   const double* w;    // target masses or nullptr
   double Wsum;
+  const double* dWsum;  // non-null: the total weight is read from this device word instead of Wsum
   int nofit;
   int64_t tgt0;
   OutMap map;

@@ -37,6 +37,7 @@
 
 #include "gbr_common.cuh"
 #include "gbr_internal.h"
+#include "gbr_mbar.cuh"
 
 namespace gbr {
 
@@ -98,7 +99,6 @@ constexpr int SMEM_BYTES = 1024 + 2 * (2 * UM * 128 + 2 * UN * 128) + EPI_BYTES 
 static_assert(SMEM_BYTES <= 232448, "one-SM kernel shared memory");
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t ACC_STRIDE = 256;
-constexpr long long TIMEOUT_CYCLES = 4000000000LL;
 
 // Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = F16
 // (bits 7-12 = 0), both K-major (bits 15-16 = 0), N >> 3 at bits 17-22,
@@ -124,51 +124,6 @@ struct TcParams {
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait: false (and *err set) when the phase does not complete in
-// time or another thread already reported an error.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
-  if (mbar_try(bar, parity)) return true;
-  const long long t0 = clock64();
-  for (uint32_t it = 1;; ++it) {
-    if (mbar_try(bar, parity)) return true;
-    if ((it & 255u) == 0) {
-      if (*(volatile int*)err != 0) return false;
-      if (clock64() - t0 > TIMEOUT_CYCLES) {
-        atomicCAS(err, 0, code);
-        return false;
-      }
-    }
-  }
-}
-
-// Bounded wait that ignores the error flag (used to drain our own TMA copies).
-__device__ __forceinline__ void mbar_wait_quiet(uint32_t bar, uint32_t parity) {
-  const long long t0 = clock64();
-  while (!mbar_try(bar, parity)) {
-    if (clock64() - t0 > TIMEOUT_CYCLES) return;
-  }
-}
 
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z,
                                             uint32_t bar) {
@@ -1008,16 +963,26 @@ static cudaError_t launch_pair_kernel(const CUtensorMap& mAh, const CUtensorMap&
   cfg.stream = st;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  static std::atomic<int> cached_clusters{0};  // per kernel instantiation; same value from every thread
-  int max_clusters = cached_clusters.load(std::memory_order_relaxed);
+  // Resident clusters, per kernel instantiation and device (devices of one
+  // process may differ in SM count); every thread computes the same value.
+  constexpr int kMaxDev = 64;
+  static std::atomic<int> cached_clusters[kMaxDev] = {};
+  int dev = 0;
+  e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
+  int max_clusters = cached_clusters[dev].load(std::memory_order_relaxed);
   if (max_clusters == 0) {
-    cfg.gridDim = dim3(2 * 76, 1, 1);
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    cfg.gridDim = dim3((unsigned)(sms & ~1), 1, 1);
     int n = 0;
     e = cudaOccupancyMaxActiveClusters(&n, k_pairs_tc2<PC, BWD>, &cfg);
     if (e != cudaSuccess) return e;
     if (n < 1) return cudaErrorInvalidConfiguration;
     max_clusters = n;
-    cached_clusters.store(n, std::memory_order_relaxed);
+    cached_clusters[dev].store(n, std::memory_order_relaxed);
   }
   const int64_t nc = std::min<int64_t>(P.n_tiles, (int64_t)max_clusters);
   cfg.gridDim = dim3((unsigned)(2 * nc), 1, 1);

@@ -50,13 +50,17 @@ __global__ void k_weight_sum(const double* mass, int n, double* W) {
   if (threadIdx.x == 0) *W = part[0];
 }
 
-bool on_device(const void* p) {
+// True when p is device (or managed) memory that belongs to device `dev`:
+// the kernels run on the current device, which cannot reach another GPU's
+// memory without peer access.
+bool on_device(const void* p, int dev) {
   cudaPointerAttributes at{};
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  if (at.type == cudaMemoryTypeManaged) return true;
+  return at.type == cudaMemoryTypeDevice && at.device == dev;
 }
 
 }  // namespace
@@ -73,9 +77,9 @@ extern "C" int gbr_allpairs_fp64_static(const void* xyz, int dtype, int64_t n_fr
   // Scratch: centres [n_frame][3] doubles, then the total weight.
   const size_t need = sizeof(double) * (3 * (size_t)n_frame + 1);
   if (need > kStaticScratchBytes) return GBR_ERR_NOMEM;  // beyond the fixed scratch (~1.39M frames)
-  if (!on_device(xyz) || !on_device(out) || (mass && !on_device(mass))) return GBR_ERR_ARG;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return GBR_ERR_CUDA;
+  if (!on_device(xyz, dev) || !on_device(out, dev) || (mass && !on_device(mass, dev))) return GBR_ERR_ARG;
   void* base = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_static_mutex);
@@ -92,12 +96,9 @@ extern "C" int gbr_allpairs_fp64_static(const void* xyz, int dtype, int64_t n_fr
   cudaStream_t st = (cudaStream_t)stream;
   double* cen = (double*)base;
   double* dW = cen + 3 * (size_t)n_frame;
+  // The total weight stays on the device: the pair kernel reads it there, and
+  // the host looks at it only after the last kernel (one wait per call).
   k_weight_sum<<<1, 256, 0, st>>>(mass, n_atom, dW);
-  double W = 0.0;
-  if (cudaMemcpyAsync(&W, dW, sizeof W, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess)
-    return GBR_ERR_CUDA;
-  if (W < 1e-14) return GBR_ERR_ZERO_MASS;
 
   PrepArgs pa{};
   pa.dtype_f64 = (dtype == GBR_F64);
@@ -121,7 +122,7 @@ extern "C" int gbr_allpairs_fp64_static(const void* xyz, int dtype, int64_t n_fr
   ex.N = n_atom;
   ex.cen = cen;
   ex.w = mass;
-  ex.Wsum = W;
+  ex.dWsum = dW;
   ex.nofit = pa.nofit;
   ex.tgt0 = 0;
   OutMap map{};
@@ -136,6 +137,12 @@ extern "C" int gbr_allpairs_fp64_static(const void* xyz, int dtype, int64_t n_fr
   ex.list = nullptr;
   ex.count = n_pairs;
   if (run_exact(ex, st) != cudaSuccess) return GBR_ERR_CUDA;
-  if (cudaStreamSynchronize(st) != cudaSuccess) return GBR_ERR_CUDA;
+  double W = 0.0;
+  if (cudaMemcpyAsync(&W, dW, sizeof W, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return GBR_ERR_CUDA;
+  // Zero total mass: the reference refuses the pair (src/Constants.h:35);
+  // the triangle written meanwhile is not a result.
+  if (W < 1e-14) return GBR_ERR_ZERO_MASS;
   return GBR_OK;
 }

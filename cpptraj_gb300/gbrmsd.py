@@ -32,7 +32,7 @@ MODES = {"fit": FIT, "nofit": NOFIT, "dme": DME}
 EXPORTED = ("gbr_create", "gbr_destroy", "gbr_last_error", "gbr_allpairs", "gbr_output_count",
             "gbr_allpairs_batched", "gbr_rmsd_backward", "gbr_get_stats", "gbr_set_option", "gbr_set_stream",
             "gbr_write_cmatrix", "gbr_superpose", "gbr_cluster_centroids",
-            "gbr_allpairs_fp64_static")
+            "gbr_allpairs_fp64_static", "gbr_selftest_bounded_wait")
 
 
 class GbrError(RuntimeError):
@@ -93,6 +93,8 @@ def load():
         L.gbr_cluster_centroids.argtypes = [vp, vp, ci, i64, i32, vp, ci, vp, vp, i64, vp]
         L.gbr_allpairs_fp64_static.restype = ci
         L.gbr_allpairs_fp64_static.argtypes = [vp, ci, i64, i32, vp, ci, vp, vp]
+        L.gbr_selftest_bounded_wait.restype = ci
+        L.gbr_selftest_bounded_wait.argtypes = [vp, i64, vp, vp]
         _lib = L
         return L
 
@@ -162,6 +164,13 @@ class Handle:
         """Use a caller's cudaStream_t (an int pointer value, e.g.
         torch.cuda.current_stream().cuda_stream); None restores the handle's own."""
         self._check(self.lib.gbr_set_stream(self.h, stream_ptr))
+
+    def selftest_bounded_wait(self, limit_cycles: int = 2_000_000):
+        """Run the bounded-wait expiry self-test; returns (site code, cycles waited)."""
+        site, waited = ctypes.c_int32(0), ctypes.c_int64(0)
+        self._check(self.lib.gbr_selftest_bounded_wait(self.h, int(limit_cycles), ctypes.byref(site),
+                                                       ctypes.byref(waited)))
+        return site.value, waited.value
 
     def stats(self) -> dict:
         s = Stats()
@@ -324,15 +333,36 @@ def default_handle(device: int = 0) -> Handle:
 
 def allpairs_fp64_static(xyz, mass=None, mode="fit", out=None, stream=None):
     """gbr_allpairs_fp64_static: FP64 all-pairs RMSD with no allocation inside
-    the library.  xyz, mass and out must be CUDA tensors; returns out."""
+    the library.  xyz ([F, N, 3] float32/float64), mass ([N] float64 or None)
+    and out ([>= F(F-1)/2] float32, allocated here when None) must be CUDA
+    tensors on one device; the call runs with that device current, on
+    ``stream`` (a cudaStream_t value) or else on torch's current stream of
+    that device.  Returns out."""
     import torch
 
-    L = load()
+    if not (isinstance(xyz, torch.Tensor) and xyz.is_cuda):
+        raise ValueError("xyz must be a CUDA tensor")
+    if xyz.dim() != 3 or xyz.shape[2] != 3:
+        raise ValueError(f"xyz must have shape (frames, atoms, 3), got {tuple(xyz.shape)}")
     F, N = int(xyz.shape[0]), int(xyz.shape[1])
+    dev = xyz.device
+    n_out = max(F * (F - 1) // 2, 0)
+    if mass is not None:
+        if not (isinstance(mass, torch.Tensor) and mass.device == dev):
+            raise ValueError("mass must be a CUDA tensor on the device of xyz")
+        if mass.dtype != torch.float64 or mass.numel() != N:
+            raise ValueError(f"mass must be float64 with {N} elements, got {mass.dtype} x {mass.numel()}")
     if out is None:
-        out = torch.empty(max(F * (F - 1) // 2, 0), dtype=torch.float32, device=xyz.device)
+        out = torch.empty(n_out, dtype=torch.float32, device=dev)
+    elif not (isinstance(out, torch.Tensor) and out.device == dev):
+        raise ValueError("out must be a CUDA tensor on the device of xyz")
+    elif out.dtype != torch.float32 or out.numel() < n_out:
+        raise ValueError(f"out must be float32 with at least {n_out} elements, got {out.dtype} x {out.numel()}")
     m = MODES[mode] if isinstance(mode, str) else mode
-    rc = L.gbr_allpairs_fp64_static(_ptr(xyz), _dtype_code(xyz), F, N, _ptr(mass), m, _ptr(out), stream)
+    L = load()
+    with torch.cuda.device(dev):
+        st = torch.cuda.current_stream(dev).cuda_stream if stream is None else stream
+        rc = L.gbr_allpairs_fp64_static(_ptr(xyz), _dtype_code(xyz), F, N, _ptr(mass), m, _ptr(out), st)
     if rc != GBR_OK:
         raise GbrError(rc, "gbr_allpairs_fp64_static failed")
     return out

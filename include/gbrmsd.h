@@ -205,8 +205,9 @@ int gbr_cluster_centroids(gbr_handle *h, const void *xyz, int dtype, int64_t n_f
  * computes the same triangle as
  * gbr_allpairs(..., GBR_TRI, GBR_PREC_FP64, ...) -- every pair directly in
  * FP64 -- for one frame set: xyz (dtype GBR_F32/GBR_F64), mass (NULL =
- * unweighted) and out (n_frame*(n_frame-1)/2 floats) must all be device
- * memory; stream may be NULL (legacy default stream).  Its only scratch is a
+ * unweighted) and out (n_frame*(n_frame-1)/2 floats) must all be memory of
+ * the current CUDA device (or managed memory), else GBR_ERR_ARG; stream may
+ * be NULL (legacy default stream).  Its only scratch is a
  * fixed 32 MiB __device__ array in this library (held by every GPU that loads
  * it until the process exits): frame counts needing more (above ~1.39 million
  * frames) are rejected with GBR_ERR_NOMEM.  The first call on a device looks
@@ -257,6 +258,18 @@ int gbr_get_stats(const gbr_handle *h, gbr_stats *out);
 enum gbr_option { GBR_OPT_TAU = 0, GBR_OPT_MAX_REFS = 1, GBR_OPT_TOL = 2, GBR_OPT_TIMING = 3,
                   GBR_OPT_TC_PIPELINE = 4, GBR_OPT_HOST_OUT = 5, GBR_OPT_INPUT_OVERLAP = 6 };
 int gbr_set_option(gbr_handle *h, int key, double value);
+
+/* Self-test of the device-side failure detection.  No counterpart in the
+ * reference (its loops run on the host).  The tensor-core pair kernels bound
+ * every mbarrier wait; when a wait runs out the kernel records a site code,
+ * returns normally and the call fails with GBR_ERR_DEVICE.  This runs that
+ * same bounded-wait helper in a one-CTA kernel (no TMA, no MMA, no peer CTA)
+ * on a barrier nothing arrives on, with a limit of limit_cycles clock cycles
+ * (1000 .. 4e9).  GBR_OK means the wait gave up as designed: every thread
+ * returned, the site code was recorded (*site_out, optional) and the context
+ * is still usable; *waited_cycles (optional) is how long thread 0 waited. */
+int gbr_selftest_bounded_wait(gbr_handle *h, int64_t limit_cycles, int32_t *site_out,
+                              int64_t *waited_cycles);
 
 #ifdef __cplusplus
 }

@@ -16,7 +16,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "librmsd_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libcpptraj_rmsd_ref.so")
-REF_SRC = "/root/reference/src"
+# The reference's source tree (cpptraj's src/), used only to build _ref/;
+# GBR_REFERENCE_SRC overrides the default location.
+REF_SRC = os.environ.get("GBR_REFERENCE_SRC", "/root/reference/src")
 
 FIT, NOFIT, QCP, DME = 0, 1, 2, 3
 TRI, FULL = 0, 1

@@ -1,5 +1,5 @@
-// A C++ caller of libgbrmsd that does what the patched
-// Analysis_Rms2d::Calculate_2D in INTEGRATION.md does: frames gathered into one
+// A C++ caller of libgbrmsd that does what a patched
+// Analysis_Rms2d::Calculate_2D does: frames gathered into one
 // host buffer of doubles (as GetFrame fills a Frame), one handle per process,
 // one gbr_allpairs call per matrix, errors reported through gbr_last_error.
 //

@@ -1,5 +1,5 @@
 """The C ABI from C++: tests/cpp/rms2d_caller.cpp, written like the cpptraj-side
-call sites in INTEGRATION.md, is compiled with g++ against include/gbrmsd.h and
+call sites of the drop-in (a patched Analysis_Rms2d::Calculate_2D), is compiled with g++ against include/gbrmsd.h and
 libgbrmsd.so, run on the GPU, and its TRI / FULL / dme outputs are compared
 with the FP64 oracle (1e-4 Angstrom, the bar of this path)."""
 import os

@@ -96,7 +96,7 @@ def _check(h, X, m, precision, mode="fit", tol=TOL, **kw):
 
 @pytest.mark.parametrize("precision", _precisions())
 def test_c0_shape(h, precision):
-    X, _ = synth.workload_c0(n_frame=160)
+    X, _ = synth.workload_c0()  # the stated 500 frames x 304 atoms, FP64
     _check(h, X, None, precision, tol=2e-6 if precision == "fp64" else TOL)
 
 

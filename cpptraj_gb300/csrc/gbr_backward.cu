@@ -9,53 +9,18 @@
 // With x'_f = r + d_f (one pre-alignment reference) and c_fh = g_fh / RMSD_fh:
 //   dL/dx'_f[a] = (w_a / W) [ E_f r[a] + C_f d_f[a] - sum_h c_fh T_fh d_h[a] ]
 //   E_f = sum_h c_fh (I - T_fh),  C_f = sum_h c_fh.
-// The pair kernel (gbr_pair_fp32.cu, backward mode) recomputes every RMSD and
-// rotation and writes c*T blocks; here the blocks are symmetrised, the sum
-// over h runs as an FP32 GEMM Z = B * plane (plane = sqrt(w) d; cuBLAS,
-// strict FP32), and the
-// result is rotated back into each frame's original orientation,
-// dL/dx_f = R_f^T dL/dx'_f.
-#include <cublas_v2.h>
-
+// The backward pair kernel (the tensor-core pair kernel's backward
+// instantiation, gbr_pair_tc.cu) recomputes every RMSD and rotation and
+// writes c*T blocks; the sum over h is the tensor-core
+// contraction Z = (B + B^T) * plane of gbr_bwd_gemm.cu (plane = sqrt(w) d,
+// FP16 hi/lo split, FP32 accumulation), and the result is rotated back into
+// each frame's original orientation, dL/dx_f = R_f^T dL/dx'_f.
 #include "gbr_common.cuh"
 #include "gbr_internal.h"
 
 namespace gbr {
 
 namespace {
-
-// B := B + B^T for a square n x n matrix with row stride ld (in place), 32 x
-// 32 tile pairs.
-__global__ void k_symmetrize(float* B, int64_t n, int64_t ld) {
-  __shared__ float t1[32][33], t2[32][33];
-  const int64_t tiles = (n + 31) / 32;
-  // blockIdx.x enumerates tile pairs (ti <= tj)
-  const int64_t l = blockIdx.x;
-  const double b = 2.0 * (double)tiles + 1.0;
-  int64_t ti = (int64_t)((b - sqrt(b * b - 8.0 * (double)l)) * 0.5);
-  auto cum = [&](int64_t x) { return x * tiles - x * (x - 1) / 2; };
-  while (ti > 0 && cum(ti) > l) --ti;
-  while (cum(ti + 1) <= l) ++ti;
-  const int64_t tj = ti + (l - cum(ti));
-  const int x = threadIdx.x, y0 = threadIdx.y;  // 32 x 8 threads
-  for (int y = y0; y < 32; y += 8) {
-    const int64_t r1 = ti * 32 + y, c1 = tj * 32 + x;
-    const int64_t r2 = tj * 32 + y, c2 = ti * 32 + x;
-    t1[y][x] = (r1 < n && c1 < n) ? B[r1 * ld + c1] : 0.f;
-    t2[y][x] = (r2 < n && c2 < n) ? B[r2 * ld + c2] : 0.f;
-  }
-  __syncthreads();
-  for (int y = y0; y < 32; y += 8) {
-    const int64_t r1 = ti * 32 + y, c1 = tj * 32 + x;
-    const int64_t r2 = tj * 32 + y, c2 = ti * 32 + x;
-    if (ti == tj) {
-      if (r1 < n && c1 < n) B[r1 * ld + c1] = t1[y][x] + t1[x][y];
-    } else {
-      if (r1 < n && c1 < n) B[r1 * ld + c1] = t1[y][x] + t2[x][y];
-      if (r2 < n && c2 < n) B[r2 * ld + c2] = t2[y][x] + t1[x][y];
-    }
-  }
-}
 
 // dL/dx_f[a] = R_f^T (J (w_a E_f r[a] + sqrt(w_a) (C_f p_f[a] - Z_f[a])) / W),
 // J the centring projection g_a -> g_a - (w_a / W) sum_b g_b.  For exactly
@@ -106,32 +71,9 @@ __global__ void __launch_bounds__(256) k_grad_final(int64_t F, int N, int Np, co
 }
 }  // namespace
 
-void* blas_create() {
-  cublasHandle_t hb = nullptr;
-  if (cublasCreate(&hb) != CUBLAS_STATUS_SUCCESS) return nullptr;
-  // strict FP32: no TF32 or other reduced-precision shortcuts
-  cublasSetMathMode(hb, CUBLAS_PEDANTIC_MATH);
-  return hb;
-}
-
-void blas_destroy(void* hb) {
-  if (hb) cublasDestroy((cublasHandle_t)hb);
-}
-
 cudaError_t run_backward_tail(const BackwardTail& T, cudaStream_t st) {
-  const int64_t n = 3 * T.F;
-  const int64_t tiles = (n + 31) / 32;
-  k_symmetrize<<<(unsigned)(tiles * (tiles + 1) / 2), dim3(32, 8), 0, st>>>(T.B, n, T.ldB);
-  // Z[3F][Np] = B[3F][3F] P[3F][Np] (row-major), a plain FP32 GEMM: cuBLAS
-  // in pedantic FP32 (64 TFLOP/s at F = 4,096, N = 1,000 on GB300, against
-  // 39 for a hand-written 128 x 128-tile CUDA-core kernel).  Column-major,
-  // that is Z^T = P^T B^T.
-  cublasHandle_t hb = (cublasHandle_t)T.blas;
-  if (!hb || cublasSetStream(hb, st) != CUBLAS_STATUS_SUCCESS) return cudaErrorInvalidResourceHandle;
-  const float one = 1.0f, zero = 0.0f;
-  if (cublasSgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, (int)T.Np, (int)n, (int)n, &one, T.plane, (int)T.Np, T.B, (int)T.ldB,
-                  &zero, T.Z, (int)T.Np) != CUBLAS_STATUS_SUCCESS)
-    return cudaErrorLaunchFailure;
+  cudaError_t e = run_backward_gemm(T.gemm, st);
+  if (e != cudaSuccess) return e;
   const int g = (int)std::min<int64_t>((T.F + 7) / 8, 152 * 16);
   k_grad_final<<<g, 256, 0, st>>>(T.F, T.N, T.Np, T.E, T.C, T.rot, T.ref0, T.w, T.sqw, 1.0 / T.W, T.plane, T.Z,
                                   T.grad);

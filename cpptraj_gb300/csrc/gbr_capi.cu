@@ -32,9 +32,51 @@ constexpr int kMaxBands = 8;  // output row bands whose copies overlap the contr
 // HBM's L2 merges but the host link does not: results written straight into
 // pinned host memory keep the shallow shape.
 constexpr int kDeepStageAtoms = 1280;
+// Default band of the streamed triangle: 256 Mi floats (1 GiB per device
+// slot, two slots on the device and two in pinned host memory).
+constexpr int64_t kDefaultBandFloats = (int64_t)1 << 28;
+
+// A streamed TRI call: rows leave in bands of at most `band` floats, handed
+// to `sink` on the host in row order.
+struct RowStream {
+  int64_t band;
+  int32_t align;  // preferred band boundary (rows), the pair kernel's tile rows
+  gbr_band_sink sink;
+  void* user;
+};
+
+int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dtype, int64_t n_ref,
+                  int64_t n_tgt, int32_t n_atom, const double* ref_mass, const double* tgt_mass, int mode,
+                  int out_kind, int precision, float* out, int64_t row_begin, int64_t row_end,
+                  const RowStream* rs);
 }
 
 extern "C" {
+
+int64_t gbr_row_bands(int64_t n_frame, int64_t band_floats, int32_t row_align, int64_t* cuts, int64_t max_cuts) {
+  if (n_frame < 0 || band_floats < 1 || row_align < 1 || !cuts || max_cuts < 2) return -1;
+  auto before = [&](int64_t r) { return r * n_frame - r * (r + 1) / 2; };  // TRI elements of rows [0, r)
+  int64_t nb = 0;
+  cuts[0] = 0;
+  int64_t r = 0;
+  while (r < n_frame) {
+    const int64_t start = r;
+    // whole groups of rows ending at multiples of row_align
+    while (r < n_frame) {
+      const int64_t g = std::min(n_frame, (r / row_align + 1) * row_align);
+      if (before(g) - before(start) > band_floats) break;
+      r = g;
+    }
+    if (r == start) {  // not even the first group fits: single rows
+      while (r < n_frame && before(r + 1) - before(start) <= band_floats) ++r;
+      if (r == start) return -1;  // one row alone exceeds the band
+    }
+    if (nb + 2 > max_cuts) return -1;
+    cuts[++nb] = r;
+  }
+  if (nb == 0) cuts[++nb] = n_frame;
+  return nb;
+}
 
 gbr_handle* gbr_create(int device) {
   if (cudaSetDevice(device) != cudaSuccess) {
@@ -61,7 +103,6 @@ void gbr_destroy(gbr_handle* h) {
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   if (h->ws) cudaFree(h->ws);
-  blas_destroy(h->blas);
   h->release_batch();
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
@@ -108,6 +149,10 @@ int gbr_set_option(gbr_handle* h, int key, double value) {
       if (value != 0.0 && value != 1.0) return h->fail(GBR_ERR_ARG, "host output mode must be 0 or 1");
       h->host_out_direct = value != 0.0;
       return GBR_OK;
+    case GBR_OPT_BAND_FLOATS:
+      if (!(value >= 0.0 && value <= 9.0e18)) return h->fail(GBR_ERR_ARG, "band size must be >= 0");
+      h->band_floats = (int64_t)value;
+      return GBR_OK;
     case GBR_OPT_INPUT_OVERLAP:
       if (value != 0.0 && value != 1.0) return h->fail(GBR_ERR_ARG, "input overlap must be 0 or 1");
       h->input_overlap = value != 0.0;
@@ -134,11 +179,35 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
                  int64_t n_tgt, int32_t n_atom, const double* ref_mass, const double* tgt_mass, int mode,
                  int out_kind, int precision, float* out, int64_t row_begin, int64_t row_end) {
   if (!h) return GBR_ERR_ARG;
+  if (!out) return h->fail(GBR_ERR_ARG, "out is NULL");
+  return allpairs_impl(h, ref_xyz, tgt_xyz, dtype, n_ref, n_tgt, n_atom, ref_mass, tgt_mass, mode, out_kind,
+                       precision, out, row_begin, row_end, nullptr);
+}
+
+int gbr_allpairs_stream(gbr_handle* h, const void* xyz, int dtype, int64_t n_frame, int32_t n_atom,
+                        const double* mass, int mode, int precision, int64_t band_floats, gbr_band_sink sink,
+                        void* user) {
+  if (!h) return GBR_ERR_ARG;
+  if (!sink) return h->fail(GBR_ERR_ARG, "stream: sink is NULL");
+  if (mode == GBR_DME) return h->fail(GBR_ERR_UNSUPPORTED, "stream: dme is not streamed (use row ranges)");
+  RowStream rs{band_floats > 0 ? band_floats : kDefaultBandFloats, 1, sink, user};
+  return allpairs_impl(h, xyz, nullptr, dtype, n_frame, n_frame, n_atom, mass, mass, mode, GBR_TRI, precision,
+                       nullptr, 0, -1, &rs);
+}
+
+}  // extern "C"
+
+namespace {
+int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dtype, int64_t n_ref,
+                  int64_t n_tgt, int32_t n_atom, const double* ref_mass, const double* tgt_mass, int mode,
+                  int out_kind, int precision, float* out, int64_t row_begin, int64_t row_end,
+                  const RowStream* rs) {
+  if (!h) return GBR_ERR_ARG;
   h->err.clear();
   h->stats = gbr_stats{};
   const auto t_start = std::chrono::steady_clock::now();
   if (!ref_xyz) return h->fail(GBR_ERR_ARG, "ref_xyz is NULL");
-  if (!out) return h->fail(GBR_ERR_ARG, "out is NULL");
+  if (!out && !rs) return h->fail(GBR_ERR_ARG, "out is NULL");
   if (dtype != GBR_F32 && dtype != GBR_F64) return h->fail(GBR_ERR_ARG, "dtype must be GBR_F32 or GBR_F64");
   if (mode != GBR_FIT && mode != GBR_NOFIT && mode != GBR_DME)
     return h->fail(GBR_ERR_ARG, "mode must be GBR_FIT, GBR_NOFIT or GBR_DME");
@@ -207,10 +276,10 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
   // its device alias (Grace-Blackwell's coherent host link carries the
   // contraction's ~60 GB/s of results while it runs), instead of staging the
   // triangle in HBM and copying it back in row bands afterwards.
-  const bool out_on_dev = is_device_ptr(out);
+  const bool out_on_dev = rs ? false : is_device_ptr(out);
   float* out_k = out;
   bool out_direct = false;
-  if (!out_on_dev && h->host_out_direct) {
+  if (!rs && !out_on_dev && h->host_out_direct) {
     cudaPointerAttributes at{};
     if (cudaPointerGetAttributes(&at, out) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer) {
       out_k = (float*)at.devicePointer;
@@ -228,7 +297,30 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
   const bool need_planes = (precision != GBR_PREC_FP64);
   const bool tc = (precision == GBR_PREC_TC);
   const int64_t total_pairs = n_out;
-  const unsigned long long flag_cap = (unsigned long long)std::min<int64_t>(total_pairs, 1 << 22);
+  // A streamed call: TRI bands of at most rs->band floats, aligned to the
+  // pair kernel's tile rows where they can be; two device slots (and two
+  // pinned host slots) take turns.
+  std::vector<int64_t> scuts;
+  int64_t sband = 0;
+  if (rs) {
+    const int var = (h->tc_variant >= 0) ? h->tc_variant : (N >= kDeepStageAtoms ? 3 : 2);
+    const int32_t align = tc ? (var >= 2 ? 84 : 42) : (need_planes ? 64 : 1);
+    scuts.resize((size_t)(n_ref + 2));
+    const int64_t nb = gbr_row_bands(n_ref, rs->band, align, scuts.data(), (int64_t)scuts.size());
+    if (nb < 1)
+      return h->fail(GBR_ERR_ARG, "stream: a band of %lld floats cannot hold one row of %lld frames",
+                     (long long)rs->band, (long long)n_ref);
+    scuts.resize((size_t)nb + 1);
+    for (int64_t b = 0; b < nb; ++b)
+      sband = std::max(sband, gbr_output_count(n_ref, n_tgt, GBR_TRI, scuts[b], scuts[b + 1]));
+    sband = std::max<int64_t>(sband, 1);
+    if (!h->ensure_xfer()) return h->fail(GBR_ERR_CUDA, "stream: cannot create the copy stream");
+    if (!h->reserve_pinned(2 * ((size_t)sband + 4) * sizeof(float)))
+      return h->fail(GBR_ERR_NOMEM, "stream: cannot allocate %.2f GB of pinned staging", 8.0 * (sband + 4) / 1e9);
+  }
+  const unsigned long long flag_cap =
+      rs ? (unsigned long long)std::min<int64_t>(sband, 1 << 21)
+         : (unsigned long long)std::min<int64_t>(total_pairs, 1 << 22);
 
   OutMap map{};
   map.n_ref = n_ref;
@@ -262,9 +354,9 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     p[17] = A.take<float>((size_t)Kmax * Kmax * kRefPairStride);        // reference-pair table
     p[18] = A.take<int>(F);                                             // frames by reference
     p[19] = A.take<int>(Kmax + 1);                                      // offsets
-    p[20] = A.take<int2>(flag_cap);                                     // flagged
+    p[20] = A.take<int2>(rs ? 2 * flag_cap : flag_cap);                 // flagged (two slots when streamed)
     p[21] = A.take<unsigned long long>(kMaxBands);                      // counts (one per band)
-    p[22] = out_dev ? nullptr : A.take<float>(n_out);                   // out staging
+    p[22] = rs ? A.take<float>(2 * (size_t)sband) : out_dev ? nullptr : A.take<float>(n_out);  // out staging
     p[23] = tc ? A.take<__half_raw>((size_t)F * 3 * Np) : nullptr;      // hi
     p[24] = tc ? A.take<__half_raw>((size_t)F * 3 * Np) : nullptr;      // lo
     p[25] = A.take<int>(2);                                             // device error, speculation flags
@@ -413,7 +505,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
   // With several references, a whole triangle is computed over frames laid
   // out grouped by reference (tiles then share their references, whose terms
   // the tensor-core epilogue stages per tile); outputs map back to frames.
-  pa.sort_frames = (map.tri && row_begin == 0 && row_end == n_ref) ? 1 : 0;
+  pa.sort_frames = (!rs && map.tri && row_begin == 0 && row_end == n_ref) ? 1 : 0;
   pa.n_chunks = n_chunks;
   for (int c = 0; c < n_chunks; ++c) {
     pa.chunk_end[c] = chunk_end[c];
@@ -435,6 +527,86 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
 
   int K = 1;
   unsigned long long nflag = 0;
+  // ---- streamed bands: compute band b into device slot b & 1 while band
+  // b - 1 is copied to pinned host memory and band b - 2 is handed to the
+  // sink on the host ----
+  using BandCompute = std::function<cudaError_t(const OutMap&, const FlagList&, int64_t)>;
+  auto run_stream = [&](const BandCompute& compute) -> int {
+    const int nbands = (int)scuts.size() - 1;
+    float* dslot[2] = {(float*)P[22], (float*)P[22] + sband};
+    float* hslot[2] = {(float*)h->pinned, (float*)h->pinned + (sband + 4)};
+    unsigned long long* counts = (unsigned long long*)P[21];
+    cudaEvent_t* comp = &h->xev[14];
+    cudaEvent_t* copied = &h->xev[16];
+    std::vector<int64_t> bcnt(nbands);
+    auto drain = [&]() {
+      cudaStreamSynchronize(h->xfer);
+      cudaStreamSynchronize(st);
+    };
+    auto deliver = [&](int b) -> int {
+      const int sl = b & 1;
+      const cudaError_t e2 = cudaEventSynchronize(copied[sl]);
+      if (e2 != cudaSuccess) return h->cuda_fail(e2, "streamed band");
+      unsigned long long c = 0;
+      std::memcpy(&c, hslot[sl] + sband, sizeof c);
+      nflag += c;
+      if (rs->sink(rs->user, scuts[b], scuts[b + 1], hslot[sl], bcnt[b]) != 0)
+        return h->fail(GBR_ERR_IO, "stream: the sink stopped the call at rows [%lld, %lld)", (long long)scuts[b],
+                       (long long)scuts[b + 1]);
+      return GBR_OK;
+    };
+    for (int b = 0; b < nbands; ++b) {
+      const int sl = b & 1;
+      const int64_t rb = scuts[b], re = scuts[b + 1];
+      bcnt[b] = gbr_output_count(n_ref, n_tgt, GBR_TRI, rb, re);
+      OutMap mb = map;
+      mb.row_begin = rb;
+      mb.row_end = re;
+      mb.base = (rb < n_ref - 1) ? tri_index(n_ref, rb, rb + 1) : 0;
+      mb.out = dslot[sl];
+      mb.perm = nullptr;
+      if (b >= 2) cudaStreamWaitEvent(st, copied[sl], 0);  // device slot free once band b - 2 left it
+      cudaMemsetAsync(counts + sl, 0, sizeof(unsigned long long), st);
+      if (bcnt[b] > 0) {
+        const FlagList fb{(int2*)P[20] + (size_t)sl * flag_cap, counts + sl, flag_cap};
+        const cudaError_t e2 = compute(mb, fb, bcnt[b]);
+        if (e2 != cudaSuccess) {
+          drain();
+          return h->cuda_fail(e2, "streamed band kernel");
+        }
+      }
+      cudaEventRecord(comp[sl], st);
+      if (b >= 2) {  // host slot free once the sink has taken band b - 2
+        const int rc = deliver(b - 2);
+        if (rc != GBR_OK) {
+          drain();
+          return rc;
+        }
+      }
+      cudaStreamWaitEvent(h->xfer, comp[sl], 0);
+      if (bcnt[b] > 0)
+        cudaMemcpyAsync(hslot[sl], dslot[sl], sizeof(float) * bcnt[b], cudaMemcpyDeviceToHost, h->xfer);
+      cudaMemcpyAsync(hslot[sl] + sband, counts + sl, sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->xfer);
+      cudaEventRecord(copied[sl], h->xfer);
+    }
+    if (h->timing) {
+      cudaEventRecord(h->ev[2], st);
+      cudaEventRecord(h->ev[3], st);
+    }
+    for (int b = std::max(0, nbands - 2); b < nbands; ++b) {
+      const int rc = deliver(b);
+      if (rc != GBR_OK) {
+        drain();
+        return rc;
+      }
+    }
+    int derr = 0;
+    cudaMemcpyAsync(&derr, P[25], sizeof derr, cudaMemcpyDeviceToHost, st);
+    const cudaError_t e2 = cudaStreamSynchronize(st);
+    if (e2 != cudaSuccess) return h->cuda_fail(e2, "streamed call");
+    if (derr != 0) return h->fail(GBR_ERR_DEVICE, "pair kernel reported device error %d (bounded wait expired)", derr);
+    return GBR_OK;
+  };
   if (!need_planes) {
     // FP64 checking mode: centres only, then every pair directly.
     PrepArgs c = pa;
@@ -443,11 +615,23 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     if ((e = run_prep(c, po, st)) != cudaSuccess) return h->cuda_fail(e, "prep");
     launches += po.launches;
     if (h->timing) cudaEventRecord(h->ev[1], st);
-    if (h->timing) cudaEventRecord(h->ev[2], st);
-    ex.list = nullptr;
-    ex.count = n_out;
-    if ((e = run_exact(ex, st)) != cudaSuccess) return h->cuda_fail(e, "exact kernel");
-    ++launches;
+    if (rs) {
+      const int rc = run_stream([&](const OutMap& mb, const FlagList&, int64_t cnt) {
+        ExactLaunch eb = ex;
+        eb.map = mb;
+        eb.list = nullptr;
+        eb.count = cnt;
+        ++launches;
+        return run_exact(eb, st);
+      });
+      if (rc != GBR_OK) return rc;
+    } else {
+      if (h->timing) cudaEventRecord(h->ev[2], st);
+      ex.list = nullptr;
+      ex.count = n_out;
+      if ((e = run_exact(ex, st)) != cudaSuccess) return h->cuda_fail(e, "exact kernel");
+      ++launches;
+    }
   } else {
     // The operand build, as run_finish does it; while chunked host input
     // lands, prep runs it speculatively for one reference (K = 1, unsorted).
@@ -595,10 +779,27 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     // band's pairs are computed and checked (FP64 re-check of its flagged
     // pairs, list length read on the device), then copied on the copy stream
     // while the next band computes.
-    const bool band_out = !out_dev && !po.sorted && is_pinned_or_device(out) &&
+    const bool band_out = !rs && !out_dev && !po.sorted && is_pinned_or_device(out) &&
                           (size_t)n_out * sizeof(float) >= (32u << 20) && h->ensure_xfer();
     int derr = 0;
-    if (!band_out) {
+    if (rs) {
+      // each band: its pairs, then the FP64 re-check of its flagged pairs
+      // (list length read on the device; an overflowing list recomputes the band)
+      const int rc = run_stream([&](const OutMap& mb, const FlagList& fb, int64_t cnt) -> cudaError_t {
+        cudaError_t e2 = launch_pairs(mb, fb);
+        if (e2 != cudaSuccess) return e2;
+        ExactLaunch exb = ex;
+        exb.map = mb;
+        exb.list = fb.pairs;
+        exb.count = (int64_t)fb.cap;
+        exb.dev_count = fb.count;
+        exb.overflow_all = 1;
+        exb.map_pairs = cnt;
+        launches += 2;
+        return run_exact(exb, st);
+      });
+      if (rc != GBR_OK) return rc;
+    } else if (!band_out) {
       FlagList fl{(int2*)P[20], (unsigned long long*)P[21], flag_cap};
       if (!spec_done) {
         if ((e = launch_pairs(pmap, fl)) != cudaSuccess) return h->cuda_fail(e, "pair kernel launch");
@@ -699,7 +900,7 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
     }
   }
   if (h->timing && !need_planes) cudaEventRecord(h->ev[3], st);
-  if (!need_planes && !out_dev) cudaMemcpyAsync(out, map.out, sizeof(float) * n_out, cudaMemcpyDefault, st);
+  if (!rs && !need_planes && !out_dev) cudaMemcpyAsync(out, map.out, sizeof(float) * n_out, cudaMemcpyDefault, st);
   if (h->xfer) {  // the copy stream's work belongs to this call
     cudaEventRecord(h->xev[h->kXev - 3], h->xfer);
     cudaStreamWaitEvent(st, h->xev[h->kXev - 3], 0);
@@ -723,6 +924,10 @@ int gbr_allpairs(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dt
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
   return GBR_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t n_atom, const double* mass,
                       const float* g, float* grad_xyz, float* rmsd_out) {
@@ -759,9 +964,11 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
     return GBR_OK;
   }
   const int Np = (N + 63) / 64 * 64;
-  // The pair pass on the tensor cores (pair-of-SMs kernel, backward
-  // instantiation) where they are usable, else on the FP32 CUDA-core kernel.
-  const bool tc = h->tc_ok != 0;
+  // The pair pass (pair-of-SMs kernel, backward instantiation) and the block
+  // contraction both run on the tensor cores.
+  if (!h->tc_ok) return h->fail(GBR_ERR_UNSUPPORTED, "backward needs an sm_103 (GB300) device");
+  const bool tc = true;
+  const int64_t ldS = bwd_gemm_ld(F);
   OutMap map{};
   map.n_ref = F;
   map.n_tgt = F;
@@ -806,8 +1013,14 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
     p[33] = tc ? A.take<__half_raw>((size_t)F * 3 * Np) : nullptr;  // FP16 lo
     p[34] = tc ? A.take<int2>(tc_tiles) : nullptr;                   // tile list
     p[35] = A.take<int>(1);                                          // device error flag
+    p[36] = A.take<__half_raw>((size_t)3 * F * ldS);                 // S = B + B^T, FP16 hi
+    p[37] = A.take<__half_raw>((size_t)3 * F * ldS);                 // S, FP16 lo
+    p[38] = A.take<__half_raw>((size_t)Np * ldS);                    // plane transposed, FP16 hi
+    p[39] = A.take<__half_raw>((size_t)Np * ldS);                    // plane transposed, FP16 lo
+    p[40] = A.take<unsigned int>(2);                                 // largest |B|, |plane|
+    p[41] = A.take<float>(2);                                        // split scales
   };
-  void* P[36];
+  void* P[42];
   Arena sizing;
   layout(sizing, P);
   if (!h->reserve(sizing.off + 256))
@@ -899,6 +1112,7 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   cudaMemsetAsync(P[21], 0, sizeof(float) * 9 * F, st);
   cudaMemsetAsync(P[22], 0, sizeof(float) * F, st);
   cudaMemsetAsync(P[35], 0, sizeof(int), st);
+  cudaMemsetAsync(P[40], 0, 2 * sizeof(unsigned int), st);
   if (h->timing) cudaEventRecord(h->ev[1], st);
   PairLaunch L{};
   L.bwd.B = B;
@@ -907,6 +1121,7 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   L.bwd.C = (float*)P[22];
   L.bwd.g = d_g;
   L.bwd.rmsd = d_rmsd;
+  L.bwd.cmax = (unsigned int*)P[40];
   L.plane = pa.plane;
   L.Np = Np;
   L.N = N;
@@ -939,11 +1154,23 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   }
   if (h->timing) cudaEventRecord(h->ev[2], st);
   BackwardTail T{};
+  T.gemm.F = F;
+  T.gemm.Np = Np;
+  T.gemm.B = B;
+  T.gemm.ldB = ldB;
+  T.gemm.plane = pa.plane;
+  T.gemm.Shi = (__half*)P[36];
+  T.gemm.Slo = (__half*)P[37];
+  T.gemm.Thi = (__half*)P[38];
+  T.gemm.Tlo = (__half*)P[39];
+  T.gemm.maxbits = (unsigned int*)P[40];
+  T.gemm.scl = (float*)P[41];
+  T.gemm.Z = (float*)P[23];
+  T.gemm.dev_error = (int*)P[35];
+  T.gemm.num_sms = h->num_sms;
   T.F = F;
   T.N = N;
   T.Np = Np;
-  T.B = B;
-  T.ldB = ldB;
   T.plane = pa.plane;
   T.Z = (float*)P[23];
   T.E = (float*)P[21];
@@ -954,10 +1181,8 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   T.sqw = pa.sqw;
   T.W = Wsum;
   T.grad = d_grad;
-  if (!h->blas && !(h->blas = blas_create())) return h->fail(GBR_ERR_NOMEM, "cannot create the cuBLAS handle");
-  T.blas = h->blas;
   if ((e = run_backward_tail(T, st)) != cudaSuccess) return h->cuda_fail(e, "backward tail");
-  launches += 4;
+  launches += 6;
   if (h->timing) cudaEventRecord(h->ev[3], st);
   if (!grad_dev) cudaMemcpyAsync(grad_xyz, d_grad, sizeof(float) * 3 * N * F, cudaMemcpyDefault, st);
   if (rmsd_out && !r_dev) cudaMemcpyAsync(rmsd_out, d_rmsd, sizeof(float) * npairs, cudaMemcpyDefault, st);

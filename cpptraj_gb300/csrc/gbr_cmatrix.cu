@@ -10,11 +10,13 @@
 //   float    rows*(rows-1)/2 distances in calcTriIndex order
 //   char     one 'T' (sieved out) / 'F' (cached) per original frame, only
 //            when the sieve value is not 1.
-// The triangle is computed into device memory by gbr_allpairs and leaves
-// through two pinned host buffers: the copy of chunk k+1 overlaps the fwrite
-// of chunk k, so the file is written at disk speed without a host round trip
-// per element (DataSet_PairwiseCache_NC::SetElement writes one element at a
-// time in the reference).
+// The triangle is streamed (gbr_allpairs_stream): it is computed in row
+// bands, each band is written to the file while the next ones compute, and
+// device memory holds two bands at a time -- a cache of any size is written
+// at disk speed without a host round trip per element
+// (DataSet_PairwiseCache_NC::SetElement writes one element at a time in the
+// reference).  GBR_DME, which is not streamed, computes the whole triangle
+// in device memory and writes it in 64 MB pieces.
 #include <cstdio>
 #include <cstring>
 
@@ -43,13 +45,6 @@ extern "C" int gbr_write_cmatrix(gbr_handle* h, const char* path, const void* xy
   }
   const int64_t n = (n_frame > 1) ? n_frame * (n_frame - 1) / 2 : 0;
   if (cudaSetDevice(h->device) != cudaSuccess) return h->cuda_fail(cudaGetLastError(), "cudaSetDevice");
-  if (n > 0 && !h->reserve_out((size_t)n)) return h->fail(GBR_ERR_NOMEM, "cmatrix: cannot hold %lld floats", (long long)n);
-  if (n > 0) {
-    const int rc = gbr_allpairs(h, xyz, nullptr, dtype, n_frame, n_frame, n_atom, mass, mass, mode, GBR_TRI,
-                                precision, h->outbuf, 0, -1);
-    if (rc != GBR_OK) return rc;
-  }
-  const gbr_stats st = h->stats;  // keep the compute call's statistics
   FILE* fp = std::fopen(path, "wb");
   if (!fp) return h->fail(GBR_ERR_IO, "cmatrix: cannot open %s for writing", path);
   bool ok = true;
@@ -60,8 +55,36 @@ extern "C" int gbr_write_cmatrix(gbr_handle* h, const char* path, const void* xy
   ok = ok && std::fwrite(&orig, sizeof orig, 1, fp) == 1;
   ok = ok && std::fwrite(&rows, sizeof rows, 1, fp) == 1;
   ok = ok && std::fwrite(&sv, sizeof sv, 1, fp) == 1;
-  const size_t chunk = (size_t)16 << 20;  // floats per chunk (64 MB)
-  if (ok && n > 0) {
+  gbr_stats st{};
+  if (ok && n > 0 && mode != GBR_DME) {
+    // each band goes to the file as it arrives, in row order
+    struct Sink {
+      FILE* fp;
+      static int write(void* user, int64_t, int64_t, const float* v, int64_t count) {
+        FILE* f = static_cast<Sink*>(user)->fp;
+        return std::fwrite(v, sizeof(float), (size_t)count, f) == (size_t)count ? 0 : 1;
+      }
+    } sink{fp};
+    const int rc = gbr_allpairs_stream(h, xyz, dtype, n_frame, n_atom, mass, mode, precision, h->band_floats,
+                                       &Sink::write, &sink);
+    if (rc != GBR_OK) {
+      std::fclose(fp);
+      return rc;
+    }
+    st = h->stats;
+  } else if (ok && n > 0) {
+    if (!h->reserve_out((size_t)n)) {
+      std::fclose(fp);
+      return h->fail(GBR_ERR_NOMEM, "cmatrix: cannot hold %lld floats", (long long)n);
+    }
+    const int rc = gbr_allpairs(h, xyz, nullptr, dtype, n_frame, n_frame, n_atom, mass, mass, mode, GBR_TRI,
+                                precision, h->outbuf, 0, -1);
+    if (rc != GBR_OK) {
+      std::fclose(fp);
+      return rc;
+    }
+    st = h->stats;  // keep the compute call's statistics
+    const size_t chunk = (size_t)16 << 20;  // floats per chunk (64 MB)
     if (!h->reserve_pinned(2 * chunk * sizeof(float))) {
       std::fclose(fp);
       return h->fail(GBR_ERR_NOMEM, "cmatrix: cannot allocate pinned staging");

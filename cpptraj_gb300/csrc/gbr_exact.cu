@@ -47,10 +47,19 @@ __global__ void __launch_bounds__(256) k_exact(ExactLaunch L) {
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   int64_t count = L.count;
-  if (L.dev_count) count = (int64_t)min((unsigned long long)L.count, *L.dev_count);
+  bool use_list = L.list != nullptr;
+  if (L.dev_count) {
+    const unsigned long long c = *L.dev_count;
+    if (L.overflow_all && c > (unsigned long long)L.count) {
+      use_list = false;  // the list overflowed: every pair of the map, directly
+      count = L.map_pairs;
+    } else {
+      count = (int64_t)min((unsigned long long)L.count, c);
+    }
+  }
   for (int64_t k = warp; k < count; k += nwarps) {
     int64_t i, jt;
-    if (L.list) {
+    if (use_list) {
       const int2 p = L.list[k];
       i = p.x;
       jt = p.y;
@@ -106,6 +115,7 @@ cudaError_t run_exact(const ExactLaunch& L, cudaStream_t st) {
   // With a device-side count the true length is unknown here: use a grid
   // that covers the capacity up to a few waves and loop inside.
   const int grid = (int)std::min<int64_t>((warps_needed + 7) / 8, L.dev_count ? 152 * 8 : 152 * 32);
+  if (L.dev_count && L.overflow_all && L.map_pairs < 0) return cudaErrorInvalidValue;
   if (L.dtype_f64)
     k_exact<double><<<grid, 256, 0, st>>>(L);
   else

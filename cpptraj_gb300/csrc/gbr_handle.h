@@ -69,7 +69,7 @@ struct gbr_handle {
   int tc_variant = -1;  // -1: pairs of SMs, stage shape chosen by atom count (see gbr_set_option)
   bool host_out_direct = true;  // kernels store into pinned host output in place
   bool input_overlap = false;   // the contraction starts on input chunks that have landed
-  void* blas = nullptr;         // cuBLAS handle of the backward pass, created on first use
+  int64_t band_floats = 0;      // gbr_write_cmatrix's band size (0: the streaming default)
   // batched path: auxiliary streams, fork/join events, pinned staging,
   // the captured graph of the last batch signature, the autotuner table
   static constexpr int kAux = 8;
@@ -87,6 +87,7 @@ struct gbr_handle {
   size_t outbuf_cap = 0;
   // copies that overlap one call's compute (input chunks in, output bands out)
   cudaStream_t xfer = nullptr;
+  // 0-7 input chunks, 8-13 output bands, 14-17 streamed bands (computed, copied), 21-23 joins
   static constexpr int kXev = 24;
   cudaEvent_t xev[kXev] = {};
 

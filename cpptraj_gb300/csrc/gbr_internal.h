@@ -1,6 +1,7 @@
 // gbr_internal.h -- host-side interfaces between the C-ABI layer (gbr_capi.cu)
 // and the kernel files.  Not part of the public ABI.
 #pragma once
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -147,6 +148,7 @@ struct BwdArgs {
   float* C;          // [F]    sum_h c_fh
   const float* g;    // TRI upstream weights (nullptr = 1)
   float* rmsd;       // TRI forward values (nullptr = not stored)
+  unsigned int* cmax;  // max |c| over the pairs (float bits, max-combined), a bound of max |B|
 };
 
 struct PairLaunch {
@@ -198,14 +200,37 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st);
 int tc_supported(int device);
 int64_t tc_max_tiles(const OutMap& m);
 
-// Backward tail: symmetrise B, Z = B * plane, assemble and rotate the gradient.
+// Backward block contraction on the tensor cores (gbr_bwd_gemm.cu):
+// Z[3F][Np] = (B + B^T) * plane with both operands scaled and split into
+// FP16 hi/lo.
+struct BackwardGemm {
+  int64_t F;
+  int Np;
+  const float* B;        // [3F][ldB] upper pair blocks c*T
+  int64_t ldB;
+  const float* plane;    // [3F][Np] sqrt(w) d
+  __half* Shi;           // [3F][bwd_gemm_ld(F)] S = B + B^T, hi part
+  __half* Slo;           //                      lo part
+  __half* Thi;           // [Np][bwd_gemm_ld(F)] plane transposed, hi part
+  __half* Tlo;           //                      lo part
+  unsigned int* maxbits; // [2] bound of max |B| (set by the backward pair kernel, BwdArgs::cmax), max |plane|
+  float* scl;            // [2] 1/scale of S, of the plane
+  float* Z;              // [3F][Np]
+  int* dev_error;        // bounded-wait error word
+  int num_sms;
+};
+// Row stride (elements) of the split operands: 3F rounded up to the 64-wide K stage.
+int64_t bwd_gemm_ld(int64_t F);
+cudaError_t run_backward_gemm(const BackwardGemm& G, cudaStream_t st);
+
+// Backward tail: Z = (B + B^T) * plane (run_backward_gemm), then assemble
+// and rotate the gradient.
 struct BackwardTail {
+  BackwardGemm gemm;
   int64_t F;
   int N, Np;
-  float* B;            // [3F][ldB], columns 3F..ldB zero
-  int64_t ldB;         // 3F rounded up to a multiple of 4
   const float* plane;  // [F][3][Np]  (= [3F][Np])
-  float* Z;            // [3F][Np]
+  const float* Z;      // [3F][Np]
   const float* E;      // [F][9]
   const float* C;      // [F]
   const double* rot;   // [F][9] pre-alignment rotations
@@ -214,12 +239,8 @@ struct BackwardTail {
   const double* sqw;   // sqrt of the masses (when w is given)
   double W;
   float* grad;         // [F][N][3]
-  void* blas;          // cuBLAS handle (blas_create)
 };
 cudaError_t run_backward_tail(const BackwardTail& T, cudaStream_t st);
-// cuBLAS handle for the backward pass's plain GEMM (strict FP32), or nullptr.
-void* blas_create();
-void blas_destroy(void* hb);
 
 // Direct FP64 recomputation (flagged pairs or every pair).
 struct ExactLaunch {
@@ -239,6 +260,8 @@ struct ExactLaunch {
   int64_t count;      // pairs in list (or total pairs when list == nullptr)
   const unsigned long long* dev_count;  // non-null: the list length is read on the device,
                                         // clamped to `count` (the list capacity)
+  int overflow_all;   // with dev_count: a length above the capacity recomputes every pair of the map
+  int64_t map_pairs;  // pairs of the map (overflow_all)
 };
 cudaError_t run_exact(const ExactLaunch& L, cudaStream_t st);
 

@@ -239,6 +239,7 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
     static_assert(kEterms <= TI * E::RB_STRIDE, "row terms fit the row buffer");
     for (int x = etid; x < kEterms; x += EPI_WARPS * 32) rowbuf[x] = 0.0f;  // ordered by the first tile's barrier
   }
+  float cmax = 0.0f;  // BWD: largest |c| this thread saw (every entry of B is at most that)
   uint32_t it = 0;
   for (int64_t t = t0; t < P.n_tiles; t += tstep, ++it) {
     const uint32_t b = it & 1u, aph = (it >> 1) & 1u;
@@ -345,6 +346,7 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
               if (P.bwd.rmsd) P.bwd.rmsd[t] = rm;
               const float gij = P.bwd.g ? P.bwd.g[t] : 1.0f;
               const float cw = (rm > 1e-6f) ? gij / rm : 0.0f;
+              cmax = fmaxf(cmax, fabsf(cw));
               const float a = qv[0], x = qv[1], y = qv[2], z = qv[3];
               // QCP rotation R(q) (row-major); T = R^T.  I - T comes straight
               // from the quaternion, so it is accurate when T ~ I.
@@ -479,6 +481,11 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
         if (idx >= 0) P.map.out[idx] = rowbuf[il * RB_STRIDE + jl];
       }
     }
+  }
+  if constexpr (BWD) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cmax = fmaxf(cmax, __shfl_xor_sync(0xffffffffu, cmax, o));
+    if (lane == 0 && cmax > 0.0f && P.bwd.cmax) atomicMax(P.bwd.cmax, __float_as_uint(cmax));
   }
 }
 

@@ -22,6 +22,7 @@ FIT, NOFIT, DME = 0, 1, 2
 TRI, FULL = 0, 1
 PREC_FP32, PREC_TC, PREC_FP64 = 0, 1, 2
 OPT_TAU, OPT_MAX_REFS, OPT_TOL, OPT_TIMING, OPT_TC_PIPELINE, OPT_HOST_OUT, OPT_INPUT_OVERLAP = 0, 1, 2, 3, 4, 5, 6
+OPT_BAND_FLOATS = 7
 #: The library's default tensor-core kernel shape (pairs of SMs).
 TC_PIPELINE_DEFAULT = -1  # automatic: deep stages from 1,280 atoms (device results), shallow otherwise
 
@@ -32,7 +33,11 @@ MODES = {"fit": FIT, "nofit": NOFIT, "dme": DME}
 EXPORTED = ("gbr_create", "gbr_destroy", "gbr_last_error", "gbr_allpairs", "gbr_output_count",
             "gbr_allpairs_batched", "gbr_rmsd_backward", "gbr_get_stats", "gbr_set_option", "gbr_set_stream",
             "gbr_write_cmatrix", "gbr_superpose", "gbr_cluster_centroids",
-            "gbr_allpairs_fp64_static", "gbr_selftest_bounded_wait")
+            "gbr_allpairs_fp64_static", "gbr_selftest_bounded_wait", "gbr_allpairs_stream", "gbr_row_bands")
+
+#: C type of gbr_band_sink: (user, row_begin, row_end, values, count) -> int.
+BAND_SINK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                             ctypes.POINTER(ctypes.c_float), ctypes.c_int64)
 
 
 class GbrError(RuntimeError):
@@ -93,6 +98,10 @@ def load():
         L.gbr_cluster_centroids.argtypes = [vp, vp, ci, i64, i32, vp, ci, vp, vp, i64, vp]
         L.gbr_allpairs_fp64_static.restype = ci
         L.gbr_allpairs_fp64_static.argtypes = [vp, ci, i64, i32, vp, ci, vp, vp]
+        L.gbr_allpairs_stream.restype = ci
+        L.gbr_allpairs_stream.argtypes = [vp, vp, ci, i64, i32, vp, ci, ci, i64, BAND_SINK, vp]
+        L.gbr_row_bands.restype = i64
+        L.gbr_row_bands.argtypes = [i64, i64, i32, vp, i64]
         L.gbr_selftest_bounded_wait.restype = ci
         L.gbr_selftest_bounded_wait.argtypes = [vp, i64, vp, vp]
         _lib = L
@@ -120,6 +129,17 @@ def _dtype_code(x):
     if dt.endswith("float64"):
         return GBR_F64
     raise TypeError(f"coordinates must be float32 or float64, got {dt}")
+
+
+def row_bands(n_frame, band_floats, row_align=1):
+    """Band boundaries of a streamed triangle (gbr_row_bands): an int64 array
+    cuts with cuts[0] = 0 and cuts[-1] = n_frame; raises ValueError when one
+    row does not fit in a band."""
+    cuts = np.zeros(int(n_frame) + 2, np.int64)
+    nb = load().gbr_row_bands(int(n_frame), int(band_floats), int(row_align), cuts.ctypes.data, len(cuts))
+    if nb < 0:
+        raise ValueError(f"a band of {band_floats} floats cannot hold one row of {n_frame} frames")
+    return cuts[: nb + 1].copy()
 
 
 def output_count(n_ref, n_tgt, out_kind, row_begin=0, row_end=-1):
@@ -286,6 +306,34 @@ class Handle:
                                            ctypes.cast(op, ctypes.c_void_p))
         self._check(rc)
         return [o[: int(t.shape[0]) * (int(t.shape[0]) - 1) // 2] for o, t in zip(outs, trajs)]
+
+    def allpairs_stream(self, xyz, sink, mass=None, mode="fit", precision="tc", band_floats=0):
+        """The triangle of one frame set in row bands (gbr_allpairs_stream).
+
+        ``sink(row_begin, row_end, values)`` is called on this thread for each
+        band in row order; ``values`` is a float32 view of the library's
+        pinned staging, valid only during the call (copy what you keep).
+        Returning False stops the call (GbrError code 7)."""
+        n_frame, n_atom = int(xyz.shape[0]), int(xyz.shape[1])
+        if mass is not None and isinstance(mass, np.ndarray):
+            mass = np.ascontiguousarray(mass, dtype=np.float64)
+        errors = []
+
+        def _cb(user, rb, re, values, count):
+            try:
+                arr = np.ctypeslib.as_array(values, shape=(int(count),)) if count > 0 else np.zeros(0, np.float32)
+                return 1 if sink(int(rb), int(re), arr) is False else 0
+            except BaseException as e:  # noqa: BLE001 - re-raised after the call
+                errors.append(e)
+                return 1
+        cb = BAND_SINK(_cb)
+        m = MODES[mode] if isinstance(mode, str) else mode
+        p = PRECISIONS[precision] if isinstance(precision, str) else precision
+        rc = self.lib.gbr_allpairs_stream(self.h, _ptr(xyz), _dtype_code(xyz), n_frame, n_atom, _ptr(mass), m, p,
+                                          int(band_floats), cb, None)
+        if errors:
+            raise errors[0]
+        self._check(rc)
 
     def write_cmatrix(self, path, xyz, mass=None, mode="fit", precision="tc", frame_to_idx=None, sieve=1):
         """Pairwise cache of one frame set straight to a cpptraj binary

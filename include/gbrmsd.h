@@ -115,6 +115,37 @@ int gbr_allpairs(gbr_handle *h, const void *ref_xyz, const void *tgt_xyz, int dt
 int64_t gbr_output_count(int64_t n_ref, int64_t n_tgt, int out_kind,
                          int64_t row_begin, int64_t row_end);
 
+/* Receives one band of a streamed triangle: the values of TRI rows
+ * [row_begin, row_end) in calcTriIndex order (count floats, which start at
+ * triangle index n*row_begin - (row_begin+1)*row_begin/2).  `values` is the
+ * library's pinned host memory, valid until the callback returns.  Return 0
+ * to go on; anything else stops the call, which then returns GBR_ERR_IO. */
+typedef int (*gbr_band_sink)(void *user, int64_t row_begin, int64_t row_end, const float *values,
+                             int64_t count);
+
+/* The triangle of one frame set (GBR_TRI, as gbr_allpairs computes it) in
+ * row bands of at most band_floats floats (<= 0: 2^28), for caches that do
+ * not fit in device memory at once: the pairwise cache behind
+ * MetricArray::CacheDistances (src/Cluster/MetricArray.cpp:722-801) with a
+ * disk cache (DataSet_PairwiseCache_NC, one SetElement per pair in the
+ * reference, src/DataSet_PairwiseCache_NC.h:27).  The frames are prepared
+ * once; band b is computed while band b-1 is copied to the host and band b-2
+ * is handed to `sink` on the calling thread, bands in row order, so device
+ * memory holds the frames and two bands only.  A band must hold at least one
+ * row (n_frame - 1 floats).  GBR_DME is not streamed (GBR_ERR_UNSUPPORTED);
+ * an empty triangle makes no callback. */
+int gbr_allpairs_stream(gbr_handle *h, const void *xyz, int dtype, int64_t n_frame, int32_t n_atom,
+                        const double *mass, int mode, int precision, int64_t band_floats,
+                        gbr_band_sink sink, void *user);
+
+/* The band boundaries gbr_allpairs_stream uses: cuts[0] = 0 < cuts[1] < ...
+ * < cuts[n] = n_frame with at most band_floats TRI elements per band, at
+ * multiples of row_align rows where a band holds whole groups of them.
+ * Returns n (the band count), or -1 when one row exceeds band_floats or
+ * max_cuts (the capacity of cuts) is too small.  Host only; no device work. */
+int64_t gbr_row_bands(int64_t n_frame, int64_t band_floats, int32_t row_align, int64_t *cuts,
+                      int64_t max_cuts);
+
 /* Many independent rms2d runs (GBR_TRI, one set each) in one call.  Trajectory
  * t has n_frames[t] frames of n_atoms[t] atoms at xyz[t] (GBR_F32), masses
  * mass[t] (NULL, or mass == NULL, for unweighted) and writes its triangle to
@@ -130,7 +161,10 @@ int gbr_allpairs_batched(gbr_handle *h, int32_t n_traj, const float *const *xyz,
  * (Cpptraj::Cluster::Cmatrix_Binary::WriteCmatrix, src/Cluster/Cmatrix_Binary.cpp:141-188).
  * The n_frame frames are the cached ones in order.  frame_to_idx (length
  * n_original, entries -1 for sieved-out frames, else the cache row) and sieve
- * go into the header and trailer; frame_to_idx NULL means no sieve. */
+ * go into the header and trailer; frame_to_idx NULL means no sieve.  The
+ * triangle is streamed to the file in row bands (gbr_allpairs_stream, band
+ * size GBR_OPT_BAND_FLOATS), so it need not fit in device memory; GBR_DME
+ * computes the whole triangle in device memory first. */
 int gbr_write_cmatrix(gbr_handle *h, const char *path, const void *xyz, int dtype, int64_t n_frame,
                       int32_t n_atom, const double *mass, int mode, int precision,
                       const int32_t *frame_to_idx, int64_t n_original, int64_t sieve);
@@ -246,6 +280,8 @@ int gbr_get_stats(const gbr_handle *h, gbr_stats *out);
  *   GBR_OPT_HOST_OUT     pinned host `out` of gbr_allpairs: 1 = the kernels
  *                        store into it directly (default), 0 = results staged
  *                        in device memory and copied back in row bands
+ *   GBR_OPT_BAND_FLOATS  band size in floats of gbr_write_cmatrix's streamed
+ *                        triangle (default 2^28; at least one row)
  *   GBR_OPT_INPUT_OVERLAP  pinned host input of one frame set, triangle into
  *                        device or directly stored host memory: 1 = the
  *                        contraction starts on the frames that have landed
@@ -256,7 +292,8 @@ int gbr_get_stats(const gbr_handle *h, gbr_stats *out);
  *                        faster than the transfer itself)
  */
 enum gbr_option { GBR_OPT_TAU = 0, GBR_OPT_MAX_REFS = 1, GBR_OPT_TOL = 2, GBR_OPT_TIMING = 3,
-                  GBR_OPT_TC_PIPELINE = 4, GBR_OPT_HOST_OUT = 5, GBR_OPT_INPUT_OVERLAP = 6 };
+                  GBR_OPT_TC_PIPELINE = 4, GBR_OPT_HOST_OUT = 5, GBR_OPT_INPUT_OVERLAP = 6,
+                  GBR_OPT_BAND_FLOATS = 7 };
 int gbr_set_option(gbr_handle *h, int key, double value);
 
 /* Self-test of the device-side failure detection.  No counterpart in the

@@ -318,7 +318,7 @@ struct F9 {
 
 // Solver part of the epilogue with every per-frame term given (by value):
 // P_ja, P_ib, trPia / trPjb (read only when a != b), rp the reference-pair
-// entry of (a, b).
+// entry of (a, b) (global memory, or its copy in shared memory: plain loads).
 static __device__ __forceinline__ float pair_solve_inl(const F9 Dv, float ni, float nj, const F9 Pjav,
                                                       const F9 Pibv, float trPia, float trPjb, const float* rp,
                                                       bool same, const FrameTerms& t, bool* flag,
@@ -350,7 +350,7 @@ static __device__ __forceinline__ float pair_solve_inl(const F9 Dv, float ni, fl
   } else {
     float U[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) U[k] = __ldg(rp + k);
+    for (int k = 0; k < 9; ++k) U[k] = rp[k];
     float uPib = 0.f, uPjaT = 0.f, trUD = 0.f;
 #pragma unroll
     for (int p = 0; p < 3; ++p)
@@ -360,7 +360,7 @@ static __device__ __forceinline__ float pair_solve_inl(const F9 Dv, float ni, fl
         uPjaT += U[p * 3 + q] * Pja[q * 3 + p];
         trUD += U[p * 3 + q] * D[q * 3 + p];
       }
-    const float h = 0.5f * (__ldg(rp + 21) + ni + nj);
+    const float h = 0.5f * (rp[21] + ni + nj);
     G00 = h + trPia - uPib - uPjaT + trPjb - trUD;
     g00mag = h + fabsf(trPia) + fabsf(uPib) + fabsf(uPjaT) + fabsf(trPjb) + fabsf(trUD);
 #pragma unroll
@@ -382,11 +382,11 @@ static __device__ __forceinline__ float pair_solve_inl(const F9 Dv, float ni, fl
   }
   float M[9];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) M[k] = __ldg(rp + 9 + k) + Y[k];
+  for (int k = 0; k < 9; ++k) M[k] = rp[9 + k] + Y[k];
   // g = G[0][1..3] = -(antisymmetric combos of M''), from the small parts.
-  const float g1 = -(Y[5] - Y[7] + __ldg(rp + 18));
-  const float g2 = -(Y[6] - Y[2] + __ldg(rp + 19));
-  const float g3 = -(Y[1] - Y[3] + __ldg(rp + 20));
+  const float g1 = -(Y[5] - Y[7] + rp[18]);
+  const float g2 = -(Y[6] - Y[2] + rp[19]);
+  const float g3 = -(Y[1] - Y[3] + rp[20]);
   const float G11 = G00 + 2.0f * (M[4] + M[8]);
   const float G22 = G00 + 2.0f * (M[0] + M[8]);
   const float G33 = G00 + 2.0f * (M[0] + M[4]);

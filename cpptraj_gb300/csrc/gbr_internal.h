@@ -239,6 +239,7 @@ struct BackwardTail {
   const double* sqw;   // sqrt of the masses (when w is given)
   double W;
   float* grad;         // [F][N][3]
+  float4* atab;        // [N][3] scratch: reference, weight and sqrt(weight) as FP32 hi + lo
 };
 cudaError_t run_backward_tail(const BackwardTail& T, cudaStream_t st);
 

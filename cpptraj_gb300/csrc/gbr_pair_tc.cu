@@ -86,9 +86,14 @@ constexpr int STAGING_BYTES = Epi1::STAGING_BYTES;
 // reference (pre-alignment) of the tile's first reference frame and B that of
 // its first target frame, each frame slot holds n, 1/scale, its reference,
 // trP against its own reference, and P against B (reference frames) or A
-// (target frames): everything a pair with references (A, B) reads.
+// (target frames): everything a pair with references (A, B) reads.  After the
+// frame slots: the reference-pair entry of (A, B) (kRefPairStride floats) and,
+// for a triangle over reference-sorted positions, each slot's frame number
+// (TI + TJ ints; -1 outside the map).
 constexpr int TERM_STRIDE = 13;
-constexpr int TERM_FLOATS = ((TI + TJ) * TERM_STRIDE + 3) & ~3;
+constexpr int TERM_RP = ((TI + TJ) * TERM_STRIDE + 3) & ~3;
+constexpr int TERM_PERM = TERM_RP + kRefPairStride;
+constexpr int TERM_FLOATS = (TERM_PERM + TI + TJ + 3) & ~3;
 template <class E>
 constexpr int epi_bytes() {
   return EPI_GROUPS * E::STAGING_BYTES + 2 * TERM_FLOATS * 4;
@@ -282,6 +287,21 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
       }
       T[x] = v;
     }
+    // The tile's reference-pair entry and, with a sorted layout, its frames.
+    if (etid < kRefPairStride) T[TERM_RP + etid] = __ldg(P.terms.RP + (size_t)(B * K + A) * kRefPairStride + etid);
+    if (P.map.perm) {
+      int* Tp = reinterpret_cast<int*>(T + TERM_PERM);
+      for (int x = etid; x < TI + TJ; x += EPI_WARPS * 32) {
+        int v = -1;
+        if (x < TI) {
+          if (i0 + x < P.i_end) v = __ldg(P.map.perm + i0 + x);
+        } else {
+          const int64_t jt = jt0 + (x - TI);
+          if (jt < P.jt_end) v = __ldg(P.map.perm + P.tgt0 + jt);
+        }
+        Tp[x] = v;
+      }
+    }
     // One thread waits; the verdict is shared so every epilogue thread takes
     // the same path through the named barriers.
     if (etid == 0) okf[b] = mbar_wait(accf0 + 8 * b, aph, P.err, 5) ? 1 : 0;
@@ -332,7 +352,7 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
               }
               in.trPia = Ti[3];
               in.trPjb = Tj[3];
-              in.rp = P.terms.RP;
+              in.rp = T + TERM_RP;  // K = 1: the entry of (0, 0)
               in.same = true;
 #pragma unroll
               for (int pj = 0; pj < 3; ++pj)
@@ -394,8 +414,15 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
             const int jl = tri ? p % CH_TGT : p / TI;
             const int64_t i = i0 + il, jt = jc0 + jl;
             if (i >= P.i_end || jt >= P.jt_end) continue;
-            const int64_t idx = out_index(P.map, i, jt);
-            if (idx < 0) continue;
+            // A pair of this call's output?  (The row stores map it to its
+            // index; out_index's own test, without its frame lookups.)
+            int64_t idx = 0;
+            if (rows) {
+              if (!(jt > i) || i < P.map.row_begin || i >= P.map.row_end || jt >= P.map.n_tgt) continue;
+            } else {
+              idx = out_index(P.map, i, jt);
+              if (idx < 0) continue;
+            }
             bool flag = false;
             const float* Ti = T + il * TERM_STRIDE;
             const float* Tj = T + (TI + c * CH_TGT + jl) * TERM_STRIDE;
@@ -416,7 +443,7 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
               }
               in.trPia = Ti[3];
               in.trPjb = Tj[3];
-              in.rp = P.terms.RP + (size_t)(B * K + A) * kRefPairStride;
+              in.rp = T + TERM_RP;
               in.same = (A == B);
             } else {
               sc = __ldg(P.inv_scale + i) * __ldg(P.inv_scale + P.tgt0 + jt);
@@ -472,13 +499,26 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
       // The next tile writes rowbuf only after its own all-group barrier,
       // which every thread reaches after these stores.
       named_sync(1 + EPI_GROUPS, EPI_WARPS * 32);
+      const float* Tt = terms + b * TERM_FLOATS;  // this tile's staged frames
+      const int* Tp = reinterpret_cast<const int*>(Tt + TERM_PERM);
 #pragma unroll 1
       for (int x = etid; x < TI * TJ; x += EPI_WARPS * 32) {
         const int il = x / TJ, jl = x % TJ;
         const int64_t i = i0 + il, jt = jt0 + jl;
         if (i >= P.i_end || jt >= P.jt_end) continue;
-        const int64_t idx = out_index(P.map, i, jt);
-        if (idx >= 0) P.map.out[idx] = rowbuf[il * RB_STRIDE + jl];
+        // out_index (TRI) with the sorted positions' frames from shared memory
+        if (!(jt > i) || i < P.map.row_begin || i >= P.map.row_end || jt >= P.map.n_tgt) continue;
+        int64_t idx;
+        if (P.map.perm) {
+          int64_t a = Tp[il], bb = Tp[TI + jl];
+          if (a > bb) {
+            const int64_t c = a; a = bb; bb = c;
+          }
+          idx = tri_index(P.map.n_ref, a, bb);
+        } else {
+          idx = tri_index(P.map.n_ref, i, jt) - P.map.base;
+        }
+        P.map.out[idx] = rowbuf[il * RB_STRIDE + jl];
       }
     }
   }

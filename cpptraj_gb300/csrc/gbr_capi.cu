@@ -384,18 +384,8 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
   // Pinned host inputs of some size travel in chunks on the copy stream; the
   // first prep pass starts on each chunk as it lands.
   const size_t in_bytes = esz * 3 * (size_t)N * (size_t)F;
-  // Device-resident frames of one set, triangle into device (or directly
-  // stored host) memory, tensor path: the same speculation as for chunked
-  // host input, over one "chunk" that is already there.  Prep builds the
-  // one-reference operands and the contraction is queued before the host
-  // learns whether one reference suffices, so the GPU does not wait on that
-  // host round trip; if it does not suffice, the skip flag turns the queued
-  // contraction into a no-op and the general path runs.
-  const bool dev_spec = need_planes && tc && ref_dev && !tgt_xyz && map.tri && out_dev && !rs &&
-                        row_begin == 0 && row_end == n_ref && in_bytes >= (32u << 20);
-  const bool chunk_in = ((need_planes && (!ref_dev || (tgt_xyz && !tgt_dev)) && in_bytes >= (32u << 20) &&
-                          is_pinned_or_device(ref_xyz) && (!tgt_xyz || is_pinned_or_device(tgt_xyz))) ||
-                         dev_spec) &&
+  const bool chunk_in = need_planes && (!ref_dev || (tgt_xyz && !tgt_dev)) && in_bytes >= (32u << 20) &&
+                        is_pinned_or_device(ref_xyz) && (!tgt_xyz || is_pinned_or_device(tgt_xyz)) &&
                         h->ensure_xfer();
   int n_chunks = 0;
   int64_t chunk_end[8];
@@ -415,7 +405,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
         chunk_end[n_chunks++] = set0 + b;
       }
     };
-    plan_chunks(ref_xyz, P[0], 0, n_ref, ref_dev, dev_spec ? 1 : tgt_xyz ? 4 : 8);
+    plan_chunks(ref_xyz, P[0], 0, n_ref, ref_dev, tgt_xyz ? 4 : 8);
     if (tgt_xyz) plan_chunks(tgt_xyz, P[1], n_ref, n_tgt, tgt_dev, 4);
   } else {
     if (!ref_dev) cudaMemcpyAsync(P[0], ref_xyz, esz * 3 * (size_t)N * n_ref, cudaMemcpyDefault, st);
@@ -440,7 +430,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
   // (grouped order kept within a stage); when prep has built the operands
   // through a chunk, the tiles ready by then are launched behind it.
   const int tc_variant = (h->tc_variant >= 0) ? h->tc_variant : (N >= kDeepStageAtoms ? 3 : 2);
-  bool overlap = (h->input_overlap || dev_spec) && n_chunks > 0 && tc && map.tri && !tgt_xyz && out_dev;
+  bool overlap = h->input_overlap && n_chunks > 0 && tc && map.tri && !tgt_xyz && out_dev;
   std::vector<int64_t> stage_off;
   std::vector<int2> stage_tiles;
   if (overlap) {

@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the secondary workloads (c0, c2, c3, c4) reported under `secondary`")
-    ap.add_argument("--tc-pipeline", type=int, default=None, choices=[-1, 0, 1, 2, 3],
+    ap.add_argument("--tc-pipeline", type=int, default=None, choices=[-1, 0, 1, 2, 3, 4],
                     help="tensor-core kernel shape (GBR_OPT_TC_PIPELINE); default: the library's")
     ap.add_argument("--profile", action="store_true",
                     help="warm up, then run exactly one all-pairs call (for ncu); prints stats only")

@@ -141,8 +141,8 @@ int gbr_set_option(gbr_handle* h, int key, double value) {
       h->timing = value != 0.0;
       return GBR_OK;
     case GBR_OPT_TC_PIPELINE:
-      if (!(value == -1.0 || value == 0.0 || value == 1.0 || value == 2.0 || value == 3.0))
-        return h->fail(GBR_ERR_ARG, "tc pipeline must be -1 (automatic), 0, 1, 2 or 3");
+      if (!(value == -1.0 || value == 0.0 || value == 1.0 || value == 2.0 || value == 3.0 || value == 4.0))
+        return h->fail(GBR_ERR_ARG, "tc pipeline must be -1 (automatic), 0, 1, 2, 3 or 4");
       h->tc_variant = (int)value;
       return GBR_OK;
     case GBR_OPT_HOST_OUT:
@@ -758,7 +758,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
     fa.built = po.built;
     if (!spec_done) {
       if ((e = run_finish(fa, st)) != cudaSuccess) return h->cuda_fail(e, "finish");
-      launches += po.built ? 1 : 2;
+      launches += po.built ? 1 : (K > 1 ? 3 : 2);  // k_build (+ k_pref with several references), k_ref_terms
     }
     // One launch of the pair kernel over the rows of map m.
     auto launch_pairs = [&](const OutMap& m, const FlagList& f) -> cudaError_t {

@@ -81,6 +81,7 @@ struct PrepScratch {
   int* pos;        // [F] frame -> position when frames are laid out sorted by reference
   int* assign_pos; // [F] reference of the frame at each position
   float* swr0;     // [N][3] sqrt(w) r_0 before refinement (scans that run after a speculative refinement)
+  int* kstate;     // [2] k-centre choice on the device: stopped flag, index of the last reference added
 };
 size_t prep_scratch_bytes(int64_t F, int N, int Kmax);
 PrepScratch prep_carve(void* base, int64_t F, int N, int Kmax);

@@ -87,13 +87,17 @@ constexpr int STAGING_BYTES = Epi1::STAGING_BYTES;
 // its first target frame, each frame slot holds n, 1/scale, its reference,
 // trP against its own reference, and P against B (reference frames) or A
 // (target frames): everything a pair with references (A, B) reads.  After the
-// frame slots: the reference-pair entry of (A, B) (kRefPairStride floats) and,
-// for a triangle over reference-sorted positions, each slot's frame number
-// (TI + TJ ints; -1 outside the map).
+// frame slots: the reference-pair entry of (A, B) (kRefPairStride floats),
+// for a triangle over reference-sorted positions each slot's frame number
+// (TI + TJ ints; -1 outside the map), and the row bases below.
 constexpr int TERM_STRIDE = 13;
 constexpr int TERM_RP = ((TI + TJ) * TERM_STRIDE + 3) & ~3;
 constexpr int TERM_PERM = TERM_RP + kRefPairStride;
-constexpr int TERM_FLOATS = (TERM_PERM + TI + TJ + 3) & ~3;
+// Then, for the row stores of a triangle in frame order, the output index of
+// (reference slot il, target slot 0) as an int64 per reference slot.
+constexpr int TERM_ROWBASE = (TERM_PERM + TI + TJ + 1) & ~1;
+constexpr int TERM_FLOATS = (TERM_ROWBASE + 2 * TI + 3) & ~3;
+static_assert(TJ == 64, "row stores split the slot index with shifts");
 template <class E>
 constexpr int epi_bytes() {
   return EPI_GROUPS * E::STAGING_BYTES + 2 * TERM_FLOATS * 4;
@@ -251,6 +255,13 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
     const int2 tl = P.tiles[t];
     const int64_t i0 = P.i_base + (int64_t)tl.x * ti_frames + i_off;
     const int64_t jt0 = P.jt_base + (int64_t)tl.y * TJ;
+    // Tile-relative limits: reference slots [0, ilim) and target slots
+    // [0, jlim) are inside the map; d0 = jt0 - i0 (a target slot jj is after
+    // reference slot il iff d0 + jj > il).
+    const int64_t irem = P.i_end - i0, jrem = P.jt_end - jt0;
+    const int ilim = irem <= 0 ? 0 : (irem < TI ? (int)irem : TI);
+    const int jlim = jrem <= 0 ? 0 : (jrem < TJ ? (int)jrem : TJ);
+    const int d0 = (int)(jt0 - i0);
     float* T = terms + b * TERM_FLOATS;
     // Loads overlap the MMAs of this tile; buffer b was last read two tiles
     // ago, before every group passed the previous tile's barrier.
@@ -289,6 +300,11 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
     }
     // The tile's reference-pair entry and, with a sorted layout, its frames.
     if (etid < kRefPairStride) T[TERM_RP + etid] = __ldg(P.terms.RP + (size_t)(B * K + A) * kRefPairStride + etid);
+    if (rows && !P.map.perm && etid < TI) {
+      // tri_index(n, i, jt0) - base for reference frame i = i0 + etid
+      const int64_t i = i0 + etid, n = P.map.n_ref;
+      reinterpret_cast<int64_t*>(T + TERM_ROWBASE)[etid] = n * i - (i + 1) * i / 2 + jt0 - i - 1 - P.map.base;
+    }
     if (P.map.perm) {
       int* Tp = reinterpret_cast<int*>(T + TERM_PERM);
       for (int x = etid; x < TI + TJ; x += EPI_WARPS * 32) {
@@ -312,11 +328,15 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
       for (int c = g; c < TJ / CH_TGT; c += EPI_GROUPS) {
         float v[CH_COLS];
         const uint32_t taddr = tmem_base + ((uint32_t)(32 * q) << 16) + b * ACC_STRIDE + c * CH_COLS;
-        if constexpr (CH_COLS == 24) {
+        if constexpr (CH_COLS == 48) {
+          tmem_ld16(taddr, v);
+          tmem_ld16(taddr + 16, v + 16);
+          tmem_ld16(taddr + 32, v + 32);
+        } else if constexpr (CH_COLS == 24) {
           tmem_ld16(taddr, v);
           tmem_ld8(taddr + 16, v + 16);
         } else {
-          static_assert(CH_COLS == 12, "chunks of 8 or 4 target frames");
+          static_assert(CH_COLS == 12, "chunks of 16, 8 or 4 target frames");
           tmem_ld4(taddr, v);
           tmem_ld4(taddr + 4, v + 4);
           tmem_ld4(taddr + 8, v + 8);
@@ -412,13 +432,16 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
           for (int p = tid; p < TI * CH_TGT; p += 128) {
             const int il = tri ? p / CH_TGT : p % TI;
             const int jl = tri ? p % CH_TGT : p / TI;
+            const int jj = c * CH_TGT + jl;  // target slot in the tile
+            if (il >= ilim || jj >= jlim) continue;
             const int64_t i = i0 + il, jt = jc0 + jl;
-            if (i >= P.i_end || jt >= P.jt_end) continue;
-            // A pair of this call's output?  (The row stores map it to its
-            // index; out_index's own test, without its frame lookups.)
+            // A pair of this call's output?  With row stores (a triangle:
+            // rows [i_base, i_end) = the map's rows, targets up to n_tgt)
+            // only target > reference remains to test; the stores map it to
+            // its index.
             int64_t idx = 0;
             if (rows) {
-              if (!(jt > i) || i < P.map.row_begin || i >= P.map.row_end || jt >= P.map.n_tgt) continue;
+              if (!(d0 + jj > il)) continue;
             } else {
               idx = out_index(P.map, i, jt);
               if (idx < 0) continue;
@@ -501,22 +524,23 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
       named_sync(1 + EPI_GROUPS, EPI_WARPS * 32);
       const float* Tt = terms + b * TERM_FLOATS;  // this tile's staged frames
       const int* Tp = reinterpret_cast<const int*>(Tt + TERM_PERM);
+      const int64_t* Trb = reinterpret_cast<const int64_t*>(Tt + TERM_ROWBASE);
+      const int64_t n = P.map.n_ref;
 #pragma unroll 1
       for (int x = etid; x < TI * TJ; x += EPI_WARPS * 32) {
-        const int il = x / TJ, jl = x % TJ;
-        const int64_t i = i0 + il, jt = jt0 + jl;
-        if (i >= P.i_end || jt >= P.jt_end) continue;
-        // out_index (TRI) with the sorted positions' frames from shared memory
-        if (!(jt > i) || i < P.map.row_begin || i >= P.map.row_end || jt >= P.map.n_tgt) continue;
+        const int il = x >> 6, jl = x & (TJ - 1);
+        // the pair loop's test: inside the map, target after reference
+        if (il >= ilim || jl >= jlim || !(d0 + jl > il)) continue;
         int64_t idx;
         if (P.map.perm) {
-          int64_t a = Tp[il], bb = Tp[TI + jl];
+          // out_index over sorted positions: the frames from shared memory
+          int a = Tp[il], bb = Tp[TI + jl];
           if (a > bb) {
-            const int64_t c = a; a = bb; bb = c;
+            const int c2 = a; a = bb; bb = c2;
           }
-          idx = tri_index(P.map.n_ref, a, bb);
+          idx = n * a - ((int64_t)a + 1) * a / 2 + (bb - a - 1);
         } else {
-          idx = tri_index(P.map.n_ref, i, jt) - P.map.base;
+          idx = Trb[il] + jl;
         }
         P.map.out[idx] = rowbuf[il * RB_STRIDE + jl];
       }
@@ -705,6 +729,9 @@ struct PairCfg {
 using PairShallow = PairCfg<32, 5, 8>;
 // Large N (operand-feed bound): 64-atom stages (128-byte rows) x 3, 4-frame chunks.
 using PairDeep = PairCfg<64, 3, 4>;
+// Small N, wider epilogue chunks: 32-atom stages x 3, 16-frame chunks (each
+// epilogue group takes one chunk per tile: half the named barriers per pair).
+using PairWide = PairCfg<32, 3, 16>;
 constexpr uint32_t IDESC2 = (1u << 4) | ((uint32_t)(UN >> 3) << 17) | ((uint32_t)(UM2 >> 4) << 24);
 
 __device__ __forceinline__ uint32_t cluster_rank() {
@@ -1062,6 +1089,7 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
   const int ka = (L.variant == 0)   ? 64
                  : (L.variant == 1) ? 32
                  : (L.variant == 3) ? PairDeep::KA2
+                 : (L.variant == 4) ? PairWide::KA2
                                     : PairShallow::KA2;
   const int bj = pair ? TJH : TJ;
   CUtensorMap mAh, mAl, mBh, mBl;
@@ -1088,14 +1116,16 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
     if (!pair) return cudaErrorInvalidValue;
     P.bwd = *L.bwd;
     P.row_stores = 0;
+    // (the wide-chunk shape has no backward instantiation: same stages as the shallow one)
     e = (L.variant == 3) ? launch_pair_kernel<PairDeep, true>(mAh, mAl, mBh, mBl, P, st)
                          : launch_pair_kernel<PairShallow, true>(mAh, mAl, mBh, mBl, P, st);
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
   }
   if (pair) {
-    e = (L.variant == 3) ? launch_pair_kernel<PairDeep>(mAh, mAl, mBh, mBl, P, st)
-                         : launch_pair_kernel<PairShallow>(mAh, mAl, mBh, mBl, P, st);
+    e = (L.variant == 3)   ? launch_pair_kernel<PairDeep>(mAh, mAl, mBh, mBl, P, st)
+        : (L.variant == 4) ? launch_pair_kernel<PairWide>(mAh, mAl, mBh, mBl, P, st)
+                           : launch_pair_kernel<PairShallow>(mAh, mAl, mBh, mBl, P, st);
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
   }

@@ -145,6 +145,7 @@ size_t prep_scratch_bytes(int64_t F, int N, int Kmax) {
   b += align256(sizeof(float) * kFtab * F);
   b += align256(sizeof(int) * F) * 2;
   b += align256(sizeof(float) * 3 * N);
+  b += align256(sizeof(int) * 2);
   return b;
 }
 
@@ -170,6 +171,7 @@ PrepScratch prep_carve(void* base, int64_t F, int N, int Kmax) {
   s.pos = (int*)take(sizeof(int) * F);
   s.assign_pos = (int*)take(sizeof(int) * F);
   s.swr0 = (float*)take(sizeof(float) * 3 * N);
+  s.kstate = (int*)take(sizeof(int) * 2);
   return s;
 }
 
@@ -458,7 +460,11 @@ template <typename T>
 __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockThreads)
     k_make_ref(FrameSrc<T> src, const int64_t* fsel, const double* cen, const double* cmass_ref,
                const double* cmass_tgt, const double* w, const double* sqw, const int* assign, int k, int use_parent,
-               int nofit, double* refs, float* swr, float2* refhl, double* Eref, double* sr, float* rmax) {
+               int nofit, double* refs, float* swr, float2* refhl, double* Eref, double* sr, float* rmax,
+               const int* gate = nullptr) {
+  // A gated round after the k-centre choice has stopped: every CTA of the
+  // cluster reads the same word and leaves before any barrier.
+  if (gate && *gate != 0) return;
   __shared__ double red[32 * 10], slots[kRefCluster * 10], bc[10];
   __shared__ double Rs[9], cs[3];
   const int N = src.N;
@@ -571,6 +577,7 @@ struct ScanArgs {
   const double* Eref;   // &Eref[k]
   double Wsum;
   int k, nofit;
+  const int* gate;      // non-null and non-zero at launch: the k-centre choice has stopped, the pass does nothing
   double* cen;
   float* dist;
   int* assign;
@@ -587,6 +594,7 @@ struct ScanArgs {
 // Later passes (reference k > 0) centre with the known c directly.
 template <typename T, bool FIRST>
 __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64_t f_begin, int64_t F, ScanArgs s) {
+  if (s.gate && *s.gate != 0) return;  // uniform over the grid: before any barrier
   __shared__ __align__(16) float sbuf[kWarps][kPipe * kStage];
   __shared__ float xpart[2][kFPB][kWPF - 1][20];  // the other parts' sums, by frame parity
   const int N = src.N, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -822,6 +830,47 @@ __global__ void k_argmax(const float* dist, int64_t F, float* out_val, int64_t* 
   }
 }
 
+// A round k of the k-centre choice run on the device: the argmax of
+// dist[0..F); if it is farther than tau, reference k is that frame (fsel) and
+// state[1] = k (k + 1 references exist); otherwise state[0] = 1 stops this
+// and every later round (their k_make_ref and k_scan launches return at
+// once).  state[0] != 0 on entry: an earlier round has stopped.
+__global__ void k_argmax_gate(const float* dist, int64_t F, float tau, int k, float* out_val, int64_t* out_idx,
+                              int* state) {
+  if (state[0] != 0) return;
+  __shared__ float sv[1024];
+  __shared__ int64_t si[1024];
+  float bv = -1.0f;
+  int64_t bi = 0;
+  for (int64_t f = threadIdx.x; f < F; f += blockDim.x) {
+    const float v = dist[f];
+    if (v > bv) { bv = v; bi = f; }
+  }
+  sv[threadIdx.x] = bv;
+  si[threadIdx.x] = bi;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      const float o = sv[threadIdx.x + s];
+      const int64_t oi = si[threadIdx.x + s];
+      if (o > sv[threadIdx.x] || (o == sv[threadIdx.x] && oi < si[threadIdx.x])) {
+        sv[threadIdx.x] = o;
+        si[threadIdx.x] = oi;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    *out_val = sv[0];
+    if (sv[0] > tau) {
+      *out_idx = si[0];
+      state[1] = k;
+    } else {
+      state[0] = 1;
+    }
+  }
+}
+
 // One thread per frame: the exact (FP64-orthogonal) rotation of the frame's
 // quaternion, t = R c, and both split into FP32 hi + lo.  No-fit: R = I, t = 0.
 __global__ void k_rot(int64_t f_begin, int64_t F, const float4* quat, const double* cen, int nofit, float* ftab,
@@ -954,6 +1003,7 @@ struct BuildArgs {
   const double* scal;   // [0] max sqrt(w)
   const float* swr;     // [K][N][3] sqrt(w) r_c
   int K, Np;
+  int K_build;          // references k_build forms P against (the rest: k_pref)
   int tc;
   __half* hi;
   __half* lo;
@@ -1072,10 +1122,11 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
       for (int q = 0; q < 9; ++q) Pf[q] = acc[q];
       b.trP[(size_t)pf * b.K] = acc[0] + acc[4] + acc[8];
     }
-    // P against the other references: read the operands back (this lane's own
-    // writes, same atom mapping, this part's atoms).
+    // P against the other references up to K_build (beyond it: k_pref after
+    // this pass): read the operands back (this lane's own writes, same atom
+    // mapping, this part's atoms).
     __syncwarp();
-    for (int c = 1; c < b.K; ++c) {
+    for (int c = 1; c < b.K_build; ++c) {
       const float* rc = b.swr + (size_t)c * N * 3;
       float h9[9];
 #pragma unroll
@@ -1102,6 +1153,53 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
     }
   }
   pipe.drain();
+}
+
+// P_fc = sum_a p_f[a] (sqrt(w) r_c[a])^T against references c = 1 .. K-1 (c = 0
+// comes with k_build), from the operands k_build wrote (the values the
+// contraction reads).  One warp per operand position, kPrefGroup references
+// per pass over its atoms, so each operand is read K / kPrefGroup times.
+constexpr int kPrefGroup = 8;
+__global__ void __launch_bounds__(256) k_pref(BuildArgs b, int64_t F, int N) {
+  const int lane = threadIdx.x & 31;
+  const int Np = b.Np, K = b.K;
+  for (int64_t pf = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; pf < F;
+       pf += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const size_t base = (size_t)pf * 3 * Np;
+    const float inv = b.tc ? b.inv_scale[pf] : 1.0f;
+    for (int c0 = 1; c0 < K; c0 += kPrefGroup) {
+      float h[kPrefGroup * 9];
+#pragma unroll
+      for (int q = 0; q < kPrefGroup * 9; ++q) h[q] = 0.0f;
+      for (int a = lane; a < N; a += 32) {
+        float v[3];
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+          const size_t i = base + (size_t)p * Np + a;
+          v[p] = b.tc ? (__half2float(b.hi[i]) + __half2float(b.lo[i])) * inv : b.plane[i];
+        }
+#pragma unroll
+        for (int g = 0; g < kPrefGroup; ++g) {
+          if (c0 + g < K) {
+            const float* rc = b.swr + ((size_t)(c0 + g) * N + a) * 3;
+            const float r0 = __ldg(rc), r1 = __ldg(rc + 1), r2 = __ldg(rc + 2);
+            float* hg = h + 9 * g;
+            hg[0] += v[0] * r0; hg[1] += v[0] * r1; hg[2] += v[0] * r2;
+            hg[3] += v[1] * r0; hg[4] += v[1] * r1; hg[5] += v[1] * r2;
+            hg[6] += v[2] * r0; hg[7] += v[2] * r1; hg[8] += v[2] * r2;
+          }
+        }
+      }
+      warp_sum_f32<kPrefGroup * 9>(h);
+      if (lane == 0) {
+        for (int g = 0; g < kPrefGroup && c0 + g < K; ++g) {
+          float* Pf = b.P + ((size_t)pf * K + c0 + g) * 9;
+          for (int q = 0; q < 9; ++q) Pf[q] = h[9 * g + q];
+          b.trP[(size_t)pf * K + c0 + g] = h[9 * g] + h[9 * g + 4] + h[9 * g + 8];
+        }
+      }
+    }
+  }
 }
 
 // Reference-pair table (kRefPairStride floats per b*K + a): the exact FP64
@@ -1315,26 +1413,43 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
     ++launches;
   }
   // Greedy k-centre: add the farthest frame as a reference while it is
-  // farther than tau from every reference.
+  // farther than tau from every reference.  The first round is decided on
+  // the host (one reference is the common case and then costs no further
+  // launch); once a second reference is needed, the remaining rounds are
+  // queued at once, each gated on the device by the round before
+  // (k_argmax_gate), so adding references costs no host round trip each.
   int K = 1;
-  while (K < A.max_refs && F > 1) {
+  if (K < A.max_refs && F > 1) {
     k_argmax<<<1, 1024, 0, st>>>(A.dist, F, A.dmax, A.fsel);
     ++launches;
     float dmax = 0.0f;
     cudaMemcpyAsync(&dmax, A.dmax, sizeof(float), cudaMemcpyDeviceToHost, st);
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return e;
-    if (!(dmax > A.tau)) break;
-    k_make_ref<T><<<kRefCluster, kOneBlockThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w,
-                                                            A.sqw, A.assign, K, 1, A.nofit, A.refs, A.swr, S.refhl,
-                                                            A.Eref, S.sr, S.rmax);
-    sa.k = K;
-    sa.swr = A.swr + (size_t)K * 3 * N;
-    sa.sr = S.sr + 3 * K;
-    sa.Eref = A.Eref + K;
-    k_scan<T, false><<<prep_grid(F, kScanBlocksPerSM, kFPB), kPrepThreads, 0, st>>>(src, 0, F, sa);
-    launches += 2;
-    ++K;
+    if (dmax > A.tau) {
+      // state = {stopped, index of the last reference added}; round 1
+      // repeats the host's check, which passed
+      cudaMemsetAsync(S.kstate, 0, 2 * sizeof(int), st);
+      for (int k = 1; k < A.max_refs; ++k) {
+        k_argmax_gate<<<1, 1024, 0, st>>>(A.dist, F, (float)A.tau, k, A.dmax, A.fsel, S.kstate);
+        ++launches;
+        k_make_ref<T><<<kRefCluster, kOneBlockThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w,
+                                                                A.sqw, A.assign, k, 1, A.nofit, A.refs, A.swr,
+                                                                S.refhl, A.Eref, S.sr, S.rmax, S.kstate);
+        ScanArgs sk = sa;
+        sk.k = k;
+        sk.swr = A.swr + (size_t)k * 3 * N;
+        sk.sr = S.sr + 3 * k;
+        sk.Eref = A.Eref + k;
+        sk.gate = S.kstate;
+        k_scan<T, false><<<prep_grid(F, kScanBlocksPerSM, kFPB), kPrepThreads, 0, st>>>(src, 0, F, sk);
+        launches += 2;
+      }
+      int kst[2] = {0, 0};
+      cudaMemcpyAsync(kst, S.kstate, sizeof kst, cudaMemcpyDeviceToHost, st);
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+      K = kst[1] + 1;
+    }
   }
   o.K = K;
   k_rot<<<rot_grid(F), kRotThreads, 0, st>>>(0, F, S.quat, A.cen, A.nofit, S.ftab, A.rot);
@@ -1390,6 +1505,7 @@ static BuildArgs build_args(const FinishArgs& fa, const PrepArgs& A, const PrepS
   b.scal = S.scal;
   b.swr = A.swr;
   b.K = fa.K;
+  b.K_build = (fa.K > 1) ? 1 : fa.K;  // P against references 1..K-1 in k_pref
   b.Np = A.Np;
   b.tc = fa.tc;
   b.hi = (__half*)fa.hi;
@@ -1413,6 +1529,8 @@ static cudaError_t finish_impl(const FinishArgs& fa, cudaStream_t st) {
   if (!fa.built) {
     const BuildArgs b = build_args(fa, A, S);
     k_build<T><<<prep_grid(A.F, kBuildBlocksPerSM, kFPB), kPrepThreads, 0, st>>>(src, 0, A.F, b);
+    if (fa.K > 1)
+      k_pref<<<(unsigned)std::min<int64_t>((A.F + 7) / 8, 152 * 16), 256, 0, st>>>(b, A.F, A.N);
   }
   k_ref_terms<<<fa.K * fa.K * kRefCluster, kOneBlockThreads, 0, st>>>(A.refs, A.N, fa.K, A.w, A.nofit, fa.RP);
   return cudaGetLastError();

@@ -113,7 +113,7 @@ def test_clustered_frames(h, precision):
     assert h.stats()["n_refs"] >= 2
 
 
-@pytest.mark.parametrize("pipeline", [1, 2, 3])
+@pytest.mark.parametrize("pipeline", [1, 2, 3, 4])
 @pytest.mark.parametrize("precision", ["fp32", "tc"])
 def test_clustered_sorted_layout(h, pipeline, precision):
     # frames from 12 interleaved centroids: a whole triangle is computed over
@@ -217,7 +217,7 @@ def test_tc_matches_fp32_closely(h):
     assert np.abs(a - b).max() <= TOL
 
 
-@pytest.mark.parametrize("pipeline", [0, 1, 2, 3])
+@pytest.mark.parametrize("pipeline", [0, 1, 2, 3, 4])
 @pytest.mark.parametrize("F,N", [(67, 129), (300, 2000), (129, 31), (2, 65), (171, 200)])
 def test_tc_pipeline_variants(h, pipeline, F, N):
     X, m = synth.trajectory(F * 7 + N, F, N, 0.1, 3.0, np.float32, True)
@@ -232,7 +232,7 @@ def test_tc_pipeline_variants(h, pipeline, F, N):
         h.set_option(gbrmsd.OPT_TC_PIPELINE, gbrmsd.TC_PIPELINE_DEFAULT)
 
 
-@pytest.mark.parametrize("pipeline", [1, 2, 3])
+@pytest.mark.parametrize("pipeline", [1, 2, 3, 4])
 def test_tc_pipeline_full_and_rows(h, pipeline):
     R, m = synth.trajectory(77, 130, 257, 0.1, 3.0, np.float32, True)
     T, _ = synth.trajectory(78, 201, 257, 0.1, 3.0, np.float32, True)

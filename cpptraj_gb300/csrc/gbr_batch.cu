@@ -34,9 +34,9 @@ namespace {
 // Kernel per trajectory: the one-SM tensor-core kernel (64- or 32-atom stages),
 // the pair-of-SMs tensor-core kernel (shallow or deep stages), the FP32
 // CUDA-core kernel, or FP64 for every pair.
-enum Choice { kTC64 = 0, kTC32 = 1, kFP32 = 2, kFP64 = 3, kTCPairS = 4, kTCPairD = 5 };
-bool is_tc(int c) { return c == kTC64 || c == kTC32 || c == kTCPairS || c == kTCPairD; }
-int tc_variant_of(int c) { return c == kTC64 ? 0 : c == kTC32 ? 1 : c == kTCPairS ? 2 : 3; }
+enum Choice { kTC64 = 0, kTC32 = 1, kFP32 = 2, kFP64 = 3, kTCPairS = 4, kTCPairD = 5, kTCPairW = 6 };
+bool is_tc(int c) { return c == kTC64 || c == kTC32 || c == kTCPairS || c == kTCPairD || c == kTCPairW; }
+int tc_variant_of(int c) { return c == kTC64 ? 0 : c == kTC32 ? 1 : c == kTCPairS ? 2 : c == kTCPairW ? 4 : 3; }
 
 struct Prob {
   int64_t F = 0;
@@ -352,6 +352,7 @@ extern "C" int gbr_allpairs_batched(gbr_handle* h, int32_t n_traj, const float* 
     if (p.F >= 84) {
       c.push_back(kTCPairS);
       c.push_back(kTCPairD);
+      c.push_back(kTCPairW);
     }
     return c;
   };

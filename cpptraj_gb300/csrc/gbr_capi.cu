@@ -32,6 +32,12 @@ constexpr int kMaxBands = 8;  // output row bands whose copies overlap the contr
 // HBM's L2 merges but the host link does not: results written straight into
 // pinned host memory keep the shallow shape.
 constexpr int kDeepStageAtoms = 1280;
+// Below this atom count the epilogue bounds the pair kernel harder still and
+// the wide-chunk shape (16-frame chunks, 3 stages: half the epilogue's named
+// barriers per pair) wins: measured 4-5 % at 300 and 500 atoms, 7 % slower at
+// 1,000.
+constexpr int kWideChunkAtoms = 768;
+int auto_tc_variant(int N) { return N >= kDeepStageAtoms ? 3 : (N < kWideChunkAtoms ? 4 : 2); }
 // Default band of the streamed triangle: 256 Mi floats (1 GiB per device
 // slot, two slots on the device and two in pinned host memory).
 constexpr int64_t kDefaultBandFloats = (int64_t)1 << 28;
@@ -303,7 +309,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
   std::vector<int64_t> scuts;
   int64_t sband = 0;
   if (rs) {
-    const int var = (h->tc_variant >= 0) ? h->tc_variant : (N >= kDeepStageAtoms ? 3 : 2);
+    const int var = (h->tc_variant >= 0) ? h->tc_variant : auto_tc_variant(N);
     const int32_t align = tc ? (var >= 2 ? 84 : 42) : (need_planes ? 64 : 1);
     scuts.resize((size_t)(n_ref + 2));
     const int64_t nb = gbr_row_bands(n_ref, rs->band, align, scuts.data(), (int64_t)scuts.size());
@@ -429,7 +435,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
   // tiles are grouped by the first chunk that completes the frames they read
   // (grouped order kept within a stage); when prep has built the operands
   // through a chunk, the tiles ready by then are launched behind it.
-  const int tc_variant = (h->tc_variant >= 0) ? h->tc_variant : (N >= kDeepStageAtoms ? 3 : 2);
+  const int tc_variant = (h->tc_variant >= 0) ? h->tc_variant : auto_tc_variant(N);
   bool overlap = h->input_overlap && n_chunks > 0 && tc && map.tri && !tgt_xyz && out_dev;
   std::vector<int64_t> stage_off;
   std::vector<int2> stage_tiles;

@@ -1157,48 +1157,109 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
 
 // P_fc = sum_a p_f[a] (sqrt(w) r_c[a])^T against references c = 1 .. K-1 (c = 0
 // comes with k_build), from the operands k_build wrote (the values the
-// contraction reads).  One warp per operand position, kPrefGroup references
-// per pass over its atoms, so each operand is read K / kPrefGroup times.
-constexpr int kPrefGroup = 8;
+// contraction reads).  A block takes 32 operand positions at a time (4 per
+// warp) and walks the atoms in chunks of kPrefAtoms: the chunk of every
+// reference (atom-major, the 3(K-1) values of an atom contiguous) and of the
+// 32 operands is staged in shared memory, then each lane owns up to
+// kPrefComb of the 3(K-1) (reference, component) columns and accumulates, for
+// its warp's 4 positions, the 3 rows of each.  Per output the sum runs over
+// the atoms in order.
+constexpr int kPrefAtoms = 64;
+constexpr int kPrefFpw = 4;   // positions per warp
+constexpr int kPrefComb = 6;  // most columns per lane: 3 (K - 1) <= 32 * 6 (K <= 65)
+size_t pref_smem_bytes(int K) {
+  return sizeof(float) * ((size_t)kPrefAtoms * 3 * (K - 1) + 8 * kPrefFpw * 3 * kPrefAtoms + 8 * kPrefFpw * 32 * kPrefComb);
+}
+template <int NC>  // columns per lane: 3 (K - 1) <= 32 * NC
 __global__ void __launch_bounds__(256) k_pref(BuildArgs b, int64_t F, int N) {
-  const int lane = threadIdx.x & 31;
-  const int Np = b.Np, K = b.K;
-  for (int64_t pf = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; pf < F;
-       pf += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    const size_t base = (size_t)pf * 3 * Np;
-    const float inv = b.tc ? b.inv_scale[pf] : 1.0f;
-    for (int c0 = 1; c0 < K; c0 += kPrefGroup) {
-      float h[kPrefGroup * 9];
+  extern __shared__ float ps[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int Np = b.Np, K = b.K, ncol = 3 * (K - 1);
+  float* rs = ps;                                            // [kPrefAtoms][ncol]
+  float* vs = rs + (size_t)kPrefAtoms * ncol;                 // [8][kPrefFpw][3][kPrefAtoms]
+  float* dg = vs + 8 * kPrefFpw * 3 * kPrefAtoms;             // [8][kPrefFpw][32 * kPrefComb] diagonal terms
+  float* vw = vs + warp * kPrefFpw * 3 * kPrefAtoms;
+  for (int64_t g0 = (int64_t)blockIdx.x * 8 * kPrefFpw; g0 < F; g0 += (int64_t)gridDim.x * 8 * kPrefFpw) {
+    const int64_t p0 = g0 + (int64_t)warp * kPrefFpw;  // this warp's first position
+    float acc[kPrefFpw][NC][3];
 #pragma unroll
-      for (int q = 0; q < kPrefGroup * 9; ++q) h[q] = 0.0f;
-      for (int a = lane; a < N; a += 32) {
-        float v[3];
+    for (int f = 0; f < kPrefFpw; ++f)
 #pragma unroll
-        for (int p = 0; p < 3; ++p) {
-          const size_t i = base + (size_t)p * Np + a;
-          v[p] = b.tc ? (__half2float(b.hi[i]) + __half2float(b.lo[i])) * inv : b.plane[i];
+      for (int j = 0; j < NC; ++j)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) acc[f][j][q] = 0.0f;
+    for (int a0 = 0; a0 < N; a0 += kPrefAtoms) {
+      const int na = min(kPrefAtoms, N - a0);
+      __syncthreads();  // the previous chunk is consumed
+      for (int x = threadIdx.x; x < na * ncol; x += blockDim.x) {
+        const int al = x / ncol, m = x - al * ncol;
+        const int c = 1 + m / 3, qq = m - (m / 3) * 3;
+        rs[x] = __ldg(b.swr + ((size_t)c * N + a0 + al) * 3 + qq);
+      }
+      for (int x = lane; x < kPrefFpw * 3 * kPrefAtoms; x += 32) {
+        const int f = x / (3 * kPrefAtoms), r = x - f * 3 * kPrefAtoms;
+        const int q = r / kPrefAtoms, al = r - q * kPrefAtoms;
+        const int64_t pf = p0 + f;
+        float v = 0.0f;
+        if (pf < F && al < na) {
+          const size_t i = (size_t)pf * 3 * Np + (size_t)q * Np + a0 + al;
+          const float inv = b.tc ? b.inv_scale[pf] : 1.0f;
+          v = b.tc ? (__half2float(b.hi[i]) + __half2float(b.lo[i])) * inv : b.plane[i];
+        }
+        vw[x] = v;
+      }
+      __syncthreads();
+      for (int al = 0; al < na; ++al) {
+        float r[NC];
+#pragma unroll
+        for (int j = 0; j < NC; ++j) {
+          const int m = lane + 32 * j;
+          r[j] = (m < ncol) ? rs[al * ncol + m] : 0.0f;
         }
 #pragma unroll
-        for (int g = 0; g < kPrefGroup; ++g) {
-          if (c0 + g < K) {
-            const float* rc = b.swr + ((size_t)(c0 + g) * N + a) * 3;
-            const float r0 = __ldg(rc), r1 = __ldg(rc + 1), r2 = __ldg(rc + 2);
-            float* hg = h + 9 * g;
-            hg[0] += v[0] * r0; hg[1] += v[0] * r1; hg[2] += v[0] * r2;
-            hg[3] += v[1] * r0; hg[4] += v[1] * r1; hg[5] += v[1] * r2;
-            hg[6] += v[2] * r0; hg[7] += v[2] * r1; hg[8] += v[2] * r2;
+        for (int f = 0; f < kPrefFpw; ++f) {
+          const float v0 = vw[(f * 3 + 0) * kPrefAtoms + al], v1 = vw[(f * 3 + 1) * kPrefAtoms + al],
+                      v2 = vw[(f * 3 + 2) * kPrefAtoms + al];
+#pragma unroll
+          for (int j = 0; j < NC; ++j) {
+            acc[f][j][0] += v0 * r[j];
+            acc[f][j][1] += v1 * r[j];
+            acc[f][j][2] += v2 * r[j];
           }
         }
       }
-      warp_sum_f32<kPrefGroup * 9>(h);
-      if (lane == 0) {
-        for (int g = 0; g < kPrefGroup && c0 + g < K; ++g) {
-          float* Pf = b.P + ((size_t)pf * K + c0 + g) * 9;
-          for (int q = 0; q < 9; ++q) Pf[q] = h[9 * g + q];
-          b.trP[(size_t)pf * K + c0 + g] = h[9 * g] + h[9 * g + 4] + h[9 * g + 8];
+    }
+    // P[pf][c][q][q'] for the lane's columns m = 3 (c - 1) + q'; the diagonal
+    // terms (q = q') go through shared memory for trP = P00 + P11 + P22.
+    float* dw = dg + warp * kPrefFpw * 32 * kPrefComb;
+#pragma unroll
+    for (int f = 0; f < kPrefFpw; ++f) {
+      const int64_t pf = p0 + f;
+#pragma unroll
+      for (int j = 0; j < NC; ++j) {
+        const int m = lane + 32 * j;
+        if (m < ncol) {
+          const int c = 1 + m / 3, qq = m - (m / 3) * 3;
+          if (pf < F) {
+            float* Pf = b.P + ((size_t)pf * K + c) * 9;
+            Pf[0 * 3 + qq] = acc[f][j][0];
+            Pf[1 * 3 + qq] = acc[f][j][1];
+            Pf[2 * 3 + qq] = acc[f][j][2];
+          }
+          dw[f * 32 * kPrefComb + m] = (qq == 0) ? acc[f][j][0] : (qq == 1) ? acc[f][j][1] : acc[f][j][2];
         }
       }
     }
+    __syncwarp();
+    for (int f = 0; f < kPrefFpw; ++f) {
+      const int64_t pf = p0 + f;
+      if (pf >= F) break;
+      for (int c = 1 + lane; c < K; c += 32) {
+        const float* d = dw + f * 32 * kPrefComb + 3 * (c - 1);
+        b.trP[(size_t)pf * K + c] = d[0] + d[1] + d[2];
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -1529,8 +1590,26 @@ static cudaError_t finish_impl(const FinishArgs& fa, cudaStream_t st) {
   if (!fa.built) {
     const BuildArgs b = build_args(fa, A, S);
     k_build<T><<<prep_grid(A.F, kBuildBlocksPerSM, kFPB), kPrepThreads, 0, st>>>(src, 0, A.F, b);
-    if (fa.K > 1)
-      k_pref<<<(unsigned)std::min<int64_t>((A.F + 7) / 8, 152 * 16), 256, 0, st>>>(b, A.F, A.N);
+    if (fa.K > 1) {
+      if (3 * (fa.K - 1) > 32 * kPrefComb) return cudaErrorInvalidValue;
+      const size_t sm = pref_smem_bytes(fa.K);
+      const int64_t groups = (A.F + 8 * kPrefFpw - 1) / (8 * kPrefFpw);
+      const unsigned grid = (unsigned)std::min<int64_t>(groups, 152 * 4);
+      auto launch = [&](auto kern) -> cudaError_t {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        kern<<<grid, 256, sm, st>>>(b, A.F, A.N);
+        return cudaGetLastError();
+      };
+      const int nc = (3 * (fa.K - 1) + 31) / 32;
+      cudaError_t e = (nc <= 1)   ? launch(k_pref<1>)
+                      : (nc == 2) ? launch(k_pref<2>)
+                      : (nc == 3) ? launch(k_pref<3>)
+                      : (nc == 4) ? launch(k_pref<4>)
+                      : (nc == 5) ? launch(k_pref<5>)
+                                  : launch(k_pref<6>);
+      if (e != cudaSuccess) return e;
+    }
   }
   k_ref_terms<<<fa.K * fa.K * kRefCluster, kOneBlockThreads, 0, st>>>(A.refs, A.N, fa.K, A.w, A.nofit, fa.RP);
   return cudaGetLastError();

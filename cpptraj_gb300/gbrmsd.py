@@ -24,7 +24,7 @@ PREC_FP32, PREC_TC, PREC_FP64 = 0, 1, 2
 OPT_TAU, OPT_MAX_REFS, OPT_TOL, OPT_TIMING, OPT_TC_PIPELINE, OPT_HOST_OUT, OPT_INPUT_OVERLAP = 0, 1, 2, 3, 4, 5, 6
 OPT_BAND_FLOATS = 7
 #: The library's default tensor-core kernel shape (pairs of SMs).
-TC_PIPELINE_DEFAULT = -1  # automatic: deep stages from 1,280 atoms (device results), shallow otherwise
+TC_PIPELINE_DEFAULT = -1  # automatic: deep stages from 1,280 atoms, wide chunks below 768, shallow between
 
 PRECISIONS = {"fp32": PREC_FP32, "tc": PREC_TC, "fp64": PREC_FP64}
 MODES = {"fit": FIT, "nofit": NOFIT, "dme": DME}

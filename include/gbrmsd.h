@@ -277,7 +277,7 @@ int gbr_get_stats(const gbr_handle *h, gbr_stats *out);
  *                        3 = pairs of SMs, 64-atom stages x 3 with narrower
  *                        epilogue chunks, 4 = pairs of SMs, 32-atom stages x 3
  *                        with wider (16-frame) epilogue chunks; -1 (default)
- *                        = 3 from 1,280 atoms on, 2 otherwise
+ *                        = 3 from 1,280 atoms on, 4 below 768, 2 between
  *   GBR_OPT_HOST_OUT     pinned host `out` of gbr_allpairs: 1 = the kernels
  *                        store into it directly (default), 0 = results staged
  *                        in device memory and copied back in row bands

@@ -56,7 +56,8 @@ def parse():
     ap.add_argument("--host-io", action="store_true",
                     help="with --profile: pinned host input and output (the e2e path) instead of HBM")
     ap.add_argument("--workload", default="c1",
-                    choices=["c1", "c2", "c3", "c4", "c4profile", "dme", "rms", "centroids", "accuracy", "hostlink"],
+                    choices=["c1", "c2", "c3", "c3profile", "c4", "c4profile", "dme", "rms", "centroids", "accuracy",
+                             "hostlink"],
                     help="c1 = the headline metric; c2/c3/c4/dme print secondary lines for the other configs; "
                          "hostlink times plain pinned host<->device copies of the c1 input and output sizes")
     return ap.parse_args()
@@ -544,6 +545,35 @@ def main_c4(args):
     print(json.dumps(sec_c4(args, _peaks())), flush=True)
 
 
+def main_c3profile(args):
+    """The batched call of the 256-trajectory workload twice (autotune and
+    graph capture, then one graph replay), nothing else on the GPU (for ncu)."""
+    import ctypes
+
+    import torch
+
+    from cpptraj_gb300 import gbrmsd, synth
+
+    batch = synth.workload_c3()
+    h = gbrmsd.Handle(0)
+    h.set_stream(torch.cuda.current_stream().cuda_stream)
+    n = len(batch)
+    dX = [torch.from_numpy(X).cuda() for X, _ in batch]
+    dm = [torch.from_numpy(m).cuda() for _, m in batch]
+    outs = [torch.empty(X.shape[0] * (X.shape[0] - 1) // 2, device="cuda") for X, _ in batch]
+    P = ctypes.c_void_p * n
+    xyz, ms_, op = P(*[x.data_ptr() for x in dX]), P(*[m.data_ptr() for m in dm]), P(*[o.data_ptr() for o in outs])
+    nf = (ctypes.c_int64 * n)(*[X.shape[0] for X, _ in batch])
+    na = (ctypes.c_int32 * n)(*[X.shape[1] for X, _ in batch])
+    for _ in range(2):
+        h._check(h.lib.gbr_allpairs_batched(h.h, n, ctypes.cast(xyz, ctypes.c_void_p), ctypes.cast(nf, ctypes.c_void_p),
+                                            ctypes.cast(na, ctypes.c_void_p), ctypes.cast(ms_, ctypes.c_void_p),
+                                            gbrmsd.FIT, gbrmsd.PREC_TC, ctypes.cast(op, ctypes.c_void_p)))
+        torch.cuda.synchronize()
+    shapes = [[int(X.shape[0]), int(X.shape[1])] for X, _ in batch]
+    print(json.dumps({"profile_batched": h.stats(), "shapes": shapes}))
+
+
 def main_c4profile(args):
     """--warmup backward calls of the gradient workload (4,096 x 1,000), then
     exactly one more, nothing else on the GPU (for ncu)."""
@@ -841,7 +871,7 @@ def main():
     if args.profile:
         return main_profile(args)
     if args.workload != "c1":
-        return {"c2": main_c2, "c3": main_c3, "c4": main_c4, "c4profile": main_c4profile, "dme": main_dme, "rms": main_rms, "centroids": main_centroids,
+        return {"c2": main_c2, "c3": main_c3, "c3profile": main_c3profile, "c4": main_c4, "c4profile": main_c4profile, "dme": main_dme, "rms": main_rms, "centroids": main_centroids,
                 "accuracy": main_accuracy, "hostlink": main_hostlink}[args.workload](args)
     import torch
     import torch.distributed as dist

@@ -172,6 +172,7 @@ cudaError_t enqueue_prob(gbr_handle* h, Prob& p, int mode, bool host_in, bool ho
   pa.sqw = p.sqw;
   pa.sqwf = p.sqwf;
   pa.scratch = p.scratch;
+  pa.RP = p.RP;
   PrepOut po;
   if ((e = run_prep(pa, po, st)) != cudaSuccess) return e;
   nl += po.launches;
@@ -231,6 +232,7 @@ cudaError_t enqueue_prob(gbr_handle* h, Prob& p, int mode, bool host_in, bool ho
     fa.w = w;
     fa.nofit = nofit;
     fa.RP = p.RP;
+    fa.self_terms = po.self_terms;
     if ((e = run_finish(fa, st)) != cudaSuccess) return e;
     cudaMemsetAsync(count, 0, sizeof(unsigned long long), st);
     cudaMemsetAsync(derr, 0, sizeof(int), st);
@@ -271,7 +273,7 @@ cudaError_t enqueue_prob(gbr_handle* h, Prob& p, int mode, bool host_in, bool ho
     ex.count = (int64_t)p.cap;
     ex.dev_count = count;
     e = run_exact(ex, st);
-    nl += 4;  // finish, reference-pair table, pair kernel, fix-up
+    nl += po.self_terms ? 3 : 4;  // finish, reference-pair table (unless prep wrote it), pair kernel, fix-up
   }
   if (e != cudaSuccess) return e;
   if (launches) *launches += nl;

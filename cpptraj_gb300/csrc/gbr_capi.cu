@@ -54,7 +54,7 @@ struct RowStream {
 int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dtype, int64_t n_ref,
                   int64_t n_tgt, int32_t n_atom, const double* ref_mass, const double* tgt_mass, int mode,
                   int out_kind, int precision, float* out, int64_t row_begin, int64_t row_end,
-                  const RowStream* rs);
+                  const RowStream* rs, bool redo = false);
 }
 
 extern "C" {
@@ -207,7 +207,7 @@ namespace {
 int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int dtype, int64_t n_ref,
                   int64_t n_tgt, int32_t n_atom, const double* ref_mass, const double* tgt_mass, int mode,
                   int out_kind, int precision, float* out, int64_t row_begin, int64_t row_end,
-                  const RowStream* rs) {
+                  const RowStream* rs, bool redo) {
   if (!h) return GBR_ERR_ARG;
   h->err.clear();
   h->stats = gbr_stats{};
@@ -513,6 +513,13 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
   // the tensor-core epilogue stages per tile); outputs map back to frames.
   pa.sort_frames = (!rs && map.tri && row_begin == 0 && row_end == n_ref) ? 1 : 0;
   pa.n_chunks = n_chunks;
+  // Whole input on the device and results written in place: the
+  // reference-count decision stays on the device (no host round trip inside
+  // prep).  A call that turns out to need several references runs again
+  // (redo), from the state its first scan left in the workspace.
+  const bool multi_hint = h->last_multi && h->last_F == F && h->last_N == N;
+  pa.defer_multi = (!redo && !multi_hint && n_chunks == 0 && !rs && out_dev && Kmax > 1) ? (int*)P[25] + 1 : nullptr;
+  pa.resume_scan = redo ? 1 : 0;
   for (int c = 0; c < n_chunks; ++c) {
     pa.chunk_end[c] = chunk_end[c];
     pa.chunk_ev[c] = h->xev[c];
@@ -663,6 +670,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
     fa.w = d_w;
     fa.nofit = nofit;
     fa.RP = (float*)P[17];
+    pa.RP = fa.RP;
     // Per-frame terms as the pair kernels read them, for K references (sorted:
     // reference-grouped operand positions).
     auto make_terms = [&](int Kt, bool sorted) {
@@ -762,14 +770,18 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
     fa.sorted = po.sorted;
     fa.K = K;
     fa.built = po.built;
+    fa.skip = po.deferred ? pa.defer_multi : nullptr;
+    fa.self_terms = po.self_terms;
     if (!spec_done) {
       if ((e = run_finish(fa, st)) != cudaSuccess) return h->cuda_fail(e, "finish");
-      launches += po.built ? 1 : (K > 1 ? 3 : 2);  // k_build (+ k_pref with several references), k_ref_terms
+      // k_build (+ k_pref with several references), k_ref_terms (unless prep wrote the one reference's)
+      launches += po.built ? 1 : (K > 1 ? 3 : (po.self_terms ? 1 : 2));
     }
     // One launch of the pair kernel over the rows of map m.
     auto launch_pairs = [&](const OutMap& m, const FlagList& f) -> cudaError_t {
-      if (tc) return launch_tc(m, f, terms, 0, 0, nullptr);
+      if (tc) return launch_tc(m, f, terms, 0, 0, fa.skip);
       PairLaunch L{};
+      L.skip = fa.skip;
       L.plane = pa.plane;
       L.Np = Np;
       L.N = N;
@@ -812,11 +824,16 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
         ++launches;
       }
       if (h->timing) cudaEventRecord(h->ev[2], st);
+      int dflags[2] = {0, 0};  // device error, several references needed (deferred decision)
       cudaMemcpyAsync(&nflag, P[21], sizeof nflag, cudaMemcpyDeviceToHost, st);
-      cudaMemcpyAsync(&derr, P[25], sizeof derr, cudaMemcpyDeviceToHost, st);
+      cudaMemcpyAsync(dflags, P[25], sizeof dflags, cudaMemcpyDeviceToHost, st);
       if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return h->cuda_fail(e, "pair kernel");
+      derr = dflags[0];
       if (derr != 0)
         return h->fail(GBR_ERR_DEVICE, "pair kernel reported device error %d (bounded wait expired)", derr);
+      if (po.deferred && dflags[1] != 0)  // every pass after the first scan did nothing
+        return allpairs_impl(h, ref_xyz, tgt_xyz, dtype, n_ref, n_tgt, n_atom, ref_mass, tgt_mass, mode, out_kind,
+                             precision, out, row_begin, row_end, rs, true);
       if (nflag > 0) {
         if (nflag <= flag_cap) {
           ex.list = (const int2*)P[20];
@@ -917,6 +934,11 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
   h->stats.n_refs = K;
   h->stats.precision = precision;
   h->stats.kernel_launches = launches;
+  if (need_planes && Kmax > 1) {
+    h->last_F = F;
+    h->last_N = N;
+    h->last_multi = (K > 1);
+  }
   if (h->timing) {
     float a = 0, b = 0, c = 0;
     cudaEventElapsedTime(&a, h->ev[0], h->ev[1]);
@@ -1073,6 +1095,7 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   pa.sqw = (double*)P[29];
   pa.sqwf = (float*)P[30];
   pa.scratch = P[31];
+  pa.RP = (float*)P[19];
   PrepOut po;
   if ((e = run_prep(pa, po, st)) != cudaSuccess) return h->cuda_fail(e, "prep");
   int launches = po.launches;
@@ -1112,8 +1135,9 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   fa.w = d_w;
   fa.nofit = 0;
   fa.RP = (float*)terms.RP;
+  fa.self_terms = po.self_terms;
   if ((e = run_finish(fa, st)) != cudaSuccess) return h->cuda_fail(e, "finish");
-  launches += 2;
+  launches += po.self_terms ? 1 : 2;
   float* B = (float*)P[20];
   cudaMemsetAsync(B, 0, sizeof(float) * 3 * F * ldB, st);
   cudaMemsetAsync(P[21], 0, sizeof(float) * 9 * F, st);

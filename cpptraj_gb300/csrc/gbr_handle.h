@@ -59,6 +59,13 @@ struct gbr_handle {
   gbr_stats stats{};
   double tau = 6.0;
   int max_refs = 32;
+  // Frames and atoms of the last call whose reference count was decided,
+  // and whether it needed several references: a call of the same shape then
+  // decides on the host at once rather than assuming one reference on the
+  // device and running again.
+  int64_t last_F = -1;
+  int last_N = -1;
+  bool last_multi = false;
   double tol = 5e-5;
   bool timing = false;
   char* ws = nullptr;

@@ -63,25 +63,38 @@ struct PrepArgs {
   // a scanned frame is farther than tau from reference 0 (the speculation
   // will fail); work enqueued through on_built may test it.
   int* spec_fail;
+  // Whole input on the device, no chunks: when non-null, the reference-count
+  // decision after the first scan is left on the device.  Prep continues as
+  // for one reference and every later pass of this call (prep, build, pair
+  // kernel) tests this int at launch; it reads 1 once a frame is farther than
+  // tau from reference 0, and then the passes do nothing and the caller
+  // repeats the call with the decision on the host (PrepOut::deferred).
+  int* defer_multi;
+  // The second run of a deferred call: weights, reference 0 and the first
+  // scan are in the workspace already (the deferred passes did nothing).
+  int resume_scan;
+  // Reference-pair terms [K][K][24] (optional): when one reference stays,
+  // the refinement writes its terms with itself here (PrepOut::self_terms).
+  float* RP;
 };
 
 // Further per-call prep buffers, carved from PrepArgs::scratch.
 struct PrepScratch {
-  float* wf;       // [N] weights in FP32 (centring masses of target frames)
-  float* wfl;      // [N] w - wf (the low part)
   float* cmf_ref;  // [N] centring masses of reference frames in FP32
-  float* cmfl_ref; // [N] their low parts
   double* scal;    // [8] max sqrt(w), sum w, sum of reference centring masses, 0, their reciprocals
   float2* refhl;   // [Kmax][N][3] references as hi + lo floats
   double* sr;      // [Kmax][3] sum_a w_a r_k,a
   float* rmax;     // [Kmax] max_a |r_k,a|
   float4* quat;    // [F] superposition quaternion onto the assigned reference
   float* ymax;     // [F] upper bound of max_a |y_a| (centred frame)
-  float* ftab;     // [F][24] rotation hi/lo (9 + 9), R c hi/lo (3 + 3)
+  float* ftab;     // [F][24] rotation hi/lo (9 + 9), centre hi/lo (3 + 3)
   int* pos;        // [F] frame -> position when frames are laid out sorted by reference
   int* assign_pos; // [F] reference of the frame at each position
-  float* swr0;     // [N][3] sqrt(w) r_0 before refinement (scans that run after a speculative refinement)
+  float4* qscan;   // [Kmax][N] {sqrt(w) r_k, sqrt(w)} of the references as chosen (the scans read these)
+  float4* qbuild;  // [Kmax][N] the same of the refined references (the operand build reads these)
   int* kstate;     // [2] k-centre choice on the device: stopped flag, index of the last reference added
+  unsigned* rcount;  // k_ref_update: blocks done (one reference's self terms)
+  double* rsu;       // k_ref_update: per-block sums of w r r^T (one reference)
 };
 size_t prep_scratch_bytes(int64_t F, int N, int Kmax);
 PrepScratch prep_carve(void* base, int64_t F, int N, int Kmax);
@@ -110,6 +123,8 @@ struct FinishArgs {
   int nofit;
   float* RP;
   int built;          // the operands are built already (speculative prep): only the reference-pair terms
+  const int* skip;    // device int or nullptr: the passes do nothing when it reads non-zero at launch
+  int self_terms;     // RP holds the one reference's terms already (PrepOut::self_terms)
 };
 cudaError_t run_finish(const FinishArgs& A, cudaStream_t st);
 
@@ -118,6 +133,8 @@ struct PrepOut {
   int launches = 0;
   int sorted = 0;  // operands and per-frame terms are at sorted positions (PrepScratch::pos)
   int built = 0;   // the operands were built during prep (one reference, chunked input)
+  int deferred = 0; // K = 1 was assumed and PrepArgs::defer_multi decides it on the device
+  int self_terms = 0;  // one reference, and PrepArgs::RP holds its terms with itself
 };
 
 cudaError_t run_prep(const PrepArgs& A, PrepOut& o, cudaStream_t st);
@@ -161,6 +178,7 @@ struct PairLaunch {
   OutMap map;
   FlagList flags;
   TileSpace tiles;
+  const int* skip;     // device int or nullptr: the kernel does nothing when it reads non-zero at launch
 };
 
 cudaError_t run_pairs_fp32(const PairLaunch& L, cudaStream_t st);

@@ -53,6 +53,7 @@ __device__ __forceinline__ void load_slab(float* dst, const float* plane, int64_
 
 template <bool BWD>
 __global__ void __launch_bounds__(THREADS, 1) k_pairs_fp32(PairLaunch L) {
+  if (L.skip && *L.skip != 0) return;  // uniform over the grid: before any barrier
   extern __shared__ __align__(16) float smem[];
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;

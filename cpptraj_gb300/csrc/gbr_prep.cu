@@ -1,13 +1,15 @@
 // gbr_prep.cu -- per-frame passes that run before the pair contraction (K1).
 //
 // GB300's FP64 rate is a small fraction of its FP32 rate, so nothing here does
-// FP64 arithmetic per atom per frame.  Per-atom work is FP32; where a value
-// must be exact to well below FP32 rounding of the raw coordinates (the
-// superposed residual p = sqrt(w)(R y - r)), it is evaluated as a compensated
-// dot product (Dot2 of Ogita, Rump and Oishi, "Accurate sum and dot product",
-// SIAM J. Sci. Comput. 26(6), 2005) over FP32 hi/lo splits of the FP64
-// rotation, translation and reference.  FP64 is kept for O(1)-per-frame and
-// O(N)-per-reference work.
+// FP64 arithmetic per atom per frame.  Per-atom work is plain FP32 (the passes
+// over the coordinates are bound by instruction issue, so every operation per
+// atom counts).  What must not be rounded to FP32 is what acts on every atom
+// of a frame alike: the rotation (kept as FP32 hi + lo of the FP64 matrix) and
+// the frame centre (hi + lo of the FP64 value).  Rounding that differs from
+// atom to atom -- of x - c, of the products R (x - c), of the sums -- enters
+// an RMSD only through its projection on the pair's residual, about
+// 2^-24 |y| / sqrt(N).  FP64 is kept for O(1)-per-frame and O(N)-per-reference
+// work.
 //
 // Passes over the coordinates (one warp per frame, 8 frames per block):
 //   k_scan<FIRST>  FIRST: the frame centre (Frame::CenterOnOrigin / the target
@@ -17,12 +19,12 @@
 //                  k-centre choice.  The fit gives the distance and the FP32
 //                  QCP quaternion; a frame keeps the nearest reference.
 //   k_rot          one thread per frame: exact FP64 rotation from the
-//                  quaternion, R c, and their hi/lo FP32 splits.
+//                  quaternion; it and the centre as hi/lo FP32 splits.
 //   k_sample_sum   mean residual d = R y - r over the first kSample frames of
 //                  each reference (fixed chunks, fixed order).
 //   k_ref_update   moves each reference to that mean: residuals shrink to each
 //                  frame's own fluctuation.
-//   k_build        p = sqrt(w)(R y - r_a) by Dot2; the FP16 hi/lo split with a
+//   k_build        p = sqrt(w)(R (x - c) - r_a); the FP16 hi/lo split with a
 //                  per-frame power-of-two scale (tensor path) or the FP32
 //                  plane; n_f = |p|^2 and P_fc = sum p (sqrt(w) r_c)^T from the
 //                  exact operand values the contraction reads.
@@ -135,7 +137,7 @@ static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 size_t prep_scratch_bytes(int64_t F, int N, int Kmax) {
   size_t b = 0;
-  b += align256(sizeof(float) * N) * 4;
+  b += align256(sizeof(float) * N);
   b += align256(sizeof(double) * 8);
   b += align256(sizeof(float2) * (size_t)Kmax * 3 * N);
   b += align256(sizeof(double) * 3 * Kmax);
@@ -144,8 +146,10 @@ size_t prep_scratch_bytes(int64_t F, int N, int Kmax) {
   b += align256(sizeof(float) * F);
   b += align256(sizeof(float) * kFtab * F);
   b += align256(sizeof(int) * F) * 2;
-  b += align256(sizeof(float) * 3 * N);
+  b += align256(sizeof(float4) * (size_t)Kmax * N) * 2;
   b += align256(sizeof(int) * 2);
+  b += align256(sizeof(unsigned));
+  b += align256(sizeof(double) * 9 * (size_t)((N + 31) / 32));  // k_ref_update's blocks
   return b;
 }
 
@@ -157,10 +161,7 @@ PrepScratch prep_carve(void* base, int64_t F, int N, int Kmax) {
     p += align256(bytes);
     return (void*)r;
   };
-  s.wf = (float*)take(sizeof(float) * N);
-  s.wfl = (float*)take(sizeof(float) * N);
   s.cmf_ref = (float*)take(sizeof(float) * N);
-  s.cmfl_ref = (float*)take(sizeof(float) * N);
   s.scal = (double*)take(sizeof(double) * 8);
   s.refhl = (float2*)take(sizeof(float2) * (size_t)Kmax * 3 * N);
   s.sr = (double*)take(sizeof(double) * 3 * Kmax);
@@ -170,8 +171,11 @@ PrepScratch prep_carve(void* base, int64_t F, int N, int Kmax) {
   s.ftab = (float*)take(sizeof(float) * kFtab * F);
   s.pos = (int*)take(sizeof(int) * F);
   s.assign_pos = (int*)take(sizeof(int) * F);
-  s.swr0 = (float*)take(sizeof(float) * 3 * N);
+  s.qscan = (float4*)take(sizeof(float4) * (size_t)Kmax * N);
+  s.qbuild = (float4*)take(sizeof(float4) * (size_t)Kmax * N);
   s.kstate = (int*)take(sizeof(int) * 2);
+  s.rcount = (unsigned*)take(sizeof(unsigned));
+  s.rsu = (double*)take(sizeof(double) * 9 * (size_t)((N + 31) / 32));
   return s;
 }
 
@@ -181,17 +185,6 @@ __device__ __forceinline__ void warp_sum_f32(float (&v)[NV]) {
   for (int k = 0; k < NV; ++k)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-}
-
-// Error-free transformations (Knuth's TwoSum; TwoProduct by FMA).
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
-  p = a * b;
-  e = fmaf(a, b, -p);
 }
 
 // One atom's coordinates as FP32 hi + lo (lo = 0 for FP32 input).
@@ -306,7 +299,7 @@ struct WarpPipe {
         const int nv = (n - head) >> 2, tail0 = head + 4 * nv;
         float* dst = ring + (issued % kPipe) * kStage + ((4 - head) & 3);
 #pragma unroll
-        for (int i = 0; i < 3; ++i) {
+        for (int i = 0; i < (3 * kChunkAtoms / 4 + 31) / 32; ++i) {
           const int j = lane + 32 * i;
           if (j < nv) cp_async16(dst + head + 4 * j, x + head + 4 * j);
         }
@@ -354,35 +347,26 @@ struct WarpPipe {
   }
 };
 
-// Row k of R x - t - r, with R, t, r given as FP32 hi + lo: Dot2 over the
-// hi products and the subtractions, lo terms into the compensation.  The
-// result is as accurate as if computed in twice FP32 precision and rounded.
-__device__ __forceinline__ float dot2_row(const float* Rh, const float* Rl, float th, float tl,
-                                          const float (&xh)[3], const float (&xl)[3], float rh, float rl) {
-  float s, c, p, e, q;
-  two_prod(Rh[0], xh[0], s, c);
-  two_prod(Rh[1], xh[1], p, e);
-  two_sum(s, p, s, q);
-  c += q + e;
-  two_prod(Rh[2], xh[2], p, e);
-  two_sum(s, p, s, q);
-  c += q + e;
-  two_sum(s, -th, s, q);
-  c += q;
-  two_sum(s, -rh, s, q);
-  c += q;
-  c += fmaf(Rl[0], xh[0], fmaf(Rl[1], xh[1], fmaf(Rl[2], xh[2], -tl - rl)));
-  c += fmaf(Rh[0], xl[0], fmaf(Rh[1], xl[1], Rh[2] * xl[2]));
-  return s + c;
-}
-
 // Weights in the forms the passes read; scal = {max sqrt(w), sum w, sum of
 // the reference centring masses, 0, 1 / sum w, 1 / sum of the reference
-// centring masses} (a reciprocal is 0 when its sum is 0).  One cluster of
-// kRefCluster CTAs.
-__global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockThreads)
-    k_weights(const double* w, const double* cmass_ref, int N, double* sqw, float* sqwf, float* wf, float* wfl,
-              float* cmf_ref, float* cmfl_ref, double* scal) {
+// centring masses} (a reciprocal is 0 when its sum is 0).  Run by the cluster
+// that builds reference 0 (k_make_ref), before it: atom a's sqrt(w) is
+// written and then read by the same thread.
+struct WeightsPass {
+  const double* w;
+  const double* cmass_ref;  // distinct reference centring masses or nullptr
+  double* sqw;
+  float* sqwf;
+  float* cmf_ref;
+  double* scal;
+};
+__device__ __forceinline__ void weights_pass(const WeightsPass& P, int N) {
+  const double* w = P.w;
+  const double* cmass_ref = P.cmass_ref;
+  double* sqw = P.sqw;
+  float* sqwf = P.sqwf;
+  float* cmf_ref = P.cmf_ref;
+  double* scal = P.scal;
   __shared__ double red[32 * 2], slots[kRefCluster * 2], bc[2];
   const int stride = kRefCluster * blockDim.x;
   double v[2] = {0.0, 0.0};
@@ -394,12 +378,9 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
     if (w) {
       sqw[a] = s;
       sqwf[a] = (float)s;
-      wf[a] = (float)wa;
-      wfl[a] = (float)(wa - (double)wf[a]);
     }
     if (cmass_ref) {
       cmf_ref[a] = (float)ca;
-      cmfl_ref[a] = (float)(ca - (double)cmf_ref[a]);
     }
     mx = fmax(mx, s);
     v[0] += wa;
@@ -454,17 +435,19 @@ __global__ void __launch_bounds__(kPrepThreads) k_centroid(FrameSrc<T> src, int6
 // Reference k := frame *fsel centred (and superposed onto reference `parent`
 // when fitting and use_parent).  Reference 0 is built before any centre is
 // known and centres its frame itself.  Writes the FP64 reference, sqrt(w) r
-// (FP32), r as hi + lo floats, sum w |r|^2, sum w r and max |r|.  FP64 per
+// (FP32, also packed with sqrt(w) for the scans), r as hi + lo floats,
+// sum w |r|^2, sum w r and max |r|.  FP64 per
 // atom: one cluster of kRefCluster CTAs shares the atoms.
 template <typename T>
 __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockThreads)
     k_make_ref(FrameSrc<T> src, const int64_t* fsel, const double* cen, const double* cmass_ref,
                const double* cmass_tgt, const double* w, const double* sqw, const int* assign, int k, int use_parent,
                int nofit, double* refs, float* swr, float2* refhl, double* Eref, double* sr, float* rmax,
-               const int* gate = nullptr) {
+               float4* qscan, const int* gate = nullptr, WeightsPass wp = WeightsPass{}) {
   // A gated round after the k-centre choice has stopped: every CTA of the
   // cluster reads the same word and leaves before any barrier.
   if (gate && *gate != 0) return;
+  if (wp.scal) weights_pass(wp, src.N);  // reference 0: the weights first
   __shared__ double red[32 * 10], slots[kRefCluster * 10], bc[10];
   __shared__ double Rs[9], cs[3];
   const int N = src.N;
@@ -541,13 +524,16 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
       r[2] = Rs[6] * y0 + Rs[7] * y1 + Rs[8] * y2;
     }
     const double sw = w ? sqw[a] : 1.0;
+    float q[3];
     for (int p = 0; p < 3; ++p) {
       rk[3 * a + p] = r[p];
-      swr[((size_t)k * N + a) * 3 + p] = (float)(sw * r[p]);
+      q[p] = (float)(sw * r[p]);
+      swr[((size_t)k * N + a) * 3 + p] = q[p];
       const float rh = (float)r[p];
       refhl[((size_t)k * N + a) * 3 + p] = make_float2(rh, (float)(r[p] - (double)rh));
       acc[1 + p] += wa * r[p];
     }
+    qscan[(size_t)k * N + a] = make_float4(q[0], q[1], q[2], (float)sw);
     const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
     acc[0] += wa * r2;
     mx = fmax(mx, r2);
@@ -563,16 +549,32 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
   }
 }
 
+// A frame's rotation table: the FP64-orthogonal rotation of its quaternion
+// and its centre, both as FP32 hi + lo (see k_rot).
+__device__ __forceinline__ void write_frame_table(float* ftab, double* rot, int64_t f, const float (&q)[4],
+                                                  const double (&c)[3], int nofit) {
+  double R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  if (!nofit) rotation_from_quat(q, R);
+  float* o = ftab + (size_t)kFtab * f;
+  for (int k = 0; k < 9; ++k) {
+    const float h = (float)R[k];
+    o[k] = h;
+    o[9 + k] = (float)(R[k] - (double)h);
+  }
+  for (int k = 0; k < 3; ++k) {
+    const float h = (float)c[k];
+    o[18 + k] = h;
+    o[21 + k] = (float)(c[k] - (double)h);
+  }
+  if (rot)
+    for (int k = 0; k < 9; ++k) rot[9 * f + k] = R[k];
+}
+
 struct ScanArgs {
-  const float* cm_ref;  // centring masses of reference frames (FP32, nullptr = geometric)
-  const float* cm_tgt;  // centring masses of target frames
-  const float* cml_ref; // low parts of those masses (exact mass = cm + cml)
-  const float* cml_tgt;
-  const float* wf;      // fit weights (FP32) or nullptr; read only when they differ from cm_ref
-  int cm_ref_is_w;      // reference frames centre with the fit weights
+  const float* cm_ref;  // centring masses of reference frames (FP32), read when cm_ref_is_w == 0
+  int cm_ref_is_w;      // reference frames centre with the fit weights (target frames always do)
   const double* scal;   // k_weights' scal: [1] sum w, [2] sum of reference centring masses, [4], [5] reciprocals
-  const float* sqwf;    // sqrt(w) or nullptr
-  const float* swr;     // sqrt(w) r_k, [N][3]
+  const float4* q;      // [N] {sqrt(w) r_k, sqrt(w)} (the weights centre too: w = sqrt(w)^2)
   const double* sr;     // sum w r_k, [3]
   const double* Eref;   // &Eref[k]
   double Wsum;
@@ -592,11 +594,15 @@ struct ScanArgs {
 //   sum w y r^T = sum w u r^T - (c - x0) (sum w r)^T
 //   sum w |y|^2 = sum w |u|^2 - 2 (c - x0).sum w u + W |c - x0|^2
 // Later passes (reference k > 0) centre with the known c directly.
+// Plain FP32 sums: an error d in a frame's centre moves every operand of the
+// frame by the same vector, which changes a best-fit RMSD only at second
+// order (|d_i - U d_j|^2 in RMSD^2), and the fit here only picks the
+// pre-alignment, which any rotation serves.
 template <typename T, bool FIRST>
 __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64_t f_begin, int64_t F, ScanArgs s) {
   if (s.gate && *s.gate != 0) return;  // uniform over the grid: before any barrier
   __shared__ __align__(16) float sbuf[kWarps][kPipe * kStage];
-  __shared__ float xpart[2][kFPB][kWPF - 1][20];  // the other parts' sums, by frame parity
+  __shared__ float xpart[2][kFPB][kWPF - 1][17];  // the other parts' sums, by frame parity
   const int N = src.N, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int grp = warp / kWPF, part = warp % kWPF;
   const bool fit = !s.nofit;
@@ -607,24 +613,14 @@ __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64
   pipe.init(src, f_first, F, f_stride, sbuf[warp], lane, part * nch / kWPF, (part + 1) * nch / kWPF);
   {
     const size_t n4 = (size_t)N * 4;
-    prefetch_l1(s.sqwf, n4);
-    prefetch_l1(s.swr, 3 * n4);
-    if (FIRST) {
-      prefetch_l1(s.cm_ref, n4);
-      prefetch_l1(s.cml_ref, n4);
-      if (s.cm_tgt != s.cm_ref && f_begin + (int64_t)gridDim.x * kFPB > src.n_ref) {
-        prefetch_l1(s.cm_tgt, n4);
-        prefetch_l1(s.cml_tgt, n4);
-      }
-    }
+    prefetch_l1(s.q, 4 * n4);
+    if (FIRST && !s.cm_ref_is_w && f_begin < src.n_ref) prefetch_l1(s.cm_ref, n4);
   }
   int it = 0;
   for (int64_t f = f_first; f < F; f += f_stride, ++it) {
     const T* x = src.frame(f);
     const bool in_ref = f < src.n_ref;
-    const float* cm = in_ref ? s.cm_ref : s.cm_tgt;
-    const float* cml = in_ref ? s.cml_ref : s.cml_tgt;
-    const bool same_w = in_ref ? (s.cm_ref_is_w != 0) : true;
+    const bool same_w = in_ref ? (s.cm_ref_is_w != 0) : true;  // centring masses = fit weights
     float o0, o1, o2;  // origin of the sums: x0 (FIRST) or the centre
     if (FIRST) {
       o0 = (float)x[0]; o1 = (float)x[1]; o2 = (float)x[2];
@@ -634,88 +630,50 @@ __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64
     }
     // v: 0-8 sum w u r^T, 9 sum w|u|^2 (fit) or sum |sqrt(w)x - sqrt(w)r|^2,
     //    10-12 sum cm u, 13-15 sum w u (weights differing from cm).
-    // The centre sums (10-12) are compensated: ce holds their error terms, so
-    // the centre is exact to ~FP32^2 (u = x - x0 and cm*u by error-free
-    // transformations, the running sums by TwoSum).
-    float v[16], ce[3] = {0.0f, 0.0f, 0.0f};
+    float v[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) v[q] = 0.0f;
-    float umax = 0.0f;
+    float umax = 0.0f;  // max |u|^2
     pipe.for_each_atom(f, lane, [&](int a, int a0, const float* xs) {
-      const float sw = s.sqwf ? __ldg(s.sqwf + a) : 1.0f;
-      float xh[3], xl[3], u[3], ue[3];
+      const float4 t = __ldg(s.q + a);
+      const float sw = t.w, r0 = t.x, r1 = t.y, r2 = t.z;
+      float xh[3], xl[3];
       fetch_atom(x, xs, a, a0, xh, xl);
-      two_sum(xh[0], -o0, u[0], ue[0]);
-      two_sum(xh[1], -o1, u[1], ue[1]);
-      two_sum(xh[2], -o2, u[2], ue[2]);
-      ue[0] += xl[0]; ue[1] += xl[1]; ue[2] += xl[2];
-      const float u0 = u[0], u1 = u[1], u2 = u[2];
-      const float r0 = __ldg(s.swr + 3 * a), r1 = __ldg(s.swr + 3 * a + 1), r2 = __ldg(s.swr + 3 * a + 2);
+      float u0 = xh[0] - o0, u1 = xh[1] - o1, u2 = xh[2] - o2;
+      if constexpr (sizeof(T) == 8) {
+        u0 += xl[0]; u1 += xl[1]; u2 += xl[2];
+      }
       const float y0 = sw * u0, y1 = sw * u1, y2 = sw * u2;
       if (fit) {
-        v[0] += y0 * r0; v[1] += y0 * r1; v[2] += y0 * r2;
-        v[3] += y1 * r0; v[4] += y1 * r1; v[5] += y1 * r2;
-        v[6] += y2 * r0; v[7] += y2 * r1; v[8] += y2 * r2;
-        v[9] += y0 * y0 + y1 * y1 + y2 * y2;
+        v[0] = fmaf(y0, r0, v[0]); v[1] = fmaf(y0, r1, v[1]); v[2] = fmaf(y0, r2, v[2]);
+        v[3] = fmaf(y1, r0, v[3]); v[4] = fmaf(y1, r1, v[4]); v[5] = fmaf(y1, r2, v[5]);
+        v[6] = fmaf(y2, r0, v[6]); v[7] = fmaf(y2, r1, v[7]); v[8] = fmaf(y2, r2, v[8]);
+        v[9] = fmaf(y0, y0, fmaf(y1, y1, fmaf(y2, y2, v[9])));
       } else {
         const float d0 = y0 - r0, d1 = y1 - r1, d2 = y2 - r2;
-        v[9] += d0 * d0 + d1 * d1 + d2 * d2;
+        v[9] = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, v[9])));
       }
       if (FIRST) {
         if (fit) {
-          const float c = cm ? __ldg(cm + a) : 1.0f;
-          const float cl = cm ? __ldg(cml + a) : 0.0f;
-#pragma unroll
-          for (int p = 0; p < 3; ++p) {
-            float pt, pe, q;
-            two_prod(c, u[p], pt, pe);
-            two_sum(v[10 + p], pt, v[10 + p], q);
-            ce[p] += q + fmaf(c, ue[p], fmaf(cl, u[p], pe));
-          }
+          const float wa = sw * sw;
+          const float c = same_w ? wa : __ldg(s.cm_ref + a);
+          v[10] = fmaf(c, u0, v[10]); v[11] = fmaf(c, u1, v[11]); v[12] = fmaf(c, u2, v[12]);
           if (!same_w) {
-            const float wa = s.wf ? __ldg(s.wf + a) : 1.0f;
-            v[13] += wa * u0; v[14] += wa * u1; v[15] += wa * u2;
+            v[13] = fmaf(wa, u0, v[13]); v[14] = fmaf(wa, u1, v[14]); v[15] = fmaf(wa, u2, v[15]);
           }
         }
-        umax = fmaxf(umax, u0 * u0 + u1 * u1 + u2 * u2);
+        umax = fmaxf(umax, fmaf(u0, u0, fmaf(u1, u1, u2 * u2)));
       }
     });
-    if (FIRST && fit) {
-      // compensated cross-lane sum of the centre terms
-#pragma unroll
-      for (int p = 0; p < 3; ++p)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const float so = __shfl_xor_sync(0xffffffffu, v[10 + p], o);
-          const float eo = __shfl_xor_sync(0xffffffffu, ce[p], o);
-          float q;
-          two_sum(v[10 + p], so, v[10 + p], q);
-          ce[p] += eo + q;
-        }
-#pragma unroll
-      for (int q = 0; q < 9; ++q)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
-#pragma unroll
-      for (int q = 9; q < 10; ++q)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
-#pragma unroll
-      for (int q = 13; q < 16; ++q)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
-    } else {
-      warp_sum_f32<16>(v);
-    }
+    warp_sum_f32<16>(v);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) umax = fmaxf(umax, __shfl_xor_sync(0xffffffffu, umax, o));
-    // The frame's other parts hand their sums to part 0 (the centre terms
-    // stay compensated: TwoSum, parts in order).
+    // The frame's other parts hand their sums to part 0 (parts in order).
     if (part != 0 && lane == 0) {
       float* o = xpart[it & 1][grp][part - 1];
 #pragma unroll
       for (int q = 0; q < 16; ++q) o[q] = v[q];
-      o[16] = ce[0]; o[17] = ce[1]; o[18] = ce[2]; o[19] = umax;
+      o[16] = umax;
     }
     group_sync(grp);
     if (part == 0 && lane == 0) {
@@ -723,16 +681,8 @@ __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64
       for (int pp = 0; pp < kWPF - 1; ++pp) {
         const float* o = xpart[it & 1][grp][pp];
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          if (q >= 10 && q < 13) {
-            float e;
-            two_sum(v[q], o[q], v[q], e);
-            ce[q - 10] += o[16 + q - 10] + e;
-          } else {
-            v[q] += o[q];
-          }
-        }
-        umax = fmaxf(umax, o[19]);
+        for (int q = 0; q < 16; ++q) v[q] += o[q];
+        umax = fmaxf(umax, o[16]);
       }
     }
     if (part == 0 && lane == 0) {
@@ -756,7 +706,7 @@ __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64
           const double iWc = (in_ref && !s.cm_ref_is_w) ? s.scal[5] : s.scal[4];
           for (int p = 0; p < 3; ++p) {
             const double xo = (p == 0) ? o0 : (p == 1) ? o1 : o2;
-            const double dd = (iWc != 0.0) ? ((double)v[10 + p] + (double)ce[p]) * iWc : -xo;  // zero mass: origin
+            const double dd = (iWc != 0.0) ? (double)v[10 + p] * iWc : -xo;  // zero mass: origin
             s.cen[3 * f + p] = xo + dd;
             del[p] = (float)dd;
           }
@@ -764,7 +714,7 @@ __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64
         }
         float su[3], sr[3];
         for (int p = 0; p < 3; ++p) {
-          su[p] = same_w ? v[10 + p] + ce[p] : v[13 + p];
+          su[p] = same_w ? v[10 + p] : v[13 + p];
           sr[p] = (float)s.sr[p];
         }
         float M[9];
@@ -801,7 +751,9 @@ __global__ void __launch_bounds__(256) k_spec_check(const float* dist, int64_t f
 }
 
 // Single-block argmax of dist[0..F): out_val, out_idx (lowest index on ties).
-__global__ void k_argmax(const float* dist, int64_t F, float* out_val, int64_t* out_idx) {
+// With multi: *multi = (max > tau), the reference-count decision on the device.
+__global__ void k_argmax(const float* dist, int64_t F, float* out_val, int64_t* out_idx, float tau = 0.0f,
+                         int* multi = nullptr) {
   __shared__ float sv[1024];
   __shared__ int64_t si[1024];
   float bv = -1.0f;
@@ -827,6 +779,7 @@ __global__ void k_argmax(const float* dist, int64_t F, float* out_val, int64_t* 
   if (threadIdx.x == 0) {
     *out_val = sv[0];
     *out_idx = si[0];
+    if (multi) *multi = (sv[0] > tau) ? 1 : 0;
   }
 }
 
@@ -872,39 +825,26 @@ __global__ void k_argmax_gate(const float* dist, int64_t F, float tau, int k, fl
 }
 
 // One thread per frame: the exact (FP64-orthogonal) rotation of the frame's
-// quaternion, t = R c, and both split into FP32 hi + lo.  No-fit: R = I, t = 0.
+// quaternion and the frame centre, both split into FP32 hi + lo.  No-fit:
+// R = I, c = 0.  R is kept to twice FP32 precision because its rounding would
+// distort every frame the same way (a shear of ~6e-8, about 1e-6 A over a
+// 20 A molecule); the rounding of the products R (x - c) is independent from
+// atom to atom and averages out of an RMSD.
 __global__ void k_rot(int64_t f_begin, int64_t F, const float4* quat, const double* cen, int nofit, float* ftab,
-                      double* rot) {
+                      double* rot, const int* skip = nullptr) {
+  if (skip && *skip != 0) return;
   for (int64_t f = f_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < F;
        f += (int64_t)gridDim.x * blockDim.x) {
-    double R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-    if (!nofit) {
-      const float4 q4 = quat[f];
-      const float q[4] = {q4.x, q4.y, q4.z, q4.w};
-      rotation_from_quat(q, R);
-    }
-    const double c0 = cen[3 * f], c1 = cen[3 * f + 1], c2 = cen[3 * f + 2];
-    double t[3];
-    for (int k = 0; k < 3; ++k) t[k] = R[3 * k] * c0 + R[3 * k + 1] * c1 + R[3 * k + 2] * c2;
-    float* o = ftab + (size_t)kFtab * f;
-    for (int k = 0; k < 9; ++k) {
-      const float h = (float)R[k];
-      o[k] = h;
-      o[9 + k] = (float)(R[k] - (double)h);
-    }
-    for (int k = 0; k < 3; ++k) {
-      const float h = (float)t[k];
-      o[18 + k] = h;
-      o[21 + k] = (float)(t[k] - (double)h);
-    }
-    if (rot)
-      for (int k = 0; k < 9; ++k) rot[9 * f + k] = R[k];
+    const float4 q4 = quat[f];
+    const float q[4] = {q4.x, q4.y, q4.z, q4.w};
+    const double c[3] = {cen[3 * f], cen[3 * f + 1], cen[3 * f + 2]};
+    write_frame_table(ftab, rot, f, q, c, nofit);
   }
 }
 
 // The frame's rotation table, loaded by lanes 0-23 and shared by shuffles.
 struct FrameTable {
-  float Rh[9], Rl[9], th[3], tl[3];
+  float Rh[9], Rl[9], ch[3], cl[3];  // rotation and centre, hi + lo
 };
 __device__ __forceinline__ void load_table(const float* ftab, int64_t f, int lane, FrameTable& T) {
   const float v = (lane < kFtab) ? ftab[(size_t)kFtab * f + lane] : 0.0f;
@@ -915,8 +855,8 @@ __device__ __forceinline__ void load_table(const float* ftab, int64_t f, int lan
   }
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    T.th[k] = __shfl_sync(0xffffffffu, v, 18 + k);
-    T.tl[k] = __shfl_sync(0xffffffffu, v, 21 + k);
+    T.ch[k] = __shfl_sync(0xffffffffu, v, 18 + k);
+    T.cl[k] = __shfl_sync(0xffffffffu, v, 21 + k);
   }
 }
 
@@ -927,7 +867,8 @@ __device__ __forceinline__ void load_table(const float* ftab, int64_t f, int lan
 template <typename T>
 __global__ void __launch_bounds__(128) k_sample_sum(FrameSrc<T> src, int64_t F, int Np, const float* ftab,
                                                     const int* order, const int* offsets, const float2* refhl,
-                                                    float* partial) {
+                                                    float* partial, const int* skip = nullptr) {
+  if (skip && *skip != 0) return;
   const int k = blockIdx.z, ch = blockIdx.y, N = src.N;
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= Np) return;
@@ -935,7 +876,7 @@ __global__ void __launch_bounds__(128) k_sample_sum(FrameSrc<T> src, int64_t F, 
   const int64_t cnt = std::min<int64_t>((offsets ? (int64_t)offsets[k + 1] : F) - lo, (int64_t)kSample);
   const int64_t per = (cnt + kMeanChunks - 1) / kMeanChunks;
   const int64_t b0 = ch * per, b1 = std::min<int64_t>(cnt, b0 + per);
-  // Plain FP32 (the hi parts of R, t and r): the mean only has to put the
+  // Plain FP32 (the hi parts of R, c and r): the mean only has to put the
   // reference near its frames, and every later pass takes the reference as
   // stored, whatever its last bits.
   float s[3] = {0.0f, 0.0f, 0.0f};
@@ -947,31 +888,50 @@ __global__ void __launch_bounds__(128) k_sample_sum(FrameSrc<T> src, int64_t F, 
       const float* tb = ftab + (size_t)kFtab * f;
       float xh[3], xl[3];
       load_atom(src.frame(f), a, xh, xl);
+      const float u0 = xh[0] - tb[18], u1 = xh[1] - tb[19], u2 = xh[2] - tb[20];
 #pragma unroll
       for (int p = 0; p < 3; ++p)
-        s[p] += fmaf(tb[3 * p], xh[0], fmaf(tb[3 * p + 1], xh[1], fmaf(tb[3 * p + 2], xh[2], -tb[18 + p]))) - rh[p];
+        s[p] += fmaf(tb[3 * p], u0, fmaf(tb[3 * p + 1], u1, tb[3 * p + 2] * u2)) - rh[p];
     }
   }
   for (int p = 0; p < 3; ++p) partial[(((size_t)k * kMeanChunks + ch) * 3 + p) * Np + a] = s[p];
 }
 
 // r_k += mean d over its sample (FP64 over the chunk sums, fixed order), and
-// the derived sqrt(w) r_k and hi/lo r_k; grid (atoms / 128, reference).
-// rmax[k] only grows (atomicMax on the non-negative float bits), so it stays
-// an upper bound of |r_k|.  Eref and sr describe the unrefined references
-// and are not read after this point.
-__global__ void __launch_bounds__(32) k_ref_update(double* refs, float* swr, float2* refhl, float* rmax,
-                                                   const float* partial, const int* offsets, int64_t F,
-                                                   const double* sqw, int N, int Np) {
+// the derived sqrt(w) r_k, hi/lo r_k and packed build table; grid (atoms /
+// 32, reference).  rmax[k] only grows (atomicMax on the non-negative float
+// bits), so it stays an upper bound of |r_k|.  Eref and sr describe the
+// unrefined references and are not read after this point.
+// With RP (one reference): also the reference's terms with itself, in place
+// of the reference-pair pass.  Each block writes its FP64 share of
+// S = sum w r r^T to `su` and counts itself done; the last block adds the
+// shares in block order (so the bits do not depend on which block was last)
+// and writes RP[0]: U = I, S, its antisymmetric combos, SS = 0.
+struct RefUpdateArgs {
+  double* refs;
+  float* swr;
+  float2* refhl;
+  float* rmax;
+  float4* qbuild;
+  const double* sqw;  // sqrt(w) or nullptr
+  const double* w;    // weights or nullptr (self terms)
+  unsigned* count;    // [1], zero at launch (self terms)
+  double* su;         // [blocks][9] (self terms)
+  float* RP;          // non-null (K = 1): write the self terms
+};
+__global__ void __launch_bounds__(32) k_ref_update(RefUpdateArgs u, const float* partial, const int* offsets,
+                                                   int64_t F, int N, int Np, const int* skip = nullptr) {
+  if (skip && *skip != 0) return;
   // one warp per block: the FP64 sums of the kMeanChunks partial means are
   // spread over as many SMs as there are 32-atom groups
   const int k = blockIdx.y;
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t cnt = std::min<int64_t>((offsets ? (int64_t)(offsets[k + 1] - offsets[k]) : F), (int64_t)kSample);
   float mx = 0.0f;
+  double sv[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   if (a < N) {
-    double* r = refs + (size_t)k * 3 * N;
-    const double sw = sqw ? sqw[a] : 1.0;
+    double* r = u.refs + (size_t)k * 3 * N;
+    const double sw = u.sqw ? u.sqw[a] : 1.0;
     double rr[3], sum[3] = {0.0, 0.0, 0.0};
     // the chunk sums in chunk order, several chunks' loads in flight at once
     const float* src = partial + (size_t)k * kMeanChunks * 3 * Np + a;
@@ -979,29 +939,72 @@ __global__ void __launch_bounds__(32) k_ref_update(double* refs, float* swr, flo
     for (int ch = 0; ch < kMeanChunks; ++ch)
 #pragma unroll
       for (int p = 0; p < 3; ++p) sum[p] += (double)src[((size_t)ch * 3 + p) * Np];
+    float q[3];
     for (int p = 0; p < 3; ++p) {
       rr[p] = r[3 * a + p] + ((cnt > 0) ? sum[p] / (double)cnt : 0.0);
       r[3 * a + p] = rr[p];
-      swr[((size_t)k * N + a) * 3 + p] = (float)(sw * rr[p]);
+      q[p] = (float)(sw * rr[p]);
+      u.swr[((size_t)k * N + a) * 3 + p] = q[p];
       const float h = (float)rr[p];
-      refhl[((size_t)k * N + a) * 3 + p] = make_float2(h, (float)(rr[p] - (double)h));
+      u.refhl[((size_t)k * N + a) * 3 + p] = make_float2(h, (float)(rr[p] - (double)h));
     }
+    u.qbuild[(size_t)k * N + a] = make_float4(q[0], q[1], q[2], (float)sw);
     mx = (float)sqrt(rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2]) * (1.0f + 1e-6f);
+    if (u.RP) {
+      const double wa = u.w ? u.w[a] : 1.0;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) sv[3 * i + j] = wa * rr[i] * rr[j];
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if (threadIdx.x == 0) atomicMax(reinterpret_cast<int*>(rmax + k), __float_as_int(mx));
+  if (threadIdx.x == 0) atomicMax(reinterpret_cast<int*>(u.rmax + k), __float_as_int(mx));
+  if (!u.RP) return;
+#pragma unroll
+  for (int q = 0; q < 9; ++q)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sv[q] += __shfl_xor_sync(0xffffffffu, sv[q], o);
+  __shared__ unsigned s_last;
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < 9; ++q) u.su[(size_t)blockIdx.x * 9 + q] = sv[q];
+    __threadfence();
+    s_last = (atomicAdd(u.count, 1u) == gridDim.x - 1);
+  }
+  __syncwarp();
+  if (!s_last) return;
+  __threadfence();  // the last block: every share is written
+  // lane l adds the shares of blocks l, l + 32, ... (loads independent), then
+  // the lanes combine in a fixed tree: the same bits whichever block is last
+  double S[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (unsigned g = threadIdx.x; g < gridDim.x; g += 32)
+#pragma unroll
+    for (int q = 0; q < 9; ++q) S[q] += __ldcg(u.su + (size_t)g * 9 + q);
+#pragma unroll
+  for (int q = 0; q < 9; ++q)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) S[q] += __shfl_xor_sync(0xffffffffu, S[q], o);
+  if (threadIdx.x != 0) return;
+  float* o = u.RP;  // K = 1: the pair (0, 0)
+  for (int q = 0; q < 9; ++q) o[q] = (q % 4 == 0) ? 1.0f : 0.0f;
+  for (int q = 0; q < 9; ++q) o[9 + q] = (float)S[q];
+  o[18] = (float)(S[5] - S[7]);
+  o[19] = (float)(S[6] - S[2]);
+  o[20] = (float)(S[1] - S[3]);
+  o[21] = 0.0f;
+  o[22] = 0.0f;
+  o[23] = 0.0f;
 }
 
 struct BuildArgs {
   const float* ftab;
   const int* assign;
-  const float2* refhl;
-  const float* sqwf;    // sqrt(w) or nullptr
   const float* ymax;    // [F] bound of max |y|
   const float* rmax;    // [K] bound of max |r_k|
   const double* scal;   // [0] max sqrt(w)
   const float* swr;     // [K][N][3] sqrt(w) r_c
+  const float4* q;      // [K][N] {sqrt(w) r_c, sqrt(w)} of the refined references
   int K, Np;
   int K_build;          // references k_build forms P against (the rest: k_pref)
   int tc;
@@ -1015,17 +1018,26 @@ struct BuildArgs {
   float* trP;
   const int* pos;       // frame -> position of its operands and terms (nullptr = same)
   int* assign_pos;      // reference of the frame at each position (with pos)
+  const int* skip;      // device int or nullptr: the pass does nothing when it reads non-zero
 };
 
-// Final operands, one warp per frame.  p = sqrt(w)(R y - r_a) by Dot2.  The
+// Final operands, two warps per frame.  p = sqrt(w) (R_h + R_l)(x - c) - s_a
+// in FP32, s_a = sqrt(w) r_a as stored (the same values P is formed with):
+// u = x - c rounds relative to the centred extent, the products R u relative
+// to |y|, both independently per atom.  Per atom the pass reads one 16-byte
+// table entry {s_a, sqrt(w)} (the per-atom table loads, not the arithmetic,
+// bounded this pass when they were four to seven separate loads).  The
 // tensor path stores p*s as FP16 hi + lo, s = 2^(14 - e) with 2^e above the
 // bound sqrt(w)max (max|y| + max|r_a|) >= max|p| (so |hi| < 2^15; a loose
 // bound only lowers the floor of the smallest representable residual, far
 // below FP32 rounding), and continues with the value hi + lo represents.
 // n_f = sum |p|^2 and P_fc = sum p (sqrt(w) r_c)^T use those exact operands.
-template <typename T>
+// MODE: 1 = FP16 hi/lo operands (tensor path), 2 = the FP32 plane, 3 = both.
+template <typename T, int MODE>
 __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int64_t f_begin, int64_t F,
                                                              BuildArgs b) {
+  if (b.skip && *b.skip != 0) return;  // uniform over the grid: before any barrier
+  constexpr bool TC = (MODE & 1) != 0, PLANE = (MODE & 2) != 0;
   __shared__ __align__(16) float sbuf[kWarps][kPipe * kStage];
   __shared__ float xpart[2][kFPB][kWPF - 1][10];  // the other parts' sums, by round parity
   const int N = src.N, Np = b.Np, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1050,9 +1062,7 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
         for (int q = 0; q < nv; ++q) acc[q] += xpart[rnd & 1][grp][pp][q];
     ++rnd;
   };
-  prefetch_l1(b.sqwf, (size_t)N * 4);
-  prefetch_l1(b.refhl, (size_t)N * 24);  // reference 0 (the only one when K = 1)
-  prefetch_l1(b.swr, (size_t)N * 12);
+  prefetch_l1(b.q, (size_t)N * 16);  // reference 0 (the only one when K = 1)
   for (int64_t f = f_first; f < F; f += f_stride) {
     const T* x = src.frame(f);
     const int ra = b.assign[f];
@@ -1061,7 +1071,7 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
     FrameTable Tb;
     load_table(b.ftab, f, lane, Tb);
     float scale = 1.0f, inv = 1.0f;
-    if (b.tc) {
+    if (TC) {
       const float B = sqwmax * (b.ymax[f] + b.rmax[ra]) * (1.0f + 1e-6f);
       int e = 0;
       if (B > 0.0f && isfinite(B)) frexpf(B, &e);
@@ -1070,24 +1080,33 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
       inv = ldexpf(1.0f, e - 14);
       if (part == 0 && lane == 0) b.inv_scale[pf] = inv;
     }
-    const float2* rr = b.refhl + (size_t)ra * 3 * N;
-    const float* r0 = b.swr;  // reference 0 for the fused P term
+    const float4* qa = b.q + (size_t)ra * N;  // the frame's reference; P is formed against reference 0
     const size_t base = (size_t)pf * 3 * Np;
     float acc[10];
 #pragma unroll
     for (int q = 0; q < 10; ++q) acc[q] = 0.0f;
     pipe.for_each_atom(f, lane, [&](int a, int a0, const float* xs) {
-        float xh[3], xl[3], v[3];
+        float xh[3], xl[3], u[3], v[3];
         fetch_atom(x, xs, a, a0, xh, xl);
-        const float sw = b.sqwf ? __ldg(b.sqwf + a) : 1.0f;
+        const float4 t = __ldg(qa + a);
+        const float sw = t.w, sr[3] = {t.x, t.y, t.z};
 #pragma unroll
         for (int p = 0; p < 3; ++p) {
-          const float2 r = __ldg(rr + 3 * a + p);
-          v[p] = sw * dot2_row(Tb.Rh + 3 * p, Tb.Rl + 3 * p, Tb.th[p], Tb.tl[p], xh, xl, r.x, r.y);
+          u[p] = xh[p] - Tb.ch[p];
+          if constexpr (sizeof(T) == 8) u[p] += xl[p];
+          u[p] -= Tb.cl[p];
         }
 #pragma unroll
         for (int p = 0; p < 3; ++p) {
-          if (b.tc) {
+          float y = fmaf(Tb.Rl[3 * p], u[0], fmaf(Tb.Rl[3 * p + 1], u[1], Tb.Rl[3 * p + 2] * u[2]));
+          y = fmaf(Tb.Rh[3 * p + 2], u[2], y);
+          y = fmaf(Tb.Rh[3 * p + 1], u[1], y);
+          y = fmaf(Tb.Rh[3 * p], u[0], y);
+          v[p] = fmaf(sw, y, -sr[p]);
+        }
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+          if (TC) {
             const float t = v[p] * scale;
             const __half h = __float2half_rn(t);
             const __half l = __float2half_rn(t - __half2float(h));
@@ -1095,23 +1114,24 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
             b.lo[base + (size_t)p * Np + a] = l;
             v[p] = (__half2float(h) + __half2float(l)) * inv;
           }
-          if (b.write_plane) b.plane[base + (size_t)p * Np + a] = v[p];
-          acc[9] += v[p] * v[p];
+          if (PLANE) b.plane[base + (size_t)p * Np + a] = v[p];
+          acc[9] = fmaf(v[p], v[p], acc[9]);
         }
-        const float c0 = __ldg(r0 + 3 * a), c1 = __ldg(r0 + 3 * a + 1), c2 = __ldg(r0 + 3 * a + 2);
-        acc[0] += v[0] * c0; acc[1] += v[0] * c1; acc[2] += v[0] * c2;
-        acc[3] += v[1] * c0; acc[4] += v[1] * c1; acc[5] += v[1] * c2;
-        acc[6] += v[2] * c0; acc[7] += v[2] * c1; acc[8] += v[2] * c2;
+        const float4 t0 = (ra != 0) ? __ldg(b.q + a) : t;
+        const float c0 = t0.x, c1 = t0.y, c2 = t0.z;
+        acc[0] = fmaf(v[0], c0, acc[0]); acc[1] = fmaf(v[0], c1, acc[1]); acc[2] = fmaf(v[0], c2, acc[2]);
+        acc[3] = fmaf(v[1], c0, acc[3]); acc[4] = fmaf(v[1], c1, acc[4]); acc[5] = fmaf(v[1], c2, acc[5]);
+        acc[6] = fmaf(v[2], c0, acc[6]); acc[7] = fmaf(v[2], c1, acc[7]); acc[8] = fmaf(v[2], c2, acc[8]);
     });
     // zero padding [N, Np), by the last part
     for (int a = N + lane; a < Np && part == kWPF - 1; a += 32) {
 #pragma unroll
       for (int p = 0; p < 3; ++p) {
-        if (b.tc) {
+        if (TC) {
           b.hi[base + (size_t)p * Np + a] = __float2half_rn(0.0f);
           b.lo[base + (size_t)p * Np + a] = __float2half_rn(0.0f);
         }
-        if (b.write_plane) b.plane[base + (size_t)p * Np + a] = 0.0f;
+        if (PLANE) b.plane[base + (size_t)p * Np + a] = 0.0f;
       }
     }
     warp_sum_f32<10>(acc);
@@ -1136,7 +1156,7 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
 #pragma unroll
         for (int p = 0; p < 3; ++p) {
           const size_t i = base + (size_t)p * Np + a;
-          v[p] = b.tc ? (__half2float(b.hi[i]) + __half2float(b.lo[i])) * inv : b.plane[i];
+          v[p] = TC ? (__half2float(b.hi[i]) + __half2float(b.lo[i])) * inv : b.plane[i];
         }
         const float c0 = rc[3 * a], c1 = rc[3 * a + 1], c2 = rc[3 * a + 2];
         h9[0] += v[0] * c0; h9[1] += v[0] * c1; h9[2] += v[0] * c2;
@@ -1267,7 +1287,8 @@ __global__ void __launch_bounds__(256) k_pref(BuildArgs b, int64_t F, int N) {
 // rotation U_ab taking r_b onto r_a, SU_ab = U_ab S_ba, its antisymmetric
 // combos and sum w |r_a - U_ab r_b|^2.  No-fit mode keeps U = I.
 __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockThreads)
-    k_ref_terms(const double* refs, int N, int K, const double* w, int nofit, float* RP) {
+    k_ref_terms(const double* refs, int N, int K, const double* w, int nofit, float* RP, const int* skip) {
+  if (skip && *skip != 0) return;  // uniform over the grid: before any cluster barrier
   __shared__ double red[32 * 10], slots[kRefCluster * 10], bc[10];
   __shared__ double Us[9];
   const int pair = blockIdx.x / kRefCluster;  // one cluster per reference pair
@@ -1337,6 +1358,18 @@ static int prep_grid(int64_t F, int per_sm = 16, int fpb = kWarps) {
 }
 constexpr int kScanBlocksPerSM = 4;   // k_scan: __launch_bounds__(kPrepThreads, 4)
 constexpr int kBuildBlocksPerSM = 3;  // k_build: __launch_bounds__(kPrepThreads, 3)
+template <typename T>
+static void launch_build(int64_t f0, int64_t f1, const FrameSrc<T>& src, const BuildArgs& b, cudaStream_t st) {
+  const dim3 grid(prep_grid(f1 - f0, kBuildBlocksPerSM, kFPB));
+  const int mode = (b.tc ? 1 : 0) | (b.write_plane ? 2 : 0);
+  if (mode == 1)
+    k_build<T, 1><<<grid, kPrepThreads, 0, st>>>(src, f0, f1, b);
+  else if (mode == 2)
+    k_build<T, 2><<<grid, kPrepThreads, 0, st>>>(src, f0, f1, b);
+  else
+    k_build<T, 3><<<grid, kPrepThreads, 0, st>>>(src, f0, f1, b);
+}
+
 // k_rot: one thread per frame, FP64 throughout; small blocks spread the
 // frames' FP64 work over more SMs.
 constexpr int kRotThreads = 64;
@@ -1362,18 +1395,21 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
   }
   const PrepScratch S = prep_carve(A.scratch, F, N, A.max_refs);
   const bool ref_distinct = A.cmass_ref != nullptr && A.cmass_ref != A.w;
-  k_weights<<<kRefCluster, kOneBlockThreads, 0, st>>>(A.w, ref_distinct ? A.cmass_ref : nullptr, N, A.sqw, A.sqwf,
-                                                      S.wf, S.wfl, S.cmf_ref, S.cmfl_ref, S.scal);
-  ++launches;
+  // The reference refinement of K references (k_sample_sum, k_ref_update);
+  // returns its launches.  RP (K = 1): also the reference's terms with itself.
+  auto refine = [&](int K, const int* order, const int* offsets, float* RP, const int* skip) -> int {
+    dim3 gs((unsigned)((A.Np + 127) / 128), (unsigned)kMeanChunks, (unsigned)K);
+    k_sample_sum<T><<<gs, 128, 0, st>>>(src, F, A.Np, S.ftab, order, offsets, S.refhl, A.partial, skip);
+    if (RP) cudaMemsetAsync(S.rcount, 0, sizeof(unsigned), st);
+    RefUpdateArgs u{A.refs, A.swr, S.refhl, S.rmax, S.qbuild, A.w ? A.sqw : nullptr, A.w, S.rcount, S.rsu, RP};
+    k_ref_update<<<dim3((unsigned)((N + 31) / 32), (unsigned)K), 32, 0, st>>>(u, A.partial, offsets, F, N, A.Np,
+                                                                            skip);
+    return 2;
+  };
   ScanArgs sa{};
-  sa.cm_tgt = A.w ? S.wf : nullptr;
-  sa.cml_tgt = A.w ? S.wfl : nullptr;
-  sa.cm_ref = ref_distinct ? S.cmf_ref : sa.cm_tgt;
-  sa.cml_ref = ref_distinct ? S.cmfl_ref : sa.cml_tgt;
-  sa.wf = A.w ? S.wf : nullptr;
+  sa.cm_ref = ref_distinct ? S.cmf_ref : nullptr;
   sa.cm_ref_is_w = !ref_distinct;
   sa.scal = S.scal;
-  sa.sqwf = A.w ? A.sqwf : nullptr;
   sa.Wsum = A.Wsum;
   sa.nofit = A.nofit;
   sa.cen = A.cen;
@@ -1381,18 +1417,23 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
   sa.assign = A.assign;
   sa.quat = S.quat;
   sa.ymax = S.ymax;
-  // Reference 0 from frame 0, then centres + fit to it in one pass (chunk by
-  // chunk when the frames are still arriving).
-  cudaMemsetAsync(A.fsel, 0, sizeof(int64_t), st);
-  if (A.n_chunks > 0) cudaStreamWaitEvent(st, A.chunk_ev[0], 0);
-  k_make_ref<T><<<kRefCluster, kOneBlockThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w, A.sqw,
-                                                          A.assign, 0, 0, A.nofit, A.refs, A.swr, S.refhl, A.Eref,
-                                                          S.sr, S.rmax);
+  // The weights and reference 0 from frame 0 (one launch), then centres + fit
+  // to it in one pass (chunk by chunk when the frames are still arriving).
+  // (resume_scan: weights, reference 0 and the first scan are in the
+  // workspace from the deferred run of this call.)
+  if (!A.resume_scan) {
+    cudaMemsetAsync(A.fsel, 0, sizeof(int64_t), st);
+    if (A.n_chunks > 0) cudaStreamWaitEvent(st, A.chunk_ev[0], 0);
+    const WeightsPass wp{A.w, ref_distinct ? A.cmass_ref : nullptr, A.sqw, A.sqwf, S.cmf_ref, S.scal};
+    k_make_ref<T><<<kRefCluster, kOneBlockThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w,
+                                                            A.sqw, A.assign, 0, 0, A.nofit, A.refs, A.swr, S.refhl,
+                                                            A.Eref, S.sr, S.rmax, S.qscan, nullptr, wp);
+    ++launches;
+  }
   sa.k = 0;
-  sa.swr = A.swr;
+  sa.q = S.qscan;  // the refinement writes qbuild: the scans always see the references as chosen
   sa.sr = S.sr;
   sa.Eref = A.Eref;
-  ++launches;
   if (A.n_chunks > 0) {
     // Frames arriving in chunks.  With spec_build, the passes after the scan
     // run speculatively for one reference as the chunks land: once the first
@@ -1402,13 +1443,7 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
     // unrefined reference 0 is restored and the general path below runs.
     const int64_t nsample = std::min<int64_t>(F, (int64_t)kSample);
     BuildArgs bspec{};
-    if (A.spec_build) {
-      bspec = build_args(*A.spec_build, A, S);
-      // every frame is scanned against the unrefined reference 0, as in the
-      // general path: the refinement rewrites swr in place
-      cudaMemcpyAsync(S.swr0, A.swr, sizeof(float) * 3 * N, cudaMemcpyDeviceToDevice, st);
-      sa.swr = S.swr0;
-    }
+    if (A.spec_build) bspec = build_args(*A.spec_build, A, S);
     bool refined = false;
     int64_t f0 = 0;
     for (int c = 0; c < A.n_chunks; ++c) {
@@ -1428,15 +1463,11 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
             ++launches;
           }
           if (!refined && f1 >= nsample) {
-            dim3 gs((unsigned)((A.Np + 127) / 128), (unsigned)kMeanChunks, 1u);
-            k_sample_sum<T><<<gs, 128, 0, st>>>(src, F, A.Np, S.ftab, nullptr, nullptr, S.refhl, A.partial);
-            k_ref_update<<<dim3((unsigned)((N + 31) / 32), 1u), 32, 0, st>>>(
-                A.refs, A.swr, S.refhl, S.rmax, A.partial, nullptr, F, A.w ? A.sqw : nullptr, N, A.Np);
-            launches += 2;
+            launches += refine(1, nullptr, nullptr, nullptr, nullptr);
             refined = true;
           }
           if (refined) {
-            k_build<T><<<prep_grid(f1 - b0, kBuildBlocksPerSM, kFPB), kPrepThreads, 0, st>>>(src, b0, f1, bspec);
+            launch_build<T>(b0, f1, src, bspec, st);
             ++launches;
             if (A.on_built) {
               const cudaError_t e = (*A.on_built)(f1);
@@ -1447,7 +1478,6 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
       }
       f0 = f1;
     }
-    sa.swr = A.swr;
     if (A.spec_build && refined) {
       k_argmax<<<1, 1024, 0, st>>>(A.dist, F, A.dmax, A.fsel);
       ++launches;
@@ -1466,10 +1496,10 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
       cudaMemsetAsync(A.fsel, 0, sizeof(int64_t), st);
       k_make_ref<T><<<kRefCluster, kOneBlockThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w,
                                                               A.sqw, A.assign, 0, 0, A.nofit, A.refs, A.swr,
-                                                              S.refhl, A.Eref, S.sr, S.rmax);
+                                                              S.refhl, A.Eref, S.sr, S.rmax, S.qscan);
       ++launches;
     }
-  } else {
+  } else if (!A.resume_scan) {
     k_scan<T, true><<<prep_grid(F, kScanBlocksPerSM, kFPB), kPrepThreads, 0, st>>>(src, 0, F, sa);
     ++launches;
   }
@@ -1480,7 +1510,15 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
   // queued at once, each gated on the device by the round before
   // (k_argmax_gate), so adding references costs no host round trip each.
   int K = 1;
-  if (K < A.max_refs && F > 1) {
+  const int* skip = nullptr;
+  if (K < A.max_refs && F > 1 && A.defer_multi && A.n_chunks == 0) {
+    // The decision stays on the device: the passes below assume one
+    // reference and return at once if the flag says otherwise.
+    k_argmax<<<1, 1024, 0, st>>>(A.dist, F, A.dmax, A.fsel, (float)A.tau, A.defer_multi);
+    ++launches;
+    skip = A.defer_multi;
+    o.deferred = 1;
+  } else if (K < A.max_refs && F > 1) {
     k_argmax<<<1, 1024, 0, st>>>(A.dist, F, A.dmax, A.fsel);
     ++launches;
     float dmax = 0.0f;
@@ -1496,10 +1534,10 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
         ++launches;
         k_make_ref<T><<<kRefCluster, kOneBlockThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w,
                                                                 A.sqw, A.assign, k, 1, A.nofit, A.refs, A.swr,
-                                                                S.refhl, A.Eref, S.sr, S.rmax, S.kstate);
+                                                                S.refhl, A.Eref, S.sr, S.rmax, S.qscan, S.kstate);
         ScanArgs sk = sa;
         sk.k = k;
-        sk.swr = A.swr + (size_t)k * 3 * N;
+        sk.q = S.qscan + (size_t)k * N;
         sk.sr = S.sr + 3 * k;
         sk.Eref = A.Eref + k;
         sk.gate = S.kstate;
@@ -1513,7 +1551,7 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
     }
   }
   o.K = K;
-  k_rot<<<rot_grid(F), kRotThreads, 0, st>>>(0, F, S.quat, A.cen, A.nofit, S.ftab, A.rot);
+  k_rot<<<rot_grid(F), kRotThreads, 0, st>>>(0, F, S.quat, A.cen, A.nofit, S.ftab, A.rot, skip);
   ++launches;
   // Frames grouped by reference (host counting sort) when there are several.
   const int* order = nullptr;
@@ -1542,11 +1580,10 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
     order = A.order;
     offsets = A.offsets;
   }
-  dim3 gs((unsigned)((A.Np + 127) / 128), (unsigned)kMeanChunks, (unsigned)K);
-  k_sample_sum<T><<<gs, 128, 0, st>>>(src, F, A.Np, S.ftab, order, offsets, S.refhl, A.partial);
-  k_ref_update<<<dim3((unsigned)((N + 31) / 32), (unsigned)K), 32, 0, st>>>(
-      A.refs, A.swr, S.refhl, S.rmax, A.partial, offsets, F, A.w ? A.sqw : nullptr, N, A.Np);
-  launches += 2;
+  // One reference: the refinement also writes its terms with itself.
+  float* RP = (K == 1) ? A.RP : nullptr;
+  launches += refine(K, order, offsets, RP, skip);
+  o.self_terms = (RP != nullptr);
   o.launches = launches;
   return cudaGetLastError();
 }
@@ -1559,12 +1596,11 @@ static BuildArgs build_args(const FinishArgs& fa, const PrepArgs& A, const PrepS
   BuildArgs b{};
   b.ftab = S.ftab;
   b.assign = A.assign;
-  b.refhl = S.refhl;
-  b.sqwf = A.w ? A.sqwf : nullptr;
   b.ymax = S.ymax;
   b.rmax = S.rmax;
   b.scal = S.scal;
   b.swr = A.swr;
+  b.q = S.qbuild;
   b.K = fa.K;
   b.K_build = (fa.K > 1) ? 1 : fa.K;  // P against references 1..K-1 in k_pref
   b.Np = A.Np;
@@ -1579,6 +1615,7 @@ static BuildArgs build_args(const FinishArgs& fa, const PrepArgs& A, const PrepS
   b.trP = fa.trP;
   b.pos = fa.sorted ? S.pos : nullptr;
   b.assign_pos = S.assign_pos;
+  b.skip = fa.skip;
   return b;
 }
 
@@ -1589,7 +1626,7 @@ static cudaError_t finish_impl(const FinishArgs& fa, cudaStream_t st) {
   const PrepScratch S = prep_carve(A.scratch, A.F, A.N, A.max_refs);
   if (!fa.built) {
     const BuildArgs b = build_args(fa, A, S);
-    k_build<T><<<prep_grid(A.F, kBuildBlocksPerSM, kFPB), kPrepThreads, 0, st>>>(src, 0, A.F, b);
+    launch_build<T>(0, A.F, src, b, st);
     if (fa.K > 1) {
       if (3 * (fa.K - 1) > 32 * kPrefComb) return cudaErrorInvalidValue;
       const size_t sm = pref_smem_bytes(fa.K);
@@ -1611,7 +1648,9 @@ static cudaError_t finish_impl(const FinishArgs& fa, cudaStream_t st) {
       if (e != cudaSuccess) return e;
     }
   }
-  k_ref_terms<<<fa.K * fa.K * kRefCluster, kOneBlockThreads, 0, st>>>(A.refs, A.N, fa.K, A.w, A.nofit, fa.RP);
+  if (!(fa.self_terms && fa.K == 1))
+    k_ref_terms<<<fa.K * fa.K * kRefCluster, kOneBlockThreads, 0, st>>>(A.refs, A.N, fa.K, A.w, A.nofit, fa.RP,
+                                                                       fa.skip);
   return cudaGetLastError();
 }
 

@@ -210,6 +210,30 @@ def test_device_pointers_match_host(h):
     np.testing.assert_array_equal(dev.cpu().numpy(), host)
 
 
+@pytest.mark.parametrize("precision", ["fp32", "tc"])
+def test_device_deferred_reference_count(h, precision):
+    # Device input and output: the one-reference assumption is checked on the
+    # device; frames around 6 centroids need more references, so the call runs
+    # again from its first scan.  A second call of the same shape decides on
+    # the host at once (the handle remembers the last shape's count).  Both
+    # must equal the host-input path bit for bit, and the oracle within the
+    # tolerance.
+    import torch
+    X, _ = synth.clustered(11, 400, 320, 6, 0.8)
+    ref = oracle.allpairs_f64(X)
+    h.allpairs(synth.trajectory(3, 20, 20, 0.1, 1.0, np.float32, False)[0], precision=precision)  # other shape
+    dX = torch.from_numpy(X).cuda()
+    dev1 = run(h, dX, precision=precision).cpu().numpy()
+    refs1 = h.stats()["n_refs"]
+    dev2 = run(h, dX, precision=precision).cpu().numpy()
+    refs2 = h.stats()["n_refs"]
+    host = run(h, X, precision=precision)
+    assert refs1 >= 2 and refs2 == refs1 and h.stats()["n_refs"] == refs1
+    np.testing.assert_array_equal(dev1, host)
+    np.testing.assert_array_equal(dev2, host)
+    assert np.abs(host - ref).max() <= TOL
+
+
 def test_tc_matches_fp32_closely(h):
     X, m = synth.trajectory(12, 256, 700, 0.1, 3.0, np.float32, True)
     a = run(h, X, tgt_mass=m, precision="fp32")

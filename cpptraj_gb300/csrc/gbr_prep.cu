@@ -342,6 +342,36 @@ struct WarpPipe {
       for (int a = c_lo * kChunkAtoms + lane; a < a_hi; a += 32) body(a, 0, ring);
     }
   }
+  // body(a, a0, xs, two) for the atom pairs (a, a + 1) of frame f, a even
+  // (lane l takes atoms 2l and 2l + 1 of each 64); two = (a + 1 < N).  A
+  // chunk holds whole pairs (kChunkAtoms is even).
+  template <class Body>
+  __device__ __forceinline__ void for_each_pair(int64_t f, int lane, Body&& body) {
+    static_assert(kChunkAtoms % 64 == 0, "a chunk holds whole pairs of every lane");
+    const int N = src.N;
+    if constexpr (sizeof(T) == 4) {
+      const float* x = (const float*)src.frame(f);
+      for (int c = c_lo; c < c_hi; ++c) {
+        const int a0 = c * kChunkAtoms;
+        const int consumed = issued - (kPipe - 1);
+        cp_async_wait<kPipe - 2>();
+        __syncwarp();
+        const float* cx = x + 3 * (size_t)a0;
+        const int n = 3 * (min(a0 + kChunkAtoms, N) - a0);
+        const float* xs = ring + (consumed % kPipe) * kStage + ((4 - chunk_head(cx, n)) & 3);
+        issue(lane);  // refills the stage consumed one chunk ago
+#pragma unroll
+        for (int kk = 0; kk < kChunkAtoms / 64; ++kk) {
+          const int a = a0 + 2 * lane + 64 * kk;
+          if (a < N) body(a, a0, xs, a + 1 < N);
+        }
+        __syncwarp();
+      }
+    } else {
+      const int a_hi = min(c_hi * kChunkAtoms, N);
+      for (int a = c_lo * kChunkAtoms + 2 * lane; a < a_hi; a += 64) body(a, 0, ring, a + 1 < N);
+    }
+  }
   __device__ __forceinline__ void drain() {
     if constexpr (sizeof(T) == 4) cp_async_wait<0>();
   }
@@ -1085,46 +1115,72 @@ __global__ void __launch_bounds__(kPrepThreads, 3) k_build(FrameSrc<T> src, int6
     float acc[10];
 #pragma unroll
     for (int q = 0; q < 10; ++q) acc[q] = 0.0f;
-    pipe.for_each_atom(f, lane, [&](int a, int a0, const float* xs) {
-        float xh[3], xl[3], u[3], v[3];
-        fetch_atom(x, xs, a, a0, xh, xl);
-        const float4 t = __ldg(qa + a);
-        const float sw = t.w, sr[3] = {t.x, t.y, t.z};
+    // One atom's operand row p = sqrt(w) R (x - c) - s_a (s_a = sqrt(w) r_a).
+    auto residual = [&](int a, int a0, const float* xs, const float4& t, float (&v)[3]) {
+      float xh[3], xl[3], u[3];
+      fetch_atom(x, xs, a, a0, xh, xl);
+#pragma unroll
+      for (int p = 0; p < 3; ++p) {
+        u[p] = xh[p] - Tb.ch[p];
+        if constexpr (sizeof(T) == 8) u[p] += xl[p];
+        u[p] -= Tb.cl[p];
+      }
+      const float sr[3] = {t.x, t.y, t.z};
+#pragma unroll
+      for (int p = 0; p < 3; ++p) {
+        float y = fmaf(Tb.Rl[3 * p], u[0], fmaf(Tb.Rl[3 * p + 1], u[1], Tb.Rl[3 * p + 2] * u[2]));
+        y = fmaf(Tb.Rh[3 * p + 2], u[2], y);
+        y = fmaf(Tb.Rh[3 * p + 1], u[1], y);
+        y = fmaf(Tb.Rh[3 * p], u[0], y);
+        v[p] = fmaf(t.w, y, -sr[p]);
+      }
+    };
+    // Two consecutive atoms per lane: their operands leave as one 4-byte
+    // (hi, lo) or 8-byte (plane) store per component, and the FP16 splits
+    // convert two values per instruction.  A lone last atom pairs with the
+    // first padding position, which holds zero.
+    pipe.for_each_pair(f, lane, [&](int a, int a0, const float* xs, bool two) {
+        const float4 t0 = __ldg(qa + a);
+        const float4 t1 = two ? __ldg(qa + a + 1) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float v0[3], v1[3] = {0.0f, 0.0f, 0.0f};
+        residual(a, a0, xs, t0, v0);
+        if (two) residual(a + 1, a0, xs, t1, v1);  // (past the frame's last atom nothing is read)
 #pragma unroll
         for (int p = 0; p < 3; ++p) {
-          u[p] = xh[p] - Tb.ch[p];
-          if constexpr (sizeof(T) == 8) u[p] += xl[p];
-          u[p] -= Tb.cl[p];
-        }
-#pragma unroll
-        for (int p = 0; p < 3; ++p) {
-          float y = fmaf(Tb.Rl[3 * p], u[0], fmaf(Tb.Rl[3 * p + 1], u[1], Tb.Rl[3 * p + 2] * u[2]));
-          y = fmaf(Tb.Rh[3 * p + 2], u[2], y);
-          y = fmaf(Tb.Rh[3 * p + 1], u[1], y);
-          y = fmaf(Tb.Rh[3 * p], u[0], y);
-          v[p] = fmaf(sw, y, -sr[p]);
-        }
-#pragma unroll
-        for (int p = 0; p < 3; ++p) {
+          const size_t i = base + (size_t)p * Np + a;
           if (TC) {
-            const float t = v[p] * scale;
-            const __half h = __float2half_rn(t);
-            const __half l = __float2half_rn(t - __half2float(h));
-            b.hi[base + (size_t)p * Np + a] = h;
-            b.lo[base + (size_t)p * Np + a] = l;
-            v[p] = (__half2float(h) + __half2float(l)) * inv;
+            const float s0 = v0[p] * scale, s1 = v1[p] * scale;
+            const __half2 h = __floats2half2_rn(s0, s1);
+            const float2 hf = __half22float2(h);
+            const __half2 l = __floats2half2_rn(s0 - hf.x, s1 - hf.y);
+            const float2 lf = __half22float2(l);
+            *reinterpret_cast<__half2*>(b.hi + i) = h;
+            *reinterpret_cast<__half2*>(b.lo + i) = l;
+            v0[p] = (hf.x + lf.x) * inv;
+            v1[p] = (hf.y + lf.y) * inv;
           }
-          if (PLANE) b.plane[base + (size_t)p * Np + a] = v[p];
-          acc[9] = fmaf(v[p], v[p], acc[9]);
+          if (PLANE) *reinterpret_cast<float2*>(b.plane + i) = make_float2(v0[p], v1[p]);
+          acc[9] = fmaf(v0[p], v0[p], fmaf(v1[p], v1[p], acc[9]));
         }
-        const float4 t0 = (ra != 0) ? __ldg(b.q + a) : t;
-        const float c0 = t0.x, c1 = t0.y, c2 = t0.z;
-        acc[0] = fmaf(v[0], c0, acc[0]); acc[1] = fmaf(v[0], c1, acc[1]); acc[2] = fmaf(v[0], c2, acc[2]);
-        acc[3] = fmaf(v[1], c0, acc[3]); acc[4] = fmaf(v[1], c1, acc[4]); acc[5] = fmaf(v[1], c2, acc[5]);
-        acc[6] = fmaf(v[2], c0, acc[6]); acc[7] = fmaf(v[2], c1, acc[7]); acc[8] = fmaf(v[2], c2, acc[8]);
+        // P against reference 0 (the frame's own unless frames have several references)
+        float4 c0 = t0, c1 = t1;
+        if (ra != 0) {
+          c0 = __ldg(b.q + a);
+          c1 = two ? __ldg(b.q + a + 1) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        acc[0] = fmaf(v0[0], c0.x, fmaf(v1[0], c1.x, acc[0]));
+        acc[1] = fmaf(v0[0], c0.y, fmaf(v1[0], c1.y, acc[1]));
+        acc[2] = fmaf(v0[0], c0.z, fmaf(v1[0], c1.z, acc[2]));
+        acc[3] = fmaf(v0[1], c0.x, fmaf(v1[1], c1.x, acc[3]));
+        acc[4] = fmaf(v0[1], c0.y, fmaf(v1[1], c1.y, acc[4]));
+        acc[5] = fmaf(v0[1], c0.z, fmaf(v1[1], c1.z, acc[5]));
+        acc[6] = fmaf(v0[2], c0.x, fmaf(v1[2], c1.x, acc[6]));
+        acc[7] = fmaf(v0[2], c0.y, fmaf(v1[2], c1.y, acc[7]));
+        acc[8] = fmaf(v0[2], c0.z, fmaf(v1[2], c1.z, acc[8]));
     });
-    // zero padding [N, Np), by the last part
-    for (int a = N + lane; a < Np && part == kWPF - 1; a += 32) {
+    // zero padding [N, Np), by the last part (an odd N's position N came with
+    // the last atom's pair)
+    for (int a = ((N + 1) & ~1) + lane; a < Np && part == kWPF - 1; a += 32) {
 #pragma unroll
       for (int p = 0; p < 3; ++p) {
         if (TC) {

@@ -310,7 +310,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
   int64_t sband = 0;
   if (rs) {
     const int var = (h->tc_variant >= 0) ? h->tc_variant : auto_tc_variant(N);
-    const int32_t align = tc ? (var >= 2 ? 84 : 42) : (need_planes ? 64 : 1);
+    const int32_t align = tc ? tc_launch_tile_rows(var) : (need_planes ? 64 : 1);
     scuts.resize((size_t)(n_ref + 2));
     const int64_t nb = gbr_row_bands(n_ref, rs->band, align, scuts.data(), (int64_t)scuts.size());
     if (nb < 1)
@@ -849,7 +849,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
       if (!out_dev) cudaMemcpyAsync(out, map.out, sizeof(float) * n_out, cudaMemcpyDefault, st);
     } else {
       // Band boundaries: equal pair counts, aligned to the kernel's tile rows.
-      const int64_t align = tc ? 84 : 64;
+      const int64_t align = tc ? tc_launch_tile_rows(tc_variant) : 64;
       const int nb = kMaxBands - 2;
       std::vector<int64_t> cut{row_begin};
       const int64_t total = n_out;

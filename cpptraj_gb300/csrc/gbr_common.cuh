@@ -309,6 +309,9 @@ __device__ inline void qcp_vec_f32(const float M[9], float E0, float q[4], float
 //   G00 = 1/2 sum w |x'_i - U_ab x'_j|^2
 //       = 1/2 (SS_ab + n_i + n_j) + trP_ia - <U,P_ib> - <U,P_ja^T> + trP_jb - tr(U D_ji)
 // (for a == b: U = I and G00 = 1/2 (n_i + n_j) - tr D_ji).
+// Everything but D_ji belongs to one frame of the pair and the pair's
+// references, so it is formed once per frame and reference pair (Side) and
+// the per-pair work is U D_ji, its trace and the eigen solve.
 // qout (optional) receives the unit quaternion (QCP convention) of the
 // optimal superposition of x'_j onto x'_i, i.e. x'_i ~ R(q)^T x'_j with R(q)
 // the rotation matrix QCP builds from q; only meaningful when t.K == 1.
@@ -316,63 +319,118 @@ struct F9 {
   float v[9];
 };
 
-// Solver part of the epilogue with every per-frame term given (by value):
-// P_ja, P_ib, trPia / trPjb (read only when a != b), rp the reference-pair
-// entry of (a, b) (global memory, or its copy in shared memory: plain loads).
-static __device__ __forceinline__ float pair_solve_inl(const F9 Dv, float ni, float nj, const F9 Pjav,
-                                                      const F9 Pibv, float trPia, float trPjb, const float* rp,
+// One frame's share of a pair with references (a, b), U = U_ab:
+//   reference frame i: Q = U P_ib^T, c = n_i/2 + trP_ia - <U, P_ib>
+//   target frame j:    Q = U P_ja,   c = n_j/2 + trP_jb - <U, P_ja^T>
+//   a == b:            U = I and the P terms of G00 cancel: c = n/2
+// m is the sum of the magnitudes in c (for the error bound), sn = sqrt(n).
+struct Side {
+  float Q[9];
+  float c, m, sn;
+};
+
+// Rounded operation by operation (no contraction left to the compiler), so
+// that the terms formed per tile in shared memory and those formed per pair
+// from global memory are the same numbers.
+static __device__ __forceinline__ void side_terms(const float P[9], float n, float trPown, const float U[9],
+                                                  bool same, bool ref_side, Side& s) {
+  const float h = __fmul_rn(0.5f, n);
+  s.sn = __fsqrt_rn(fmaxf(n, 0.0f));
+  if (same) {
+#pragma unroll
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) s.Q[p * 3 + q] = ref_side ? P[q * 3 + p] : P[p * 3 + q];
+    s.c = h;
+    s.m = h;
+    return;
+  }
+#pragma unroll
+  for (int p = 0; p < 3; ++p)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      // column q of P^T (reference side) or of P (target side)
+      const float b0 = ref_side ? P[q * 3 + 0] : P[0 * 3 + q];
+      const float b1 = ref_side ? P[q * 3 + 1] : P[1 * 3 + q];
+      const float b2 = ref_side ? P[q * 3 + 2] : P[2 * 3 + q];
+      s.Q[p * 3 + q] = __fmaf_rn(U[p * 3 + 2], b2, __fmaf_rn(U[p * 3 + 1], b1, __fmul_rn(U[p * 3], b0)));
+    }
+  float uP = __fmul_rn(U[0], P[0]);
+#pragma unroll
+  for (int k = 1; k < 9; ++k) uP = __fmaf_rn(U[k], ref_side ? P[k] : P[(k % 3) * 3 + k / 3], uP);
+  s.c = __fsub_rn(__fadd_rn(h, trPown), uP);
+  s.m = __fadd_rn(__fadd_rn(h, fabsf(trPown)), fabsf(uP));
+}
+
+// The reference-pair entry of (a, b) as the solver reads it (see
+// kRefPairStride): U_ab, SU_ab, the antisymmetric combos and SS_ab.
+struct RefPair {
+  float4 v[6];
+};
+// From global memory (16-byte aligned entries).
+static __device__ __forceinline__ void load_refpair(const float* rp, RefPair& r) {
+  const float4* p = reinterpret_cast<const float4*>(rp);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) r.v[k] = __ldg(p + k);
+}
+static __device__ __forceinline__ float rpv(const RefPair& r, int k) {
+  const float4& q = r.v[k >> 2];
+  return (k & 3) == 0 ? q.x : (k & 3) == 1 ? q.y : (k & 3) == 2 ? q.z : q.w;
+}
+
+// The solver, given D_ji (unscaled), both sides' terms and the pair's
+// reference-pair entry (in registers, from global or shared memory).
+//
+// The smallest eigenvalue of G = [[G00, g^T], [g, Gs]] is found around
+// q = (1, v): with A = Gs - G00 I and mu = G00 + delta,
+//   v = -(A - delta I)^-1 g,  delta = g.v.
+// When A is positive definite and |delta| is below its smallest eigenvalue
+// lambda, (A - delta I)^-1 = sum_k delta^k A^-(k+1).  With w0 = A^-1 g,
+// w1 = A^-1 w0 and s_k = g^T A^-(k+1) g <= s0 / lambda^k, the exact delta
+// solves delta = -sum_k delta^k s_k; its first-order solution
+// delta0 = -s0 / (1 + s1) (s0 = g.w0, s1 = w0.w0) gives v = -(w0 + delta0 w1).
+// With rho = |delta| / lambda (bounded through tr(adj A) / det A >= 1/lambda),
+// the dropped terms of v are at most |w0| rho^2 / (1 - rho) and the error of
+// delta0 adds |w0| rho^3 / (1 - rho); the Rayleigh quotient below turns an
+// error e of v into at most tr(G) |e|^2.  This path is taken when that bound
+// is negligible; otherwise the fixed-point iteration on the secular equation
+// and, failing that, QCP (Theobald 2005; Liu, Agrafiotis & Theobald 2010) on
+// K(M) give q.  The result is the Rayleigh quotient of G at q in either case,
+// written as G00 + (2 q0 g.qv + qv^T A qv) / |q|^2 (qv = (q1, q2, q3)), whose
+// terms are all small next to E0.
+static __device__ __forceinline__ float pair_solve_inl(const F9 Dv, const Side& si, const Side& sj, const RefPair& rp,
                                                       bool same, const FrameTerms& t, bool* flag,
                                                       float* qout = nullptr) {
   const float* D = Dv.v;
-  const float* Pja = Pjav.v;
-  const float* Pib = Pibv.v;
   const float W = t.W;
-  // X = P_ja + P_ib^T + D_ji
-  float X[9];
-  X[0] = Pja[0] + Pib[0] + D[0];
-  X[1] = Pja[1] + Pib[3] + D[1];
-  X[2] = Pja[2] + Pib[6] + D[2];
-  X[3] = Pja[3] + Pib[1] + D[3];
-  X[4] = Pja[4] + Pib[4] + D[4];
-  X[5] = Pja[5] + Pib[7] + D[5];
-  X[6] = Pja[6] + Pib[2] + D[6];
-  X[7] = Pja[7] + Pib[5] + D[7];
-  X[8] = Pja[8] + Pib[8] + D[8];
-  float G00, g00mag;
-  float Y[9];
+  const float trD = D[0] + D[4] + D[8];
+  float Y[9], G00, g00mag;
   if (same) {
-    const float trD = D[0] + D[4] + D[8];
-    const float h = 0.5f * (ni + nj);
-    G00 = h - trD;
-    g00mag = h + fabsf(trD);
 #pragma unroll
-    for (int k = 0; k < 9; ++k) Y[k] = X[k];
+    for (int k = 0; k < 9; ++k) Y[k] = (si.Q[k] + sj.Q[k]) + D[k];
+    G00 = (si.c + sj.c) - trD;
+    g00mag = (si.m + sj.m) + fabsf(trD);
   } else {
     float U[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) U[k] = rp[k];
-    float uPib = 0.f, uPjaT = 0.f, trUD = 0.f;
+    for (int k = 0; k < 9; ++k) U[k] = rpv(rp, k);
+    float trUD = 0.f;
 #pragma unroll
     for (int p = 0; p < 3; ++p)
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
-        uPib += U[p * 3 + q] * Pib[p * 3 + q];
-        uPjaT += U[p * 3 + q] * Pja[q * 3 + p];
         trUD += U[p * 3 + q] * D[q * 3 + p];
+        Y[p * 3 + q] = (si.Q[p * 3 + q] + sj.Q[p * 3 + q]) + (U[p * 3] * D[q] + U[p * 3 + 1] * D[3 + q] +
+                                                              U[p * 3 + 2] * D[6 + q]);
       }
-    const float h = 0.5f * (rp[21] + ni + nj);
-    G00 = h + trPia - uPib - uPjaT + trPjb - trUD;
-    g00mag = h + fabsf(trPia) + fabsf(uPib) + fabsf(uPjaT) + fabsf(trPjb) + fabsf(trUD);
-#pragma unroll
-    for (int p = 0; p < 3; ++p)
-#pragma unroll
-      for (int q = 0; q < 3; ++q)
-        Y[p * 3 + q] = U[p * 3] * X[q] + U[p * 3 + 1] * X[3 + q] + U[p * 3 + 2] * X[6 + q];
+    const float hs = 0.5f * rpv(rp, 21);
+    G00 = hs + (si.c + sj.c) - trUD;
+    g00mag = hs + (si.m + sj.m) + fabsf(trUD);
   }
   // Contraction error: products of uncorrelated residuals sum with random
   // signs (error ~ eps*sqrt(n_i n_j), independent of N), correlated ones with
   // one sign (rounding errors random-walk: ~ eps*sqrt(N)*|tr D|).
-  const float gem = t.gem_s * sqrtf(fmaxf(ni, 0.0f) * fmaxf(nj, 0.0f)) + t.gem_c * fabsf(D[0] + D[4] + D[8]);
+  const float gem = t.gem_s * (si.sn * sj.sn) + t.gem_c * fabsf(trD);
   if (t.nofit) {
     // RMSD_NoFit: sum w |x_i - x_j|^2 / W = 2*G00/W (references are not rotated).
     const float r = sqrtf(fmaxf(G00 * t.two_over_w, 0.0f));
@@ -382,49 +440,73 @@ static __device__ __forceinline__ float pair_solve_inl(const F9 Dv, float ni, fl
   }
   float M[9];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) M[k] = rp[9 + k] + Y[k];
+  for (int k = 0; k < 9; ++k) M[k] = rpv(rp, 9 + k) + Y[k];
   // g = G[0][1..3] = -(antisymmetric combos of M''), from the small parts.
-  const float g1 = -(Y[5] - Y[7] + rp[18]);
-  const float g2 = -(Y[6] - Y[2] + rp[19]);
-  const float g3 = -(Y[1] - Y[3] + rp[20]);
-  const float G11 = G00 + 2.0f * (M[4] + M[8]);
-  const float G22 = G00 + 2.0f * (M[0] + M[8]);
-  const float G33 = G00 + 2.0f * (M[0] + M[4]);
-  const float G12 = -(M[1] + M[3]);
-  const float G13 = -(M[6] + M[2]);
-  const float G23 = -(M[5] + M[7]);
-  // Fast path: secular iteration mu = G00 + g.v, v = -(Gs - mu I)^-1 g.
-  float mu = G00, v1 = 0.f, v2 = 0.f, v3 = 0.f, det = 0.f, m2 = 0.f;
-  bool conv = false;
+  const float g1 = -(Y[5] - Y[7] + rpv(rp, 18));
+  const float g2 = -(Y[6] - Y[2] + rpv(rp, 19));
+  const float g3 = -(Y[1] - Y[3] + rpv(rp, 20));
+  // A = Gs - G00 I
+  const float a00 = 2.0f * (M[4] + M[8]), a11 = 2.0f * (M[0] + M[8]), a22 = 2.0f * (M[0] + M[4]);
+  const float a01 = -(M[1] + M[3]), a02 = -(M[6] + M[2]), a12 = -(M[5] + M[7]);
+  // Power-series solve.
+  const float c00 = a11 * a22 - a12 * a12, c01 = a02 * a12 - a01 * a22, c02 = a01 * a12 - a02 * a11;
+  const float c11 = a00 * a22 - a02 * a02, c12 = a01 * a02 - a00 * a12, c22 = a00 * a11 - a01 * a01;
+  const float det = a00 * c00 + a01 * c01 + a02 * c02;
+  const float id = __fdividef(1.0f, det);
+  const float w0x = (c00 * g1 + c01 * g2 + c02 * g3) * id;
+  const float w0y = (c01 * g1 + c11 * g2 + c12 * g3) * id;
+  const float w0z = (c02 * g1 + c12 * g2 + c22 * g3) * id;
+  const float w1x = (c00 * w0x + c01 * w0y + c02 * w0z) * id;
+  const float w1y = (c01 * w0x + c11 * w0y + c12 * w0z) * id;
+  const float w1z = (c02 * w0x + c12 * w0y + c22 * w0z) * id;
+  const float s0 = g1 * w0x + g2 * w0y + g3 * w0z;
+  const float s1 = w0x * w0x + w0y * w0y + w0z * w0z;
+  const float dl = -__fdividef(s0, 1.0f + s1);
+  // |delta| <= |delta0| (1 + rho^2 / (1 - rho)) <= 1.09 |delta0| while rho < 1/4.
+  const float rho = 1.125f * fabsf(dl) * ((c00 + c11 + c22) * id);
+  float q0 = 1.0f;
+  float q1 = -(w0x + dl * w1x), q2 = -(w0y + dl * w1y), q3 = -(w0z + dl * w1z);
+  // |e|^2 <= s1 rho^4 ((1 + rho) / (1 - rho))^2 <= 2.78 s1 rho^4 for rho < 1/4
+  const float rho2 = rho * rho;
+  const float trG = 4.0f * G00 + (a00 + a11 + a22);
+  float trunc = trG * (2.78f * s1 * rho2 * rho2);
+  const bool fast = (a00 > 0.0f) && (c22 > 0.0f) && (det > 0.0f) && (rho < 0.25f) && (s1 < 0.25f) &&
+                    (q1 * q1 + q2 * q2 + q3 * q3 < 0.25f) && (trunc <= 0.125f * t.epi_coef * g00mag);
+  if (!fast) {
+    trunc = 0.0f;
+    // Fixed-point iteration on the secular equation: delta = g.v(delta).
+    float d = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f, det2 = 0.f, m2 = 0.f;
+    bool conv = false;
 #pragma unroll 1
-  for (int it = 0; it < 5; ++it) {
-    det = solve_sym3(G11 - mu, G12, G13, G22 - mu, G23, G33 - mu, -g1, -g2, -g3, v1, v2, v3, m2);
-    const float mn = G00 + g1 * v1 + g2 * v2 + g3 * v3;
-    conv = fabsf(mn - mu) <= 1e-5f * fabsf(mn) + 1e-30f;
-    mu = mn;
-    if (conv) break;
-  }
-  const float a00 = G11 - mu;
-  const bool pd = (a00 > 0.0f) && ((G11 - mu) * (G22 - mu) - G12 * G12 > 0.0f) && (det > 0.0f);
-  float q0, q1, q2, q3;
-  if (conv && pd && (v1 * v1 + v2 * v2 + v3 * v3) < 0.25f) {
-    q0 = 1.0f; q1 = v1; q2 = v2; q3 = v3;
-  } else {
-    float q[4];
-    qcp_vec_f32(M, G00 + M[0] + M[4] + M[8], q);
-    q0 = q[0]; q1 = q[1]; q2 = q[2]; q3 = q[3];
+    for (int it = 0; it < 5; ++it) {
+      det2 = solve_sym3(a00 - d, a01, a02, a11 - d, a12, a22 - d, -g1, -g2, -g3, v1, v2, v3, m2);
+      const float dn = g1 * v1 + g2 * v2 + g3 * v3;
+      conv = fabsf(dn - d) <= 1e-5f * fabsf(G00 + dn) + 1e-30f;
+      d = dn;
+      if (conv) break;
+    }
+    const float b00 = a00 - d;
+    const bool pd = (b00 > 0.0f) && (b00 * (a11 - d) - a01 * a01 > 0.0f) && (det2 > 0.0f);
+    if (conv && pd && (v1 * v1 + v2 * v2 + v3 * v3) < 0.25f) {
+      q1 = v1; q2 = v2; q3 = v3;
+    } else {
+      float q[4];
+      qcp_vec_f32(M, G00 + M[0] + M[4] + M[8], q);
+      q0 = q[0]; q1 = q[1]; q2 = q[2]; q3 = q[3];
+    }
   }
   const float qq = q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3;
-  const float t00 = q0 * q0 * G00, t01 = 2.f * q0 * (q1 * g1 + q2 * g2 + q3 * g3);
-  const float t11 = q1 * q1 * G11 + q2 * q2 * G22 + q3 * q3 * G33;
-  const float t12 = 2.f * (q1 * q2 * G12 + q1 * q3 * G13 + q2 * q3 * G23);
-  const float iqq = __fdividef(1.0f, qq);  // qq in [1, 2) on the fast path
-  const float rq = (t00 + t01 + t11 + t12) * iqq;
-  const float mag = (q0 * q0 * g00mag + 2.f * fabsf(q0) * (fabsf(q1 * g1) + fabsf(q2 * g2) + fabsf(q3 * g3)) +
-                     fabsf(t11) + 2.f * (fabsf(q1 * q2 * G12) + fabsf(q1 * q3 * G13) + fabsf(q2 * q3 * G23))) *
-                    iqq;
+  const float iqq = __fdividef(1.0f, qq);  // qq in [1, 1.25) on the iterative paths
+  const float tg = q1 * g1 + q2 * g2 + q3 * g3;
+  const float d11 = a00 * q1 * q1, d22 = a11 * q2 * q2, d33 = a22 * q3 * q3;
+  const float o12 = a01 * q1 * q2, o13 = a02 * q1 * q3, o23 = a12 * q2 * q3;
+  const float corr = 2.0f * q0 * tg + (d11 + d22 + d33) + 2.0f * (o12 + o13 + o23);
+  const float rq = G00 + corr * iqq;
+  const float mag = g00mag + (2.0f * fabsf(q0) * (fabsf(q1 * g1) + fabsf(q2 * g2) + fabsf(q3 * g3)) +
+                              (fabsf(d11) + fabsf(d22) + fabsf(d33)) + 2.0f * (fabsf(o12) + fabsf(o13) + fabsf(o23))) *
+                                 iqq;
   const float r = sqrtf(fmaxf(rq * t.two_over_w, 0.0f));
-  const float err = t.epi_coef * mag + 2.0f * gem;
+  const float err = t.epi_coef * mag + 2.0f * gem + trunc;
   *flag = !(err <= t.tol * W * fmaxf(r, 1e-3f));
   if (qout) {
     const float inv = rsqrtf(qq);
@@ -436,42 +518,39 @@ static __device__ __forceinline__ float pair_solve_inl(const F9 Dv, float ni, fl
 
 // The same as a call: the CUDA-core kernels, whose per-thread state already
 // fills the register file, keep the solver out of line.
-static __device__ __noinline__ float pair_solve(const F9 Dv, float ni, float nj, const F9 Pjav, const F9 Pibv,
-                                                float trPia, float trPjb, const float* rp, bool same,
-                                                const FrameTerms& t, bool* flag, float* qout = nullptr) {
-  return pair_solve_inl(Dv, ni, nj, Pjav, Pibv, trPia, trPjb, rp, same, t, flag, qout);
+static __device__ __noinline__ float pair_solve(const F9 Dv, const Side& si, const Side& sj, const RefPair& rp,
+                                                bool same, const FrameTerms& t, bool* flag, float* qout = nullptr) {
+  return pair_solve_inl(Dv, si, sj, rp, same, t, flag, qout);
 }
 
-// The pair epilogue with its per-frame terms read from global memory.
-// The solver's inputs for pair (i, j): every per-frame term read from
-// global memory.
+// The solver's inputs for pair (i, j), every per-frame term read from
+// global memory and combined with the pair's references.
 struct PairIn {
-  F9 pja, pib;
-  float ni, nj, trPia, trPjb;
-  const float* rp;
+  Side si, sj;
+  RefPair rp;
   bool same;
 };
 static __device__ __forceinline__ void pair_terms(int64_t i, int64_t j, const FrameTerms& t, PairIn& in) {
   const int K = t.K;
   const int a = (K > 1) ? __ldg(t.assign + i) : 0;
   const int b = (K > 1) ? __ldg(t.assign + j) : 0;
-  in.ni = __ldg(t.nrm + i);
-  in.nj = __ldg(t.nrm + j);
-  const float* Pja = t.P + ((size_t)j * K + a) * 9;
-  const float* Pib = t.P + ((size_t)i * K + b) * 9;
-  in.rp = t.RP + (size_t)(b * K + a) * kRefPairStride;
+  const bool same = (a == b);
+  const float* rp = t.RP + (size_t)(b * K + a) * kRefPairStride;
+  load_refpair(rp, in.rp);
+  float Pib[9], Pja[9], U[9];
+  const float* pib = t.P + ((size_t)i * K + b) * 9;
+  const float* pja = t.P + ((size_t)j * K + a) * 9;
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
-    in.pja.v[k] = __ldg(Pja + k);
-    in.pib.v[k] = __ldg(Pib + k);
+    Pib[k] = __ldg(pib + k);
+    Pja[k] = __ldg(pja + k);
+    U[k] = same ? 0.0f : rpv(in.rp, k);
   }
-  in.trPia = 0.0f;
-  in.trPjb = 0.0f;
-  if (a != b) {
-    in.trPia = __ldg(t.trP + i * K + a);
-    in.trPjb = __ldg(t.trP + j * K + b);
-  }
-  in.same = (a == b);
+  const float trPia = same ? 0.0f : __ldg(t.trP + i * K + a);
+  const float trPjb = same ? 0.0f : __ldg(t.trP + j * K + b);
+  side_terms(Pib, __ldg(t.nrm + i), trPia, U, same, true, in.si);
+  side_terms(Pja, __ldg(t.nrm + j), trPjb, U, same, false, in.sj);
+  in.same = same;
 }
 
 static __device__ __forceinline__ float pair_epilogue(const float D[9], int64_t i, int64_t j, const FrameTerms& t,
@@ -481,7 +560,7 @@ static __device__ __forceinline__ float pair_epilogue(const float D[9], int64_t 
   F9 dv;
 #pragma unroll
   for (int k = 0; k < 9; ++k) dv.v[k] = D[k];
-  return pair_solve(dv, in.ni, in.nj, in.pja, in.pib, in.trPia, in.trPjb, in.rp, in.same, t, flag, qout);
+  return pair_solve(dv, in.si, in.sj, in.rp, in.same, t, flag, qout);
 }
 
 __host__ __device__ inline int64_t tri_index(int64_t n, int64_t i, int64_t j) {

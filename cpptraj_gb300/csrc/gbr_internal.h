@@ -215,6 +215,8 @@ int64_t tc_build_tile_list(const OutMap& m, std::vector<int2>& tiles, TcTileInfo
 // Frame range [0, end) a tile of this list reads (reference and target rows),
 // for launching tiles as their frames become ready; unclamped.
 int64_t tc_tile_frame_end(const TcTileInfo& info, int2 tile, int variant);
+// Reference frames per launch tile of a tensor-core kernel shape.
+int tc_launch_tile_rows(int variant);
 cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st);
 int tc_supported(int device);
 int64_t tc_max_tiles(const OutMap& m);

@@ -42,7 +42,7 @@
 namespace gbr {
 
 namespace {
-constexpr int TI = 42;                 // reference frames per tile
+constexpr int TI = 42;                 // reference frames per tile (per CTA), the default shape
 constexpr int TJ = 64;                 // target frames per tile
 constexpr int UM = 128;                // MMA M
 constexpr int UN = 3 * TJ;             // MMA N = 192
@@ -69,8 +69,9 @@ constexpr int THREADS = 64 + 32 * EPI_WARPS;
 // group.  Wider chunks give each group more pairs per barrier (the epilogue-
 // bound small-N case); narrower ones leave shared memory for deeper operand
 // pipelines (large N).
-template <int CH>
+template <int CH, int TI_ = TI>
 struct Epi {
+  static constexpr int TIE = TI_;       // reference frames per CTA tile
   static constexpr int CH_TGT = CH;
   static constexpr int CH_COLS = 3 * CH;
   static constexpr int ST_STRIDE = CH_COLS + 1;
@@ -78,29 +79,34 @@ struct Epi {
   // Result rows of one tile (pair kernels, triangle output): TI rows of TJ
   // values, padded by one chunk so the chunk writes hit 32 distinct banks.
   static constexpr int RB_STRIDE = TJ + CH;
-  static constexpr int ROWBUF_BYTES = TI * RB_STRIDE * 4;
+  static constexpr int ROWBUF_BYTES = TI_ * RB_STRIDE * 4;
+  // Staged frame terms (below): slots, reference-pair entry, frame numbers,
+  // row bases.
+  static constexpr int TERM_RP = ((TI_ + TJ) * 16 + 3) & ~3;
+  static constexpr int TERM_PERM = TERM_RP + kRefPairStride;
+  static constexpr int TERM_ROWBASE = (TERM_PERM + TI_ + TJ + 1) & ~1;
+  static constexpr int TERM_FLOATS = (TERM_ROWBASE + 2 * TI_ + 3) & ~3;
 };
 using Epi1 = Epi<8>;  // the one-SM kernels: 24 accumulator columns per chunk
 constexpr int STAGING_BYTES = Epi1::STAGING_BYTES;
 // Per-tile frame terms staged in shared memory, two buffers.  With A the
 // reference (pre-alignment) of the tile's first reference frame and B that of
-// its first target frame, each frame slot holds n, 1/scale, its reference,
-// trP against its own reference, and P against B (reference frames) or A
-// (target frames): everything a pair with references (A, B) reads.  After the
+// its first target frame, each frame slot holds its Side terms for a pair
+// with references (A, B) (Q, c, m, sqrt n), 1/scale and its own reference, as
+// four float4s: 0 = Q0..Q3, 1 = Q4..Q7, 2 = (Q8, c, m, sn), 3 = (1/scale,
+// reference, -, -).  Float4 k of slot s sits at 4 s + (k ^ ((s >> 1) & 3)), so
+// the k-th float4s of 8 consecutive slots fall in distinct banks.  After the
 // frame slots: the reference-pair entry of (A, B) (kRefPairStride floats),
 // for a triangle over reference-sorted positions each slot's frame number
 // (TI + TJ ints; -1 outside the map), and the row bases below.
-constexpr int TERM_STRIDE = 13;
-constexpr int TERM_RP = ((TI + TJ) * TERM_STRIDE + 3) & ~3;
-constexpr int TERM_PERM = TERM_RP + kRefPairStride;
 // Then, for the row stores of a triangle in frame order, the output index of
-// (reference slot il, target slot 0) as an int64 per reference slot.
-constexpr int TERM_ROWBASE = (TERM_PERM + TI + TJ + 1) & ~1;
-constexpr int TERM_FLOATS = (TERM_ROWBASE + 2 * TI + 3) & ~3;
+// (reference slot il, target slot 0) as an int64 per reference slot (Epi's
+// TERM_* offsets).
+__device__ __forceinline__ int slot_f4(int s, int k) { return 4 * s + (k ^ ((s >> 1) & 3)); }
 static_assert(TJ == 64, "row stores split the slot index with shifts");
 template <class E>
 constexpr int epi_bytes() {
-  return EPI_GROUPS * E::STAGING_BYTES + 2 * TERM_FLOATS * 4;
+  return EPI_GROUPS * E::STAGING_BYTES + 2 * E::TERM_FLOATS * 4;
 }
 constexpr int EPI_BYTES = epi_bytes<Epi1>();
 constexpr int BAR_BYTES = 128;
@@ -207,6 +213,25 @@ __device__ __forceinline__ void mbar_arrive_remote(uint32_t caddr) {
   asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(caddr) : "memory");
 }
 
+// A staged slot's Side terms (float4s 0-2) and, optionally, its 1/scale.
+__device__ __forceinline__ void load_slot(const float* T, int s, Side& sd) {
+  const float4* T4 = reinterpret_cast<const float4*>(T);
+  const float4 v0 = T4[slot_f4(s, 0)], v1 = T4[slot_f4(s, 1)], v2 = T4[slot_f4(s, 2)];
+  sd.Q[0] = v0.x; sd.Q[1] = v0.y; sd.Q[2] = v0.z; sd.Q[3] = v0.w;
+  sd.Q[4] = v1.x; sd.Q[5] = v1.y; sd.Q[6] = v1.z; sd.Q[7] = v1.w;
+  sd.Q[8] = v2.x; sd.c = v2.y; sd.m = v2.z; sd.sn = v2.w;
+}
+// The tile's reference-pair entry, staged at Trp (16-byte aligned).
+__device__ __forceinline__ void load_refpair_smem(const float* Trp, RefPair& r) {
+  const float4* p = reinterpret_cast<const float4*>(Trp);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) r.v[k] = p[k];
+}
+__device__ __forceinline__ void load_slot(const float* T, int s, Side& sd, float& inv_scale) {
+  load_slot(T, s, sd);
+  inv_scale = reinterpret_cast<const float4*>(T)[slot_f4(s, 3)].x;
+}
+
 // Epilogue warps (2 .. 2 + EPI_WARPS): for tiles t0, t0 + tstep, ... wait for
 // the accumulator, stage the tile's frame terms (one reference), read the
 // 128 x 192 FP32 block from tensor memory in 24-column chunks (group g takes
@@ -224,6 +249,8 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
                                                float* rowbuf, volatile int* okf, uint32_t accf0, uint32_t acce_bar,
                                                bool remote, int64_t t0, int64_t tstep, int ti_frames, int i_off,
                                                int warp, int lane) {
+  constexpr int TI = E::TIE, TERM_RP = E::TERM_RP, TERM_PERM = E::TERM_PERM, TERM_ROWBASE = E::TERM_ROWBASE,
+                TERM_FLOATS = E::TERM_FLOATS;
   const int e = warp - 2;
   const int g = e >> 2;
   const int q = warp & 3;               // TMEM lane quadrant this warp may access
@@ -267,36 +294,48 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
     // ago, before every group passed the previous tile's barrier.
     const int A = (K > 1 && i0 < P.i_end) ? __ldg(P.terms.assign + i0) : 0;
     const int B = (K > 1 && jt0 < P.jt_end) ? __ldg(P.terms.assign + P.tgt0 + jt0) : 0;
-    for (int x = etid; x < (TI + TJ) * TERM_STRIDE; x += EPI_WARPS * 32) {
-      const int sl = x / TERM_STRIDE, k = x - sl * TERM_STRIDE;
-      int64_t f;
-      bool valid;
-      int other;
-      if (sl < TI) {
-        f = i0 + sl;
-        valid = f < P.i_end;
-        other = B;
-      } else {
-        const int64_t jt = jt0 + (sl - TI);
-        f = P.tgt0 + jt;
-        valid = jt < P.jt_end;
-        other = A;
-      }
-      float v = 0.0f;
-      if (valid) {
-        if (k == 0) {
-          v = __ldg(P.terms.nrm + f);
-        } else if (k == 1) {
-          v = __ldg(P.inv_scale + f);
-        } else if (k == 2) {
-          v = __int_as_float(K > 1 ? __ldg(P.terms.assign + f) : 0);
-        } else if (k == 3) {
-          v = (K > 1) ? __ldg(P.terms.trP + f * K + __ldg(P.terms.assign + f)) : 0.0f;
+    // Each slot's Side terms against the tile's references (A, B).
+    {
+      const bool same_t = (A == B);
+      const float* Ug = P.terms.RP + (size_t)(B * K + A) * kRefPairStride;
+      float4* T4 = reinterpret_cast<float4*>(T);
+      for (int sl = etid; sl < TI + TJ; sl += EPI_WARPS * 32) {
+        int64_t f;
+        bool valid;
+        int other;
+        const bool ref_side = sl < TI;
+        if (ref_side) {
+          f = i0 + sl;
+          valid = f < P.i_end;
+          other = B;
         } else {
-          v = __ldg(P.terms.P + (f * K + other) * 9 + (k - 4));
+          const int64_t jt = jt0 + (sl - TI);
+          f = P.tgt0 + jt;
+          valid = jt < P.jt_end;
+          other = A;
         }
+        float4 o0 = make_float4(0.f, 0.f, 0.f, 0.f), o1 = o0, o2 = o0, o3 = o0;
+        if (valid) {
+          const int own = (K > 1) ? __ldg(P.terms.assign + f) : 0;
+          const float trPown = (K > 1) ? __ldg(P.terms.trP + f * K + own) : 0.0f;
+          float Pv[9], U[9];
+#pragma unroll
+          for (int k = 0; k < 9; ++k) {
+            Pv[k] = __ldg(P.terms.P + (f * K + other) * 9 + k);
+            U[k] = same_t ? 0.0f : __ldg(Ug + k);
+          }
+          Side sd;
+          side_terms(Pv, __ldg(P.terms.nrm + f), trPown, U, same_t, ref_side, sd);
+          o0 = make_float4(sd.Q[0], sd.Q[1], sd.Q[2], sd.Q[3]);
+          o1 = make_float4(sd.Q[4], sd.Q[5], sd.Q[6], sd.Q[7]);
+          o2 = make_float4(sd.Q[8], sd.c, sd.m, sd.sn);
+          o3 = make_float4(__ldg(P.inv_scale + f), __int_as_float(own), 0.f, 0.f);
+        }
+        T4[slot_f4(sl, 0)] = o0;
+        T4[slot_f4(sl, 1)] = o1;
+        T4[slot_f4(sl, 2)] = o2;
+        T4[slot_f4(sl, 3)] = o3;
       }
-      T[x] = v;
     }
     // The tile's reference-pair entry and, with a sorted layout, its frames.
     if (etid < kRefPairStride) T[TERM_RP + etid] = __ldg(P.terms.RP + (size_t)(B * K + A) * kRefPairStride + etid);
@@ -358,30 +397,25 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
 #pragma unroll
             for (int k = 0; k < 10; ++k) er[k] = ec[k] = 0.0f;
             if (p < TI * CH_TGT && i < P.i_end && j < P.jt_end && j > i) {
-              const float* Ti = T + il * TERM_STRIDE;
-              const float* Tj = T + (TI + c * CH_TGT + jl) * TERM_STRIDE;
-              PairIn in;
-              F9 D;
-              const float sc = Ti[1] * Tj[1];
-              in.ni = Ti[0];
-              in.nj = Tj[0];
-#pragma unroll
-              for (int k = 0; k < 9; ++k) {
-                in.pja.v[k] = Tj[4 + k];
-                in.pib.v[k] = Ti[4 + k];
+              Side si, sj;
+              float sc;
+              load_slot(T, il, si, sc);
+              {
+                float scj;
+                load_slot(T, TI + c * CH_TGT + jl, sj, scj);
+                sc *= scj;
               }
-              in.trPia = Ti[3];
-              in.trPjb = Tj[3];
-              in.rp = T + TERM_RP;  // K = 1: the entry of (0, 0)
-              in.same = true;
+              F9 D;
 #pragma unroll
               for (int pj = 0; pj < 3; ++pj)
 #pragma unroll
                 for (int pi = 0; pi < 3; ++pi) D.v[pj * 3 + pi] = st[(3 * il + pi) * ST_STRIDE + 3 * jl + pj] * sc;
               bool flag = false;
               float qv[4];
-              const float rm = pair_solve_inl(D, in.ni, in.nj, in.pja, in.pib, in.trPia, in.trPjb, in.rp, in.same,
-                                              P.terms, &flag, qv);
+              // K = 1: the reference-pair entry of (0, 0)
+              RefPair rp;
+              load_refpair_smem(T + TERM_RP, rp);
+              const float rm = pair_solve_inl(D, si, sj, rp, true, P.terms, &flag, qv);
               const int64_t t = tri_index(P.map.n_ref, i, j);
               if (P.bwd.rmsd) P.bwd.rmsd[t] = rm;
               const float gij = P.bwd.g ? P.bwd.g[t] : 1.0f;
@@ -447,38 +481,39 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
               if (idx < 0) continue;
             }
             bool flag = false;
-            const float* Ti = T + il * TERM_STRIDE;
-            const float* Tj = T + (TI + c * CH_TGT + jl) * TERM_STRIDE;
             // The solver's inputs from the tile's staged terms when the pair's
             // references are the tile's, else from global memory; one inlined
-            // solve for both, so a pair's result never depends on its tile.
-            PairIn in;
-            F9 D;
+            // solve for both, and the same Side arithmetic, so a pair's result
+            // never depends on its tile.
+            const float4* T4 = reinterpret_cast<const float4*>(T);
+            const int sj_slot = TI + c * CH_TGT + jl;
+            const float4 i3 = T4[slot_f4(il, 3)], j3 = T4[slot_f4(sj_slot, 3)];
+            Side si, sj;
+            RefPair rp;
+            bool same;
             float sc;
-            if (__float_as_int(Ti[2]) == A && __float_as_int(Tj[2]) == B) {
-              sc = Ti[1] * Tj[1];
-              in.ni = Ti[0];
-              in.nj = Tj[0];
-#pragma unroll
-              for (int k = 0; k < 9; ++k) {
-                in.pja.v[k] = Tj[4 + k];
-                in.pib.v[k] = Ti[4 + k];
-              }
-              in.trPia = Ti[3];
-              in.trPjb = Tj[3];
-              in.rp = T + TERM_RP;
-              in.same = (A == B);
+            if (__float_as_int(i3.y) == A && __float_as_int(j3.y) == B) {
+              sc = i3.x * j3.x;
+              load_slot(T, il, si);
+              load_slot(T, sj_slot, sj);
+              load_refpair_smem(T + TERM_RP, rp);
+              same = (A == B);
             } else {
               sc = __ldg(P.inv_scale + i) * __ldg(P.inv_scale + P.tgt0 + jt);
+              PairIn in;
               pair_terms(i, P.tgt0 + jt, P.terms, in);
+              si = in.si;
+              sj = in.sj;
+              rp = in.rp;
+              same = in.same;
             }
+            F9 D;
 #pragma unroll
             for (int pj = 0; pj < 3; ++pj)
 #pragma unroll
               for (int pi = 0; pi < 3; ++pi) D.v[pj * 3 + pi] = st[(3 * il + pi) * ST_STRIDE + 3 * jl + pj] * sc;
-            // inline: the tensor-core kernels have registers to spare (96 of 113)
-            const float r = pair_solve_inl(D, in.ni, in.nj, in.pja, in.pib, in.trPia, in.trPjb, in.rp, in.same,
-                                           P.terms, &flag);
+            // inline: the tensor-core kernels have registers to spare
+            const float r = pair_solve_inl(D, si, sj, rp, same, P.terms, &flag);
             if (flag) flag_pair(P.flags, P.map, i, jt);
             if (rows)
               rowbuf[il * RB_STRIDE + c * CH_TGT + jl] = r;
@@ -698,7 +733,6 @@ __global__ void __launch_bounds__(THREADS, 1)
 //   accf[b]  in each CTA: CTA 0's commit arrives on both.
 //   acce[b]  in CTA 0: the epilogue warps of both CTAs arrive.
 // ---------------------------------------------------------------------------
-constexpr int TI2 = 2 * TI;            // reference frames per cluster tile (84)
 constexpr int TJH = TJ / 2;            // target frames per CTA half of B (32)
 constexpr int UM2 = 256;
 constexpr int UNH = 3 * TJH;           // 96 B rows per CTA
@@ -706,15 +740,16 @@ constexpr int BAR2_BYTES = 256;
 // Pipeline and epilogue shape of the pair kernel: KA atoms per stage (rows of
 // 2 KA bytes, 64- or 128-byte swizzle), STAGES stages, epilogue chunks of CH
 // target frames.
-template <int KA_, int STAGES_, int CH_>
+template <int KA_, int STAGES_, int CH_, int TI_ = TI>
 struct PairCfg {
+  static constexpr int TIP = TI_;       // reference frames per CTA (2 TI_ per cluster tile)
   static constexpr int KA2 = KA_;
   static constexpr int ROW2 = 2 * KA_;
   static constexpr int STAGES2 = STAGES_;
-  using E = Epi<CH_>;
+  using E = Epi<CH_, TI_>;
   static constexpr int A2_BYTES = UM * ROW2;  // per CTA: 128 rows, TMA writes 126
   static constexpr int BH_BYTES = UNH * ROW2;
-  static constexpr int A2_TX = 3 * TI * ROW2;
+  static constexpr int A2_TX = 3 * TI_ * ROW2;
   static constexpr int BH_TX = UNH * ROW2;
   static constexpr int STAGE2_BYTES = 2 * A2_BYTES + 2 * BH_BYTES;
   static constexpr int EPI2_BYTES = epi_bytes<E>() + E::ROWBUF_BYTES;
@@ -730,8 +765,12 @@ using PairShallow = PairCfg<32, 5, 8>;
 // Large N (operand-feed bound): 64-atom stages (128-byte rows) x 3, 4-frame chunks.
 using PairDeep = PairCfg<64, 3, 4>;
 // Small N, wider epilogue chunks: 32-atom stages x 3, 16-frame chunks (each
-// epilogue group takes one chunk per tile: half the named barriers per pair).
-using PairWide = PairCfg<32, 3, 16>;
+// epilogue group takes one chunk per tile: half the named barriers per pair),
+// 40 reference frames per CTA (rows 120-127 of A unused) so that a chunk's
+// 40 x 16 pairs and a tile's 40 x 64 row stores split evenly over 128 and 512
+// threads (5 each) instead of 5.25.
+constexpr int TI_WIDE = 40;
+using PairWide = PairCfg<32, 3, 16, TI_WIDE>;
 constexpr uint32_t IDESC2 = (1u << 4) | ((uint32_t)(UN >> 3) << 17) | ((uint32_t)(UM2 >> 4) << 24);
 
 __device__ __forceinline__ uint32_t cluster_rank() {
@@ -795,6 +834,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     k_pairs_tc2(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                 const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
                 const TcParams P) {
+  constexpr int TI = PC::TIP, TI2 = 2 * PC::TIP, TERM_FLOATS = PC::E::TERM_FLOATS;
   constexpr int KA2 = PC::KA2, STAGES2 = PC::STAGES2, A2_BYTES = PC::A2_BYTES, BH_BYTES = PC::BH_BYTES,
                 A2_TX = PC::A2_TX, BH_TX = PC::BH_TX, STAGE2_BYTES = PC::STAGE2_BYTES,
                 STAGING_BYTES = PC::E::STAGING_BYTES, EPI_BYTES = PC::EPI2_BYTES;
@@ -1008,12 +1048,17 @@ int64_t tc_build_tiles(const OutMap& m, std::vector<int2>& tiles, int64_t& i_bas
   return (int64_t)tiles.size();
 }
 
+// Reference frames per CTA tile and per launch tile of each kernel shape.
+static int cta_tile_rows(int variant) { return variant == 4 ? PairWide::TIP : TI; }
+static int launch_tile_rows(int variant) { return variant >= 2 ? 2 * cta_tile_rows(variant) : TI; }
+int tc_launch_tile_rows(int variant) { return launch_tile_rows(variant); }
+
 int64_t tc_build_tile_list(const OutMap& m, std::vector<int2>& tiles, TcTileInfo& info, int variant) {
-  return tc_build_tiles(m, tiles, info.i_base, info.jt_base, info.i_end, info.jt_end, variant >= 2 ? TI2 : TI);
+  return tc_build_tiles(m, tiles, info.i_base, info.jt_base, info.i_end, info.jt_end, launch_tile_rows(variant));
 }
 
 int64_t tc_tile_frame_end(const TcTileInfo& info, int2 tile, int variant) {
-  const int64_t i1 = info.i_base + (int64_t)(tile.x + 1) * (variant >= 2 ? TI2 : TI);
+  const int64_t i1 = info.i_base + (int64_t)(tile.x + 1) * launch_tile_rows(variant);
   const int64_t j1 = info.jt_base + (int64_t)(tile.y + 1) * TJ;
   return std::max(i1, j1);
 }
@@ -1069,7 +1114,7 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
   int64_t n;
   cudaError_t e = cudaSuccess;
   const bool pair = (L.variant >= 2);
-  const int ti_frames = pair ? TI2 : TI;
+  const int ti_frames = launch_tile_rows(L.variant);
   if (L.ready_tiles > 0) {
     // The caller uploaded the list already (batched / graph-captured path).
     TcTileInfo info;
@@ -1093,7 +1138,8 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
                                     : PairShallow::KA2;
   const int bj = pair ? TJH : TJ;
   CUtensorMap mAh, mAl, mBh, mBl;
-  if (!make_map(&mAh, L.hi, L.F, L.Np, TI, ka) || !make_map(&mAl, L.lo, L.F, L.Np, TI, ka) ||
+  const int bi = cta_tile_rows(L.variant);
+  if (!make_map(&mAh, L.hi, L.F, L.Np, bi, ka) || !make_map(&mAl, L.lo, L.F, L.Np, bi, ka) ||
       !make_map(&mBh, L.hi, L.F, L.Np, bj, ka) || !make_map(&mBl, L.lo, L.F, L.Np, bj, ka))
     return cudaErrorInvalidValue;
   TcParams P{};
@@ -1151,7 +1197,8 @@ int64_t tc_max_tiles(const OutMap& m) {
     ni = m.n_ref;
     nj = m.row_end - m.row_begin;
   }
-  return ((ni + TI - 1) / TI) * ((nj + TJ - 1) / TJ);
+  // the smallest tile of any shape (the wide one's TI_WIDE reference frames)
+  return ((ni + TI_WIDE - 1) / TI_WIDE) * ((nj + TJ - 1) / TJ);
 }
 
 }  // namespace gbr

@@ -378,8 +378,10 @@ static __device__ __forceinline__ float rpv(const RefPair& r, int k) {
   return (k & 3) == 0 ? q.x : (k & 3) == 1 ? q.y : (k & 3) == 2 ? q.z : q.w;
 }
 
-// The solver, given D_ji (unscaled), both sides' terms and the pair's
-// reference-pair entry (in registers, from global or shared memory).
+// The solver, given D_ji as sc * Dv (Dv the contraction of the scaled
+// operand planes, sc the product of the two frames' 1/scale), both sides'
+// terms and the pair's reference-pair entry (in registers, from global or
+// shared memory).
 //
 // The smallest eigenvalue of G = [[G00, g^T], [g, Gs]] is found around
 // q = (1, v): with A = Gs - G00 I and mu = G00 + delta,
@@ -398,30 +400,31 @@ static __device__ __forceinline__ float rpv(const RefPair& r, int k) {
 // K(M) give q.  The result is the Rayleigh quotient of G at q in either case,
 // written as G00 + (2 q0 g.qv + qv^T A qv) / |q|^2 (qv = (q1, q2, q3)), whose
 // terms are all small next to E0.
-static __device__ __forceinline__ float pair_solve_inl(const F9 Dv, const Side& si, const Side& sj, const RefPair& rp,
-                                                      bool same, const FrameTerms& t, bool* flag,
+static __device__ __forceinline__ float pair_solve_inl(const F9 Dv, float sc, const Side& si, const Side& sj,
+                                                      const RefPair& rp, bool same, const FrameTerms& t, bool* flag,
                                                       float* qout = nullptr) {
   const float* D = Dv.v;
   const float W = t.W;
-  const float trD = D[0] + D[4] + D[8];
+  const float trD = sc * (D[0] + D[4] + D[8]);
   float Y[9], G00, g00mag;
   if (same) {
 #pragma unroll
-    for (int k = 0; k < 9; ++k) Y[k] = (si.Q[k] + sj.Q[k]) + D[k];
+    for (int k = 0; k < 9; ++k) Y[k] = fmaf(sc, D[k], si.Q[k] + sj.Q[k]);
     G00 = (si.c + sj.c) - trD;
     g00mag = (si.m + sj.m) + fabsf(trD);
   } else {
+    // sc folded into U: Y = Q_i + Q_j + (sc U) Dv
     float U[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) U[k] = rpv(rp, k);
+    for (int k = 0; k < 9; ++k) U[k] = sc * rpv(rp, k);
     float trUD = 0.f;
 #pragma unroll
     for (int p = 0; p < 3; ++p)
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
-        trUD += U[p * 3 + q] * D[q * 3 + p];
-        Y[p * 3 + q] = (si.Q[p * 3 + q] + sj.Q[p * 3 + q]) + (U[p * 3] * D[q] + U[p * 3 + 1] * D[3 + q] +
-                                                              U[p * 3 + 2] * D[6 + q]);
+        trUD = fmaf(U[p * 3 + q], D[q * 3 + p], trUD);
+        Y[p * 3 + q] = fmaf(U[p * 3 + 2], D[6 + q],
+                            fmaf(U[p * 3 + 1], D[3 + q], fmaf(U[p * 3], D[q], si.Q[p * 3 + q] + sj.Q[p * 3 + q])));
       }
     const float hs = 0.5f * rpv(rp, 21);
     G00 = hs + (si.c + sj.c) - trUD;
@@ -520,7 +523,7 @@ static __device__ __forceinline__ float pair_solve_inl(const F9 Dv, const Side& 
 // fills the register file, keep the solver out of line.
 static __device__ __noinline__ float pair_solve(const F9 Dv, const Side& si, const Side& sj, const RefPair& rp,
                                                 bool same, const FrameTerms& t, bool* flag, float* qout = nullptr) {
-  return pair_solve_inl(Dv, si, sj, rp, same, t, flag, qout);
+  return pair_solve_inl(Dv, 1.0f, si, sj, rp, same, t, flag, qout);
 }
 
 // The solver's inputs for pair (i, j), every per-frame term read from

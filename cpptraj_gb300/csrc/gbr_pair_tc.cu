@@ -64,12 +64,15 @@ struct Pipe {
 constexpr int EPI_WARPS = 16;          // four groups of four warps (one per TMEM lane quadrant)
 constexpr int EPI_GROUPS = EPI_WARPS / 4;
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
+// The pair-of-SMs kernel adds one warp that stages each tile's frame terms a
+// tile ahead of the epilogue.
+constexpr int THREADS2 = THREADS + 32;
 // Epilogue shape: CH target frames (3 CH accumulator columns) per chunk read
 // from tensor memory and staged in shared memory, one staging buffer per
 // group.  Wider chunks give each group more pairs per barrier (the epilogue-
 // bound small-N case); narrower ones leave shared memory for deeper operand
 // pipelines (large N).
-template <int CH, int TI_ = TI>
+template <int CH, int TI_ = TI, bool ROWS_ = true>
 struct Epi {
   static constexpr int TIE = TI_;       // reference frames per CTA tile
   static constexpr int CH_TGT = CH;
@@ -80,14 +83,16 @@ struct Epi {
   // values, padded by one chunk so the chunk writes hit 32 distinct banks.
   static constexpr int RB_STRIDE = TJ + CH;
   static constexpr int ROWBUF_BYTES = TI_ * RB_STRIDE * 4;
-  // Staged frame terms (below): slots, reference-pair entry, frame numbers,
-  // row bases.
+  // Staged frame terms (below): slots, reference-pair entry, the tile
+  // (tile row, tile column, A, B), frame numbers, row bases (kernels with
+  // row stores only).
   static constexpr int TERM_RP = ((TI_ + TJ) * 16 + 3) & ~3;
-  static constexpr int TERM_PERM = TERM_RP + kRefPairStride;
+  static constexpr int TERM_META = TERM_RP + kRefPairStride;
+  static constexpr int TERM_PERM = TERM_META + 4;
   static constexpr int TERM_ROWBASE = (TERM_PERM + TI_ + TJ + 1) & ~1;
-  static constexpr int TERM_FLOATS = (TERM_ROWBASE + 2 * TI_ + 3) & ~3;
+  static constexpr int TERM_FLOATS = (TERM_ROWBASE + (ROWS_ ? 2 * (TI_ + TJ) : 0) + 3) & ~3;
 };
-using Epi1 = Epi<8>;  // the one-SM kernels: 24 accumulator columns per chunk
+using Epi1 = Epi<8, TI, false>;  // the one-SM kernels: 24 accumulator columns per chunk, no row stores
 constexpr int STAGING_BYTES = Epi1::STAGING_BYTES;
 // Per-tile frame terms staged in shared memory, two buffers.  With A the
 // reference (pre-alignment) of the tile's first reference frame and B that of
@@ -97,11 +102,14 @@ constexpr int STAGING_BYTES = Epi1::STAGING_BYTES;
 // reference, -, -).  Float4 k of slot s sits at 4 s + (k ^ ((s >> 1) & 3)), so
 // the k-th float4s of 8 consecutive slots fall in distinct banks.  After the
 // frame slots: the reference-pair entry of (A, B) (kRefPairStride floats),
-// for a triangle over reference-sorted positions each slot's frame number
-// (TI + TJ ints; -1 outside the map), and the row bases below.
-// Then, for the row stores of a triangle in frame order, the output index of
-// (reference slot il, target slot 0) as an int64 per reference slot (Epi's
-// TERM_* offsets).
+// the tile (tile row, tile column, A, B as ints), for a triangle over
+// reference-sorted positions each slot's frame number (TI + TJ ints; -1
+// outside the map), and the row bases below.
+// Then, for the row stores of a triangle, an int64 per slot: in frame order,
+// the output index of (reference slot il, target slot 0) per reference slot;
+// over sorted positions, n f - f (f + 1) / 2 - f - 1 for the slot's frame f,
+// so that a pair's index is the base of its smaller frame plus the larger
+// frame (Epi's TERM_* offsets).
 __device__ __forceinline__ int slot_f4(int s, int k) { return 4 * s + (k ^ ((s >> 1) & 3)); }
 static_assert(TJ == 64, "row stores split the slot index with shifts");
 template <class E>
@@ -232,25 +240,117 @@ __device__ __forceinline__ void load_slot(const float* T, int s, Side& sd, float
   inv_scale = reinterpret_cast<const float4*>(T)[slot_f4(s, 3)].x;
 }
 
+// Stages tile t's frame terms into T (one buffer of the layout above) with
+// nthr threads (this one is thread tid): the tile, its references (A, B),
+// each slot's Side terms against (A, B), the reference-pair entry and, for
+// row stores, the frame numbers and row bases.
+template <class E, bool BWD>
+__device__ __forceinline__ void stage_tile_terms(const TcParams& P, float* T, int64_t t, int ti_frames, int i_off,
+                                                 bool has_rowbuf, int tid, int nthr) {
+  constexpr int TI = E::TIE;
+  const int K = P.terms.K;
+  const int2 tl = P.tiles[t];
+  const int64_t i0 = P.i_base + (int64_t)tl.x * ti_frames + i_off;
+  const int64_t jt0 = P.jt_base + (int64_t)tl.y * TJ;
+  const int A = (K > 1 && i0 < P.i_end) ? __ldg(P.terms.assign + i0) : 0;
+  const int B = (K > 1 && jt0 < P.jt_end) ? __ldg(P.terms.assign + P.tgt0 + jt0) : 0;
+  const bool same_t = (A == B);
+  const float* Ug = P.terms.RP + (size_t)(B * K + A) * kRefPairStride;
+  float4* T4 = reinterpret_cast<float4*>(T);
+  for (int sl = tid; sl < TI + TJ; sl += nthr) {
+    int64_t f;
+    bool valid;
+    int other;
+    const bool ref_side = sl < TI;
+    if (ref_side) {
+      f = i0 + sl;
+      valid = f < P.i_end;
+      other = B;
+    } else {
+      const int64_t jt = jt0 + (sl - TI);
+      f = P.tgt0 + jt;
+      valid = jt < P.jt_end;
+      other = A;
+    }
+    float4 o0 = make_float4(0.f, 0.f, 0.f, 0.f), o1 = o0, o2 = o0, o3 = o0;
+    if (valid) {
+      const int own = (K > 1) ? __ldg(P.terms.assign + f) : 0;
+      const float trPown = (K > 1) ? __ldg(P.terms.trP + f * K + own) : 0.0f;
+      float Pv[9], U[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        Pv[k] = __ldg(P.terms.P + (f * K + other) * 9 + k);
+        U[k] = same_t ? 0.0f : __ldg(Ug + k);
+      }
+      Side sd;
+      side_terms(Pv, __ldg(P.terms.nrm + f), trPown, U, same_t, ref_side, sd);
+      o0 = make_float4(sd.Q[0], sd.Q[1], sd.Q[2], sd.Q[3]);
+      o1 = make_float4(sd.Q[4], sd.Q[5], sd.Q[6], sd.Q[7]);
+      o2 = make_float4(sd.Q[8], sd.c, sd.m, sd.sn);
+      o3 = make_float4(__ldg(P.inv_scale + f), __int_as_float(own), 0.f, 0.f);
+    }
+    T4[slot_f4(sl, 0)] = o0;
+    T4[slot_f4(sl, 1)] = o1;
+    T4[slot_f4(sl, 2)] = o2;
+    T4[slot_f4(sl, 3)] = o3;
+  }
+  for (int x = tid; x < kRefPairStride; x += nthr) T[E::TERM_RP + x] = __ldg(Ug + x);
+  if (tid == 0) {
+    int* meta = reinterpret_cast<int*>(T + E::TERM_META);
+    meta[0] = tl.x;
+    meta[1] = tl.y;
+    meta[2] = A;
+    meta[3] = B;
+  }
+  const bool rows = !BWD && has_rowbuf && P.map.tri && P.row_stores != 0;
+  const int64_t n = P.map.n_ref;
+  if (P.map.perm) {
+    int* Tp = reinterpret_cast<int*>(T + E::TERM_PERM);
+    int64_t* Trb = reinterpret_cast<int64_t*>(T + E::TERM_ROWBASE);
+    for (int x = tid; x < TI + TJ; x += nthr) {
+      int v = -1;
+      if (x < TI) {
+        if (i0 + x < P.i_end) v = __ldg(P.map.perm + i0 + x);
+      } else {
+        const int64_t jt = jt0 + (x - TI);
+        if (jt < P.jt_end) v = __ldg(P.map.perm + P.tgt0 + jt);
+      }
+      Tp[x] = v;
+      if (rows) {
+        const int64_t fv = v;
+        Trb[x] = n * fv - (fv + 1) * fv / 2 - fv - 1;
+      }
+    }
+  } else if (rows) {
+    // tri_index(n, i, jt0) - base for reference frame i = i0 + x
+    for (int x = tid; x < TI; x += nthr) {
+      const int64_t i = i0 + x;
+      reinterpret_cast<int64_t*>(T + E::TERM_ROWBASE)[x] = n * i - (i + 1) * i / 2 + jt0 - i - 1 - P.map.base;
+    }
+  }
+}
+
 // Epilogue warps (2 .. 2 + EPI_WARPS): for tiles t0, t0 + tstep, ... wait for
-// the accumulator, stage the tile's frame terms (one reference), read the
-// 128 x 192 FP32 block from tensor memory in 24-column chunks (group g takes
-// chunks g, g + 4, ...), and run the per-pair solve.  The reference frames of
-// a tile start at i_base + ti * ti_frames + i_off.  acce_bar is the address
-// the warps arrive on when the buffer is free (remote: CTA 0 of a pair).
+// the accumulator and the tile's staged frame terms (staged here by all
+// epilogue threads, or, with STAGER, by the staging warp a tile ahead: tfull
+// / tempty hand the two buffers over), read the 128 x 192 FP32 block from
+// tensor memory in chunks of 3 CH_TGT columns (group g takes chunks g,
+// g + 4, ...), and run the per-pair solve.  The reference frames of a tile
+// start at i_base + ti * ti_frames + i_off.  acce_bar is the address the
+// warps arrive on when the accumulator is free (remote: CTA 0 of a pair).
 // BWD (one frame set, TRI, one reference): for each pair i < j, with
 // c = g_ij / RMSD_ij and T the rotation taking x'_j onto x'_i, the block
 // B[3i..3i+2][3j..3j+2] = c T and the row terms E_i += c (I - T),
 // E_j += c (I - T^T), C_i += c, C_j += c.  The row terms are summed across
 // the warp's lanes that share a frame, then in shared memory per tile
 // (rowbuf), and added to E / C once per tile.
-template <class E, bool BWD = false>
+template <class E, bool BWD = false, bool STAGER = false>
 __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_base, float* staging, float* terms,
                                                float* rowbuf, volatile int* okf, uint32_t accf0, uint32_t acce_bar,
                                                bool remote, int64_t t0, int64_t tstep, int ti_frames, int i_off,
-                                               int warp, int lane) {
+                                               int warp, int lane, uint32_t tfull0 = 0, uint32_t tempty0 = 0) {
   constexpr int TI = E::TIE, TERM_RP = E::TERM_RP, TERM_PERM = E::TERM_PERM, TERM_ROWBASE = E::TERM_ROWBASE,
-                TERM_FLOATS = E::TERM_FLOATS;
+                TERM_FLOATS = E::TERM_FLOATS, TERM_META = E::TERM_META;
   const int e = warp - 2;
   const int g = e >> 2;
   const int q = warp & 3;               // TMEM lane quadrant this warp may access
@@ -265,7 +365,6 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
   // pieces, which matters when the output is host memory across the link.
   const bool rows = !BWD && rowbuf != nullptr && tri && P.row_stores != 0;
   constexpr int RB_STRIDE = E::RB_STRIDE;
-  const int K = P.terms.K;
   // BWD: this CTA's row terms, [TI][10] for its reference frames then
   // [TJ][10] for the tile's target frames, zero between tiles.
   float* Erow = rowbuf;
@@ -279,7 +378,23 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
   uint32_t it = 0;
   for (int64_t t = t0; t < P.n_tiles; t += tstep, ++it) {
     const uint32_t b = it & 1u, aph = (it >> 1) & 1u;
-    const int2 tl = P.tiles[t];
+    float* T = terms + b * TERM_FLOATS;
+    // Buffer b was last read two tiles ago, before every group passed the
+    // previous tile's barrier (inline staging), or is handed over by the
+    // staging warp through tfull / tempty.
+    if constexpr (!STAGER) stage_tile_terms<E, BWD>(P, T, t, ti_frames, i_off, rowbuf != nullptr, etid, EPI_WARPS * 32);
+    // One thread waits; the verdict is shared so every epilogue thread takes
+    // the same path through the named barriers.
+    if (etid == 0) {
+      bool okw = mbar_wait(accf0 + 8 * b, aph, P.err, 5);
+      if constexpr (STAGER) okw = okw && mbar_wait(tfull0 + 8 * b, aph, P.err, 15);
+      okf[b] = okw ? 1 : 0;
+    }
+    named_sync(1 + EPI_GROUPS, EPI_WARPS * 32);
+    const bool ok = okf[b] != 0;
+    const int* meta = reinterpret_cast<const int*>(T + TERM_META);
+    const int2 tl = make_int2(meta[0], meta[1]);
+    const int A = meta[2], B = meta[3];
     const int64_t i0 = P.i_base + (int64_t)tl.x * ti_frames + i_off;
     const int64_t jt0 = P.jt_base + (int64_t)tl.y * TJ;
     // Tile-relative limits: reference slots [0, ilim) and target slots
@@ -289,79 +404,6 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
     const int ilim = irem <= 0 ? 0 : (irem < TI ? (int)irem : TI);
     const int jlim = jrem <= 0 ? 0 : (jrem < TJ ? (int)jrem : TJ);
     const int d0 = (int)(jt0 - i0);
-    float* T = terms + b * TERM_FLOATS;
-    // Loads overlap the MMAs of this tile; buffer b was last read two tiles
-    // ago, before every group passed the previous tile's barrier.
-    const int A = (K > 1 && i0 < P.i_end) ? __ldg(P.terms.assign + i0) : 0;
-    const int B = (K > 1 && jt0 < P.jt_end) ? __ldg(P.terms.assign + P.tgt0 + jt0) : 0;
-    // Each slot's Side terms against the tile's references (A, B).
-    {
-      const bool same_t = (A == B);
-      const float* Ug = P.terms.RP + (size_t)(B * K + A) * kRefPairStride;
-      float4* T4 = reinterpret_cast<float4*>(T);
-      for (int sl = etid; sl < TI + TJ; sl += EPI_WARPS * 32) {
-        int64_t f;
-        bool valid;
-        int other;
-        const bool ref_side = sl < TI;
-        if (ref_side) {
-          f = i0 + sl;
-          valid = f < P.i_end;
-          other = B;
-        } else {
-          const int64_t jt = jt0 + (sl - TI);
-          f = P.tgt0 + jt;
-          valid = jt < P.jt_end;
-          other = A;
-        }
-        float4 o0 = make_float4(0.f, 0.f, 0.f, 0.f), o1 = o0, o2 = o0, o3 = o0;
-        if (valid) {
-          const int own = (K > 1) ? __ldg(P.terms.assign + f) : 0;
-          const float trPown = (K > 1) ? __ldg(P.terms.trP + f * K + own) : 0.0f;
-          float Pv[9], U[9];
-#pragma unroll
-          for (int k = 0; k < 9; ++k) {
-            Pv[k] = __ldg(P.terms.P + (f * K + other) * 9 + k);
-            U[k] = same_t ? 0.0f : __ldg(Ug + k);
-          }
-          Side sd;
-          side_terms(Pv, __ldg(P.terms.nrm + f), trPown, U, same_t, ref_side, sd);
-          o0 = make_float4(sd.Q[0], sd.Q[1], sd.Q[2], sd.Q[3]);
-          o1 = make_float4(sd.Q[4], sd.Q[5], sd.Q[6], sd.Q[7]);
-          o2 = make_float4(sd.Q[8], sd.c, sd.m, sd.sn);
-          o3 = make_float4(__ldg(P.inv_scale + f), __int_as_float(own), 0.f, 0.f);
-        }
-        T4[slot_f4(sl, 0)] = o0;
-        T4[slot_f4(sl, 1)] = o1;
-        T4[slot_f4(sl, 2)] = o2;
-        T4[slot_f4(sl, 3)] = o3;
-      }
-    }
-    // The tile's reference-pair entry and, with a sorted layout, its frames.
-    if (etid < kRefPairStride) T[TERM_RP + etid] = __ldg(P.terms.RP + (size_t)(B * K + A) * kRefPairStride + etid);
-    if (rows && !P.map.perm && etid < TI) {
-      // tri_index(n, i, jt0) - base for reference frame i = i0 + etid
-      const int64_t i = i0 + etid, n = P.map.n_ref;
-      reinterpret_cast<int64_t*>(T + TERM_ROWBASE)[etid] = n * i - (i + 1) * i / 2 + jt0 - i - 1 - P.map.base;
-    }
-    if (P.map.perm) {
-      int* Tp = reinterpret_cast<int*>(T + TERM_PERM);
-      for (int x = etid; x < TI + TJ; x += EPI_WARPS * 32) {
-        int v = -1;
-        if (x < TI) {
-          if (i0 + x < P.i_end) v = __ldg(P.map.perm + i0 + x);
-        } else {
-          const int64_t jt = jt0 + (x - TI);
-          if (jt < P.jt_end) v = __ldg(P.map.perm + P.tgt0 + jt);
-        }
-        Tp[x] = v;
-      }
-    }
-    // One thread waits; the verdict is shared so every epilogue thread takes
-    // the same path through the named barriers.
-    if (etid == 0) okf[b] = mbar_wait(accf0 + 8 * b, aph, P.err, 5) ? 1 : 0;
-    named_sync(1 + EPI_GROUPS, EPI_WARPS * 32);
-    const bool ok = okf[b] != 0;
     if (ok) {
       tc_fence_after();
       for (int c = g; c < TJ / CH_TGT; c += EPI_GROUPS) {
@@ -409,13 +451,13 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
 #pragma unroll
               for (int pj = 0; pj < 3; ++pj)
 #pragma unroll
-                for (int pi = 0; pi < 3; ++pi) D.v[pj * 3 + pi] = st[(3 * il + pi) * ST_STRIDE + 3 * jl + pj] * sc;
+                for (int pi = 0; pi < 3; ++pi) D.v[pj * 3 + pi] = st[(3 * il + pi) * ST_STRIDE + 3 * jl + pj];
               bool flag = false;
               float qv[4];
               // K = 1: the reference-pair entry of (0, 0)
               RefPair rp;
               load_refpair_smem(T + TERM_RP, rp);
-              const float rm = pair_solve_inl(D, si, sj, rp, true, P.terms, &flag, qv);
+              const float rm = pair_solve_inl(D, sc, si, sj, rp, true, P.terms, &flag, qv);
               const int64_t t = tri_index(P.map.n_ref, i, j);
               if (P.bwd.rmsd) P.bwd.rmsd[t] = rm;
               const float gij = P.bwd.g ? P.bwd.g[t] : 1.0f;
@@ -511,9 +553,9 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
 #pragma unroll
             for (int pj = 0; pj < 3; ++pj)
 #pragma unroll
-              for (int pi = 0; pi < 3; ++pi) D.v[pj * 3 + pi] = st[(3 * il + pi) * ST_STRIDE + 3 * jl + pj] * sc;
+              for (int pi = 0; pi < 3; ++pi) D.v[pj * 3 + pi] = st[(3 * il + pi) * ST_STRIDE + 3 * jl + pj];
             // inline: the tensor-core kernels have registers to spare
-            const float r = pair_solve_inl(D, si, sj, rp, same, P.terms, &flag);
+            const float r = pair_solve_inl(D, sc, si, sj, rp, same, P.terms, &flag);
             if (flag) flag_pair(P.flags, P.map, i, jt);
             if (rows)
               rowbuf[il * RB_STRIDE + c * CH_TGT + jl] = r;
@@ -560,7 +602,6 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
       const float* Tt = terms + b * TERM_FLOATS;  // this tile's staged frames
       const int* Tp = reinterpret_cast<const int*>(Tt + TERM_PERM);
       const int64_t* Trb = reinterpret_cast<const int64_t*>(Tt + TERM_ROWBASE);
-      const int64_t n = P.map.n_ref;
 #pragma unroll 1
       for (int x = etid; x < TI * TJ; x += EPI_WARPS * 32) {
         const int il = x >> 6, jl = x & (TJ - 1);
@@ -568,17 +609,21 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
         if (il >= ilim || jl >= jlim || !(d0 + jl > il)) continue;
         int64_t idx;
         if (P.map.perm) {
-          // out_index over sorted positions: the frames from shared memory
-          int a = Tp[il], bb = Tp[TI + jl];
-          if (a > bb) {
-            const int c2 = a; a = bb; bb = c2;
-          }
-          idx = n * a - ((int64_t)a + 1) * a / 2 + (bb - a - 1);
+          // out_index over sorted positions: the smaller frame's base plus
+          // the larger frame
+          const int a = Tp[il], bb = Tp[TI + jl];
+          idx = (a < bb) ? Trb[il] + bb : Trb[TI + jl] + a;
         } else {
           idx = Trb[il] + jl;
         }
         P.map.out[idx] = rowbuf[il * RB_STRIDE + jl];
       }
+    }
+    if constexpr (STAGER) {
+      // This warp's last read of buffer b (slots, entry, frames, row bases)
+      // is done: hand it back to the staging warp.
+      __syncwarp();
+      if (lane == 0) mbar_arrive(tempty0 + 8 * b);
     }
   }
   if constexpr (BWD) {
@@ -830,7 +875,7 @@ __device__ __forceinline__ uint64_t smem_desc_pair(uint32_t addr) {
 }
 
 template <class PC, bool BWD = false>
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __launch_bounds__(THREADS2, 1)
     k_pairs_tc2(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                 const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
                 const TcParams P) {
@@ -851,12 +896,16 @@ __global__ void __launch_bounds__(THREADS, 1)
   float* terms = (float*)(smem + STAGES2 * STAGE2_BYTES + EPI_GROUPS * STAGING_BYTES);
   float* rowbuf = terms + 2 * TERM_FLOATS;
   uint64_t* bars = (uint64_t*)(smem + STAGES2 * STAGE2_BYTES + EPI_BYTES);
-  // bars: full[STAGES2] empty[STAGES2] accf[2] acce[2] done; TMEM address; verdicts.
+  // bars: full[STAGES2] empty[STAGES2] accf[2] acce[2] done; TMEM address;
+  // verdicts; tfull[2] tempty[2] (the staged frame terms' two buffers).
   constexpr int kFull = 0, kEmpty = STAGES2, kAccf = 2 * STAGES2, kAcce = 2 * STAGES2 + 2, kDone = 2 * STAGES2 + 4;
+  constexpr int kTfull = kDone + 3, kTempty = kDone + 5;
+  static_assert((kTempty + 2) * 8 <= BAR2_BYTES, "barrier area");
   uint32_t* tmem_slot = (uint32_t*)(bars + kDone + 1);
   volatile int* okf = (volatile int*)(bars + kDone + 2);
   const uint32_t full0 = smem_u32(bars + kFull), empty0 = smem_u32(bars + kEmpty), accf0 = smem_u32(bars + kAccf),
-                 acce0 = smem_u32(bars + kAcce), done = smem_u32(bars + kDone);
+                 acce0 = smem_u32(bars + kAcce), done = smem_u32(bars + kDone), tfull0 = smem_u32(bars + kTfull),
+                 tempty0 = smem_u32(bars + kTempty);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t rank = cluster_rank();
   const int64_t cluster = blockIdx.x >> 1, n_clusters = gridDim.x >> 1;
@@ -869,6 +918,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     for (int b = 0; b < 2; ++b) {
       mbar_init(accf0 + 8 * b, 1);
       mbar_init(acce0 + 8 * b, 2 * EPI_WARPS);  // used in CTA 0
+      mbar_init(tfull0 + 8 * b, 32);            // every lane of the staging warp
+      mbar_init(tempty0 + 8 * b, EPI_WARPS);    // one arrival per epilogue warp
     }
     mbar_init(done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -956,10 +1007,22 @@ __global__ void __launch_bounds__(THREADS, 1)
       umma_commit_pair_local(done);
       mbar_wait_quiet(done, 0);
     }
+  } else if (warp == 2 + EPI_WARPS) {
+    // ---------------- frame-term staging (both CTAs) ----------------
+    // Tile by tile, in the epilogue's order: wait until the epilogue warps
+    // have released buffer b (two tiles ago), stage the tile, publish.
+    uint32_t it = 0;
+    for (int64_t t = cluster; t < P.n_tiles; t += n_clusters, ++it) {
+      const uint32_t b = it & 1u, ph = (it >> 1) & 1u;
+      if (!mbar_wait(tempty0 + 8 * b, ph ^ 1u, P.err, 16)) break;
+      stage_tile_terms<typename PC::E, BWD>(P, terms + b * TERM_FLOATS, t, TI2, (int)rank * TI, true, lane, 32);
+      mbar_arrive(tfull0 + 8 * b);
+    }
   } else {
     // ---------------- epilogue (both CTAs) ----------------
-    epilogue_tiles<typename PC::E, BWD>(P, tmem_base, staging, terms, rowbuf, okf, accf0, mapa_rank(acce0, 0), true,
-                                   cluster, n_clusters, TI2, (int)rank * TI, warp, lane);
+    epilogue_tiles<typename PC::E, BWD, true>(P, tmem_base, staging, terms, rowbuf, okf, accf0, mapa_rank(acce0, 0),
+                                              true, cluster, n_clusters, TI2, (int)rank * TI, warp, lane, tfull0,
+                                              tempty0);
   }
 
   tc_fence_before();
@@ -1077,7 +1140,7 @@ static cudaError_t launch_pair_kernel(const CUtensorMap& mAh, const CUtensorMap&
   attr[0].val.clusterDim.x = 2;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
-  cfg.blockDim = dim3(THREADS, 1, 1);
+  cfg.blockDim = dim3(THREADS2, 1, 1);
   cfg.dynamicSmemBytes = PC::SMEM2_BYTES;
   cfg.stream = st;
   cfg.attrs = attr;

@@ -255,7 +255,7 @@ cudaError_t enqueue_prob(gbr_handle* h, Prob& p, int mode, bool host_in, bool ho
       L.dev_error = derr;
       L.num_sms = h->num_sms;
       L.variant = tc_variant_of(p.choice);
-      L.row_stores = 1;
+      L.row_stores = 0;  // the triangle is in device memory (caller's or staging)
       if (p.n_tiles > 0 && (e = run_pairs_tc(L, st)) != cudaSuccess) return e;
     } else {
       PairLaunch L{};

@@ -716,7 +716,9 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
       L.dev_error = (int*)P[25];
       L.num_sms = h->num_sms;
       L.variant = tc_variant;
-      L.row_stores = 1;
+      // whole-row stores where the triangle lands in host memory across the
+      // link; direct per-pair stores into device memory
+      L.row_stores = out_direct ? 1 : 0;
       L.skip = skip;
       return run_pairs_tc(L, st);
     };

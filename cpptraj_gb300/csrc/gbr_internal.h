@@ -201,9 +201,11 @@ struct TcLaunch {
   int num_sms;
   int variant;       // 0: 64-atom stages (128B swizzle, 2 stages); 1: 32-atom stages (64B swizzle, 4 stages);
                      // 2: pairs of SMs (cta_group::2), 32-atom stages x 5, 8-frame epilogue chunks;
-                     // 3: pairs of SMs, 64-atom stages x 3, 4-frame epilogue chunks
+                     // 3: pairs of SMs, 64-atom stages x 3, 4-frame epilogue chunks;
+                     // 4: pairs of SMs, 32-atom stages x 3, 16-frame epilogue chunks, 40 reference frames per CTA
   int64_t ready_tiles;  // > 0: tile_buf already holds this many tiles (no host build or copy)
   int row_stores;       // pair kernels, triangle output: gather each tile's results and store whole rows
+                        // (host memory across the link); 0: each pair stored directly (device memory)
   const int* skip;      // device int or nullptr: when it reads non-zero at launch, the kernel does nothing
   const BwdArgs* bwd;   // non-null: the backward pass (variants 2 and 3, one set, TRI, one reference)
 };

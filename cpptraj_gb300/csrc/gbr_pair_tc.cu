@@ -77,7 +77,11 @@ struct Epi {
   static constexpr int TIE = TI_;       // reference frames per CTA tile
   static constexpr int CH_TGT = CH;
   static constexpr int CH_COLS = 3 * CH;
-  static constexpr int ST_STRIDE = CH_COLS + 1;
+  // Rows of the staged chunk: 16-frame chunks are written as float4s (row
+  // stride 52 = 20 mod 32: the float4s of 8 consecutive rows hit distinct
+  // banks); narrower ones as floats with an odd stride.
+  static constexpr bool ST_VEC = (CH >= 16);
+  static constexpr int ST_STRIDE = ST_VEC ? CH_COLS + 4 : CH_COLS + 1;
   static constexpr int STAGING_BYTES = 128 * ST_STRIDE * 4;
   // Result rows of one tile (pair kernels, triangle output): TI rows of TJ
   // values, padded by one chunk so the chunk writes hit 32 distinct banks.
@@ -302,7 +306,9 @@ __device__ __forceinline__ void stage_tile_terms(const TcParams& P, float* T, in
     meta[2] = A;
     meta[3] = B;
   }
-  const bool rows = !BWD && has_rowbuf && P.map.tri && P.row_stores != 0;
+  // Row bases for every triangle a pair kernel writes (row stores or direct
+  // stores); the one-SM kernels index through out_index.
+  const bool rows = !BWD && has_rowbuf && P.map.tri;
   const int64_t n = P.map.n_ref;
   if (P.map.perm) {
     int* Tp = reinterpret_cast<int*>(T + E::TERM_PERM);
@@ -364,6 +370,10 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
   // whole rows of the triangle (TJ contiguous values) instead of CH_TGT-value
   // pieces, which matters when the output is host memory across the link.
   const bool rows = !BWD && rowbuf != nullptr && tri && P.row_stores != 0;
+  // Direct stores (triangle in device memory): each pair's value leaves from
+  // its thread, indexed through the tile's staged row bases, with no row
+  // buffer and no barrier before the stores.
+  const bool direct = !BWD && rowbuf != nullptr && tri && P.row_stores == 0;
   constexpr int RB_STRIDE = E::RB_STRIDE;
   // BWD: this CTA's row terms, [TI][10] for its reference frames then
   // [TJ][10] for the tile's target frames, zero between tiles.
@@ -423,8 +433,14 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
           tmem_ld4(taddr + 8, v + 8);
         }
         tmem_wait_ld();
+        if constexpr (E::ST_VEC) {
+          float4* st4 = reinterpret_cast<float4*>(st + row * ST_STRIDE);
 #pragma unroll
-        for (int k = 0; k < CH_COLS; ++k) st[row * ST_STRIDE + k] = v[k];
+          for (int k = 0; k < CH_COLS / 4; ++k) st4[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < CH_COLS; ++k) st[row * ST_STRIDE + k] = v[k];
+        }
         named_sync(1 + g, 128);
         const int64_t jc0 = jt0 + (int64_t)c * CH_TGT;
         if constexpr (BWD) {
@@ -516,7 +532,7 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
             // only target > reference remains to test; the stores map it to
             // its index.
             int64_t idx = 0;
-            if (rows) {
+            if (rows || direct) {
               if (!(d0 + jj > il)) continue;
             } else {
               idx = out_index(P.map, i, jt);
@@ -557,13 +573,28 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
             // inline: the tensor-core kernels have registers to spare
             const float r = pair_solve_inl(D, sc, si, sj, rp, same, P.terms, &flag);
             if (flag) flag_pair(P.flags, P.map, i, jt);
-            if (rows)
+            if (rows) {
               rowbuf[il * RB_STRIDE + c * CH_TGT + jl] = r;
-            else
+            } else if (direct) {
+              const int64_t* Trb = reinterpret_cast<const int64_t*>(T + TERM_ROWBASE);
+              if (P.map.perm) {
+                // over sorted positions: the smaller frame's base plus the larger frame
+                const int* Tp = reinterpret_cast<const int*>(T + TERM_PERM);
+                const int a = Tp[il], bb = Tp[TI + jj];
+                idx = (a < bb) ? Trb[il] + bb : Trb[TI + jj] + a;
+              } else {
+                idx = Trb[il] + jj;
+              }
               P.map.out[idx] = r;
+            } else {
+              P.map.out[idx] = r;
+            }
           }
         }
-        named_sync(1 + g, 128);
+        // The group's staging buffer is written again by its next chunk: of
+        // this tile, after this barrier; of the next tile, after that tile's
+        // all-epilogue barrier (so none is needed after the last chunk).
+        if (c + EPI_GROUPS < TJ / CH_TGT) named_sync(1 + g, 128);
       }
     }
     // Every tensor-memory read of this tile has completed (tmem_wait_ld per

@@ -95,6 +95,7 @@ struct PrepScratch {
   int* kstate;     // [2] k-centre choice on the device: stopped flag, index of the last reference added
   unsigned* rcount;  // k_ref_update: blocks done (one reference's self terms)
   double* rsu;       // k_ref_update: per-block sums of w r r^T (one reference)
+  float* dref;       // [Kmax] k-centre round k: FP32 distances from reference k to references 0..k-1
 };
 size_t prep_scratch_bytes(int64_t F, int N, int Kmax);
 PrepScratch prep_carve(void* base, int64_t F, int N, int Kmax);

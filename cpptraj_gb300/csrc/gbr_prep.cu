@@ -52,6 +52,7 @@ struct FrameSrc {
 };
 
 constexpr int kPrepThreads = 256;
+constexpr int kScanList = 1024;  // frames listed per block and range in a pruned k-centre scan
 constexpr int kWarps = kPrepThreads / 32;
 // k_scan and k_build split each frame's atom chunks over kWPF warps: a chunk
 // of input (1,250 frames) then keeps twice the warps busy.  The parts' sums
@@ -150,6 +151,7 @@ size_t prep_scratch_bytes(int64_t F, int N, int Kmax) {
   b += align256(sizeof(int) * 2);
   b += align256(sizeof(unsigned));
   b += align256(sizeof(double) * 9 * (size_t)((N + 31) / 32));  // k_ref_update's blocks
+  b += align256(sizeof(float) * Kmax);
   return b;
 }
 
@@ -176,6 +178,7 @@ PrepScratch prep_carve(void* base, int64_t F, int N, int Kmax) {
   s.kstate = (int*)take(sizeof(int) * 2);
   s.rcount = (unsigned*)take(sizeof(unsigned));
   s.rsu = (double*)take(sizeof(double) * 9 * (size_t)((N + 31) / 32));
+  s.dref = (float*)take(sizeof(float) * Kmax);
   return s;
 }
 
@@ -270,12 +273,17 @@ struct WarpPipe {
   int64_t f_next, F, stride;  // next frame to issue, end, this warp's frame stride
   int c_next, c_lo, c_hi, issued;  // next chunk of f_next, this warp's chunks [c_lo, c_hi), chunks issued
   float* ring;                // kPipe * kStage floats, 16-byte aligned
+  const int* list = nullptr;  // optional: f_next indexes a list of frames base + list[f_next]
+  int64_t base = 0;
+  __device__ __forceinline__ int64_t frame_at(int64_t i) const { return list ? base + list[i] : i; }
 
   // The warp streams chunks [c_lo, c_hi) of each of its frames (its part of
   // a frame shared by kWPF warps).
   __device__ __forceinline__ void init(const FrameSrc<T>& s, int64_t f0, int64_t f_end, int64_t str, float* buf,
-                                       int lane, int lo, int hi) {
+                                       int lane, int lo, int hi, const int* lst = nullptr, int64_t lbase = 0) {
     src = s;
+    list = lst;
+    base = lbase;
     f_next = f0;
     F = f_end;
     stride = str;
@@ -293,7 +301,7 @@ struct WarpPipe {
     if constexpr (sizeof(T) == 4) {
       if (f_next < F && c_hi > c_lo) {
         const int N = src.N, a0 = c_next * kChunkAtoms;
-        const float* x = (const float*)src.frame(f_next) + 3 * (size_t)a0;
+        const float* x = (const float*)src.frame(frame_at(f_next)) + 3 * (size_t)a0;
         const int n = 3 * (min(a0 + kChunkAtoms, N) - a0);
         const int head = chunk_head(x, n);
         const int nv = (n - head) >> 2, tail0 = head + 4 * nv;
@@ -462,8 +470,9 @@ __global__ void __launch_bounds__(kPrepThreads) k_centroid(FrameSrc<T> src, int6
   }
 }
 
-// Reference k := frame *fsel centred (and superposed onto reference `parent`
-// when fitting and use_parent).  Reference 0 is built before any centre is
+// Reference k := frame *fsel centred (and, when fitting and use_parent,
+// superposed onto its nearest reference with the quaternion its scan kept).
+// Reference 0 is built before any centre is
 // known and centres its frame itself.  Writes the FP64 reference, sqrt(w) r
 // (FP32, also packed with sqrt(w) for the scans), r as hi + lo floats,
 // sum w |r|^2, sum w r and max |r|.  FP64 per
@@ -473,7 +482,8 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
     k_make_ref(FrameSrc<T> src, const int64_t* fsel, const double* cen, const double* cmass_ref,
                const double* cmass_tgt, const double* w, const double* sqw, const int* assign, int k, int use_parent,
                int nofit, double* refs, float* swr, float2* refhl, double* Eref, double* sr, float* rmax,
-               float4* qscan, const int* gate = nullptr, WeightsPass wp = WeightsPass{}) {
+               float4* qscan, const int* gate = nullptr, WeightsPass wp = WeightsPass{},
+               const float4* quat = nullptr, float* dref = nullptr, double Wsum = 1.0) {
   // A gated round after the k-centre choice has stopped: every CTA of the
   // cluster reads the same word and leaves before any barrier.
   if (gate && *gate != 0) return;
@@ -521,23 +531,17 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
   }
   __syncthreads();
   double* rk = refs + (size_t)k * 3 * N;
+  // Orientation: the frame superposed onto its parent reference with the
+  // quaternion its scan kept (an FP64-orthogonal rotation; any rotation
+  // serves, since the rotations between references are computed exactly
+  // from the references themselves).
   const int parent = use_parent ? assign[f] : -1;
   if (!nofit && parent >= 0) {
-    const double* rp = refs + (size_t)parent * 3 * N;
-    double v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int a = a_first; a < N; a += stride) {
-      const double wa = w ? w[a] : 1.0;
-      const double y0 = (double)x[3 * a] - c0, y1 = (double)x[3 * a + 1] - c1, y2 = (double)x[3 * a + 2] - c2;
-      const double r0 = rp[3 * a], r1 = rp[3 * a + 1], r2 = rp[3 * a + 2];
-      v[0] += wa * y0 * r0; v[1] += wa * y0 * r1; v[2] += wa * y0 * r2;
-      v[3] += wa * y1 * r0; v[4] += wa * y1 * r1; v[5] += wa * y1 * r2;
-      v[6] += wa * y2 * r0; v[7] += wa * y2 * r1; v[8] += wa * y2 * r2;
-      v[9] += wa * (y0 * y0 + y1 * y1 + y2 * y2 + r0 * r0 + r1 * r1 + r2 * r2);
-    }
-    cluster_sum_f64<10>(v, red, slots, bc);
-    if (threadIdx.x == 0) {  // the same totals in every CTA give the same rotation
+    if (threadIdx.x == 0) {
+      const float4 qf = quat[f];
+      const float q4[4] = {qf.x, qf.y, qf.z, qf.w};
       double R[9];
-      qcp_lambda_rot(v, 0.5 * v[9], R);
+      rotation_from_quat(q4, R);
       for (int q = 0; q < 9; ++q) Rs[q] = R[q];
     }
     __syncthreads();
@@ -577,6 +581,41 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
     sr[3 * k + 2] = acc[3];
     rmax[k] = (float)sqrt(mx);
   }
+  if (dref) {
+    // Distances from reference k to references 0..k-1, one warp each, with
+    // the arithmetic of the scans (FP32 sums of sqrt(w) r, FP32 QCP): the
+    // k-centre round's scan skips a frame that reference k cannot take
+    // (triangle inequality).  The swr rows of reference k were written by
+    // every CTA of the cluster before the cluster barriers above.
+    const int lane = threadIdx.x & 31;
+    const int a = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
+    if (a < k) {
+      const float* rk_f = swr + (size_t)k * 3 * N;
+      const float* ra_f = swr + (size_t)a * 3 * N;
+      float M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      for (int i = lane; i < N; i += 32) {
+        const float y0 = rk_f[3 * i], y1 = rk_f[3 * i + 1], y2 = rk_f[3 * i + 2];
+        const float r0 = ra_f[3 * i], r1 = ra_f[3 * i + 1], r2 = ra_f[3 * i + 2];
+        M[0] = fmaf(y0, r0, M[0]); M[1] = fmaf(y0, r1, M[1]); M[2] = fmaf(y0, r2, M[2]);
+        M[3] = fmaf(y1, r0, M[3]); M[4] = fmaf(y1, r1, M[4]); M[5] = fmaf(y1, r2, M[5]);
+        M[6] = fmaf(y2, r0, M[6]); M[7] = fmaf(y2, r1, M[7]); M[8] = fmaf(y2, r2, M[8]);
+      }
+#pragma unroll
+      for (int q = 0; q < 9; ++q)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) M[q] += __shfl_xor_sync(0xffffffffu, M[q], o);
+      if (lane == 0) {
+        const float E0 = (float)(0.5 * (acc[0] + Eref[a]));
+        float d2 = 0.0f;
+        if (E0 > 0.0f) {
+          float q[4], lr = 1.0f;
+          qcp_vec_f32(M, E0, q, &lr);
+          d2 = 2.0f * E0 * (1.0f - lr) * (float)(1.0 / Wsum);
+        }
+        dref[a] = sqrtf(fmaxf(d2, 0.0f));
+      }
+    }
+  }
 }
 
 // A frame's rotation table: the FP64-orthogonal rotation of its quaternion
@@ -615,6 +654,8 @@ struct ScanArgs {
   int* assign;
   float4* quat;
   float* ymax;
+  const float* dref;    // rounds k > 0: distances from reference k to references 0..k-1 (nullptr: fit every frame)
+  float margin;         // Angstrom added to the skip test for the FP32 distances
 };
 
 // FIRST: centre + extent + fit to reference 0 in one read of the frame.  The
@@ -640,14 +681,15 @@ __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64
   const int64_t f_stride = (int64_t)gridDim.x * kFPB;
   const int nch = (N + kChunkAtoms - 1) / kChunkAtoms;
   WarpPipe<T> pipe;
-  pipe.init(src, f_first, F, f_stride, sbuf[warp], lane, part * nch / kWPF, (part + 1) * nch / kWPF);
+  const int c_lo = part * nch / kWPF, c_hi = (part + 1) * nch / kWPF;
   {
     const size_t n4 = (size_t)N * 4;
     prefetch_l1(s.q, 4 * n4);
     if (FIRST && !s.cm_ref_is_w && f_begin < src.n_ref) prefetch_l1(s.cm_ref, n4);
   }
-  int it = 0;
-  for (int64_t f = f_first; f < F; f += f_stride, ++it) {
+  // One frame: its atoms through this warp's pipe (the frame the pipe
+  // streams next), the parts' sums, the per-frame tail.
+  auto frame_body = [&](const int64_t f, const int it) {
     const T* x = src.frame(f);
     const bool in_ref = f < src.n_ref;
     const bool same_w = in_ref ? (s.cm_ref_is_w != 0) : true;  // centring masses = fit weights
@@ -766,7 +808,42 @@ __global__ void __launch_bounds__(kPrepThreads, 4) k_scan(FrameSrc<T> src, int64
         s.quat[f] = make_float4(q[0], q[1], q[2], q[3]);
       }
     }
+  };
+  if constexpr (!FIRST) {
+    if (s.dref) {
+      // Rounds k > 0 with the triangle inequality: a frame at distance
+      // dist from its reference a cannot come nearer to reference k than
+      // D(a, k) - dist, so it keeps its assignment when D(a, k) > 2 dist
+      // (plus a margin for the FP32 distances) and its fit is skipped.  Each
+      // block takes a contiguous range of frames, lists the ones to fit in
+      // shared memory, and its groups stream that list.
+      __shared__ int flist[kScanList];
+      __shared__ int fcount;
+      const int64_t span = (F - f_begin + gridDim.x - 1) / gridDim.x;
+      const int64_t b0 = f_begin + (int64_t)blockIdx.x * span, b1 = min(F, b0 + span);
+      int it = 0;
+      for (int64_t c0 = b0; c0 < b1; c0 += kScanList) {
+        const int64_t c1 = min(b1, c0 + (int64_t)kScanList);
+        if (threadIdx.x == 0) fcount = 0;
+        __syncthreads();
+        for (int64_t f = c0 + threadIdx.x; f < c1; f += kPrepThreads) {
+          const float df = s.dist[f];
+          const float D = s.dref[s.assign[f]];
+          if (!(D > 2.0f * df + s.margin + 2e-3f * D)) flist[atomicAdd(&fcount, 1)] = (int)(f - c0);
+        }
+        __syncthreads();
+        const int n = fcount;
+        pipe.init(src, grp, n, kFPB, sbuf[warp], lane, c_lo, c_hi, flist, c0);
+        for (int i = grp; i < n; i += kFPB, ++it) frame_body(c0 + flist[i], it);
+        pipe.drain();
+        __syncthreads();  // the list is rewritten by the next range
+      }
+      return;
+    }
   }
+  pipe.init(src, f_first, F, f_stride, sbuf[warp], lane, c_lo, c_hi);
+  int it = 0;
+  for (int64_t f = f_first; f < F; f += f_stride, ++it) frame_body(f, it);
   pipe.drain();
 }
 
@@ -1342,18 +1419,39 @@ __global__ void __launch_bounds__(256) k_pref(BuildArgs b, int64_t F, int N) {
 // Reference-pair table (kRefPairStride floats per b*K + a): the exact FP64
 // rotation U_ab taking r_b onto r_a, SU_ab = U_ab S_ba, its antisymmetric
 // combos and sum w |r_a - U_ab r_b|^2.  No-fit mode keeps U = I.
-__global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockThreads)
+// One block of kRefTermThreads per reference pair: all K^2 pairs run side by
+// side, each with its own FP64 solve (a cluster per pair left most of the
+// GPU idle behind a few clusters' serial QCP solves).
+constexpr int kRefTermThreads = 128;
+template <int NV>
+__device__ __forceinline__ void block_sum_f64_small(double (&v)[NV], double* red /* >= 4*NV */) {
+  static_assert(kRefTermThreads == 128, "four warps");
+#pragma unroll
+  for (int k = 0; k < NV; ++k)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) red[warp * NV + k] = v[k];
+  __syncthreads();
+  // warps summed in a fixed order: the same totals in every thread
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = ((red[k] + red[NV + k]) + red[2 * NV + k]) + red[3 * NV + k];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kRefTermThreads)
     k_ref_terms(const double* refs, int N, int K, const double* w, int nofit, float* RP, const int* skip) {
-  if (skip && *skip != 0) return;  // uniform over the grid: before any cluster barrier
-  __shared__ double red[32 * 10], slots[kRefCluster * 10], bc[10];
+  if (skip && *skip != 0) return;
+  __shared__ double red[4 * 10];
   __shared__ double Us[9];
-  const int pair = blockIdx.x / kRefCluster;  // one cluster per reference pair
+  const int pair = blockIdx.x;  // one block per reference pair
   const int b = pair / K, a = pair % K;
-  const int i_first = (blockIdx.x % kRefCluster) * blockDim.x + threadIdx.x, stride = kRefCluster * blockDim.x;
   const double* rb = refs + (size_t)b * 3 * N;
   const double* ra = refs + (size_t)a * 3 * N;
   double v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  for (int i = i_first; i < N; i += stride) {
+  for (int i = threadIdx.x; i < N; i += kRefTermThreads) {
     const double wa = w ? w[i] : 1.0;
     const double b0 = rb[3 * i], b1 = rb[3 * i + 1], b2 = rb[3 * i + 2];
     const double a0 = ra[3 * i], a1 = ra[3 * i + 1], a2 = ra[3 * i + 2];
@@ -1362,18 +1460,18 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
     v[6] += wa * b2 * a0; v[7] += wa * b2 * a1; v[8] += wa * b2 * a2;
     v[9] += wa * (b0 * b0 + b1 * b1 + b2 * b2 + a0 * a0 + a1 * a1 + a2 * a2);
   }
-  cluster_sum_f64<10>(v, red, slots, bc);
-  if (threadIdx.x == 0) {  // the same totals in every CTA give the same rotation
+  block_sum_f64_small<10>(v, red);
+  if (threadIdx.x == 0) {
     double U[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     if (a != b && !nofit) qcp_lambda_rot(v, 0.5 * v[9], U);
     for (int k = 0; k < 9; ++k) Us[k] = U[k];
   }
   __syncthreads();
   // SS_ab = sum w |r_a - U r_b|^2, accumulated directly (no cancellation);
-  // 0 for a reference with itself (a and b are the same in the whole cluster).
+  // 0 for a reference with itself.
   double e[1] = {0.0};
   if (a != b) {
-    for (int i = i_first; i < N; i += stride) {
+    for (int i = threadIdx.x; i < N; i += kRefTermThreads) {
       const double wa = w ? w[i] : 1.0;
       const double b0 = rb[3 * i], b1 = rb[3 * i + 1], b2 = rb[3 * i + 2];
       const double d0 = ra[3 * i] - (Us[0] * b0 + Us[1] * b1 + Us[2] * b2);
@@ -1381,9 +1479,9 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
       const double d2 = ra[3 * i + 2] - (Us[6] * b0 + Us[7] * b1 + Us[8] * b2);
       e[0] += wa * (d0 * d0 + d1 * d1 + d2 * d2);
     }
-    cluster_sum_f64<1>(e, red, slots, bc);
+    block_sum_f64_small<1>(e, red);
   }
-  if (blockIdx.x % kRefCluster == 0 && threadIdx.x == 0) {
+  if (threadIdx.x == 0) {
     double SU[9];
     for (int p = 0; p < 3; ++p)
       for (int q = 0; q < 3; ++q)
@@ -1588,15 +1686,21 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
       for (int k = 1; k < A.max_refs; ++k) {
         k_argmax_gate<<<1, 1024, 0, st>>>(A.dist, F, (float)A.tau, k, A.dmax, A.fsel, S.kstate);
         ++launches;
+        // (no-fit distances are not the fitted ones the pruning bound uses:
+        // every frame is fitted then)
+        float* dref = A.nofit ? nullptr : S.dref;
         k_make_ref<T><<<kRefCluster, kOneBlockThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w,
                                                                 A.sqw, A.assign, k, 1, A.nofit, A.refs, A.swr,
-                                                                S.refhl, A.Eref, S.sr, S.rmax, S.qscan, S.kstate);
+                                                                S.refhl, A.Eref, S.sr, S.rmax, S.qscan, S.kstate,
+                                                                WeightsPass{}, S.quat, dref, A.Wsum);
         ScanArgs sk = sa;
         sk.k = k;
         sk.q = S.qscan + (size_t)k * N;
         sk.sr = S.sr + 3 * k;
         sk.Eref = A.Eref + k;
         sk.gate = S.kstate;
+        sk.dref = dref;
+        sk.margin = 0.25f;
         k_scan<T, false><<<prep_grid(F, kScanBlocksPerSM, kFPB), kPrepThreads, 0, st>>>(src, 0, F, sk);
         launches += 2;
       }
@@ -1705,8 +1809,7 @@ static cudaError_t finish_impl(const FinishArgs& fa, cudaStream_t st) {
     }
   }
   if (!(fa.self_terms && fa.K == 1))
-    k_ref_terms<<<fa.K * fa.K * kRefCluster, kOneBlockThreads, 0, st>>>(A.refs, A.N, fa.K, A.w, A.nofit, fa.RP,
-                                                                       fa.skip);
+    k_ref_terms<<<fa.K * fa.K, kRefTermThreads, 0, st>>>(A.refs, A.N, fa.K, A.w, A.nofit, fa.RP, fa.skip);
   return cudaGetLastError();
 }
 

@@ -393,15 +393,27 @@ __device__ __forceinline__ void epilogue_tiles(const TcParams& P, uint32_t tmem_
     // previous tile's barrier (inline staging), or is handed over by the
     // staging warp through tfull / tempty.
     if constexpr (!STAGER) stage_tile_terms<E, BWD>(P, T, t, ti_frames, i_off, rowbuf != nullptr, etid, EPI_WARPS * 32);
-    // One thread waits; the verdict is shared so every epilogue thread takes
-    // the same path through the named barriers.
-    if (etid == 0) {
-      bool okw = mbar_wait(accf0 + 8 * b, aph, P.err, 5);
-      if constexpr (STAGER) okw = okw && mbar_wait(tfull0 + 8 * b, aph, P.err, 15);
-      okf[b] = okw ? 1 : 0;
+    // One thread waits; the verdict is shared so every thread that passes the
+    // barrier behind it takes the same path.  With direct stores (no barrier
+    // of all epilogue warps later in the tile) each group waits for itself,
+    // so a group held up in one tile holds back only its own next tile;
+    // otherwise one thread waits for all 16 warps.
+    const bool group_wait = STAGER && !BWD && !rows;
+    if (group_wait) {
+      if (tid == 0) {
+        const bool okw = mbar_wait(accf0 + 8 * b, aph, P.err, 5) && mbar_wait(tfull0 + 8 * b, aph, P.err, 15);
+        okf[2 * g + b] = okw ? 1 : 0;
+      }
+      named_sync(1 + g, 128);
+    } else {
+      if (etid == 0) {
+        bool okw = mbar_wait(accf0 + 8 * b, aph, P.err, 5);
+        if constexpr (STAGER) okw = okw && mbar_wait(tfull0 + 8 * b, aph, P.err, 15);
+        okf[b] = okw ? 1 : 0;
+      }
+      named_sync(1 + EPI_GROUPS, EPI_WARPS * 32);
     }
-    named_sync(1 + EPI_GROUPS, EPI_WARPS * 32);
-    const bool ok = okf[b] != 0;
+    const bool ok = okf[group_wait ? 2 * g + b : b] != 0;
     const int* meta = reinterpret_cast<const int*>(T + TERM_META);
     const int2 tl = make_int2(meta[0], meta[1]);
     const int A = meta[2], B = meta[3];
@@ -928,12 +940,12 @@ __global__ void __launch_bounds__(THREADS2, 1)
   float* rowbuf = terms + 2 * TERM_FLOATS;
   uint64_t* bars = (uint64_t*)(smem + STAGES2 * STAGE2_BYTES + EPI_BYTES);
   // bars: full[STAGES2] empty[STAGES2] accf[2] acce[2] done; TMEM address;
-  // verdicts; tfull[2] tempty[2] (the staged frame terms' two buffers).
+  // tfull[2] tempty[2] (the staged frame terms' two buffers); verdicts.
   constexpr int kFull = 0, kEmpty = STAGES2, kAccf = 2 * STAGES2, kAcce = 2 * STAGES2 + 2, kDone = 2 * STAGES2 + 4;
   constexpr int kTfull = kDone + 3, kTempty = kDone + 5;
-  static_assert((kTempty + 2) * 8 <= BAR2_BYTES, "barrier area");
+  static_assert((kTempty + 2) * 8 + 2 * EPI_GROUPS * 4 <= BAR2_BYTES, "barrier area");
   uint32_t* tmem_slot = (uint32_t*)(bars + kDone + 1);
-  volatile int* okf = (volatile int*)(bars + kDone + 2);
+  volatile int* okf = (volatile int*)(bars + kTempty + 2);  // verdicts: [group][buffer] (or [buffer])
   const uint32_t full0 = smem_u32(bars + kFull), empty0 = smem_u32(bars + kEmpty), accf0 = smem_u32(bars + kAccf),
                  acce0 = smem_u32(bars + kAcce), done = smem_u32(bars + kDone), tfull0 = smem_u32(bars + kTfull),
                  tempty0 = smem_u32(bars + kTempty);

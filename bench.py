@@ -31,7 +31,7 @@ FLOPS_PER_PAIR = 18 * N_ATOM  # algorithmic: 9 products x N atoms x 2 (the split
 # DRAM bytes (read + write) of one k_pairs_tc2 launch on this workload (the
 # deep 64-atom-stage shape the library picks at 2,000 atoms), from an ncu
 # capture of `python bench.py --profile --warmup 2` (profiles/k_pairs_tc2_10000x2000_full.md).
-K2_TRAFFIC_BYTES = {(N_FRAME, N_ATOM): 1.873646e9 + 0.193895e9}
+K2_TRAFFIC_BYTES = {(N_FRAME, N_ATOM): 1.867730e9 + 0.193599e9}
 
 
 def parse():

@@ -1039,16 +1039,23 @@ __global__ void __launch_bounds__(32) k_ref_update(RefUpdateArgs u, const float*
   if (a < N) {
     double* r = u.refs + (size_t)k * 3 * N;
     const double sw = u.sqw ? u.sqw[a] : 1.0;
-    double rr[3], sum[3] = {0.0, 0.0, 0.0};
-    // the chunk sums in chunk order, several chunks' loads in flight at once
+    double rr[3];
+    // The chunk sums in chunk order, several chunks' loads in flight at once,
+    // in FP32 (four independent partial sums per coordinate): the mean only
+    // has to move the reference near its frames, and every later pass reads
+    // the reference as stored.  (In FP64 these adds, a warp instruction each
+    // on GB300's narrow FP64 pipe, were most of this kernel's time.)
     const float* src = partial + (size_t)k * kMeanChunks * 3 * Np + a;
+    float s4[4][3] = {};
 #pragma unroll 8
     for (int ch = 0; ch < kMeanChunks; ++ch)
 #pragma unroll
-      for (int p = 0; p < 3; ++p) sum[p] += (double)src[((size_t)ch * 3 + p) * Np];
+      for (int p = 0; p < 3; ++p) s4[ch & 3][p] += src[((size_t)ch * 3 + p) * Np];
+    const float icnt = (cnt > 0) ? 1.0f / (float)cnt : 0.0f;
     float q[3];
     for (int p = 0; p < 3; ++p) {
-      rr[p] = r[3 * a + p] + ((cnt > 0) ? sum[p] / (double)cnt : 0.0);
+      const float mean = ((s4[0][p] + s4[1][p]) + (s4[2][p] + s4[3][p])) * icnt;
+      rr[p] = r[3 * a + p] + (double)mean;
       r[3 * a + p] = rr[p];
       q[p] = (float)(sw * rr[p]);
       u.swr[((size_t)k * N + a) * 3 + p] = q[p];
@@ -1056,7 +1063,10 @@ __global__ void __launch_bounds__(32) k_ref_update(RefUpdateArgs u, const float*
       u.refhl[((size_t)k * N + a) * 3 + p] = make_float2(h, (float)(rr[p] - (double)h));
     }
     u.qbuild[(size_t)k * N + a] = make_float4(q[0], q[1], q[2], (float)sw);
-    mx = (float)sqrt(rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2]) * (1.0f + 1e-6f);
+    {
+      const float r0 = (float)rr[0], r1 = (float)rr[1], r2 = (float)rr[2];
+      mx = sqrtf(fmaf(r0, r0, fmaf(r1, r1, r2 * r2))) * (1.0f + 1e-5f);  // an upper bound of |r|
+    }
     if (u.RP) {
       const double wa = u.w ? u.w[a] : 1.0;
 #pragma unroll

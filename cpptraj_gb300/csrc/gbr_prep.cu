@@ -587,6 +587,7 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
     // k-centre round's scan skips a frame that reference k cannot take
     // (triangle inequality).  The swr rows of reference k were written by
     // every CTA of the cluster before the cluster barriers above.
+    static_assert(kRefCluster * (kOneBlockThreads / 32) >= kMaxRefs, "one warp per earlier reference");
     const int lane = threadIdx.x & 31;
     const int a = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
     if (a < k) {

@@ -698,7 +698,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
     // One tensor-core launch: over the tiles of map m, or (n_ready > 0) over
     // n_ready tiles already in the tile buffer from tile0 on.
     auto launch_tc = [&](const OutMap& m, const FlagList& f, const FrameTerms& t, int64_t tile0, int64_t n_ready,
-                         const int* skip) -> cudaError_t {
+                         const int* skip, int2* stage = nullptr) -> cudaError_t {
       TcLaunch L{};
       L.hi = P[23];
       L.lo = P[24];
@@ -720,6 +720,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
       // link; direct per-pair stores into device memory
       L.row_stores = out_direct ? 1 : 0;
       L.skip = skip;
+      L.tile_stage = stage;
       return run_pairs_tc(L, st);
     };
     // Speculative stages (see above): launched from prep through on_built.
@@ -780,8 +781,8 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
       launches += po.built ? 1 : (K > 1 ? 3 : (po.self_terms ? 1 : 2));
     }
     // One launch of the pair kernel over the rows of map m.
-    auto launch_pairs = [&](const OutMap& m, const FlagList& f) -> cudaError_t {
-      if (tc) return launch_tc(m, f, terms, 0, 0, fa.skip);
+    auto launch_pairs = [&](const OutMap& m, const FlagList& f, int2* stage = nullptr) -> cudaError_t {
+      if (tc) return launch_tc(m, f, terms, 0, 0, fa.skip, stage);
       PairLaunch L{};
       L.skip = fa.skip;
       L.plane = pa.plane;
@@ -822,7 +823,14 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
     } else if (!band_out) {
       FlagList fl{(int2*)P[20], (unsigned long long*)P[21], flag_cap};
       if (!spec_done) {
-        if ((e = launch_pairs(pmap, fl)) != cudaSuccess) return h->cuda_fail(e, "pair kernel launch");
+        // One contraction launch in this call: its tile list goes through the
+        // handle's pinned staging, so the host queues the launch behind the
+        // prep passes at once instead of waiting for them (the staging is
+        // free: every call has synchronised before it returns).
+        int2* stage = (tc && h->reserve_pinned(sizeof(int2) * (size_t)std::max<int64_t>(tc_tiles, 1)))
+                          ? (int2*)h->pinned
+                          : nullptr;
+        if ((e = launch_pairs(pmap, fl, stage)) != cudaSuccess) return h->cuda_fail(e, "pair kernel launch");
         ++launches;
       }
       if (h->timing) cudaEventRecord(h->ev[2], st);

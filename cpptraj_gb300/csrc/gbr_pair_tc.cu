@@ -38,6 +38,7 @@
 #include "gbr_common.cuh"
 #include "gbr_internal.h"
 #include "gbr_mbar.cuh"
+#include <cstring>
 
 namespace gbr {
 
@@ -1232,10 +1233,15 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
     n = tc_build_tiles(L.map, tiles, i_base, jt_base, i_end, jt_end, ti_frames);
     if (n == 0) return cudaSuccess;
     if (!L.tile_buf || n > L.tile_cap) return cudaErrorInvalidValue;
-    e = cudaMemcpyAsync(L.tile_buf, tiles.data(), sizeof(int2) * n, cudaMemcpyHostToDevice, st);
+    if (L.tile_stage) {
+      std::memcpy(L.tile_stage, tiles.data(), sizeof(int2) * n);
+      e = cudaMemcpyAsync(L.tile_buf, L.tile_stage, sizeof(int2) * n, cudaMemcpyHostToDevice, st);
+    } else {
+      // From pageable memory cudaMemcpyAsync returns after the source has
+      // been consumed, so `tiles` may go out of scope.
+      e = cudaMemcpyAsync(L.tile_buf, tiles.data(), sizeof(int2) * n, cudaMemcpyHostToDevice, st);
+    }
     if (e != cudaSuccess) return e;
-    // The copy reads `tiles` asynchronously from pageable memory; cudaMemcpyAsync
-    // from pageable memory returns after the source has been consumed.
   }
   const int ka = (L.variant == 0)   ? 64
                  : (L.variant == 1) ? 32

@@ -135,6 +135,63 @@ def test_clustered_sorted_layout(h, pipeline, precision):
         h.set_option(gbrmsd.OPT_TC_PIPELINE, gbrmsd.TC_PIPELINE_DEFAULT)
 
 
+@pytest.mark.parametrize("pipeline", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("precision", ["fp32", "tc"])
+def test_clustered_full_row_ranges_bit_identical(h, pipeline, precision):
+    # FULL output between two clustered sets: row ranges (target frames) shift
+    # the tiles, so a pair whose references are its tile's reads the tile's
+    # staged frame terms in one call and forms them from global memory in
+    # another.  Both use the same rounded arithmetic: the same bits.
+    X, _ = synth.clustered(5, 700, 300, 12, 0.8)
+    A, B = X[:300], X[300:]
+    h.set_option(gbrmsd.OPT_TC_PIPELINE, pipeline)
+    try:
+        whole = run(h, A, B, precision=precision)
+        assert h.stats()["n_refs"] >= 2
+        parts = [run(h, A, B, precision=precision, row_begin=a, row_end=b)
+                 for a, b in ((0, 1), (1, 77), (77, 333), (333, 400))]
+        np.testing.assert_array_equal(np.concatenate(parts), whole)
+    finally:
+        h.set_option(gbrmsd.OPT_TC_PIPELINE, gbrmsd.TC_PIPELINE_DEFAULT)
+
+
+@pytest.mark.parametrize("pipeline", [0, 3, 4])
+@pytest.mark.parametrize("precision", ["fp32", "tc"])
+def test_clustered_tri_sorted_vs_rows(h, pipeline, precision):
+    # A whole triangle over reference-sorted positions computes some pairs
+    # with their two frames' roles exchanged (the RMSD is symmetric, its last
+    # bit need not be); row ranges keep the original order.
+    X, _ = synth.clustered(5, 700, 300, 12, 0.8)
+    h.set_option(gbrmsd.OPT_TC_PIPELINE, pipeline)
+    try:
+        whole = run(h, X, precision=precision)
+        parts = np.concatenate([run(h, X, precision=precision, row_begin=a, row_end=b)
+                                for a, b in ((0, 1), (1, 250), (250, 699), (699, 700))])
+        np.testing.assert_allclose(parts, whole, rtol=4e-7, atol=1e-7)
+    finally:
+        h.set_option(gbrmsd.OPT_TC_PIPELINE, gbrmsd.TC_PIPELINE_DEFAULT)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "tc"])
+def test_many_references(h, precision):
+    # widely scattered frames (independent displacements up to 3 A over 300
+    # atoms): the k-centre choice goes past 32 references when allowed 64
+    X, m = synth.trajectory(5, 3000, 300, 0.1, 3.0, np.float32, True)
+    h.set_option(gbrmsd.OPT_MAX_REFS, 64)
+    try:
+        _check(h, X, m, precision)
+        assert h.stats()["n_refs"] > 32, h.stats()
+    finally:
+        h.set_option(gbrmsd.OPT_MAX_REFS, 32)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "tc"])
+def test_nofit_clustered(h, precision):
+    # several references without fitting (the k-centre scans then fit every frame)
+    X, _ = synth.clustered(7, 400, 200, 6, 0.8)
+    _check(h, X, None, precision, mode="nofit")
+
+
 @pytest.mark.parametrize("precision", _precisions())
 def test_nofit(h, precision):
     X, m = synth.trajectory(8, 130, 77, 0.2, 2.0, np.float32, True)

@@ -75,7 +75,7 @@ struct gbr_handle {
   int tc_ok = 0;
   int tc_variant = -1;  // -1: pairs of SMs, stage shape chosen by atom count (see gbr_set_option)
   bool host_out_direct = true;  // kernels store into pinned host output in place
-  bool input_overlap = false;   // the contraction starts on input chunks that have landed
+  bool input_overlap = true;    // the contraction starts on input chunks that have landed
   int64_t band_floats = 0;      // gbr_write_cmatrix's band size (0: the streaming default)
   // batched path: auxiliary streams, fork/join events, pinned staging,
   // the captured graph of the last batch signature, the autotuner table
@@ -97,6 +97,12 @@ struct gbr_handle {
   // 0-7 input chunks, 8-13 output bands, 14-17 streamed bands (computed, copied), 21-23 joins
   static constexpr int kXev = 24;
   cudaEvent_t xev[kXev] = {};
+  // Input overlap: the chunk passes run on their own stream, so that the
+  // early contraction stages queued on the caller's stream (on a capped
+  // number of SMs) do not hold them back; pev: one per chunk, fork, join.
+  cudaStream_t prep_stream = nullptr;
+  static constexpr int kPev = 16;
+  cudaEvent_t pev[kPev] = {};
 
   int fail(int code, const char* fmt, ...) {
     char buf[512];
@@ -157,6 +163,17 @@ struct gbr_handle {
       if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
     return true;
   }
+  bool ensure_prep_stream() {
+    if (prep_stream) return true;
+    if (cudaStreamCreateWithFlags(&prep_stream, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaGetLastError();
+      prep_stream = nullptr;
+      return false;
+    }
+    for (auto& e : pev)
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
+    return true;
+  }
   bool reserve_out(size_t floats) {
     if (floats <= outbuf_cap) return true;
     if (outbuf) cudaFree(outbuf);
@@ -181,6 +198,9 @@ struct gbr_handle {
     if (pinned) cudaFreeHost(pinned);
     if (xfer) cudaStreamDestroy(xfer);
     for (auto& e : xev)
+      if (e) cudaEventDestroy(e);
+    if (prep_stream) cudaStreamDestroy(prep_stream);
+    for (auto& e : pev)
       if (e) cudaEventDestroy(e);
   }
 };

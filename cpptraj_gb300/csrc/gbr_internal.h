@@ -209,6 +209,8 @@ struct TcLaunch {
                         // (host memory across the link); 0: each pair stored directly (device memory)
   const int* skip;      // device int or nullptr: when it reads non-zero at launch, the kernel does nothing
   const BwdArgs* bwd;   // non-null: the backward pass (variants 2 and 3, one set, TRI, one reference)
+  int cluster_cap;      // pairs of SMs: > 0 caps the persistent grid at this many clusters, < 0 leaves
+                        // that many of the resident clusters free
   int2* tile_stage;     // pinned host buffer of tile_cap entries, or nullptr: the tile list is uploaded
                         // from it (the host returns at once) instead of from pageable memory (the host
                         // waits until the copy has run, i.e. until the stream's earlier work is done)

@@ -1174,7 +1174,7 @@ int64_t tc_tile_frame_end(const TcTileInfo& info, int2 tile, int variant) {
 // as can be resident at once (one CTA per SM), at most one per tile.
 template <class PC, bool BWD = false>
 static cudaError_t launch_pair_kernel(const CUtensorMap& mAh, const CUtensorMap& mAl, const CUtensorMap& mBh,
-                                      const CUtensorMap& mBl, const TcParams& P, cudaStream_t st) {
+                                      const CUtensorMap& mBl, const TcParams& P, cudaStream_t st, int cap = 0) {
   cudaError_t e =
       cudaFuncSetAttribute(k_pairs_tc2<PC, BWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, PC::SMEM2_BYTES);
   if (e != cudaSuccess) return e;
@@ -1210,7 +1210,10 @@ static cudaError_t launch_pair_kernel(const CUtensorMap& mAh, const CUtensorMap&
     max_clusters = n;
     cached_clusters[dev].store(n, std::memory_order_relaxed);
   }
-  const int64_t nc = std::min<int64_t>(P.n_tiles, (int64_t)max_clusters);
+  // cap > 0: at most cap clusters; cap < 0: leave -cap of the resident clusters free
+  int64_t nc = std::min<int64_t>(P.n_tiles, (int64_t)max_clusters);
+  if (cap > 0) nc = std::min<int64_t>(nc, cap);
+  if (cap < 0) nc = std::min<int64_t>(nc, std::max<int64_t>(1, (int64_t)max_clusters + cap));
   cfg.gridDim = dim3((unsigned)(2 * nc), 1, 1);
   return cudaLaunchKernelEx(&cfg, k_pairs_tc2<PC, BWD>, mAh, mAl, mBh, mBl, P);
 }
@@ -1281,9 +1284,9 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
     return cudaGetLastError();
   }
   if (pair) {
-    e = (L.variant == 3)   ? launch_pair_kernel<PairDeep>(mAh, mAl, mBh, mBl, P, st)
-        : (L.variant == 4) ? launch_pair_kernel<PairWide>(mAh, mAl, mBh, mBl, P, st)
-                           : launch_pair_kernel<PairShallow>(mAh, mAl, mBh, mBl, P, st);
+    e = (L.variant == 3)   ? launch_pair_kernel<PairDeep>(mAh, mAl, mBh, mBl, P, st, L.cluster_cap)
+        : (L.variant == 4) ? launch_pair_kernel<PairWide>(mAh, mAl, mBh, mBl, P, st, L.cluster_cap)
+                           : launch_pair_kernel<PairShallow>(mAh, mAl, mBh, mBl, P, st, L.cluster_cap);
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
   }

@@ -284,13 +284,12 @@ int gbr_get_stats(const gbr_handle *h, gbr_stats *out);
  *   GBR_OPT_BAND_FLOATS  band size in floats of gbr_write_cmatrix's streamed
  *                        triangle (default 2^28; at least one row)
  *   GBR_OPT_INPUT_OVERLAP  pinned host input of one frame set, triangle into
- *                        device or directly stored host memory: 1 = the
- *                        contraction starts on the frames that have landed
- *                        while the rest of the input transfers, 0 = it starts
- *                        after the whole input is prepared (default: the
- *                        per-chunk preparation then hides behind the
- *                        transfer, which pays more while it is not much
- *                        faster than the transfer itself)
+ *                        device or directly stored host memory: 1 (default) =
+ *                        the contraction starts on the frames that have
+ *                        landed while the rest of the input transfers (the
+ *                        first tiles on part of the SMs, beside the per-chunk
+ *                        preparation), 0 = it starts after the whole input is
+ *                        prepared
  */
 enum gbr_option { GBR_OPT_TAU = 0, GBR_OPT_MAX_REFS = 1, GBR_OPT_TOL = 2, GBR_OPT_TIMING = 3,
                   GBR_OPT_TC_PIPELINE = 4, GBR_OPT_HOST_OUT = 5, GBR_OPT_INPUT_OVERLAP = 6,

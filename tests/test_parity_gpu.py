@@ -395,7 +395,7 @@ def test_pinned_input_speculative_prep(h, sig_hi, expect_refs, overlap):
     try:
         run(h, hX, tgt_mass=m, precision="tc", out=hout)
     finally:
-        h.set_option(gbrmsd.OPT_INPUT_OVERLAP, 0)
+        h.set_option(gbrmsd.OPT_INPUT_OVERLAP, 1)  # the default
     assert h.stats()["n_refs"] == refs_dev
     if expect_refs is not None:
         assert refs_dev == expect_refs
@@ -405,8 +405,8 @@ def test_pinned_input_speculative_prep(h, sig_hi, expect_refs, overlap):
 
 
 def test_pinned_input_late_speculation_failure(h):
-    # With GBR_OPT_INPUT_OVERLAP the contraction starts on the chunks that
-    # have landed; a far frame in the last chunk ends the speculation after
+    # With GBR_OPT_INPUT_OVERLAP (the default) the contraction starts on the
+    # chunks that have landed; a far frame in the last chunk ends the speculation after
     # several stages already ran.  Their results are discarded and the general
     # path recomputes the whole triangle: bit-identical to the device-resident
     # call.
@@ -430,4 +430,4 @@ def test_pinned_input_late_speculation_failure(h):
         np.testing.assert_array_equal(hout.numpy(), dev1)
     finally:
         h.set_option(gbrmsd.OPT_MAX_REFS, 32)
-        h.set_option(gbrmsd.OPT_INPUT_OVERLAP, 0)
+        h.set_option(gbrmsd.OPT_INPUT_OVERLAP, 1)  # the default

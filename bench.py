@@ -1000,6 +1000,8 @@ def main():
                 "h2d_bytes_per_step": int(hX.numel() * 4 + hm.numel() * 8),
                 "d2h_bytes_per_step": int(hout.numel() * 4), "ms_per_step": e2e_ms,
                 "result_path": "kernels store into the pinned host triangle over the host link",
+                "input_path": "8 chunks on a copy stream; per-chunk passes as they land, the first quarter of "
+                              "the contraction's tiles beside them on all but 10 clusters",
                 "ms_per_step_banded_copy": e2e_banded_ms},
         "gpu_launches": launches,
         "clocks": clk,

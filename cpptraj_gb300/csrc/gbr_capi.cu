@@ -752,13 +752,26 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
     int next_stage = 0;
     bool spec_terms = false;
     FlagList fl_spec{(int2*)P[20], (unsigned long long*)P[21], flag_cap};
+    bool rest_launched = false;
+    // The tiles no stage took, on every SM, behind the last chunk's passes
+    // on their stream (not behind the stages, which may still be running),
+    // queued as soon as the last chunk is built: before prep's host-side
+    // reference-count check, which the speculation flag covers.
+    auto launch_rest = [&]() -> cudaError_t {
+      if (rest_launched || !spec_terms || staged_end >= n_stage_tiles) return cudaSuccess;
+      rest_launched = true;
+      ++launches;
+      return launch_tc(map, fl_spec, terms1, staged_end, n_stage_tiles - staged_end, (const int*)P[25] + 1, nullptr,
+                       0, ps);
+    };
     std::function<cudaError_t(int64_t)> on_built = [&](int64_t built_end) -> cudaError_t {
       int c1 = next_stage;
       while (c1 < n_chunks && chunk_end[c1] <= built_end) ++c1;
       if (c1 == next_stage) return cudaSuccess;
       const int64_t t0 = stage_off[next_stage], t1 = stage_off[c1];
       next_stage = c1;
-      if (t1 == t0 || t0 >= stage_budget) return cudaSuccess;  // beyond the budget: the final launch
+      if (t1 == t0 || t0 >= stage_budget)  // beyond the budget: the final launch
+        return (c1 == n_chunks) ? launch_rest() : cudaSuccess;
       cudaError_t e2;
       if (!spec_terms) {  // reference-pair terms of reference 0, as run_finish computes them
         FinishArgs f1 = fa;
@@ -778,6 +791,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
                      split ? -kStageFreeClusters : 0);
       staged_end = t1;
       ++launches;
+      if (e2 == cudaSuccess && c1 == n_chunks) e2 = launch_rest();
       return e2;
     };
     if (overlap) {
@@ -787,14 +801,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
     if (n_chunks > 0) pa.spec_build = &fa;
     PrepOut po;
     if ((e = run_prep(pa, po, ps)) != cudaSuccess) return h->cuda_fail(e, "prep");
-    if (overlap && po.built && spec_terms && staged_end < n_stage_tiles) {
-      // The tiles no stage took, on every SM, behind the last chunk's passes
-      // (on their stream: not behind the stages, which may still be running).
-      if ((e = launch_tc(map, fl_spec, terms1, staged_end, n_stage_tiles - staged_end, (const int*)P[25] + 1,
-                         nullptr, 0, ps)) != cudaSuccess)
-        return h->cuda_fail(e, "pair kernel launch");
-      ++launches;
-    }
+    if (overlap && po.built && (e = launch_rest()) != cudaSuccess) return h->cuda_fail(e, "pair kernel launch");
     if (split) {  // everything after prep (and the remainder) follows it on the caller's stream
       cudaEventRecord(h->pev[h->kPev - 1], ps);
       cudaStreamWaitEvent(st, h->pev[h->kPev - 1], 0);

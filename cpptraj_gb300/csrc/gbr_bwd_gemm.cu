@@ -307,12 +307,22 @@ __device__ __forceinline__ void split_store(float v, __half* hi, __half* lo, int
   lo[idx] = __float2half_rn(v - __half2float(h));
 }
 
-// S = B + B^T (B: upper 3x3 blocks, row stride ldB), scaled and split into
-// FP16 hi/lo rows of stride ldS; 64 x 64 tile pairs (I <= J), 32 x 8 threads.
+// S = B + B^T, scaled and split into FP16 hi/lo rows of stride ldS.  B holds
+// the upper 3x3 blocks (block row i < block column j, written by the pair
+// pass; nothing else of B is written or read), so
+//   S[r][c] = B[r][c] for r/3 < c/3,  B[c][r] for r/3 > c/3,  0 for r/3 == c/3.
+// One 64 x 64 tile of B per block (tile pairs I <= J, 32 x 8 threads, two
+// columns per thread): S at (I, J) and, transposed, at (J, I).
+__device__ __forceinline__ void split_store2(float v0, float v1, __half* hi, __half* lo, int64_t idx) {
+  const __half2 h = __floats2half2_rn(v0, v1);
+  const float2 hf = __half22float2(h);
+  *reinterpret_cast<__half2*>(hi + idx) = h;
+  *reinterpret_cast<__half2*>(lo + idx) = __floats2half2_rn(v0 - hf.x, v1 - hf.y);
+}
 __global__ void __launch_bounds__(256) k_split_sym(const float* __restrict__ B, int64_t n, int64_t ldB,
                                                    const unsigned int* maxbits, __half* Shi, __half* Slo,
                                                    int64_t ldS, float* scl) {
-  __shared__ float t1[64][65], t2[64][65];
+  __shared__ float t1[64][65];
   const float s = split_scale(*maxbits);
   if (blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) scl[0] = 1.0f / s;
   const int64_t tiles = (n + 63) / 64;
@@ -323,22 +333,57 @@ __global__ void __launch_bounds__(256) k_split_sym(const float* __restrict__ B, 
   while (ti > 0 && cum(ti) > l) --ti;
   while (cum(ti + 1) <= l) ++ti;
   const int64_t tj = ti + (l - cum(ti));
-  const int x = threadIdx.x, y0 = threadIdx.y;
-  for (int y = y0; y < 64; y += 8)
-    for (int xx = x; xx < 64; xx += 32) {
-      const int64_t r1 = ti * 64 + y, c1 = tj * 64 + xx;
-      const int64_t r2 = tj * 64 + y, c2 = ti * 64 + xx;
-      t1[y][xx] = (r1 < n && c1 < n) ? B[r1 * ldB + c1] : 0.f;
-      t2[y][xx] = (r2 < n && c2 < n) ? B[r2 * ldB + c2] : 0.f;
+  const int x2 = 2 * threadIdx.x, y0 = threadIdx.y;
+  const bool vec = ((n | ldB | ldS) & 1) == 0;  // pairs of columns stay inside rows and aligned
+  for (int y = y0; y < 64; y += 8) {
+    const int64_t r = ti * 64 + y, c = tj * 64 + x2;
+    float v0 = 0.f, v1 = 0.f;
+    if (r < n) {
+      if (vec && c + 1 < n) {
+        const float2 b = *reinterpret_cast<const float2*>(B + r * ldB + c);
+        v0 = b.x;
+        v1 = b.y;
+      } else {
+        if (c < n) v0 = B[r * ldB + c];
+        if (c + 1 < n) v1 = B[r * ldB + c + 1];
+      }
     }
+    t1[y][x2] = (r / 3 < c / 3) ? v0 : 0.f;
+    t1[y][x2 + 1] = (r / 3 < (c + 1) / 3) ? v1 : 0.f;
+  }
   __syncthreads();
-  for (int y = y0; y < 64; y += 8)
-    for (int xx = x; xx < 64; xx += 32) {
-      const int64_t r1 = ti * 64 + y, c1 = tj * 64 + xx;
-      const int64_t r2 = tj * 64 + y, c2 = ti * 64 + xx;
-      if (r1 < n && c1 < n) split_store((t1[y][xx] + t2[xx][y]) * s, Shi, Slo, r1 * ldS + c1);
-      if (ti != tj && r2 < n && c2 < n) split_store((t2[y][xx] + t1[xx][y]) * s, Shi, Slo, r2 * ldS + c2);
+  for (int y = y0; y < 64; y += 8) {
+    // (I, J): the upper entries, and on a diagonal tile the lower ones by transposition
+    {
+      const int64_t r = ti * 64 + y, c = tj * 64 + x2;
+      float v0 = t1[y][x2], v1 = t1[y][x2 + 1];
+      if (ti == tj) {
+        v0 += t1[x2][y];
+        v1 += t1[x2 + 1][y];
+      }
+      if (r < n) {
+        if (vec && c + 1 < n) {
+          split_store2(v0 * s, v1 * s, Shi, Slo, r * ldS + c);
+        } else {
+          if (c < n) split_store(v0 * s, Shi, Slo, r * ldS + c);
+          if (c + 1 < n) split_store(v1 * s, Shi, Slo, r * ldS + c + 1);
+        }
+      }
     }
+    // (J, I): the transpose
+    if (ti != tj) {
+      const int64_t r = tj * 64 + y, c = ti * 64 + x2;
+      const float v0 = t1[x2][y], v1 = t1[x2 + 1][y];
+      if (r < n) {
+        if (vec && c + 1 < n) {
+          split_store2(v0 * s, v1 * s, Shi, Slo, r * ldS + c);
+        } else {
+          if (c < n) split_store(v0 * s, Shi, Slo, r * ldS + c);
+          if (c + 1 < n) split_store(v1 * s, Shi, Slo, r * ldS + c + 1);
+        }
+      }
+    }
+  }
 }
 
 // planeT[a][k] = plane[k][a] scaled and split (k < K rows of the plane,

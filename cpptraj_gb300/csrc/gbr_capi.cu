@@ -1194,8 +1194,7 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   fa.self_terms = po.self_terms;
   if ((e = run_finish(fa, st)) != cudaSuccess) return h->cuda_fail(e, "finish");
   launches += po.self_terms ? 1 : 2;
-  float* B = (float*)P[20];
-  cudaMemsetAsync(B, 0, sizeof(float) * 3 * F * ldB, st);
+  float* B = (float*)P[20];  // the pair pass writes its upper 3x3 blocks, all that is read of it
   cudaMemsetAsync(P[21], 0, sizeof(float) * 9 * F, st);
   cudaMemsetAsync(P[22], 0, sizeof(float) * F, st);
   cudaMemsetAsync(P[35], 0, sizeof(int), st);

@@ -256,12 +256,10 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
   std::vector<double> w_h, wref_h;
   if (tgt_mass) {
     w_h.resize(N);
-    if (cudaMemcpy(w_h.data(), tgt_mass, sizeof(double) * N, cudaMemcpyDefault) != cudaSuccess)
-      return h->cuda_fail(cudaGetLastError(), "reading tgt_mass");
+    if (!read_host_doubles(w_h.data(), tgt_mass, N)) return h->cuda_fail(cudaGetLastError(), "reading tgt_mass");
     if (ref_mass && tgt_xyz != nullptr) {
       wref_h.resize(N);
-      if (cudaMemcpy(wref_h.data(), ref_mass, sizeof(double) * N, cudaMemcpyDefault) != cudaSuccess)
-        return h->cuda_fail(cudaGetLastError(), "reading ref_mass");
+      if (!read_host_doubles(wref_h.data(), ref_mass, N)) return h->cuda_fail(cudaGetLastError(), "reading ref_mass");
     }
   }
   double Wsum = 0.0;
@@ -417,17 +415,32 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
     if (!ref_dev) cudaMemcpyAsync(P[0], ref_xyz, esz * 3 * (size_t)N * n_ref, cudaMemcpyDefault, st);
     if (tgt_xyz && !tgt_dev) cudaMemcpyAsync(P[1], tgt_xyz, esz * 3 * (size_t)N * n_tgt, cudaMemcpyDefault, st);
   }
-  // Copies from pageable memory (weights, tile list) go before the chunk
-  // copies are queued: a pageable copy returns only once it has been done,
-  // and behind the queued chunks that would hold the host until the whole
-  // input has landed.
+  // The small copies (weights, staged tile list) go on the caller's stream
+  // before the chunk copies are queued (behind them they would wait for the
+  // whole input). With chunked input they leave from a tail of the handle's
+  // pinned staging, past the part a single contraction launch stages its
+  // tile list in, so that queueing them does not hold the host (a pageable
+  // copy returns only once it is done). The staging is free: every call
+  // has synchronised before it returns.
+  const size_t pin_tail = ((sizeof(int2) * (size_t)std::max<int64_t>(tc_tiles, 1)) + 15) & ~size_t(15);
+  const size_t pin_w = ((sizeof(double) * (size_t)N) + 15) & ~size_t(15);
+  char* pin = (chunk_in && !rs && h->reserve_pinned(pin_tail + 2 * pin_w + sizeof(int2) * (size_t)tc_tiles))
+                  ? (char*)h->pinned + pin_tail
+                  : nullptr;
+  auto put = [&](void* dst, const void* src, size_t bytes, size_t at) {
+    if (pin) {
+      std::memcpy(pin + at, src, bytes);
+      src = pin + at;
+    }
+    cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+  };
   double* d_w = tgt_mass ? (double*)P[2] : nullptr;
   double* d_wref = nullptr;
   if (tgt_mass) {
-    cudaMemcpyAsync(d_w, w_h.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st);
+    put(d_w, w_h.data(), sizeof(double) * N, 0);
     if (!wref_h.empty()) {
       d_wref = (double*)P[3];
-      cudaMemcpyAsync(d_wref, wref_h.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st);
+      put(d_wref, wref_h.data(), sizeof(double) * N, pin_w);
     }
   }
   // Chunked input of one frame set, triangle into device (or mapped host)
@@ -437,30 +450,18 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
   // through a chunk, the tiles ready by then are launched behind it.
   const int tc_variant = (h->tc_variant >= 0) ? h->tc_variant : auto_tc_variant(N);
   bool overlap = h->input_overlap && n_chunks > 0 && tc && map.tri && !tgt_xyz && out_dev;
-  std::vector<int64_t> stage_off;
-  std::vector<int2> stage_tiles;
+  int64_t stage_off[9] = {};
   if (overlap) {
-    TcTileInfo info;
-    std::vector<int2> tiles;
-    const int64_t nt = tc_build_tile_list(map, tiles, info, tc_variant);
-    if (nt > tc_tiles) {
+    // Grouped by stage straight into the pinned staging when there is one.
+    std::vector<int2>& sorted = h->tile_sorted;
+    if (!pin) sorted.resize((size_t)std::max<int64_t>(tc_tiles, 1));
+    int2* dst = pin ? (int2*)(pin + 2 * pin_w) : sorted.data();
+    const int64_t nt = build_tiles_staged(tc_tile_grid(map, tc_variant), chunk_end, n_chunks, F, dst, tc_tiles,
+                                          stage_off, h->tile_scratch);
+    if (nt < 0)
       overlap = false;
-    } else {
-      std::vector<int> stage(nt);
-      stage_off.assign(n_chunks + 1, 0);
-      for (int64_t t = 0; t < nt; ++t) {
-        const int64_t fe = std::min(tc_tile_frame_end(info, tiles[t], tc_variant), F);
-        int c = 0;
-        while (c < n_chunks - 1 && chunk_end[c] < fe) ++c;
-        stage[t] = c;
-        stage_off[c + 1]++;
-      }
-      for (int c = 0; c < n_chunks; ++c) stage_off[c + 1] += stage_off[c];
-      stage_tiles.resize(nt);
-      std::vector<int64_t> fill(stage_off.begin(), stage_off.end() - 1);
-      for (int64_t t = 0; t < nt; ++t) stage_tiles[fill[stage[t]]++] = tiles[t];
-      if (nt > 0) cudaMemcpyAsync(P[26], stage_tiles.data(), sizeof(int2) * nt, cudaMemcpyHostToDevice, st);
-    }
+    else if (nt > 0)
+      cudaMemcpyAsync(P[26], dst, sizeof(int2) * nt, cudaMemcpyHostToDevice, st);
   }
   if (chunk_in) {
     cudaEventRecord(h->xev[h->kXev - 1], st);  // the copies follow earlier work on the caller's stream

@@ -5,6 +5,7 @@
 
 #include <cstdarg>
 #include <cstdio>
+#include <cstring>
 #include <map>
 #include <string>
 #include <utility>
@@ -49,6 +50,21 @@ inline bool is_pinned_or_device(const void* p) {
   return at.type != cudaMemoryTypeUnregistered;
 }
 
+// Reads n doubles the caller passed (masses) into host memory: a plain copy
+// from host memory, pinned or not, and a synchronous copy from device memory.
+inline bool read_host_doubles(double* dst, const void* src, int n) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, src) != cudaSuccess) {
+    cudaGetLastError();
+    at.type = cudaMemoryTypeUnregistered;
+  }
+  if (at.type == cudaMemoryTypeUnregistered || at.type == cudaMemoryTypeHost) {
+    std::memcpy(dst, src, sizeof(double) * (size_t)n);
+    return true;
+  }
+  return cudaMemcpy(dst, src, sizeof(double) * (size_t)n, cudaMemcpyDefault) == cudaSuccess;
+}
+
 }  // namespace gbr
 
 struct gbr_handle {
@@ -85,6 +101,9 @@ struct gbr_handle {
   void* pinned = nullptr;
   size_t pinned_cap = 0;
   std::vector<unsigned long long> graph_sig;
+  // Host scratch of the input-overlap tile grouping, reused across calls.
+  std::vector<int2> tile_sorted;
+  std::vector<int64_t> tile_scratch;
   cudaGraphExec_t graph_exec = nullptr;
   int graph_launches = 0;
   bool last_batch_graph = false;

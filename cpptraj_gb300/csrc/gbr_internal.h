@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "gbr_common.cuh"
+#include "gbr_tiles.h"
 
 namespace gbr {
 
@@ -220,9 +221,8 @@ struct TcTileInfo {
   int64_t i_base, jt_base, i_end, jt_end;
 };
 int64_t tc_build_tile_list(const OutMap& m, std::vector<int2>& tiles, TcTileInfo& info, int variant = 1);
-// Frame range [0, end) a tile of this list reads (reference and target rows),
-// for launching tiles as their frames become ready; unclamped.
-int64_t tc_tile_frame_end(const TcTileInfo& info, int2 tile, int variant);
+// The output region and tile shape of that list (for build_tiles_staged).
+TileGrid tc_tile_grid(const OutMap& m, int variant);
 // Reference frames per launch tile of a tensor-core kernel shape.
 int tc_launch_tile_rows(int variant);
 cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st);

@@ -1119,40 +1119,36 @@ int tc_supported(int device) {
   return (major == 10 && minor == 3 && encode_fn() != nullptr) ? 1 : 0;
 }
 
-int tc_tile_rows() { return TI; }
-int tc_tile_cols() { return TJ; }
+// The output region a tile list covers, with `rows` reference frames per
+// launch tile.
+static TileGrid grid_of(const OutMap& m, int rows) {
+  TileGrid g{};
+  if (m.tri) {
+    g.i_base = m.row_begin;
+    g.i_end = m.row_end;
+    g.jt_base = m.row_begin;
+    g.jt_end = m.n_tgt;
+  } else {
+    g.i_base = 0;
+    g.i_end = m.n_ref;
+    g.jt_base = m.row_begin;
+    g.jt_end = m.row_end;
+  }
+  g.rows = rows;
+  g.cols = TJ;
+  g.tri = m.tri;
+  return g;
+}
 
-// Tile list in grouped order: groups of G tile-rows are swept column by
-// column so the CTAs in flight share A and B frames in L2.
+// Tile list in grouped order (gbr_tiles.h).
 int64_t tc_build_tiles(const OutMap& m, std::vector<int2>& tiles, int64_t& i_base, int64_t& jt_base,
                        int64_t& i_end, int64_t& jt_end, int ti_frames = TI) {
-  if (m.tri) {
-    i_base = m.row_begin;
-    i_end = m.row_end;
-    jt_base = m.row_begin;
-    jt_end = m.n_tgt;
-  } else {
-    i_base = 0;
-    i_end = m.n_ref;
-    jt_base = m.row_begin;
-    jt_end = m.row_end;
-  }
-  tiles.clear();
-  const int64_t Ti = (i_end - i_base + ti_frames - 1) / ti_frames, Tj = (jt_end - jt_base + TJ - 1) / TJ;
-  const int64_t G = 8;
-  for (int64_t g0 = 0; g0 < Ti; g0 += G) {
-    for (int64_t tj = 0; tj < Tj; ++tj) {
-      for (int64_t ti = g0; ti < std::min(Ti, g0 + G); ++ti) {
-        if (m.tri) {
-          const int64_t ilo = i_base + ti * ti_frames;
-          const int64_t jhi = jt_base + tj * TJ + TJ - 1;
-          if (jhi <= ilo) continue;  // no pair with target > reference
-        }
-        tiles.push_back(make_int2((int)ti, (int)tj));
-      }
-    }
-  }
-  return (int64_t)tiles.size();
+  const TileGrid g = grid_of(m, ti_frames);
+  i_base = g.i_base;
+  i_end = g.i_end;
+  jt_base = g.jt_base;
+  jt_end = g.jt_end;
+  return build_tiles_grouped(g, tiles);
 }
 
 // Reference frames per CTA tile and per launch tile of each kernel shape.
@@ -1164,11 +1160,8 @@ int64_t tc_build_tile_list(const OutMap& m, std::vector<int2>& tiles, TcTileInfo
   return tc_build_tiles(m, tiles, info.i_base, info.jt_base, info.i_end, info.jt_end, launch_tile_rows(variant));
 }
 
-int64_t tc_tile_frame_end(const TcTileInfo& info, int2 tile, int variant) {
-  const int64_t i1 = info.i_base + (int64_t)(tile.x + 1) * launch_tile_rows(variant);
-  const int64_t j1 = info.jt_base + (int64_t)(tile.y + 1) * TJ;
-  return std::max(i1, j1);
-}
+TileGrid tc_tile_grid(const OutMap& m, int variant) { return grid_of(m, launch_tile_rows(variant)); }
+
 
 // Launch of the pair-of-SMs kernel: clusters of two CTAs, as many clusters
 // as can be resident at once (one CTA per SM), at most one per tile.
@@ -1226,11 +1219,13 @@ cudaError_t run_pairs_tc(const TcLaunch& L, cudaStream_t st) {
   const bool pair = (L.variant >= 2);
   const int ti_frames = launch_tile_rows(L.variant);
   if (L.ready_tiles > 0) {
-    // The caller uploaded the list already (batched / graph-captured path).
-    TcTileInfo info;
-    std::vector<int2> none;
-    tc_build_tiles(L.map, none, info.i_base, info.jt_base, info.i_end, info.jt_end, ti_frames);
-    i_base = info.i_base; jt_base = info.jt_base; i_end = info.i_end; jt_end = info.jt_end;
+    // The caller uploaded the list already (batched, graph-captured and
+    // input-overlap paths).
+    const TileGrid g = grid_of(L.map, ti_frames);
+    i_base = g.i_base;
+    jt_base = g.jt_base;
+    i_end = g.i_end;
+    jt_end = g.jt_end;
     n = L.ready_tiles;
   } else {
     n = tc_build_tiles(L.map, tiles, i_base, jt_base, i_end, jt_end, ti_frames);

@@ -35,33 +35,6 @@ namespace gbr {
 constexpr int kMaxRefs = 64;
 
 // --------------------------------------------------------------------------
-// Block reductions (blockDim.x a multiple of 32, <= 1024).
-// --------------------------------------------------------------------------
-template <int NV>
-__device__ __forceinline__ void block_sum_f64(double (&v)[NV], double* scratch /* >= 32*NV */) {
-#pragma unroll
-  for (int k = 0; k < NV; ++k) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-  }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  __syncthreads();
-  if (lane == 0) {
-#pragma unroll
-    for (int k = 0; k < NV; ++k) scratch[k * 32 + warp] = v[k];
-  }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    double s = (lane < nw) ? scratch[k * 32 + lane] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    v[k] = s;
-  }
-  __syncthreads();
-}
-
-// --------------------------------------------------------------------------
 // FP64 QCP on a 3x3 cross-covariance A[p][q] = sum w t_p r_q (target first):
 // the largest eigenvalue lambda of the key matrix by Newton from E0, and the
 // proper rotation R (row-major) minimising sum w |R t - r|^2.  R is the

@@ -83,16 +83,35 @@ namespace cg = cooperative_groups;
 // the cluster must call it (it contains block and cluster barriers).
 template <int NV>
 __device__ __forceinline__ void cluster_sum_f64(double (&v)[NV], double* red, double* slots, double* bc) {
-  block_sum_f64<NV>(v, red);
+  static_assert(NV <= 32, "lane k keeps value k");
+  // This CTA's totals: a shuffle tree per warp, then warp 0 alone adds the
+  // warps' sums by the same tree (FP64 adds are slow on GB300: the other
+  // warps would only repeat them), lane k keeping value k.
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();  // `red` may still be read by an earlier reduction
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) red[k * 32 + warp] = v[k];
+  }
+  __syncthreads();
   cg::cluster_group cl = cg::this_cluster();
   const unsigned rank = cl.block_rank(), n = cl.num_blocks();
-  // Thread k handles value k (the slots of the NV values side by side, each
-  // summed in rank order).
-  if (threadIdx.x < NV) {
+  // The CTA totals go to CTA 0's slots (the NV values side by side, each
+  // summed in rank order below).
+  if (warp == 0) {
     double* dst = cl.map_shared_rank(slots, 0);
 #pragma unroll
-    for (int k = 0; k < NV; ++k)
-      if ((int)threadIdx.x == k) dst[rank * NV + k] = v[k];
+    for (int k = 0; k < NV; ++k) {
+      double t = (lane < nw) ? red[k * 32 + lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (lane == k) dst[rank * NV + k] = t;
+    }
   }
   cl.sync();
   if (threadIdx.x < NV) {

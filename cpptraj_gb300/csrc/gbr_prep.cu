@@ -70,84 +70,73 @@ __device__ __forceinline__ void group_sync(int grp) {
 constexpr int kOneBlockThreads = 256;
 // Those kernels run as one cluster of kRefCluster CTAs (on as many SMs): each
 // CTA walks every kRefCluster-th block of atoms and the sums are combined
-// across the cluster in distributed shared memory (cluster_sum_f64).
+// across the cluster in distributed shared memory (cluster_reduce_f64).
 constexpr int kRefCluster = 8;
 
 namespace cg = cooperative_groups;
 
-// Sums of NV doubles over all threads of all CTAs of this cluster, returned
-// to every thread.  Each CTA's total goes to CTA 0's `slots`; after a cluster
-// barrier every CTA adds the slots in rank order, so all CTAs see the same
-// (deterministic) totals.  red: >= 32*NV doubles, slots: >= kRefCluster*NV,
-// bc: >= NV doubles of this CTA's shared memory.  Every thread of every CTA of
-// the cluster must call it (it contains block and cluster barriers).
-template <int NV>
-__device__ __forceinline__ void cluster_sum_f64(double (&v)[NV], double* red, double* slots, double* bc) {
+// Sums of NS doubles and maxima of NM non-negative doubles over all threads
+// of all CTAs of this cluster, returned to every thread, in one exchange.
+// Per value: a shuffle tree per warp, then warp 0 alone combines the warps'
+// results by the same tree (FP64 adds are slow on GB300: the other warps
+// would only repeat them), lane k keeping value k; each CTA's result goes to
+// CTA 0's `slots`, and after a cluster barrier every CTA combines the slots
+// in rank order, so all CTAs see the same (deterministic) totals.  red: >=
+// 32*(NS+NM) doubles, slots: >= kRefCluster*(NS+NM), bc: >= NS+NM doubles of
+// this CTA's shared memory.  Every thread of every CTA of the cluster must
+// call it (it contains block and cluster barriers).
+template <int NS, int NM>
+__device__ __forceinline__ void cluster_reduce_f64(double (&v)[NS], double (&m)[NM], double* red, double* slots,
+                                                   double* bc) {
+  constexpr int NV = NS + NM;
   static_assert(NV <= 32, "lane k keeps value k");
-  // This CTA's totals: a shuffle tree per warp, then warp 0 alone adds the
-  // warps' sums by the same tree (FP64 adds are slow on GB300: the other
-  // warps would only repeat them), lane k keeping value k.
 #pragma unroll
-  for (int k = 0; k < NV; ++k) {
+  for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    for (int k = 0; k < NS; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+#pragma unroll
+    for (int k = 0; k < NM; ++k) m[k] = fmax(m[k], __shfl_xor_sync(0xffffffffu, m[k], o));
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   __syncthreads();  // `red` may still be read by an earlier reduction
   if (lane == 0) {
 #pragma unroll
-    for (int k = 0; k < NV; ++k) red[k * 32 + warp] = v[k];
+    for (int k = 0; k < NS; ++k) red[k * 32 + warp] = v[k];
+#pragma unroll
+    for (int k = 0; k < NM; ++k) red[(NS + k) * 32 + warp] = m[k];
   }
   __syncthreads();
   cg::cluster_group cl = cg::this_cluster();
   const unsigned rank = cl.block_rank(), n = cl.num_blocks();
-  // The CTA totals go to CTA 0's slots (the NV values side by side, each
-  // summed in rank order below).
   if (warp == 0) {
     double* dst = cl.map_shared_rank(slots, 0);
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
       double t = (lane < nw) ? red[k * 32 + lane] : 0.0;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      for (int o = 16; o > 0; o >>= 1) {
+        const double u = __shfl_xor_sync(0xffffffffu, t, o);
+        t = (k < NS) ? t + u : fmax(t, u);
+      }
       if (lane == k) dst[rank * NV + k] = t;
     }
   }
   cl.sync();
   if (threadIdx.x < NV) {
     const double* src = cl.map_shared_rank(slots, 0);
+    const bool is_sum = (int)threadIdx.x < NS;
     double t = 0.0;
-    for (unsigned r = 0; r < n; ++r) t += src[r * NV + threadIdx.x];
+    for (unsigned r = 0; r < n; ++r) {
+      const double u = src[r * NV + threadIdx.x];
+      t = is_sum ? t + u : fmax(t, u);
+    }
     bc[threadIdx.x] = t;
   }
   cl.sync();  // CTA 0's slots are free again; bc is visible in this CTA
 #pragma unroll
-  for (int k = 0; k < NV; ++k) v[k] = bc[k];
-}
-
-// Maximum of a non-negative value over the cluster (same scheme, one slot per CTA).
-__device__ __forceinline__ double cluster_max_f64(double m, double* red, double* slots, double* bc) {
+  for (int k = 0; k < NS; ++k) v[k] = bc[k];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-  __syncthreads();
-  cg::cluster_group cl = cg::this_cluster();
-  const unsigned rank = cl.block_rank(), n = cl.num_blocks();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t = fmax(t, red[k]);
-    cl.map_shared_rank(slots, 0)[rank] = t;
-  }
-  cl.sync();
-  if (threadIdx.x == 0) {
-    const double* src = cl.map_shared_rank(slots, 0);
-    double t = 0.0;
-    for (unsigned r = 0; r < n; ++r) t = fmax(t, src[r]);
-    bc[0] = t;
-  }
-  cl.sync();
-  return bc[0];
+  for (int k = 0; k < NM; ++k) m[k] = bc[NS + k];
 }
 constexpr int kSample = 2048;      // frames per reference that set its refined mean
 constexpr int kMeanChunks = 64;    // fixed partition of those frames
@@ -407,7 +396,7 @@ struct WarpPipe {
 // Weights in the forms the passes read; scal = {max sqrt(w), sum w, sum of
 // the reference centring masses, 0, 1 / sum w, 1 / sum of the reference
 // centring masses} (a reciprocal is 0 when its sum is 0).  Run by the cluster
-// that builds reference 0 (k_make_ref), before it: atom a's sqrt(w) is
+// that builds reference 0 (k_make_ref), at its start: atom a's sqrt(w) is
 // written and then read by the same thread.
 struct WeightsPass {
   const double* w;
@@ -417,42 +406,32 @@ struct WeightsPass {
   float* cmf_ref;
   double* scal;
 };
-__device__ __forceinline__ void weights_pass(const WeightsPass& P, int N) {
-  const double* w = P.w;
-  const double* cmass_ref = P.cmass_ref;
-  double* sqw = P.sqw;
-  float* sqwf = P.sqwf;
-  float* cmf_ref = P.cmf_ref;
-  double* scal = P.scal;
-  __shared__ double red[32 * 2], slots[kRefCluster * 2], bc[2];
+// This thread's atoms: writes their weight forms, adds {sum w, sum of the
+// reference centring masses} into v and the largest sqrt(w) into mx.
+__device__ __forceinline__ void weights_local(const WeightsPass& P, int N, double* v, double& mx) {
   const int stride = kRefCluster * blockDim.x;
-  double v[2] = {0.0, 0.0};
-  double mx = 0.0;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < N; a += stride) {
-    const double wa = w ? w[a] : 1.0;
-    const double ca = cmass_ref ? cmass_ref[a] : 1.0;
+    const double wa = P.w ? P.w[a] : 1.0;
+    const double ca = P.cmass_ref ? P.cmass_ref[a] : 1.0;
     const double s = sqrt(wa);
-    if (w) {
-      sqw[a] = s;
-      sqwf[a] = (float)s;
+    if (P.w) {
+      P.sqw[a] = s;
+      P.sqwf[a] = (float)s;
     }
-    if (cmass_ref) {
-      cmf_ref[a] = (float)ca;
-    }
+    if (P.cmass_ref) P.cmf_ref[a] = (float)ca;
     mx = fmax(mx, s);
     v[0] += wa;
     v[1] += ca;
   }
-  cluster_sum_f64<2>(v, red, slots, bc);
-  mx = cluster_max_f64(mx, red, slots, bc);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    scal[0] = mx;
-    scal[1] = v[0];
-    scal[2] = v[1];
-    scal[3] = 0.0;
-    scal[4] = (v[0] != 0.0) ? 1.0 / v[0] : 0.0;
-    scal[5] = (v[1] != 0.0) ? 1.0 / v[1] : 0.0;
-  }
+}
+__device__ __forceinline__ void weights_store(const WeightsPass& P, const double* v, double mx) {
+  double* scal = P.scal;
+  scal[0] = mx;
+  scal[1] = v[0];
+  scal[2] = v[1];
+  scal[3] = 0.0;
+  scal[4] = (v[0] != 0.0) ? 1.0 / v[0] : 0.0;
+  scal[5] = (v[1] != 0.0) ? 1.0 / v[1] : 0.0;
 }
 
 // FP64-accumulated centres (the FP64 checking mode only).
@@ -506,7 +485,6 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
   // A gated round after the k-centre choice has stopped: every CTA of the
   // cluster reads the same word and leaves before any barrier.
   if (gate && *gate != 0) return;
-  if (wp.scal) weights_pass(wp, src.N);  // reference 0: the weights first
   __shared__ double red[32 * 10], slots[kRefCluster * 10], bc[10];
   __shared__ double Rs[9], cs[3];
   const int N = src.N;
@@ -514,6 +492,10 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
   const int64_t f = *fsel;
   const T* x = src.frame(f);
   if (threadIdx.x < 9) Rs[threadIdx.x] = (threadIdx.x % 4 == 0) ? 1.0 : 0.0;
+  // Reference 0: the weights first (their sums travel in the same cluster
+  // exchange as the frame's centre).
+  double wv[2] = {0.0, 0.0}, wmx[1] = {0.0};
+  if (wp.scal) weights_local(wp, N, wv, wmx[0]);
   double c0 = 0.0, c1 = 0.0, c2 = 0.0;
   if (nofit || use_parent) {
     if (!nofit) {
@@ -521,9 +503,13 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
       c1 = cen[3 * f + 1];
       c2 = cen[3 * f + 2];
     }
+    if (wp.scal) {
+      cluster_reduce_f64<2, 1>(wv, wmx, red, slots, bc);
+      if (blockIdx.x == 0 && threadIdx.x == 0) weights_store(wp, wv, wmx[0]);
+    }
   } else {
     const double* m = (f < src.n_ref) ? cmass_ref : cmass_tgt;
-    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    double v[6] = {0.0, 0.0, 0.0, 0.0, wv[0], wv[1]};
     for (int a = a_first; a < N; a += stride) {
       const double wm = m ? m[a] : 1.0;
       v[0] += wm * (double)x[3 * a];
@@ -531,9 +517,10 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
       v[2] += wm * (double)x[3 * a + 2];
       v[3] += wm;
     }
-    cluster_sum_f64<4>(v, red, slots, bc);
+    cluster_reduce_f64<6, 1>(v, wmx, red, slots, bc);
     // one thread divides (an FP64 division is a long sequence on the FP64 pipe)
     if (threadIdx.x == 0) {
+      if (wp.scal && blockIdx.x == 0) weights_store(wp, v + 4, wmx[0]);
       double wt = m ? v[3] : (double)N;
       if (m && wt == 0.0) {
         wt = 1.0;
@@ -591,8 +578,9 @@ __global__ void __cluster_dims__(kRefCluster, 1, 1) __launch_bounds__(kOneBlockT
     acc[0] += wa * r2;
     mx = fmax(mx, r2);
   }
-  cluster_sum_f64<4>(acc, red, slots, bc);
-  mx = cluster_max_f64(mx, red, slots, bc);
+  double mxa[1] = {mx};
+  cluster_reduce_f64<4, 1>(acc, mxa, red, slots, bc);
+  mx = mxa[0];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     Eref[k] = acc[0];
     sr[3 * k] = acc[1];

@@ -67,12 +67,13 @@ inline int64_t build_tiles_grouped(const TileGrid& g, std::vector<int2>& tiles) 
 // every frame the tile reads, i.e. the number of chunk ends below
 // min(max(i_base + (ti + 1) * rows, jt_base + (tj + 1) * cols), F).
 // stage_off[0..n_chunks] receives the stage offsets. Writes nothing and
-// returns -1 if the list holds more than cap tiles; else returns its length.
+// returns -1 if the list holds more than cap tiles or n_chunks is outside
+// [1, 64]; else returns its length.
 // Within a run the reference end grows with ti, so the tiles up to the one
 // whose reference end passes the run's target end share the run's stage.
-// n_chunks is at most 64.
 inline int64_t build_tiles_staged(const TileGrid& g, const int64_t* chunk_end, int n_chunks, int64_t F, int2* dst,
                                   int64_t cap, int64_t* stage_off, std::vector<int64_t>& scratch) {
+  if (n_chunks < 1 || n_chunks > 64) return -1;
   const int64_t Ti = (g.i_end - g.i_base + g.rows - 1) / g.rows, Tj = (g.jt_end - g.jt_base + g.cols - 1) / g.cols;
   auto stage_of = [&](int64_t fe) {
     fe = std::min(fe, F);

@@ -131,6 +131,35 @@ def _dtype_code(x):
     raise TypeError(f"coordinates must be float32 or float64, got {dt}")
 
 
+def _shape(x):
+    return tuple(int(d) for d in x.shape)
+
+
+def _kind(x):
+    return str(x.dtype).split(".")[-1]
+
+
+def _check_coords(x, name="xyz", dtypes=("float32", "float64")):
+    """x must be [frames, atoms, 3] of one of `dtypes`."""
+    if len(_shape(x)) != 3 or _shape(x)[2] != 3:
+        raise ValueError(f"{name} must have shape (frames, atoms, 3), got {_shape(x)}")
+    if _kind(x) not in dtypes:
+        raise TypeError(f"{name} must be {' or '.join(dtypes)}, got {_kind(x)}")
+
+
+def _check_buffer(x, name, dtype, count, exact=False):
+    """x (or None) must hold `dtype` values, exactly / at least `count` of them.
+    The library writes or reads that many through the raw pointer."""
+    if x is None:
+        return
+    if _kind(x) != dtype:
+        raise TypeError(f"{name} must be {dtype}, got {_kind(x)}")
+    n = int(np.prod(_shape(x))) if len(_shape(x)) else 1
+    if (n != count) if exact else (n < count):
+        need = f"{count}" if exact else f"at least {count}"
+        raise ValueError(f"{name} must have {need} elements, got {n}")
+
+
 def row_bands(n_frame, band_floats, row_align=1):
     """Band boundaries of a streamed triangle (gbr_row_bands): an int64 array
     cuts with cuts[0] = 0 and cuts[-1] = n_frame; raises ValueError when one
@@ -211,7 +240,12 @@ class Handle:
         Returns ``out`` (allocated like ``ref`` -- numpy or torch, same
         device -- when not given).  TRI for one set, FULL when ``tgt`` is given.
         """
+        _check_coords(ref, "ref")
         n_ref, n_atom = int(ref.shape[0]), int(ref.shape[1])
+        if tgt is not None:
+            _check_coords(tgt, "tgt")
+            if int(tgt.shape[1]) != n_atom or _kind(tgt) != _kind(ref):
+                raise ValueError("tgt must have the atom count and dtype of ref")
         n_tgt = int(tgt.shape[0]) if tgt is not None else n_ref
         if out_kind is None:
             out_kind = TRI if tgt is None else FULL
@@ -224,10 +258,13 @@ class Handle:
             else:
                 import torch
                 out = torch.zeros(count, dtype=torch.float32, device=ref.device)
+        _check_buffer(out, "out", "float32", count)
         if tgt_mass is not None and isinstance(tgt_mass, np.ndarray):
             tgt_mass = np.ascontiguousarray(tgt_mass, dtype=np.float64)
         if ref_mass is not None and isinstance(ref_mass, np.ndarray):
             ref_mass = np.ascontiguousarray(ref_mass, dtype=np.float64)
+        _check_buffer(tgt_mass, "tgt_mass", "float64", n_atom, exact=True)
+        _check_buffer(ref_mass, "ref_mass", "float64", n_atom, exact=True)
         self.allpairs_raw(ref, tgt, n_ref, n_tgt, n_atom, _dtype_code(ref), ref_mass, tgt_mass, m, out_kind, p,
                           out, row_begin, row_end)
         return out
@@ -239,7 +276,10 @@ class Handle:
         move: optional [frames, n_move, 3] array of that dtype, moved in place.
         Returns (rmsd [F], rot [F, 3, 3], tgt_trans [F, 3], ref_trans [3]) as
         float64 arrays of the same kind and device as ``xyz``."""
+        _check_coords(xyz)
         F, N = int(xyz.shape[0]), int(xyz.shape[1])
+        if _shape(ref) != (N, 3) or _kind(ref) != _kind(xyz):
+            raise ValueError(f"ref must have shape ({N}, 3) and the dtype of xyz")
         m = MODES[mode] if isinstance(mode, str) else mode
         if isinstance(xyz, np.ndarray):
             def mk(*shape):
@@ -253,10 +293,15 @@ class Handle:
 
             def mk(*shape):
                 return torch.zeros(shape, dtype=torch.float64, device=xyz.device)
+        _check_buffer(mass, "mass", "float64", N, exact=True)
+        _check_buffer(ref_mass, "ref_mass", "float64", N, exact=True)
         rmsd, rot, tt, rt = mk(F), mk(F, 3, 3), mk(F, 3), mk(3)
         n_move = 0 if move is None else int(move.shape[1])
-        if move is not None and _dtype_code(move) != _dtype_code(xyz):
-            raise TypeError("move must have the dtype of xyz")
+        if move is not None:
+            if _dtype_code(move) != _dtype_code(xyz):
+                raise TypeError("move must have the dtype of xyz")
+            if len(_shape(move)) != 3 or _shape(move)[0] != F or _shape(move)[2] != 3:
+                raise ValueError(f"move must have shape ({F}, atoms, 3), got {_shape(move)}")
         self._check(self.lib.gbr_superpose(self.h, _ptr(ref), _ptr(xyz), _dtype_code(xyz), F, N, _ptr(ref_mass),
                                            _ptr(mass), m, _ptr(rmsd), _ptr(rot), _ptr(tt), _ptr(rt), _ptr(move),
                                            n_move))
@@ -269,6 +314,7 @@ class Handle:
         offsets (int64, [n_cluster + 1]): cluster c is members[offsets[c]:
         offsets[c + 1]] in visiting order.  Returns [n_cluster, atoms, 3]
         float64 of the same kind and device as ``xyz``."""
+        _check_coords(xyz)
         F, N = int(xyz.shape[0]), int(xyz.shape[1])
         nc = int(offsets.shape[0]) - 1
         m = MODES[mode] if isinstance(mode, str) else mode
@@ -282,6 +328,9 @@ class Handle:
             import torch
 
             out = torch.zeros((max(nc, 0), N, 3), dtype=torch.float64, device=xyz.device)
+        _check_buffer(members, "members", "int32", 0)
+        _check_buffer(offsets, "offsets", "int64", max(nc + 1, 1), exact=True)
+        _check_buffer(mass, "mass", "float64", N, exact=True)
         self._check(self.lib.gbr_cluster_centroids(self.h, _ptr(xyz), _dtype_code(xyz), F, N, _ptr(mass), m,
                                                    _ptr(members), _ptr(offsets), nc, _ptr(out)))
         return out
@@ -289,6 +338,10 @@ class Handle:
     def allpairs_batched(self, trajs, masses=None, mode="fit", precision="fp32"):
         """trajs: list of float32 [F_t, N_t, 3] arrays; returns list of TRI outputs."""
         n = len(trajs)
+        for t, x in enumerate(trajs):
+            _check_coords(x, f"trajs[{t}]", ("float32",))
+        if masses is not None and len(masses) != n:
+            raise ValueError("masses must have one entry per trajectory")
         outs = [np.zeros(max(int(t.shape[0]) * (int(t.shape[0]) - 1) // 2, 1), np.float32) for t in trajs]
         xyz = (ctypes.c_void_p * n)(*[_ptr(t) for t in trajs])
         nf = (ctypes.c_int64 * n)(*[int(t.shape[0]) for t in trajs])
@@ -296,6 +349,8 @@ class Handle:
         ms = None
         if masses is not None:
             masses = [None if m is None else np.ascontiguousarray(m, np.float64) for m in masses]
+            for t, (mt, x) in enumerate(zip(masses, trajs)):
+                _check_buffer(mt, f"masses[{t}]", "float64", int(x.shape[1]), exact=True)
             ms = (ctypes.c_void_p * n)(*[_ptr(m) for m in masses])
         op = (ctypes.c_void_p * n)(*[_ptr(o) for o in outs])
         m = MODES[mode] if isinstance(mode, str) else mode
@@ -314,9 +369,11 @@ class Handle:
         band in row order; ``values`` is a float32 view of the library's
         pinned staging, valid only during the call (copy what you keep).
         Returning False stops the call (GbrError code 7)."""
+        _check_coords(xyz)
         n_frame, n_atom = int(xyz.shape[0]), int(xyz.shape[1])
         if mass is not None and isinstance(mass, np.ndarray):
             mass = np.ascontiguousarray(mass, dtype=np.float64)
+        _check_buffer(mass, "mass", "float64", n_atom, exact=True)
         errors = []
 
         def _cb(user, rb, re, values, count):
@@ -338,9 +395,11 @@ class Handle:
     def write_cmatrix(self, path, xyz, mass=None, mode="fit", precision="tc", frame_to_idx=None, sieve=1):
         """Pairwise cache of one frame set straight to a cpptraj binary
         cluster-matrix file (CTM version 2)."""
+        _check_coords(xyz)
         n_frame, n_atom = int(xyz.shape[0]), int(xyz.shape[1])
         if mass is not None and isinstance(mass, np.ndarray):
             mass = np.ascontiguousarray(mass, dtype=np.float64)
+        _check_buffer(mass, "mass", "float64", n_atom, exact=True)
         f2i = None
         n_orig = n_frame
         if frame_to_idx is not None:
@@ -354,7 +413,9 @@ class Handle:
 
     def backward(self, xyz, mass=None, g=None, grad=None, rmsd_out=None):
         """dL/dxyz for L = sum_{i<j} g_ij RMSD_ij (float32 frames)."""
+        _check_coords(xyz, dtypes=("float32",))
         n_frame, n_atom = int(xyz.shape[0]), int(xyz.shape[1])
+        n_pairs = n_frame * (n_frame - 1) // 2
         if grad is None:
             if isinstance(xyz, np.ndarray):
                 grad = np.zeros_like(xyz)
@@ -363,6 +424,10 @@ class Handle:
                 grad = torch.zeros_like(xyz)
         if mass is not None and isinstance(mass, np.ndarray):
             mass = np.ascontiguousarray(mass, dtype=np.float64)
+        _check_buffer(mass, "mass", "float64", n_atom, exact=True)
+        _check_buffer(g, "g", "float32", n_pairs)
+        _check_buffer(grad, "grad", "float32", n_frame * n_atom * 3)
+        _check_buffer(rmsd_out, "rmsd_out", "float32", n_pairs)
         rc = self.lib.gbr_rmsd_backward(self.h, _ptr(xyz), n_frame, n_atom, _ptr(mass), _ptr(g), _ptr(grad),
                                         _ptr(rmsd_out))
         self._check(rc)

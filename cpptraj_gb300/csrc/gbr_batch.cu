@@ -317,6 +317,7 @@ extern "C" int gbr_allpairs_batched(gbr_handle* h, int32_t n_traj, const float* 
     if (p.F < 0 || p.F > INT32_MAX) return h->fail(GBR_ERR_ARG, "trajectory %d: bad frame count", t);
     if (p.N < 1) return h->fail(GBR_ERR_ARG, "trajectory %d: n_atom must be >= 1", t);
     if (!xyz[t] || !out[t]) return h->fail(GBR_ERR_ARG, "trajectory %d: null pointer", t);
+    if (int rc = h->check_local({xyz[t], out[t]}, "batched")) return rc;
     p.Np = (p.N + 63) / 64 * 64;
     p.xyz = xyz[t];
     p.out = out[t];

@@ -221,6 +221,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
   if (precision < GBR_PREC_FP32 || precision > GBR_PREC_FP64) return h->fail(GBR_ERR_ARG, "bad precision");
   if (n_atom < 1) return h->fail(GBR_ERR_ARG, "n_atom must be >= 1 (no atoms selected)");
   if (n_ref < 0 || n_tgt < 0) return h->fail(GBR_ERR_ARG, "negative frame count");
+  if (int rc = h->check_local({ref_xyz, tgt_xyz, out}, "allpairs")) return rc;
   if (tgt_xyz == nullptr || tgt_xyz == ref_xyz) {
     tgt_xyz = nullptr;
     n_tgt = n_ref;
@@ -1023,6 +1024,7 @@ int gbr_rmsd_backward(gbr_handle* h, const float* xyz, int64_t n_frame, int32_t 
   if (!xyz || !grad_xyz) return h->fail(GBR_ERR_ARG, "backward: xyz and grad_xyz must not be NULL");
   if (n_atom < 1) return h->fail(GBR_ERR_ARG, "n_atom must be >= 1");
   if (n_frame < 0 || n_frame > 60000) return h->fail(GBR_ERR_ARG, "backward supports 0..60000 frames");
+  if (int rc = h->check_local({xyz, g, grad_xyz, rmsd_out}, "backward")) return rc;
   if (cudaSetDevice(h->device) != cudaSuccess) return h->cuda_fail(cudaGetLastError(), "cudaSetDevice");
   cudaStream_t st = h->stream;
   const int N = n_atom;

@@ -598,6 +598,7 @@ extern "C" int gbr_cluster_centroids(gbr_handle* h, const void* xyz, int dtype, 
   if (mode != GBR_FIT && mode != GBR_NOFIT) return h->fail(GBR_ERR_ARG, "mode must be GBR_FIT or GBR_NOFIT");
   if (n_atom < 1) return h->fail(GBR_ERR_ARG, "n_atom must be >= 1 (no atoms selected)");
   if (n_frame < 0) return h->fail(GBR_ERR_ARG, "negative frame count");
+  if (int rc = h->check_local({xyz, centroids}, "cluster_centroids")) return rc;
   if (cudaSetDevice(h->device) != cudaSuccess) return h->cuda_fail(cudaGetLastError(), "cudaSetDevice");
   cudaStream_t st = h->stream;
   const int N = n_atom;

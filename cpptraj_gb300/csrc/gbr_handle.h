@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <map>
 #include <string>
 #include <utility>
@@ -134,6 +135,23 @@ struct gbr_handle {
   }
   int cuda_fail(cudaError_t e, const char* where) {
     return fail(GBR_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+  }
+  // GBR_ERR_ARG when a buffer the kernels access in place is device memory of
+  // another GPU than this handle's (they would reach it without peer access).
+  // Host and managed memory pass; NULL entries are skipped.
+  int check_local(std::initializer_list<const void*> ps, const char* what) {
+    for (const void* p : ps) {
+      if (!p) continue;
+      cudaPointerAttributes at{};
+      if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        continue;
+      }
+      if (at.type == cudaMemoryTypeDevice && at.device != device)
+        return fail(GBR_ERR_ARG, "%s: a buffer is on device %d, this handle runs on device %d", what, at.device,
+                    device);
+    }
+    return GBR_OK;
   }
   bool reserve(size_t bytes) {
     if (bytes <= ws_cap) return true;

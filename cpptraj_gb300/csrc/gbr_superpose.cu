@@ -141,6 +141,7 @@ extern "C" int gbr_superpose(gbr_handle* h, const void* ref_xyz, const void* xyz
   if (n_frame < 0) return h->fail(GBR_ERR_ARG, "negative frame count");
   if (!move_xyz) n_move = 0;
   if (n_move < 0) return h->fail(GBR_ERR_ARG, "negative n_move");
+  if (int rc = h->check_local({ref_xyz, xyz, rmsd, rot, tgt_trans, ref_trans, move_xyz}, "superpose")) return rc;
   if (cudaSetDevice(h->device) != cudaSuccess) return h->cuda_fail(cudaGetLastError(), "cudaSetDevice");
   cudaStream_t st = h->stream;
   const int N = n_atom;

@@ -50,7 +50,9 @@
  *     Zero total mass (< 1e-14, src/Constants.h:35) is an error for the call
  *     (the reference returns -1 for the pair and prints an error).
  *   - Pointers may be host or device memory (detected per call).  Host
- *     buffers are staged through the handle's device memory.
+ *     buffers are staged through the handle's device memory.  Device
+ *     buffers must be on the handle's device (GBR_ERR_ARG otherwise); masses,
+ *     offsets and member lists are read once and may be on any device.
  *   - Return value: GBR_OK (0) or an error code; gbr_last_error gives text.
  *     No exception crosses the ABI.  One handle must not be used from two
  *     threads at once; separate handles are independent.

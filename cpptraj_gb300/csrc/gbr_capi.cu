@@ -109,6 +109,7 @@ void gbr_destroy(gbr_handle* h) {
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   if (h->ws) cudaFree(h->ws);
+  if (h->ostage) cudaFree(h->ostage);
   h->release_batch();
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
@@ -294,6 +295,12 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
     }
   }
   const bool out_dev = out_on_dev || out_direct;  // kernels can write `out_k` in place
+  // The kernels' results go to the host through the link as whole tile rows
+  // (pinned host `out`), and `out` is filled by one copy at the end (host
+  // `out` the kernels do not write in place); both may change once prep has
+  // laid the frames out by reference (below).
+  bool rows_to_host = out_direct;
+  bool copy_back = !out_dev;
   const size_t esz = (dtype == GBR_F64) ? 8 : 4;
   const int64_t F = (tgt_xyz ? n_ref + n_tgt : n_ref);
   const int64_t tgt0 = tgt_xyz ? n_ref : 0;
@@ -450,7 +457,10 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
   // (grouped order kept within a stage); when prep has built the operands
   // through a chunk, the tiles ready by then are launched behind it.
   const int tc_variant = (h->tc_variant >= 0) ? h->tc_variant : auto_tc_variant(N);
-  bool overlap = h->input_overlap && n_chunks > 0 && tc && map.tri && !tgt_xyz && out_dev;
+  // The last call of this shape needed several references: no one-reference
+  // speculation (it would be thrown away).
+  const bool multi_hint = h->last_multi && h->last_F == F && h->last_N == N;
+  bool overlap = h->input_overlap && n_chunks > 0 && tc && map.tri && !tgt_xyz && out_dev && !multi_hint;
   int64_t stage_off[9] = {};
   if (overlap) {
     // Grouped by stage straight into the pinned staging when there is one.
@@ -519,7 +529,6 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
   // reference-count decision stays on the device (no host round trip inside
   // prep).  A call that turns out to need several references runs again
   // (redo), from the state its first scan left in the workspace.
-  const bool multi_hint = h->last_multi && h->last_F == F && h->last_N == N;
   pa.defer_multi = (!redo && !multi_hint && n_chunks == 0 && !rs && out_dev && Kmax > 1) ? (int*)P[25] + 1 : nullptr;
   pa.resume_scan = redo ? 1 : 0;
   for (int c = 0; c < n_chunks; ++c) {
@@ -721,7 +730,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
       L.variant = tc_variant;
       // whole-row stores where the triangle lands in host memory across the
       // link; direct per-pair stores into device memory
-      L.row_stores = out_direct ? 1 : 0;
+      L.row_stores = rows_to_host ? 1 : 0;
       L.skip = skip;
       L.tile_stage = stage;
       L.cluster_cap = cap;
@@ -800,7 +809,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
       pa.on_built = &on_built;
       pa.spec_fail = (int*)P[25] + 1;
     }
-    if (n_chunks > 0) pa.spec_build = &fa;
+    if (n_chunks > 0 && !multi_hint) pa.spec_build = &fa;
     PrepOut po;
     if ((e = run_prep(pa, po, ps)) != cudaSuccess) return h->cuda_fail(e, "prep");
     if (overlap && po.built && (e = launch_rest()) != cudaSuccess) return h->cuda_fail(e, "pair kernel launch");
@@ -815,6 +824,19 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
     const bool spec_done = overlap && po.built && spec_terms;
     if (overlap && !spec_done)
       cudaMemsetAsync(P[21], 0, sizeof(unsigned long long) * kMaxBands, st);  // discard speculative flags
+    if (out_direct && po.sorted) {
+      // A triangle over reference-sorted positions scatters its values over
+      // the whole output, which the host link serves at a fraction of its
+      // rate (10x slower at 50,000 x 500 with 20 references): it is computed
+      // into device memory and copied back whole.
+      if (!h->reserve_ostage(sizeof(float) * (size_t)n_out))
+        return h->fail(GBR_ERR_NOMEM, "cannot allocate %.2f GB of device memory for the result",
+                       4.0 * n_out / 1e9);
+      map.out = (float*)h->ostage;
+      ex.map.out = map.out;
+      rows_to_host = false;
+      copy_back = true;
+    }
     OutMap pmap = map;  // the pair kernels' view: sorted positions when po.sorted
     if (po.sorted) pmap.perm = pa.order;
     const FrameTerms terms = make_terms(K, po.sorted != 0);
@@ -904,7 +926,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
         ++launches;
       }
       if (h->timing) cudaEventRecord(h->ev[3], st);
-      if (!out_dev) cudaMemcpyAsync(out, map.out, sizeof(float) * n_out, cudaMemcpyDefault, st);
+      if (copy_back) cudaMemcpyAsync(out, map.out, sizeof(float) * n_out, cudaMemcpyDefault, st);
     } else {
       // Band boundaries: equal pair counts, aligned to the kernel's tile rows.
       const int64_t align = tc ? tc_launch_tile_rows(tc_variant) : 64;
@@ -981,7 +1003,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
     }
   }
   if (h->timing && !need_planes) cudaEventRecord(h->ev[3], st);
-  if (!rs && !need_planes && !out_dev) cudaMemcpyAsync(out, map.out, sizeof(float) * n_out, cudaMemcpyDefault, st);
+  if (!rs && !need_planes && copy_back) cudaMemcpyAsync(out, map.out, sizeof(float) * n_out, cudaMemcpyDefault, st);
   if (h->xfer) {  // the copy stream's work belongs to this call
     cudaEventRecord(h->xev[h->kXev - 3], h->xfer);
     cudaStreamWaitEvent(st, h->xev[h->kXev - 3], 0);

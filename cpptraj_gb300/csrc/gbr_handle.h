@@ -170,6 +170,22 @@ struct gbr_handle {
     ws_cap = bytes;
     return true;
   }
+  // Device memory for a result bound for pinned host memory that the kernels
+  // cannot store across the link efficiently (grown on demand, kept).
+  void* ostage = nullptr;
+  size_t ostage_cap = 0;
+  bool reserve_ostage(size_t bytes) {
+    if (bytes <= ostage_cap) return true;
+    if (ostage) cudaFree(ostage);
+    ostage = nullptr;
+    ostage_cap = 0;
+    if (cudaMalloc(&ostage, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    ostage_cap = bytes;
+    return true;
+  }
   bool reserve_pinned(size_t bytes) {
     if (bytes <= pinned_cap) return true;
     if (pinned) cudaFreeHost(pinned);

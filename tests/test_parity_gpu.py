@@ -404,6 +404,32 @@ def test_pinned_input_speculative_prep(h, sig_hi, expect_refs, overlap):
     np.testing.assert_array_equal(hout.numpy(), dev)
 
 
+@pytest.mark.parametrize("precision", ["tc", "fp32"])
+def test_pinned_clustered_result(h, precision):
+    # Several references: the triangle is computed over reference-sorted
+    # positions, whose results scatter over the whole output; bound for pinned
+    # host memory it is computed into device memory and copied back whole.
+    # The first pinned call speculates on one reference (and throws that
+    # away), a repeated call of the same shape does not.  Both equal the
+    # device-resident call bit for bit.
+    torch = pytest.importorskip("torch")
+    X, _ = synth.clustered(95, 3000, 400, 6, 0.8)
+    dev = run(h, torch.from_numpy(X).cuda(), precision=precision).cpu().numpy()
+    assert h.stats()["n_refs"] > 1
+    run(h, synth.trajectory(3, 20, 20, 0.1, 1.0, np.float32, False)[0], precision=precision)  # other shape
+    hX = torch.from_numpy(X).pin_memory()
+    hout = torch.empty(dev.size, dtype=torch.float32).pin_memory()
+    run(h, hX, precision=precision, out=hout)
+    np.testing.assert_array_equal(hout.numpy(), dev)
+    hout.fill_(-1.0)
+    run(h, hX, precision=precision, out=hout)
+    np.testing.assert_array_equal(hout.numpy(), dev)
+    ref = oracle.allpairs_f64(X[:600])
+    k = np.concatenate([np.arange(i * 3000 - i * (i + 1) // 2, i * 3000 - i * (i + 1) // 2 + 599 - i)
+                        for i in range(599)])
+    assert np.abs(hout.numpy()[k] - ref).max() <= TOL
+
+
 def test_pinned_input_late_speculation_failure(h):
     # With GBR_OPT_INPUT_OVERLAP (the default) the contraction starts on the
     # chunks that have landed; a far frame in the last chunk ends the speculation after

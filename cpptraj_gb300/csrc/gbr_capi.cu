@@ -38,6 +38,46 @@ constexpr int kDeepStageAtoms = 1280;
 // 1,000.
 constexpr int kWideChunkAtoms = 768;
 int auto_tc_variant(int N) { return N >= kDeepStageAtoms ? 3 : (N < kWideChunkAtoms ? 4 : 2); }
+
+// Whole rows of a triangle, from device memory to the caller's buffer (the
+// device alias of pinned host memory, 16-byte aligned like the source): row
+// i = rows[r] for r in [0, nrows), the n - 1 - i values from
+// tri_index(n, i, i + 1) = n i - i (i + 1) / 2 on, the same positions in
+// both.  One warp per row at a time: a scalar head up to a 16-byte boundary,
+// then 16-byte pieces four at a time per lane (whole 128-byte lines per
+// warp store across the host link), then the scalar tail.  The contraction
+// bands run on all but kCopyFreeClusters clusters; the copy's blocks take the
+// SMs left free (their shared-memory reservation, unused, keeps them from
+// sharing an SM with a contraction CTA, which slowed the contraction as much
+// as the overlap saved).
+constexpr int kCopyFreeClusters = 4, kCopyBlocks = 2 * kCopyFreeClusters, kCopyThreads = 1024;
+constexpr int kCopySmem = 64 << 10;
+__global__ void __launch_bounds__(kCopyThreads) k_copy_rows(const int* rows, int64_t nrows, int64_t n,
+                                                            const float* src, float* dst) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); r < nrows; r += warps) {
+    const int64_t i = rows[r];
+    const int64_t len = n - 1 - i, base = n * i - i * (i + 1) / 2;
+    if (len <= 0) continue;
+    const int64_t head = min(len, (4 - (base & 3)) & 3);
+    if (lane < head) dst[base + lane] = __ldcs(src + base + lane);
+    const int64_t nv = (len - head) >> 2;
+    const float4* s4 = reinterpret_cast<const float4*>(src + base + head);
+    float4* d4 = reinterpret_cast<float4*>(dst + base + head);
+    int64_t k = lane;
+    for (; k + 96 < nv; k += 128) {
+      const float4 a = __ldcs(s4 + k), b = __ldcs(s4 + k + 32), c = __ldcs(s4 + k + 64), d = __ldcs(s4 + k + 96);
+      d4[k] = a;
+      d4[k + 32] = b;
+      d4[k + 64] = c;
+      d4[k + 96] = d;
+    }
+    for (; k < nv; k += 32) d4[k] = __ldcs(s4 + k);
+    const int64_t t0 = head + 4 * nv;
+    if (t0 + lane < len) dst[base + t0 + lane] = __ldcs(src + base + t0 + lane);
+  }
+}
 // Default band of the streamed triangle: 256 Mi floats (1 GiB per device
 // slot, two slots on the device and two in pinned host memory).
 constexpr int64_t kDefaultBandFloats = (int64_t)1 << 28;
@@ -851,8 +891,8 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
       launches += po.built ? 1 : (K > 1 ? 3 : (po.self_terms ? 1 : 2));
     }
     // One launch of the pair kernel over the rows of map m.
-    auto launch_pairs = [&](const OutMap& m, const FlagList& f, int2* stage = nullptr) -> cudaError_t {
-      if (tc) return launch_tc(m, f, terms, 0, 0, fa.skip, stage);
+    auto launch_pairs = [&](const OutMap& m, const FlagList& f, int2* stage = nullptr, int cap = 0) -> cudaError_t {
+      if (tc) return launch_tc(m, f, terms, 0, 0, fa.skip, stage, cap);
       PairLaunch L{};
       L.skip = fa.skip;
       L.plane = pa.plane;
@@ -870,8 +910,16 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
     // band's pairs are computed and checked (FP64 re-check of its flagged
     // pairs, list length read on the device), then copied on the copy stream
     // while the next band computes.
-    const bool band_out = !rs && !out_dev && !po.sorted && is_pinned_or_device(out) &&
-                          (size_t)n_out * sizeof(float) >= (32u << 20) && h->ensure_xfer();
+    // A reference-sorted triangle bound for pinned host memory (computed into
+    // device memory, see above) leaves the same way: a band of sorted rows
+    // completes the caller's rows of its frames (every pair sits in the tile
+    // row of its smaller position), which a copy kernel then writes whole.
+    const bool sorted_to_host = out_direct && po.sorted && ((uintptr_t)out_k & 15) == 0;
+    const bool band_out = !rs &&
+                          ((!out_dev && !po.sorted && is_pinned_or_device(out) &&
+                            (size_t)n_out * sizeof(float) >= (32u << 20)) ||
+                           sorted_to_host) &&
+                          h->ensure_xfer();
     int derr = 0;
     if (rs) {
       // each band: its pairs, then the FP64 re-check of its flagged pairs
@@ -929,13 +977,17 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
       if (copy_back) cudaMemcpyAsync(out, map.out, sizeof(float) * n_out, cudaMemcpyDefault, st);
     } else {
       // Band boundaries: equal pair counts, aligned to the kernel's tile rows.
+      // A reference-sorted triangle is cut into equal numbers of rows instead:
+      // each band's copy then moves about the same bytes (the caller's rows
+      // of its frames), and the last band, the copy nothing overlaps, is no
+      // larger than the others.
       const int64_t align = tc ? tc_launch_tile_rows(tc_variant) : 64;
       const int nb = kMaxBands - 2;
       std::vector<int64_t> cut{row_begin};
-      const int64_t total = n_out;
+      const int64_t total = sorted_to_host ? row_end - row_begin : n_out;
       int64_t acc = 0;
       for (int64_t r = row_begin; r < row_end && (int)cut.size() < nb; ++r) {
-        acc += map.tri ? (n_ref - 1 - r) : n_ref;
+        acc += sorted_to_host ? 1 : map.tri ? (n_ref - 1 - r) : n_ref;
         const int64_t r1 = r + 1;
         if (acc * nb >= total * (int64_t)cut.size() && (r1 - row_begin) % align == 0 && r1 < row_end) cut.push_back(r1);
       }
@@ -947,11 +999,14 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
         const int64_t rb = cut[b], re = cut[b + 1];
         const int64_t cnt = gbr_output_count(n_ref, n_tgt, out_kind, rb, re);
         if (cnt <= 0) continue;
-        OutMap mb = map;
+        OutMap mb = sorted_to_host ? pmap : map;
         mb.row_begin = rb;
         mb.row_end = re;
-        int64_t off;
-        if (map.tri) {
+        int64_t off = 0;
+        if (sorted_to_host) {
+          // rows of sorted positions; the stores go through the permutation to
+          // the caller's positions in the whole device-side triangle
+        } else if (map.tri) {
           mb.base = (rb < n_ref - 1) ? tri_index(n_ref, rb, rb + 1) : 0;
           off = mb.base - map.base;
         } else {
@@ -959,9 +1014,10 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
         }
         mb.out = map.out + off;
         FlagList fb{(int2*)P[20] + (size_t)b * capb, counts + b, capb};
-        if ((e = launch_pairs(mb, fb)) != cudaSuccess) return h->cuda_fail(e, "pair kernel launch");
+        if ((e = launch_pairs(mb, fb, nullptr, sorted_to_host ? -kCopyFreeClusters : 0)) != cudaSuccess)
+          return h->cuda_fail(e, "pair kernel launch");
         ExactLaunch exb = ex;
-        exb.map = mb;
+        if (!sorted_to_host) exb.map = mb;  // flagged pairs are frames: the caller's map places them
         exb.list = fb.pairs;
         exb.count = (int64_t)capb;
         exb.dev_count = counts + b;
@@ -969,7 +1025,18 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
         launches += 2;
         cudaEventRecord(h->xev[8 + b], st);
         cudaStreamWaitEvent(h->xfer, h->xev[8 + b], 0);
-        cudaMemcpyAsync(out + off, mb.out, sizeof(float) * cnt, cudaMemcpyDeviceToHost, h->xfer);
+        if (sorted_to_host) {
+          const int64_t nrows = re - rb;
+          if (b == 0 &&
+              (e = cudaFuncSetAttribute(k_copy_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, kCopySmem)) !=
+                  cudaSuccess)
+            return h->cuda_fail(e, "row copy");
+          k_copy_rows<<<kCopyBlocks, kCopyThreads, kCopySmem, h->xfer>>>(pa.order + rb, nrows, n_ref, map.out,
+                                                                        out_k);
+          ++launches;
+        } else {
+          cudaMemcpyAsync(out + off, mb.out, sizeof(float) * cnt, cudaMemcpyDeviceToHost, h->xfer);
+        }
       }
       if (h->timing) {
         cudaEventRecord(h->ev[2], st);

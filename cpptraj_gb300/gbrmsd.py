@@ -135,13 +135,20 @@ def _shape(x):
     return tuple(int(d) for d in x.shape)
 
 
+_KINDS = {}
+
+
 def _kind(x):
-    return str(x.dtype).split(".")[-1]
+    """'float32', 'int64', ... for a numpy array or a torch tensor."""
+    k = _KINDS.get(x.dtype)
+    if k is None:
+        k = _KINDS[x.dtype] = str(x.dtype).split(".")[-1]
+    return k
 
 
 def _check_coords(x, name="xyz", dtypes=("float32", "float64")):
     """x must be [frames, atoms, 3] of one of `dtypes`."""
-    if len(_shape(x)) != 3 or _shape(x)[2] != 3:
+    if x.ndim != 3 or x.shape[2] != 3:
         raise ValueError(f"{name} must have shape (frames, atoms, 3), got {_shape(x)}")
     if _kind(x) not in dtypes:
         raise TypeError(f"{name} must be {' or '.join(dtypes)}, got {_kind(x)}")
@@ -154,7 +161,7 @@ def _check_buffer(x, name, dtype, count, exact=False):
         return
     if _kind(x) != dtype:
         raise TypeError(f"{name} must be {dtype}, got {_kind(x)}")
-    n = int(np.prod(_shape(x))) if len(_shape(x)) else 1
+    n = x.size if isinstance(x, np.ndarray) else x.numel()
     if (n != count) if exact else (n < count):
         need = f"{count}" if exact else f"at least {count}"
         raise ValueError(f"{name} must have {need} elements, got {n}")

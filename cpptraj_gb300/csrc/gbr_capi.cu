@@ -437,8 +437,12 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
   // first prep pass starts on each chunk as it lands.
   const size_t in_bytes = esz * 3 * (size_t)N * (size_t)F;
   const bool chunk_in = need_planes && (!ref_dev || (tgt_xyz && !tgt_dev)) && in_bytes >= (32u << 20) &&
-                        is_pinned_or_device(ref_xyz) && (!tgt_xyz || is_pinned_or_device(tgt_xyz)) &&
                         h->ensure_xfer();
+  // Pageable host input: a copy from it holds the host until it is done, so
+  // the chunk copies are issued one by one from prep, each just before the
+  // first pass that needs it (the passes of the earlier chunks run meanwhile).
+  const bool chunk_lazy =
+      chunk_in && !(is_pinned_or_device(ref_xyz) && (!tgt_xyz || is_pinned_or_device(tgt_xyz)));
   int n_chunks = 0;
   int64_t chunk_end[8];
   struct ChunkCopy {
@@ -514,15 +518,22 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
     else if (nt > 0)
       cudaMemcpyAsync(P[26], dst, sizeof(int2) * nt, cudaMemcpyHostToDevice, st);
   }
-  if (chunk_in) {
-    cudaEventRecord(h->xev[h->kXev - 1], st);  // the copies follow earlier work on the caller's stream
-    cudaStreamWaitEvent(h->xfer, h->xev[h->kXev - 1], 0);
-    for (int c = 0; c < n_chunks; ++c) {
-      const ChunkCopy& cc = chunk_copies[c];
+  // Issues the chunk copies up to chunk c (those not issued yet) on the copy
+  // stream, each followed by its event.
+  int chunks_issued = 0;
+  const std::function<void(int)> chunk_copy = [&](int c) {
+    for (; chunks_issued <= c && chunks_issued < n_chunks; ++chunks_issued) {
+      const int k = chunks_issued;
+      if (k == 0) {
+        cudaEventRecord(h->xev[h->kXev - 1], st);  // the copies follow earlier work on the caller's stream
+        cudaStreamWaitEvent(h->xfer, h->xev[h->kXev - 1], 0);
+      }
+      const ChunkCopy& cc = chunk_copies[k];
       if (cc.dst) cudaMemcpyAsync(cc.dst, cc.src, cc.bytes, cudaMemcpyHostToDevice, h->xfer);
-      cudaEventRecord(h->xev[c], h->xfer);
+      cudaEventRecord(h->xev[k], h->xfer);
     }
-  }
+  };
+  if (chunk_in && !chunk_lazy) chunk_copy(n_chunks - 1);  // pinned: queued at once
   cudaMemsetAsync(P[21], 0, sizeof(unsigned long long) * kMaxBands, st);
   cudaMemsetAsync(P[25], 0, 2 * sizeof(int), st);
 
@@ -575,6 +586,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
     pa.chunk_end[c] = chunk_end[c];
     pa.chunk_ev[c] = h->xev[c];
   }
+  pa.chunk_copy = chunk_lazy ? &chunk_copy : nullptr;
 
   ExactLaunch ex{};
   ex.dtype_f64 = pa.dtype_f64;
@@ -851,7 +863,9 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
     }
     if (n_chunks > 0 && !multi_hint) pa.spec_build = &fa;
     PrepOut po;
-    if ((e = run_prep(pa, po, ps)) != cudaSuccess) return h->cuda_fail(e, "prep");
+    const cudaError_t ep = run_prep(pa, po, ps);
+    if (chunk_in) chunk_copy(n_chunks - 1);  // every chunk issued, whatever prep did
+    if ((e = ep) != cudaSuccess) return h->cuda_fail(e, "prep");
     if (overlap && po.built && (e = launch_rest()) != cudaSuccess) return h->cuda_fail(e, "pair kernel launch");
     if (split) {  // everything after prep (and the remainder) follows it on the caller's stream
       cudaEventRecord(h->pev[h->kPev - 1], ps);
@@ -916,8 +930,7 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
     // row of its smaller position), which a copy kernel then writes whole.
     const bool sorted_to_host = out_direct && po.sorted && ((uintptr_t)out_k & 15) == 0;
     const bool band_out = !rs &&
-                          ((!out_dev && !po.sorted && is_pinned_or_device(out) &&
-                            (size_t)n_out * sizeof(float) >= (32u << 20)) ||
+                          ((!out_dev && !po.sorted && (size_t)n_out * sizeof(float) >= (32u << 20)) ||
                            sorted_to_host) &&
                           h->ensure_xfer();
     int derr = 0;
@@ -995,6 +1008,16 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
       const int nbands = (int)cut.size() - 1;
       const unsigned long long capb = flag_cap / (unsigned long long)nbands;
       unsigned long long* counts = (unsigned long long*)P[21];
+      // Band b's copy is issued after band b + 1 is queued: a copy into
+      // pageable host memory holds the host until it is done, and the GPU
+      // then has the next band to compute meanwhile.
+      std::function<cudaError_t()> pending_copy;
+      auto flush_copy = [&]() -> cudaError_t {
+        cudaError_t ec = cudaSuccess;
+        if (pending_copy) ec = pending_copy();
+        pending_copy = nullptr;
+        return ec;
+      };
       for (int b = 0; b < nbands; ++b) {
         const int64_t rb = cut[b], re = cut[b + 1];
         const int64_t cnt = gbr_output_count(n_ref, n_tgt, out_kind, rb, re);
@@ -1024,20 +1047,22 @@ int allpairs_impl(gbr_handle* h, const void* ref_xyz, const void* tgt_xyz, int d
         if ((e = run_exact(exb, st)) != cudaSuccess) return h->cuda_fail(e, "fix-up kernel");
         launches += 2;
         cudaEventRecord(h->xev[8 + b], st);
-        cudaStreamWaitEvent(h->xfer, h->xev[8 + b], 0);
-        if (sorted_to_host) {
-          const int64_t nrows = re - rb;
-          if (b == 0 &&
-              (e = cudaFuncSetAttribute(k_copy_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, kCopySmem)) !=
-                  cudaSuccess)
-            return h->cuda_fail(e, "row copy");
-          k_copy_rows<<<kCopyBlocks, kCopyThreads, kCopySmem, h->xfer>>>(pa.order + rb, nrows, n_ref, map.out,
-                                                                        out_k);
-          ++launches;
-        } else {
-          cudaMemcpyAsync(out + off, mb.out, sizeof(float) * cnt, cudaMemcpyDeviceToHost, h->xfer);
-        }
+        if ((e = flush_copy()) != cudaSuccess) return h->cuda_fail(e, "result copy");
+        pending_copy = [&, b, rb, re, off, cnt, src = mb.out]() -> cudaError_t {
+          cudaStreamWaitEvent(h->xfer, h->xev[8 + b], 0);
+          if (sorted_to_host) {
+            const cudaError_t ea =
+                cudaFuncSetAttribute(k_copy_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, kCopySmem);
+            if (ea != cudaSuccess) return ea;
+            k_copy_rows<<<kCopyBlocks, kCopyThreads, kCopySmem, h->xfer>>>(pa.order + rb, re - rb, n_ref, map.out,
+                                                                          out_k);
+            ++launches;
+            return cudaGetLastError();
+          }
+          return cudaMemcpyAsync(out + off, src, sizeof(float) * cnt, cudaMemcpyDeviceToHost, h->xfer);
+        };
       }
+      if ((e = flush_copy()) != cudaSuccess) return h->cuda_fail(e, "result copy");
       if (h->timing) {
         cudaEventRecord(h->ev[2], st);
         cudaEventRecord(h->ev[3], st);

@@ -53,6 +53,11 @@ struct PrepArgs {
   int n_chunks;
   int64_t chunk_end[8];
   cudaEvent_t chunk_ev[8];
+  // When non-null, called on the host just before a pass first waits on
+  // chunk_ev[c], to issue chunk c's copy then (pageable host input, whose
+  // copies hold the host until they are done: issued one by one between the
+  // chunks' passes, each overlaps the passes of the chunks before it).
+  const std::function<void(int)>* chunk_copy;
   // With chunks: the operand build for one reference (K = 1, unsorted), run
   // speculatively while the chunks land (PrepOut::built reports success).
   const struct FinishArgs* spec_build;

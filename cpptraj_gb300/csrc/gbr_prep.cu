@@ -1595,7 +1595,10 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
   // workspace from the deferred run of this call.)
   if (!A.resume_scan) {
     cudaMemsetAsync(A.fsel, 0, sizeof(int64_t), st);
-    if (A.n_chunks > 0) cudaStreamWaitEvent(st, A.chunk_ev[0], 0);
+    if (A.n_chunks > 0) {
+      if (A.chunk_copy) (*A.chunk_copy)(0);
+      cudaStreamWaitEvent(st, A.chunk_ev[0], 0);
+    }
     const WeightsPass wp{A.w, ref_distinct ? A.cmass_ref : nullptr, A.sqw, A.sqwf, S.cmf_ref, S.scal};
     k_make_ref<T><<<kRefCluster, kOneBlockThreads, 0, st>>>(src, A.fsel, A.cen, A.cmass_ref, A.cmass_tgt, A.w,
                                                             A.sqw, A.assign, 0, 0, A.nofit, A.refs, A.swr, S.refhl,
@@ -1619,6 +1622,7 @@ static cudaError_t prep_impl(const PrepArgs& A, PrepOut& o, cudaStream_t st) {
     bool refined = false;
     int64_t f0 = 0;
     for (int c = 0; c < A.n_chunks; ++c) {
+      if (A.chunk_copy) (*A.chunk_copy)(c);  // (chunk 0: already issued, a no-op)
       if (c > 0) cudaStreamWaitEvent(st, A.chunk_ev[c], 0);
       const int64_t f1 = A.chunk_end[c];
       if (f1 > f0) {

@@ -405,6 +405,31 @@ def test_pinned_input_speculative_prep(h, sig_hi, expect_refs, overlap):
 
 
 @pytest.mark.parametrize("precision", ["tc", "fp32"])
+def test_pageable_host_buffers(h, precision):
+    # Pageable host input (chunk copies issued one by one between the chunks'
+    # passes) and a pageable host result (row bands, each copied while the
+    # next computes), with one reference and with several: bit for bit the
+    # device-resident call.
+    torch = pytest.importorskip("torch")
+    X, m = synth.trajectory(96, 4200, 800, 0.1, 3.0, np.float32, True)
+    dev = run(h, torch.from_numpy(X).cuda(), tgt_mass=m, precision=precision).cpu().numpy()
+    out = np.full(dev.size, -1.0, np.float32)
+    run(h, X, tgt_mass=m, precision=precision, out=out)
+    np.testing.assert_array_equal(out, dev)
+    T, _ = synth.trajectory(98, 3000, 1000, 0.1, 0.5, np.float32, True)  # one reference
+    devt = run(h, torch.from_numpy(T).cuda(), precision=precision).cpu().numpy()
+    assert h.stats()["n_refs"] == 1
+    outt = run(h, T, precision=precision)
+    assert h.stats()["n_refs"] == 1
+    np.testing.assert_array_equal(outt, devt)
+    C, _ = synth.clustered(97, 3000, 1000, 6, 0.8)
+    devc = run(h, torch.from_numpy(C).cuda(), precision=precision).cpu().numpy()
+    assert h.stats()["n_refs"] > 1
+    outc = run(h, C, precision=precision)
+    np.testing.assert_array_equal(outc, devc)
+
+
+@pytest.mark.parametrize("precision", ["tc", "fp32"])
 def test_pinned_clustered_result(h, precision):
     # Several references: the triangle is computed over reference-sorted
     # positions, whose results scatter over the whole output; bound for pinned

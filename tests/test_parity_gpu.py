@@ -427,6 +427,13 @@ def test_pageable_host_buffers(h, precision):
     assert h.stats()["n_refs"] > 1
     outc = run(h, C, precision=precision)
     np.testing.assert_array_equal(outc, devc)
+    # FULL, two pageable sets (chunks of both), the result in bands of target rows
+    R = X[:2100]
+    T2, _ = synth.trajectory(99, 4200, 800, 0.1, 3.0, np.float32, True)
+    devf = run(h, torch.from_numpy(R).cuda(), torch.from_numpy(T2).cuda(), tgt_mass=m,
+               precision=precision).cpu().numpy()
+    outf = run(h, R, T2, tgt_mass=m, precision=precision)
+    np.testing.assert_array_equal(outf, devf)
 
 
 @pytest.mark.parametrize("precision", ["tc", "fp32"])

@@ -456,6 +456,10 @@ def test_pinned_clustered_result(h, precision):
     hout.fill_(-1.0)
     run(h, hX, precision=precision, out=hout)
     np.testing.assert_array_equal(hout.numpy(), dev)
+    # a result buffer 4 bytes past a 16-byte boundary: copied back whole instead
+    shifted = torch.full((dev.size + 1,), -1.0, dtype=torch.float32).pin_memory()[1:]
+    run(h, hX, precision=precision, out=shifted)
+    np.testing.assert_array_equal(shifted.numpy(), dev)
     ref = oracle.allpairs_f64(X[:600])
     k = np.concatenate([np.arange(i * 3000 - i * (i + 1) // 2, i * 3000 - i * (i + 1) // 2 + 599 - i)
                         for i in range(599)])

@@ -174,9 +174,11 @@ int gbr_write_cmatrix(gbr_handle *h, const char *path, const void *xyz, int dtyp
 /* Gradient of L = sum_{i<j} g[tri(i,j)] * RMSD_ij (best fit, one set, GBR_F32)
  * with respect to every coordinate.  g NULL means g = 1.  grad_xyz has the
  * shape of xyz.  rmsd_out (optional, may be NULL) receives the forward TRI.
- * Pairs with RMSD == 0 contribute no gradient.  The pair pass runs on the
- * tensor cores where they are usable (gbr_stats.precision = GBR_PREC_TC),
- * else on the FP32 CUDA cores; the block GEMM is strict FP32. */
+ * Pairs with RMSD == 0 contribute no gradient.  Needs an sm_103 (GB300)
+ * device (GBR_ERR_UNSUPPORTED otherwise): the pair pass and the block
+ * contraction (S = B + B^T times the operand plane, FP16 hi/lo operands,
+ * three products, FP32 accumulation: ~2^-22 of the largest product) both
+ * run on the tensor cores; at most 60,000 frames. */
 int gbr_rmsd_backward(gbr_handle *h, const float *xyz, int64_t n_frame, int32_t n_atom,
                       const double *mass, const float *g, float *grad_xyz, float *rmsd_out);
 

@@ -283,8 +283,12 @@ int gbr_get_stats(const gbr_handle *h, gbr_stats *out);
  *                        with wider (16-frame) epilogue chunks; -1 (default)
  *                        = 3 from 1,280 atoms on, 4 below 768, 2 between
  *   GBR_OPT_HOST_OUT     pinned host `out` of gbr_allpairs: 1 = the kernels
- *                        store into it directly (default), 0 = results staged
- *                        in device memory and copied back in row bands
+ *                        store into it directly (default; a triangle over
+ *                        reference-sorted frames, with several references,
+ *                        is computed in device memory in row bands whose
+ *                        rows are copied while the next band computes),
+ *                        0 = results staged in device memory and copied back
+ *                        in row bands
  *   GBR_OPT_BAND_FLOATS  band size in floats of gbr_write_cmatrix's streamed
  *                        triangle (default 2^28; at least one row)
  *   GBR_OPT_INPUT_OVERLAP  pinned host input of one frame set, triangle into

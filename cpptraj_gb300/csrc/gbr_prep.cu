@@ -650,7 +650,7 @@ __device__ __forceinline__ void write_frame_table(float* ftab, double* rot, int6
 struct ScanArgs {
   const float* cm_ref;  // centring masses of reference frames (FP32), read when cm_ref_is_w == 0
   int cm_ref_is_w;      // reference frames centre with the fit weights (target frames always do)
-  const double* scal;   // k_weights' scal: [1] sum w, [2] sum of reference centring masses, [4], [5] reciprocals
+  const double* scal;   // the weights' scal (k_make_ref): [1] sum w, [2] sum of reference centring masses, [4], [5] reciprocals
   const float4* q;      // [N] {sqrt(w) r_k, sqrt(w)} (the weights centre too: w = sqrt(w)^2)
   const double* sr;     // sum w r_k, [3]
   const double* Eref;   // &Eref[k]
